@@ -1,0 +1,698 @@
+// api.cu -- the C ABI of include/filament_gb.h.
+//
+// One handle = one problem on the current device, one CUDA stream.  The
+// field state lives in HBM as the analytic half spectrum S[Mpad][Nt/2]
+// (transverse points padded to a multiple of 128 with zero rows for the
+// Hankel GEMMs).  A z-step is four kernels:
+//   k_rowreduce (fil_run only)  Imax / fluence of the current field
+//   k_control   (fil_run only)  adaptive dz, stop tests, z update
+//   k_rowstep                    plasma + t<->w + nonlinear RK step, per row
+//   k_dht (x2)                   Hankel transform, propagator, inverse
+// fil_run captures a few steps into a CUDA graph and replays it until the
+// on-device controller raises its done flag.
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/filament_gb.h"
+#include "launch.h"
+#include "rowkernels.cuh"
+#include "dht_simt.cuh"
+
+namespace {
+thread_local std::string g_err;
+const int kGraphSteps = 8;
+const int kGraphsPerCheck = 4;
+}
+
+struct fil_handle {
+  fil_config cfg;
+  std::string err;
+  int geom, n1, n2, nt, nh, nrows, mpad, nc;
+  bool fp64;
+  cudaStream_t st = nullptr;
+  // device buffers (void* to serve both precisions)
+  void* S = nullptr;      // state [mpad][nh] complex
+  void* W1 = nullptr;     // row-kernel output
+  void* W2 = nullptr;     // DHT intermediate
+  void* M1 = nullptr;     // [mpad][mpad]
+  void* M2 = nullptr;
+  void* tw = nullptr;     // [nt] complex
+  void* g1 = nullptr; void* g2 = nullptr; void* gt = nullptr;
+  void* Cc = nullptr; void* Cf = nullptr; void* Cl = nullptr;
+  void* kt2 = nullptr; void* beta = nullptr; void* dfr = nullptr; void* kmax2 = nullptr; void* wg = nullptr;
+  void* rho_g = nullptr; void* kdrho_g = nullptr;
+  void* stage = nullptr;  // field staging [nrows][nt] complex
+  double* fluence = nullptr;   // [nrows]
+  double* power = nullptr;     // [nt]
+  double* pw = nullptr;        // [nrows] transverse weights
+  double* rho_end = nullptr;   // [nrows]
+  DevCtl* ctl = nullptr;
+  DevCtl* ctl_host = nullptr;  // pinned
+  PlasmaParams pp;
+  int ns;
+  double A0[4], A1[4], B[4];
+  bool field_set = false, store_plasma = false;
+  int bugcompat = 0, clamp_last = 0, timing = 0;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev[8];
+  double tsum[3] = {0, 0, 0};
+  long tcount = 0;
+};
+
+static int fail(fil_handle* h, int code, const std::string& m) {
+  if (h) h->err = m; else g_err = m;
+  return code;
+}
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return fail(h, FIL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// ----------------------------------------------------------------- tables --
+template <typename R> static std::vector<R> cvt(const std::vector<double>& v) {
+  return std::vector<R>(v.begin(), v.end());
+}
+
+template <typename R>
+static int upload(fil_handle* h, void** dst, const std::vector<double>& v) {
+  std::vector<R> t = cvt<R>(v);
+  CK(cudaMalloc(dst, t.size() * sizeof(R)));
+  CK(cudaMemcpy(*dst, t.data(), t.size() * sizeof(R), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+static void rk_tableau(int alg, int* s, double a[4][4], double b[4], double c[4]) {
+  std::memset(a, 0, sizeof(double) * 16);
+  std::memset(b, 0, sizeof(double) * 4);
+  std::memset(c, 0, sizeof(double) * 4);
+  if (alg == FIL_ALG_RK2) {
+    *s = 2; a[1][0] = 0.5; b[1] = 1.0; c[1] = 0.5;
+  } else if (alg == FIL_ALG_RK3) {
+    *s = 3; a[1][0] = 0.5; a[2][0] = -1.0; a[2][1] = 2.0;
+    b[0] = 1.0 / 6.0; b[1] = 4.0 / 6.0; b[2] = 1.0 / 6.0; c[1] = 0.5; c[2] = 1.0;
+  } else {
+    *s = 4; a[1][0] = 0.5; a[2][1] = 0.5; a[3][2] = 1.0;
+    b[0] = 1.0 / 6.0; b[1] = 1.0 / 3.0; b[2] = 1.0 / 3.0; b[3] = 1.0 / 6.0;
+    c[1] = 0.5; c[2] = 0.5; c[3] = 1.0;
+  }
+}
+
+template <typename R>
+static int create_tables(fil_handle* h, const fil_tables* t) {
+  const fil_config& c = h->cfg;
+  const int n1 = h->n1, nt = h->nt, nh = h->nh, mp = h->mpad, nr = h->nrows;
+  typedef std::complex<double> cd;
+  // twiddles exp(-2 pi i m / nt)
+  {
+    std::vector<double> v(2 * nt);
+    for (int m = 0; m < nt; ++m) {
+      double a = -2.0 * M_PI * (double)m / (double)nt;
+      v[2 * m] = std::cos(a);
+      v[2 * m + 1] = std::sin(a);
+    }
+    if (upload<R>(h, &h->tw, v)) return FIL_ERR_CUDA;
+  }
+  // guards
+  {
+    std::vector<double> g(n1, 1.0), gtt(nt, 1.0);
+    if (t->guard1) g.assign(t->guard1, t->guard1 + n1);
+    if (t->guardt) gtt.assign(t->guardt, t->guardt + nt);
+    if (upload<R>(h, &h->g1, g) || upload<R>(h, &h->gt, gtt)) return FIL_ERR_CUDA;
+  }
+  // nonlinear coefficients C_ch[k] = i QZ Rnl_ch (k ? 2 : 1), k < nh
+  {
+    auto comb = [&](const double* rnl, void** dst) -> int {
+      std::vector<double> v(2 * nh, 0.0);
+      if (rnl && t->qz)
+        for (int k = 0; k < nh; ++k) {
+          cd q(t->qz[2 * k], t->qz[2 * k + 1]), r(rnl[2 * k], rnl[2 * k + 1]);
+          cd x = cd(0, 1) * q * r * (k ? 2.0 : 1.0);
+          v[2 * k] = x.real();
+          v[2 * k + 1] = x.imag();
+        }
+      return upload<R>(h, dst, v);
+    };
+    if (comb(t->rnl_cubic, &h->Cc) || comb(t->rnl_free, &h->Cf) || comb(t->rnl_losses, &h->Cl)) return FIL_ERR_CUDA;
+  }
+  // propagator tables
+  {
+    std::vector<double> kt2(mp, 0.0), be(2 * nh), df(2 * nh);
+    for (int i = 0; i < n1; ++i) kt2[i] = t->kt1[i] * t->kt1[i];
+    for (int k = 0; k < 2 * nh; ++k) { be[k] = t->beta[k]; df[k] = t->dfr[k]; }
+    if (upload<R>(h, &h->kt2, kt2) || upload<R>(h, &h->beta, be) || upload<R>(h, &h->dfr, df)) return FIL_ERR_CUDA;
+    if (t->kmax) {
+      std::vector<double> km(nh);
+      for (int k = 0; k < nh; ++k) km[k] = t->kmax[k] * t->kmax[k];
+      if (upload<R>(h, &h->kmax2, km)) return FIL_ERR_CUDA;
+    }
+    if (t->wguard) {
+      std::vector<double> w(t->wguard, t->wguard + nh);
+      if (upload<R>(h, &h->wg, w)) return FIL_ERR_CUDA;
+    }
+  }
+  // Hankel matrices M1 = T diag(s), M2 = diag(1/s) T, zero padded
+  {
+    std::vector<double> m1((size_t)mp * mp, 0.0), m2((size_t)mp * mp, 0.0);
+    for (int i = 0; i < n1; ++i)
+      for (int k = 0; k < n1; ++k) {
+        double T = t->dht[(size_t)i * n1 + k];
+        m1[(size_t)i * mp + k] = T * t->dht_s[k];
+        m2[(size_t)i * mp + k] = T / t->dht_s[i];
+      }
+    if (upload<R>(h, &h->M1, m1) || upload<R>(h, &h->M2, m2)) return FIL_ERR_CUDA;
+  }
+  // transverse weights 2 pi r dr
+  {
+    std::vector<double> w(nr);
+    for (int i = 0; i < nr; ++i) w[i] = 2.0 * M_PI * (t->rdr ? t->rdr[i] : 0.0);
+    CK(cudaMalloc(&h->pw, nr * sizeof(double)));
+    CK(cudaMemcpy(h->pw, w.data(), nr * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  // plasma
+  if (c.plasma) {
+    PlasmaParams& P = h->pp;
+    std::memset(&P, 0, sizeof P);
+    int nc = c.plasma_ncomp, n = c.rate_n;
+    P.nc = nc;
+    double a[4][4], b[4], cc[4];
+    rk_tableau(c.plasma_alg, &P.ns, a, b, cc);
+    for (int s = 0; s < 4; ++s) {
+      P.b[s] = b[s];
+      for (int l = 0; l < 4; ++l) P.a[s][l] = a[s][l];
+      P.pidx[s] = cc[s] == 0.0 ? 0 : (cc[s] == 1.0 ? 2 : 1);
+    }
+    P.kdep = c.plasma_kdep;
+    P.ereal = c.plasma_ereal;
+    P.rate_n = n;
+    P.dt = c.dt;
+    P.rho0 = c.rho0;
+    P.maxit = 8;
+    P.tol = h->fp64 ? 1e-13 : 1e-6;
+    bool pl = true;
+    for (int i = 0; i < nc; ++i) {
+      P.rho_nt[i] = t->rho_nt[i];
+      P.rava_nt[i] = t->rava[i] / t->rho_nt[i];
+      P.kfix[i] = t->kfix[i];
+      if (t->rava[i] != 0.0) P.avalanche = 1;
+      double s0 = 0;
+      for (int q = 0; q < n; ++q) {
+        P.lx[i][q] = t->rate_lx[i * n + q];
+        P.ly[i][q] = t->rate_ly[i * n + q];
+      }
+      for (int q = 0; q < n - 1; ++q) {
+        double s = (P.ly[i][q + 1] - P.ly[i][q]) / (P.lx[i][q + 1] - P.lx[i][q]);
+        P.sl[i][q] = s;
+        if (q == 0) s0 = s;
+        else if (std::fabs(s - s0) > 1e-12 * std::fabs(s0)) pl = false;
+      }
+      P.sl[i][n - 1] = P.sl[i][n - 2];
+    }
+    P.powerlaw = pl ? 1 : 0;
+  }
+  return 0;
+}
+
+template <typename R> static RowParams<R> row_params(fil_handle* h) {
+  typedef typename C2T<R>::type C;
+  RowParams<R> P;
+  std::memset(&P, 0, sizeof P);
+  const fil_config& c = h->cfg;
+  P.nrows = h->nrows;
+  P.n2 = h->n2;
+  P.geom = h->geom;
+  P.ld = h->nh;
+  P.tw = (const C*)h->tw;
+  P.g1 = (const R*)h->g1;
+  P.g2 = (const R*)h->g2;
+  P.gt = (const R*)h->gt;
+  P.gt_bug = (h->geom == FIL_GEOM_XYT) ? h->bugcompat : 0;
+  P.dt = (R)c.dt;
+  P.nonlin = c.nonlinearity;
+  P.has_cubic = (c.resp_mask & FIL_RESP_CUBIC) ? 1 : 0;
+  P.has_free = (c.resp_mask & FIL_RESP_FREE) && c.plasma ? 1 : 0;
+  P.has_losses = (c.resp_mask & FIL_RESP_LOSSES) && c.plasma ? 1 : 0;
+  P.cubic_thg = c.cubic_thg;
+  P.losses_ereal = c.losses_ereal;
+  P.Cc = (const C*)h->Cc;
+  P.Cf = (const C*)h->Cf;
+  P.Cl = (const C*)h->Cl;
+  P.ns = h->ns;
+  for (int s = 0; s < 4; ++s) { P.A0[s] = h->A0[s]; P.A1[s] = h->A1[s]; P.B[s] = h->B[s]; }
+  P.plasma = c.plasma;
+  P.pp = h->pp;
+  P.rho_g = (R*)h->rho_g;
+  P.kdrho_g = (R*)h->kdrho_g;
+  P.store_plasma = h->store_plasma ? 1 : 0;
+  P.rho_end = h->rho_end;
+  P.ctl = h->ctl;
+  return P;
+}
+
+template <typename R> static PropParams<R> prop_params(fil_handle* h) {
+  typedef typename C2T<R>::type C;
+  PropParams<R> p;
+  p.kt2 = (const R*)h->kt2;
+  p.beta = (const C*)h->beta;
+  p.dfr = (const C*)h->dfr;
+  p.kmax2 = (const R*)h->kmax2;
+  p.wg = (const R*)h->wg;
+  p.kparaxial = h->cfg.kparaxial;
+  return p;
+}
+
+// one z-step: row kernel (W1 <- S), DHT forward + propagator (W2 <- W1),
+// inverse (S <- W2)
+template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
+  RowParams<R> P = row_params<R>(h);
+  P.S_in = (const typename C2T<R>::type*)h->S;
+  P.S_out = (typename C2T<R>::type*)h->W1;
+  PropParams<R> pp = prop_params<R>(h);
+  const int Nc = 2 * h->nh;
+  if (timed) CK(cudaEventRecord(h->ev[0], h->st));
+  CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[1], h->st));
+  CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 1, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[2], h->st));
+  CK(launch_dht_simt<R>((const R*)h->M2, (const R*)h->W2, (R*)h->S, h->mpad, Nc, h->mpad, pp, h->ctl, 2, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[3], h->st));
+  return 0;
+}
+
+template <typename R> static int enqueue_reduce(fil_handle* h, double* power, int check_done) {
+  RowParams<R> P = row_params<R>(h);
+  P.S_in = (const typename C2T<R>::type*)h->S;
+  CK(launch_rowreduce<R>(P, h->nt, h->fluence, power, h->pw, check_done, h->st));
+  return 0;
+}
+
+static int zstep(fil_handle* h, bool timed) {
+  return h->fp64 ? enqueue_zstep<double>(h, timed) : enqueue_zstep<float>(h, timed);
+}
+static int reduce(fil_handle* h, double* power, int check_done) {
+  return h->fp64 ? enqueue_reduce<double>(h, power, check_done) : enqueue_reduce<float>(h, power, check_done);
+}
+
+static int read_ctl(fil_handle* h) {
+  CK(cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+static void free_all(fil_handle* h) {
+  void* bufs[] = {h->S, h->W1, h->W2, h->M1, h->M2, h->tw, h->g1, h->g2, h->gt, h->Cc, h->Cf, h->Cl,
+                  h->kt2, h->beta, h->dfr, h->kmax2, h->wg, h->rho_g, h->kdrho_g, h->stage,
+                  h->fluence, h->power, h->pw, h->rho_end, h->ctl};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (h->ctl_host) cudaFreeHost(h->ctl_host);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (int i = 0; i < 8; ++i)
+    if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+  if (h->st) cudaStreamDestroy(h->st);
+}
+
+// host layout conversion: user array -> row-major complex R staging
+template <typename R>
+static void to_rows(const fil_handle* h, const void* src, int dtype, int layout, std::vector<R>& out) {
+  const long nr = h->nrows, nt = h->nt;
+  out.assign((size_t)nr * nt * 2, (R)0);
+  for (long p = 0; p < nr; ++p)
+    for (long j = 0; j < nt; ++j) {
+      long s = layout == FIL_LAYOUT_ROWMAJOR ? p * nt + j
+                                             : j * nr + (h->n2 > 1 ? (p % h->n2) * h->n1 + p / h->n2 : p);
+      double re, im;
+      if (dtype == FIL_DTYPE_C128) { re = ((const double*)src)[2 * s]; im = ((const double*)src)[2 * s + 1]; }
+      else { re = ((const float*)src)[2 * s]; im = ((const float*)src)[2 * s + 1]; }
+      out[2 * (p * nt + j)] = (R)re;
+      out[2 * (p * nt + j) + 1] = (R)im;
+    }
+}
+template <typename R>
+static void from_rows(const fil_handle* h, const std::vector<R>& in, void* dst, int dtype, int layout, int ncomp) {
+  const long nr = h->nrows, nt = h->nt;
+  for (long p = 0; p < nr; ++p)
+    for (long j = 0; j < nt; ++j) {
+      long s = layout == FIL_LAYOUT_ROWMAJOR ? p * nt + j
+                                             : j * nr + (h->n2 > 1 ? (p % h->n2) * h->n1 + p / h->n2 : p);
+      if (ncomp == 2) {
+        double re = in[2 * (p * nt + j)], im = in[2 * (p * nt + j) + 1];
+        if (dtype == FIL_DTYPE_C128) { ((double*)dst)[2 * s] = re; ((double*)dst)[2 * s + 1] = im; }
+        else { ((float*)dst)[2 * s] = (float)re; ((float*)dst)[2 * s + 1] = (float)im; }
+      } else {
+        double v = in[p * nt + j];
+        if (dtype == FIL_DTYPE_F64) ((double*)dst)[s] = v;
+        else ((float*)dst)[s] = (float)v;
+      }
+    }
+}
+
+template <typename R> static int set_field_t(fil_handle* h, const void* E, int dtype, int layout, int analytic) {
+  typedef typename C2T<R>::type C;
+  std::vector<R> rows;
+  to_rows<R>(h, E, dtype, layout, rows);
+  CK(cudaMemcpyAsync(h->stage, rows.data(), rows.size() * sizeof(R), cudaMemcpyHostToDevice, h->st));
+  CK(launch_field_in<R>((const C*)h->stage, (C*)h->S, h->nh, (const C*)h->tw, analytic, h->nrows, h->nt, h->st));
+  // control block: fresh simulation, no pending guard
+  DevCtl c;
+  std::memset(&c, 0, sizeof c);
+  c.first = 1;
+  CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemsetAsync(h->rho_end, 0, h->nrows * sizeof(double), h->st));
+  if (h->cfg.plasma) {   // Models.jl:66: plasma solved on the initial field
+    RowParams<R> P = row_params<R>(h);
+    P.S_in = (const C*)h->S;
+    CK(launch_rowstep<R>(P, h->nt, h->nc, 1, h->st));
+  }
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+template <typename R> static int get_field_t(fil_handle* h, void* E, int dtype, int layout) {
+  typedef typename C2T<R>::type C;
+  RowParams<R> P = row_params<R>(h);
+  P.S_in = (const C*)h->S;
+  CK(launch_field_out<R>(P, h->nt, (C*)h->stage, h->st));
+  std::vector<R> rows((size_t)h->nrows * h->nt * 2);
+  CK(cudaMemcpyAsync(rows.data(), h->stage, rows.size() * sizeof(R), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  from_rows<R>(h, rows, E, dtype, layout, 2);
+  return 0;
+}
+
+// =================================================================== ABI ==
+extern "C" {
+
+const char* fil_last_error(const fil_handle* h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+int fil_destroy(fil_handle* h) {
+  if (!h) return FIL_OK;
+  free_all(h);
+  delete h;
+  return FIL_OK;
+}
+
+int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
+  fil_handle* h = nullptr;
+  if (!cfg || !t || !out) return fail(h, FIL_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (cfg->abi_version != FIL_ABI_VERSION) return fail(h, FIL_ERR_ARG, "ABI version mismatch");
+  if (cfg->geometry != FIL_GEOM_RT)
+    return fail(h, FIL_ERR_UNSUPPORTED, "this build runs the RT geometry on the GPU");
+  if (!is_pow2(cfg->nt) || cfg->nt < 512 || cfg->nt > 4096)
+    return fail(h, FIL_ERR_UNSUPPORTED, "nt must be a power of two in [512, 4096]");
+  if (cfg->n1 < 1 || cfg->n1 > 65536) return fail(h, FIL_ERR_ARG, "bad n1");
+  if (cfg->nonlinearity && !cfg->qparaxial)
+    return fail(h, FIL_ERR_UNSUPPORTED, "QPARAXIAL=false is not built");
+  if (cfg->nonlinearity && (cfg->resp_mask & FIL_RESP_RAMAN))
+    return fail(h, FIL_ERR_UNSUPPORTED, "the Raman response is not built");
+  if (cfg->plasma && (cfg->plasma_ncomp < 1 || cfg->plasma_ncomp > FIL_MAXCOMP))
+    return fail(h, FIL_ERR_UNSUPPORTED, "plasma_ncomp must be 1 or 2");
+  if (cfg->plasma && (cfg->rate_n < 2 || cfg->rate_n > FIL_MAXRATE))
+    return fail(h, FIL_ERR_ARG, "rate_n must be in [2, 32]");
+  if (!t->kt1 || !t->beta || !t->dfr || !t->dht || !t->dht_s)
+    return fail(h, FIL_ERR_ARG, "missing propagator or DHT tables");
+  if (cfg->nonlinearity && !t->qz) return fail(h, FIL_ERR_ARG, "missing QZ table");
+  if (cfg->plasma && (!t->rho_nt || !t->rava || !t->kfix || !t->rate_lx || !t->rate_ly))
+    return fail(h, FIL_ERR_ARG, "missing plasma tables");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(h, FIL_ERR_CUDA, "no CUDA device");
+  h = new fil_handle();
+  std::memset(h->ev, 0, sizeof h->ev);
+  h->cfg = *cfg;
+  h->geom = cfg->geometry;
+  h->n1 = cfg->n1;
+  h->n2 = cfg->n2;
+  h->nt = cfg->nt;
+  h->nh = cfg->nt / 2;
+  h->nrows = cfg->n1 * cfg->n2;
+  h->mpad = (h->nrows + 127) / 128 * 128;
+  h->nc = cfg->plasma ? cfg->plasma_ncomp : 0;
+  h->fp64 = cfg->precision == FIL_PREC_FP64;
+  {
+    double a[4][4], b[4], c[4];
+    rk_tableau(cfg->alg, &h->ns, a, b, c);
+    for (int s = 0; s < 4; ++s) {
+      h->B[s] = b[s];
+      h->A0[s] = s >= 1 ? a[s][0] : 0.0;
+      h->A1[s] = s >= 2 ? a[s][s - 1] : 0.0;
+    }
+  }
+  int rc = 0;
+  const size_t es = h->fp64 ? sizeof(double2) : sizeof(float2);
+  const size_t sz = (size_t)h->mpad * h->nh * es;
+#define CKC(call)                                                                    \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      g_err = std::string(#call) + ": " + cudaGetErrorString(e_);                   \
+      free_all(h); delete h;                                                         \
+      return FIL_ERR_CUDA;                                                           \
+    }                                                                                \
+  } while (0)
+  CKC(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  for (int i = 0; i < 8; ++i) CKC(cudaEventCreate(&h->ev[i]));
+  CKC(cudaMalloc(&h->S, sz));
+  CKC(cudaMalloc(&h->W1, sz));
+  CKC(cudaMalloc(&h->W2, sz));
+  CKC(cudaMemset(h->S, 0, sz));
+  CKC(cudaMemset(h->W1, 0, sz));
+  CKC(cudaMemset(h->W2, 0, sz));
+  CKC(cudaMalloc(&h->stage, (size_t)h->nrows * h->nt * es));
+  CKC(cudaMalloc(&h->fluence, h->nrows * sizeof(double)));
+  CKC(cudaMalloc(&h->power, h->nt * sizeof(double)));
+  CKC(cudaMalloc(&h->rho_end, h->nrows * sizeof(double)));
+  CKC(cudaMemset(h->rho_end, 0, h->nrows * sizeof(double)));
+  CKC(cudaMalloc(&h->ctl, sizeof(DevCtl)));
+  CKC(cudaMemset(h->ctl, 0, sizeof(DevCtl)));
+  CKC(cudaMallocHost(&h->ctl_host, sizeof(DevCtl)));
+  rc = h->fp64 ? create_tables<double>(h, t) : create_tables<float>(h, t);
+  if (rc) {
+    g_err = h->err;
+    free_all(h);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return FIL_OK;
+}
+
+int fil_set_option(fil_handle* h, int option, int64_t value) {
+  if (!h) return fail(h, FIL_ERR_ARG, "null handle");
+  if (option == FIL_OPT_STORE_PLASMA) {
+    bool on = value != 0;
+    if (on && !h->rho_g) {
+      size_t es = h->fp64 ? sizeof(double) : sizeof(float);
+      CK(cudaMalloc(&h->rho_g, (size_t)h->nrows * h->nt * es));
+      CK(cudaMalloc(&h->kdrho_g, (size_t)h->nrows * h->nt * es));
+      CK(cudaMemset(h->rho_g, 0, (size_t)h->nrows * h->nt * es));
+      CK(cudaMemset(h->kdrho_g, 0, (size_t)h->nrows * h->nt * es));
+    }
+    h->store_plasma = on;
+  } else if (option == FIL_OPT_XYT_GUARD_BUGCOMPAT) {
+    h->bugcompat = value != 0;
+  } else if (option == FIL_OPT_CLAMP_LAST_DZ) {
+    h->clamp_last = value != 0;
+  } else if (option == 4) {  // per-kernel timing of fil_step (diagnostic)
+    h->timing = value != 0;
+  } else {
+    return fail(h, FIL_ERR_ARG, "unknown option");
+  }
+  if (h->graph) {           // parameters baked into the graph changed
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return FIL_OK;
+}
+
+int fil_set_field(fil_handle* h, const void* E, int dtype, int layout, int analytic) {
+  if (!h || !E) return fail(h, FIL_ERR_ARG, "null argument");
+  if (dtype != FIL_DTYPE_C64 && dtype != FIL_DTYPE_C128) return fail(h, FIL_ERR_ARG, "field dtype must be complex");
+  int rc = h->fp64 ? set_field_t<double>(h, E, dtype, layout, analytic) : set_field_t<float>(h, E, dtype, layout, analytic);
+  if (rc) return rc;
+  h->field_set = true;
+  return FIL_OK;
+}
+
+int fil_get_field(fil_handle* h, void* E, int dtype, int layout) {
+  if (!h || !E) return fail(h, FIL_ERR_ARG, "null argument");
+  if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
+  if (dtype != FIL_DTYPE_C64 && dtype != FIL_DTYPE_C128) return fail(h, FIL_ERR_ARG, "field dtype must be complex");
+  return h->fp64 ? get_field_t<double>(h, E, dtype, layout) : get_field_t<float>(h, E, dtype, layout);
+}
+
+int fil_get_plasma(fil_handle* h, int which, void* out, int dtype, int layout) {
+  if (!h || !out) return fail(h, FIL_ERR_ARG, "null argument");
+  if (!h->store_plasma || !h->rho_g) return fail(h, FIL_ERR_STATE, "FIL_OPT_STORE_PLASMA is off");
+  if (dtype != FIL_DTYPE_F32 && dtype != FIL_DTYPE_F64) return fail(h, FIL_ERR_ARG, "dtype must be real");
+  size_t n = (size_t)h->nrows * h->nt;
+  void* src = which == 0 ? h->rho_g : h->kdrho_g;
+  if (h->fp64) {
+    std::vector<double> v(n);
+    CK(cudaMemcpyAsync(v.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    from_rows<double>(h, v, out, dtype, layout, 1);
+  } else {
+    std::vector<float> v(n);
+    CK(cudaMemcpyAsync(v.data(), src, n * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    from_rows<float>(h, v, out, dtype, layout, 1);
+  }
+  return FIL_OK;
+}
+
+int fil_step(fil_handle* h, double z, double dz) {
+  if (!h) return fail(h, FIL_ERR_ARG, "null handle");
+  if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
+  CK(launch_setdz(h->ctl, z, dz, h->st));
+  int rc = zstep(h, h->timing != 0);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->st));
+  if (h->timing) {
+    float ms;
+    for (int i = 0; i < 3; ++i) {
+      CK(cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]));
+      h->tsum[i] += ms;
+    }
+    h->tcount += 1;
+  }
+  return FIL_OK;
+}
+
+static int build_graph(fil_handle* h) {
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  int rc = 0;
+  for (int s = 0; s < kGraphSteps && !rc; ++s) {
+    rc = reduce(h, nullptr, 1);
+    if (!rc) {
+      cudaError_t e = launch_control(h->ctl, h->fluence, h->pw, h->nrows, h->st);
+      if (e != cudaSuccess) rc = fail(h, FIL_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (!rc) rc = zstep(h, false);
+  }
+  cudaError_t e = cudaStreamEndCapture(h->st, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(h, FIL_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(h, FIL_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stats) {
+  if (!h) return fail(h, FIL_ERR_ARG, "null handle");
+  if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
+  // arm the controller
+  CK(cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  DevCtl c = *h->ctl_host;
+  c.z = z0;
+  c.zmax = zmax;
+  c.nmax = nmax;
+  c.run_steps = 0;
+  c.done = 0;
+  c.status = 0;
+  c.flags &= ~(FIL_FLAG_ISTOP);
+  c.dz0 = h->cfg.dz0;
+  c.phimax = h->cfg.phimax;
+  c.phik = h->cfg.phik;
+  c.phip = h->cfg.phip;
+  c.istop = h->cfg.istop;
+  c.nonlinearity = h->cfg.nonlinearity;
+  c.clamp_last = h->clamp_last;
+  c.imax_acc = 0;
+  CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
+  if (!h->graph) {
+    int rc = build_graph(h);
+    if (rc) return rc;
+  }
+  for (;;) {
+    for (int i = 0; i < kGraphsPerCheck; ++i) CK(cudaGraphLaunch(h->graph, h->st));
+    int rc = read_ctl(h);
+    if (rc) return rc;
+    if (h->ctl_host->done) break;
+  }
+  const DevCtl& r = *h->ctl_host;
+  if (stats) {
+    stats->z = r.z;
+    stats->dz = r.dz;
+    stats->imax = r.imax;
+    stats->rhomax = r.rhomax;
+    stats->energy = r.energy;
+    stats->steps = r.steps;
+    stats->status = r.status;
+    stats->flags = r.flags;
+  }
+  if (r.status < 0) return fail(h, r.status, "non-finite field during fil_run");
+  return r.status;
+}
+
+int fil_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power, double* rho_end) {
+  if (!h) return fail(h, FIL_ERR_ARG, "null handle");
+  if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
+  CK(cudaMemsetAsync(h->power, 0, h->nt * sizeof(double), h->st));
+  // fresh Imax accumulator
+  CK(cudaMemsetAsync((char*)h->ctl + offsetof(DevCtl, imax_acc), 0, sizeof(unsigned long long), h->st));
+  int rc = reduce(h, h->power, 0);
+  if (rc) return rc;
+  std::vector<double> F(h->nrows), P(h->nt), re(h->nrows), w(h->nrows);
+  CK(cudaMemcpyAsync(F.data(), h->fluence, h->nrows * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(P.data(), h->power, h->nt * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(re.data(), h->rho_end, h->nrows * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(w.data(), h->pw, h->nrows * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  rc = read_ctl(h);
+  if (rc) return rc;
+  const DevCtl& c = *h->ctl_host;
+  if (fluence) std::memcpy(fluence, F.data(), F.size() * sizeof(double));
+  if (power) std::memcpy(power, P.data(), P.size() * sizeof(double));
+  if (rho_end) std::memcpy(rho_end, re.data(), re.size() * sizeof(double));
+  if (st) {
+    double e = 0;
+    for (int i = 0; i < h->nrows; ++i) e += F[i] * w[i];
+    st->z = c.z;
+    st->dz = c.dz;
+    double im, rm;
+    std::memcpy(&im, &c.imax_acc, sizeof im);
+    std::memcpy(&rm, &c.rhomax_acc, sizeof rm);
+    st->imax = im;
+    st->rhomax = rm;   // maximum of the last plasma solve
+    st->energy = e;
+    st->steps = c.steps;
+    st->status = c.status;
+    st->flags = c.flags;
+  }
+  if (c.flags & FIL_FLAG_NAN) return fail(h, FIL_ERR_NAN, "non-finite field");
+  return FIL_OK;
+}
+
+int fil_get_stats(fil_handle* h, fil_stats* st) {
+  if (!h || !st) return fail(h, FIL_ERR_ARG, "null argument");
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  const DevCtl& c = *h->ctl_host;
+  st->z = c.z;
+  st->dz = c.dz;
+  st->imax = c.imax;
+  st->rhomax = c.rhomax;
+  st->energy = c.energy;
+  st->steps = c.steps;
+  st->status = c.status;
+  st->flags = c.flags;
+  return FIL_OK;
+}
+
+int fil_kernel_times(fil_handle* h, double* ms, int n) {
+  if (!h || !ms) return fail(h, FIL_ERR_ARG, "null argument");
+  for (int i = 0; i < n; ++i) ms[i] = (i < 3 && h->tcount) ? h->tsum[i] / h->tcount : 0.0;
+  return FIL_OK;
+}
+
+}  // extern "C"

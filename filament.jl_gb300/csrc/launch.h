@@ -1,0 +1,25 @@
+// launch.h -- host-side launch wrappers shared by the translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+struct DevCtl;
+template <typename R> struct RowParams;
+template <typename R> struct PropParams;
+
+template <typename R>
+cudaError_t launch_rowstep(const RowParams<R>& P, int n, int nc, int mode, cudaStream_t st);
+template <typename R>
+cudaError_t launch_rowreduce(const RowParams<R>& P, int n, double* fluence, double* power_out,
+                             const double* power_w, int check_done, cudaStream_t st);
+template <typename R>
+cudaError_t launch_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S, int ld,
+                            const typename C2T<R>::type* tw, int analytic, int nrows, int n, cudaStream_t st);
+template <typename R>
+cudaError_t launch_field_out(const RowParams<R>& P, int n, typename C2T<R>::type* E, cudaStream_t st);
+template <typename R>
+cudaError_t launch_dht_simt(const R* A, const R* B, R* C, int M, int N, int K, const PropParams<R>& pp,
+                            DevCtl* ctl, int epi, cudaStream_t st);
+cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
+cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);

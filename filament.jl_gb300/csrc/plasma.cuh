@@ -1,0 +1,225 @@
+// plasma.cuh -- parallel-in-time solve of the multiphoton/avalanche plasma
+// equation of one transverse point (one row of E(t) in shared memory).
+//
+// Reference: src/modules/plasma_equations.jl:46-72 (sequential RK over t per
+// point) with the right-hand sides of
+// src/modules/plasma_equations/photoionization_avalanche.jl:119-205:
+//   drho_i/dt  = W_i(I) (rho_nt,i - rho_i) + Rava_i E^2 (rho_nt,i - rho_i)/rho_nt,i * sum(rho)
+//   drho'_i/dt = W_i(I) (rho_nt,i - rho'_i)                 (photoionisation only)
+//   Kdrho(t_j) = sum_i K_i(I_j) W_i(I_j) (rho_nt,i - rho'_i(t_{j+1}))
+// with E linearly interpolated at the stage times t_j + c_s dt.
+//
+// Instead of one thread walking 4095 steps, every explicit-RK step is written
+// as a map u_{j+1} = Phi_j(u_j).  For the photoionisation-only equation Phi_j
+// is affine, so u_j for all j follows from one block-wide associative scan of
+// affine maps (each thread composes a 16-step chunk, a warp/block scan joins
+// the chunks, each thread re-applies its chunk from its incoming prefix).
+// With avalanche the map is polynomial; Newton's method on the whole
+// sequence linearises every Phi_j around the previous iterate, which is again
+// an affine scan.  Iteration starts from the photoionisation-only solution
+// (avalanche is a small correction) and stops when the update is below a
+// relative tolerance; its fixed point is the sequential RK solution.
+//
+// Affine maps are stored as u -> (I - L) u + B with L = I - dPhi/du kept
+// explicitly, so products of thousands of near-identity maps do not lose the
+// small deviations to rounding.
+#pragma once
+#include "common.cuh"
+
+#define FIL_MAXCOMP 2
+#define FIL_MAXRATE 32
+
+struct PlasmaParams {
+  int nc;                 // species
+  int ns;                 // RK stages
+  int kdep, ereal, powerlaw, rate_n;
+  int pidx[4];            // stage time: 0 = t_j, 1 = midpoint, 2 = t_{j+1}
+  double a[4][4], b[4];   // RK tableau
+  double dt, rho0;
+  double rho_nt[FIL_MAXCOMP], rava_nt[FIL_MAXCOMP], kfix[FIL_MAXCOMP];
+  double lx[FIL_MAXCOMP][FIL_MAXRATE], ly[FIL_MAXCOMP][FIL_MAXRATE], sl[FIL_MAXCOMP][FIL_MAXRATE];
+  int avalanche;          // any rava != 0
+  int maxit;              // Newton iteration cap
+  double tol;             // Newton relative tolerance
+};
+
+template <typename R> struct PlasmaSmem {
+  R lx[FIL_MAXCOMP][FIL_MAXRATE], ly[FIL_MAXCOMP][FIL_MAXRATE], sl[FIL_MAXCOMP][FIL_MAXRATE];
+};
+
+template <typename R, int NC> struct Aff {
+  R L[NC][NC];
+  R B[NC];
+};
+
+template <typename R, int NC> FIL_DEV Aff<R, NC> aff_identity() {
+  Aff<R, NC> m;
+#pragma unroll
+  for (int i = 0; i < NC; ++i) {
+    m.B[i] = 0;
+#pragma unroll
+    for (int l = 0; l < NC; ++l) m.L[i][l] = 0;
+  }
+  return m;
+}
+
+// second o first : u -> (I-L2)((I-L1)u + B1) + B2
+template <typename R, int NC> FIL_DEV Aff<R, NC> aff_compose(const Aff<R, NC>& m2, const Aff<R, NC>& m1) {
+  Aff<R, NC> r;
+#pragma unroll
+  for (int i = 0; i < NC; ++i) {
+    R b = m1.B[i] + m2.B[i];
+#pragma unroll
+    for (int l = 0; l < NC; ++l) {
+      R p = 0;
+#pragma unroll
+      for (int m = 0; m < NC; ++m) p += m2.L[i][m] * m1.L[m][l];
+      r.L[i][l] = m1.L[i][l] + m2.L[i][l] - p;
+      b -= m2.L[i][l] * m1.B[l];
+    }
+    r.B[i] = b;
+  }
+  return r;
+}
+
+template <typename R, int NC> FIL_DEV void aff_apply(const Aff<R, NC>& m, const R* u, R* out) {
+#pragma unroll
+  for (int i = 0; i < NC; ++i) {
+    R v = u[i] + m.B[i];
+#pragma unroll
+    for (int l = 0; l < NC; ++l) v -= m.L[i][l] * u[l];
+    out[i] = v;
+  }
+}
+
+template <typename R, int NC> FIL_DEV Aff<R, NC> aff_shfl_up(const Aff<R, NC>& m, int off) {
+  Aff<R, NC> r;
+#pragma unroll
+  for (int i = 0; i < NC; ++i) {
+    r.B[i] = __shfl_up_sync(0xffffffffu, m.B[i], off);
+#pragma unroll
+    for (int l = 0; l < NC; ++l) r.L[i][l] = __shfl_up_sync(0xffffffffu, m.L[i][l], off);
+  }
+  return r;
+}
+
+// Exclusive block scan: returns G_{t-1} o ... o G_0 for thread t (identity
+// for t = 0).  scratch holds blockDim/32 maps.
+template <typename R, int NC> FIL_DEV Aff<R, NC> aff_block_exclusive_scan(Aff<R, NC> g, Aff<R, NC>* scratch) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  Aff<R, NC> inc = g;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    Aff<R, NC> o = aff_shfl_up<R, NC>(inc, off);
+    if (lane >= off) inc = aff_compose<R, NC>(inc, o);
+  }
+  Aff<R, NC> exc = aff_shfl_up<R, NC>(inc, 1);
+  if (lane == 0) exc = aff_identity<R, NC>();
+  __syncthreads();
+  if (lane == 31) scratch[w] = inc;
+  __syncthreads();
+  if (w > 0) {
+    Aff<R, NC> pre = scratch[0];
+    for (int k = 1; k < w; ++k) pre = aff_compose<R, NC>(scratch[k], pre);
+    exc = aff_compose<R, NC>(exc, pre);
+  }
+  (void)nw;
+  __syncthreads();
+  return exc;
+}
+
+// W(I) and its log-log slope (TabulatedFunctions restatement: linear
+// interpolation of ln W over ln I, end segments extended, W(I<=0) = 0).
+template <typename R> FIL_DEV R rate_eval(const PlasmaParams& P, const PlasmaSmem<R>& T, int c, R I, R* slope) {
+  int n = P.rate_n;
+  if (!(I > (R)0)) {
+    *slope = T.sl[c][0];
+    return (R)0;
+  }
+  R l = log(I);
+  int i = 0;
+  if (!P.powerlaw) {
+    int lo = 0, hi = n - 2;
+    while (lo < hi) {   // largest i in [0, n-2] with lx[i] <= l
+      int mid = (lo + hi + 1) >> 1;
+      if (T.lx[c][mid] <= l) lo = mid; else hi = mid - 1;
+    }
+    i = lo;
+  }
+  *slope = T.sl[c][i];
+  return exp(T.ly[c][i] + (l - T.lx[c][i]) * T.sl[c][i]);
+}
+
+// One RK step u -> Phi(u) of the full (aval = true) or photoionisation-only
+// equation, linearised at u: returns the affine map (L, B) with
+// Phi(v) ~= (I - L) v + B exact for the affine case.
+template <typename R, int NC>
+FIL_DEV Aff<R, NC> step_map(const PlasmaParams& P, const R* u, const R (&W)[3][NC], const R (&ava)[3],
+                            bool aval) {
+  R k[4][NC], dk[4][NC][NC];
+  const R dt = (R)P.dt;
+  for (int s = 0; s < P.ns; ++s) {
+    R U[NC], dU[NC][NC];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+      U[i] = u[i];
+#pragma unroll
+      for (int l = 0; l < NC; ++l) dU[i][l] = (i == l) ? (R)1 : (R)0;
+    }
+    for (int l = 0; l < s; ++l) {
+      R al = (R)P.a[s][l];
+      if (al != (R)0) {
+#pragma unroll
+        for (int i = 0; i < NC; ++i) {
+          U[i] += dt * al * k[l][i];
+#pragma unroll
+          for (int m = 0; m < NC; ++m) dU[i][m] += dt * al * dk[l][i][m];
+        }
+      }
+    }
+    const int p = P.pidx[s];
+    R S = 0;
+#pragma unroll
+    for (int i = 0; i < NC; ++i) S += U[i];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+      const R rn = (R)P.rho_nt[i];
+      const R ai = aval ? (R)P.rava_nt[i] * ava[p] : (R)0;
+      const R g = W[p][i] + ai * S;
+      k[s][i] = (rn - U[i]) * g;
+      // Df_im = -delta_im g + (rn - U_i) a_i
+#pragma unroll
+      for (int m = 0; m < NC; ++m) {
+        R d = 0;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+          R Df = ((i == q) ? -g : (R)0) + (rn - U[i]) * ai;
+          d += Df * dU[q][m];
+        }
+        dk[s][i][m] = d;
+      }
+    }
+  }
+  Aff<R, NC> M;
+#pragma unroll
+  for (int i = 0; i < NC; ++i) {
+    R inc = 0;
+    R Lrow[NC];
+#pragma unroll
+    for (int l = 0; l < NC; ++l) Lrow[l] = 0;
+    for (int s = 0; s < P.ns; ++s) {
+      R bs = (R)P.b[s];
+      inc += bs * k[s][i];
+#pragma unroll
+      for (int l = 0; l < NC; ++l) Lrow[l] += bs * dk[s][i][l];
+    }
+    R B = dt * inc;
+#pragma unroll
+    for (int l = 0; l < NC; ++l) {
+      M.L[i][l] = -dt * Lrow[l];
+      B += M.L[i][l] * u[l];
+    }
+    M.B[i] = B;
+  }
+  return M;
+}

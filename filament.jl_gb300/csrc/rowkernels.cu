@@ -1,0 +1,183 @@
+// rowkernels.cu -- instantiations of the row and DHT kernels and the
+// controller kernel, plus host-side launch wrappers used by api.cu.
+#include <cstdio>
+
+#include "launch.h"
+#include "rowkernels.cuh"
+#include "dht_simt.cuh"
+
+// ---------------------------------------------------------------------------
+// Controller (AdaptiveSteps.jl:96-107, Filament.jl:123-164): one block.
+__global__ void k_control(DevCtl* c, const double* __restrict__ fluence, const double* __restrict__ w,
+                          int nrows) {
+  __shared__ double sc[32];
+  if (c->done) return;
+  double e = 0;
+  for (int i = threadIdx.x; i < nrows; i += blockDim.x) e += fluence[i] * w[i];
+  e = block_sum<double>(e, sc);
+  if (threadIdx.x != 0) return;
+  const double imax = __longlong_as_double((long long)c->imax_acc);
+  const double rhomax = __longlong_as_double((long long)c->rhomax_acc);
+  c->imax = imax;
+  c->rhomax = rhomax;
+  c->energy = e;
+  c->imax_acc = 0;
+  if (c->flags & FIL_FLAG_NAN) { c->done = 1; c->status = -3; return; }
+  if (!c->first && imax > c->istop) { c->done = 1; c->status = 2; c->flags |= FIL_FLAG_ISTOP; return; }
+  if (!(c->z < c->zmax)) { c->done = 1; c->status = 1; return; }
+  if (c->run_steps >= c->nmax) { c->done = 1; c->status = 3; return; }
+  double dz = c->dz0;
+  if (c->nonlinearity) {
+    if (imax > 0) dz = fmin(dz, c->phimax / (c->phik * imax));
+    if (c->phip > 0 && rhomax > 0) dz = fmin(dz, c->phimax / (c->phip * rhomax));
+  }
+  if (c->clamp_last && c->z + dz > c->zmax) dz = c->zmax - c->z;
+  c->z += dz;
+  c->dz = dz;
+  c->steps += 1;
+  c->run_steps += 1;
+  c->first = 0;
+  c->rhomax_acc = 0;
+}
+
+// fil_step: latch the plasma maximum of the previous solve, set z and dz.
+__global__ void k_setdz(DevCtl* c, double z, double dz) {
+  c->done = 0;
+  c->rhomax = __longlong_as_double((long long)c->rhomax_acc);
+  c->rhomax_acc = 0;
+  c->z = z;
+  c->dz = dz;
+  c->steps += 1;
+  c->first = 0;
+}
+
+// ---------------------------------------------------------------------------
+template <typename R, int N, int NC>
+static size_t rowstep_smem() {
+  typedef typename C2T<R>::type C;
+  constexpr int NP = N + N / 16;
+  return 2 * NP * sizeof(C) + 2 * N * sizeof(R) + 32 * sizeof(R) + 32 * sizeof(Aff<R, (NC > 0 ? NC : 1)>) +
+         sizeof(PlasmaSmem<R>);
+}
+template <typename R, int N> static size_t x_smem() {
+  typedef typename C2T<R>::type C;
+  return (N + N / 16) * sizeof(C) + 64 * sizeof(double);
+}
+
+template <typename R, int N, int NC>
+static cudaError_t launch_rowstep_t(const RowParams<R>& P, int mode, cudaStream_t st) {
+  size_t sm = rowstep_smem<R, N, NC>();
+  cudaError_t e = cudaFuncSetAttribute(k_rowstep<R, N, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_rowstep<R, N, NC><<<P.nrows, N / 16, sm, st>>>(P, mode);
+  return cudaGetLastError();
+}
+
+template <typename R, int N>
+static cudaError_t launch_rowstep_n(const RowParams<R>& P, int nc, int mode, cudaStream_t st) {
+  if (nc == 0) return launch_rowstep_t<R, N, 0>(P, mode, st);
+  if (nc == 1) return launch_rowstep_t<R, N, 1>(P, mode, st);
+  return launch_rowstep_t<R, N, 2>(P, mode, st);
+}
+
+template <typename R>
+cudaError_t launch_rowstep(const RowParams<R>& P, int n, int nc, int mode, cudaStream_t st) {
+  switch (n) {
+    case 512: return launch_rowstep_n<R, 512>(P, nc, mode, st);
+    case 1024: return launch_rowstep_n<R, 1024>(P, nc, mode, st);
+    case 2048: return launch_rowstep_n<R, 2048>(P, nc, mode, st);
+    case 4096: return launch_rowstep_n<R, 4096>(P, nc, mode, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename R, int N>
+static cudaError_t launch_rowreduce_n(const RowParams<R>& P, double* fl, double* pw_out, const double* pw,
+                                      int check_done, cudaStream_t st) {
+  size_t sm = x_smem<R, N>();
+  cudaError_t e = cudaFuncSetAttribute(k_rowreduce<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_rowreduce<R, N><<<P.nrows, N / 16, sm, st>>>(P, fl, pw_out, pw, check_done);
+  return cudaGetLastError();
+}
+template <typename R>
+cudaError_t launch_rowreduce(const RowParams<R>& P, int n, double* fl, double* pw_out, const double* pw,
+                             int check_done, cudaStream_t st) {
+  switch (n) {
+    case 512: return launch_rowreduce_n<R, 512>(P, fl, pw_out, pw, check_done, st);
+    case 1024: return launch_rowreduce_n<R, 1024>(P, fl, pw_out, pw, check_done, st);
+    case 2048: return launch_rowreduce_n<R, 2048>(P, fl, pw_out, pw, check_done, st);
+    case 4096: return launch_rowreduce_n<R, 4096>(P, fl, pw_out, pw, check_done, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename R, int N>
+static cudaError_t launch_field_in_n(const typename C2T<R>::type* E, typename C2T<R>::type* S, int ld,
+                                     const typename C2T<R>::type* tw, int analytic, int nrows, cudaStream_t st) {
+  size_t sm = x_smem<R, N>();
+  cudaError_t e = cudaFuncSetAttribute(k_field_in<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_field_in<R, N><<<nrows, N / 16, sm, st>>>(E, S, ld, tw, analytic);
+  return cudaGetLastError();
+}
+template <typename R>
+cudaError_t launch_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S, int ld,
+                            const typename C2T<R>::type* tw, int analytic, int nrows, int n, cudaStream_t st) {
+  switch (n) {
+    case 512: return launch_field_in_n<R, 512>(E, S, ld, tw, analytic, nrows, st);
+    case 1024: return launch_field_in_n<R, 1024>(E, S, ld, tw, analytic, nrows, st);
+    case 2048: return launch_field_in_n<R, 2048>(E, S, ld, tw, analytic, nrows, st);
+    case 4096: return launch_field_in_n<R, 4096>(E, S, ld, tw, analytic, nrows, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename R, int N>
+static cudaError_t launch_field_out_n(const RowParams<R>& P, typename C2T<R>::type* E, cudaStream_t st) {
+  size_t sm = x_smem<R, N>();
+  cudaError_t e = cudaFuncSetAttribute(k_field_out<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_field_out<R, N><<<P.nrows, N / 16, sm, st>>>(P, E);
+  return cudaGetLastError();
+}
+template <typename R>
+cudaError_t launch_field_out(const RowParams<R>& P, int n, typename C2T<R>::type* E, cudaStream_t st) {
+  switch (n) {
+    case 512: return launch_field_out_n<R, 512>(P, E, st);
+    case 1024: return launch_field_out_n<R, 1024>(P, E, st);
+    case 2048: return launch_field_out_n<R, 2048>(P, E, st);
+    case 4096: return launch_field_out_n<R, 4096>(P, E, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename R>
+cudaError_t launch_dht_simt(const R* A, const R* B, R* C, int M, int N, int K, const PropParams<R>& pp,
+                            DevCtl* ctl, int epi, cudaStream_t st) {
+  dim3 grid(N / 128, M / 128);
+  if (epi == 1) k_dht_simt<R, 1><<<grid, 256, 0, st>>>(A, B, C, M, N, K, pp, ctl);
+  else k_dht_simt<R, 2><<<grid, 256, 0, st>>>(A, B, C, M, N, K, pp, ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_control(DevCtl* c, const double* fl, const double* w, int nrows, cudaStream_t st) {
+  k_control<<<1, 256, 0, st>>>(c, fl, w, nrows);
+  return cudaGetLastError();
+}
+cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st) {
+  k_setdz<<<1, 1, 0, st>>>(c, z, dz);
+  return cudaGetLastError();
+}
+
+#define INST(R)                                                                                          \
+  template cudaError_t launch_rowstep<R>(const RowParams<R>&, int, int, int, cudaStream_t);            \
+  template cudaError_t launch_rowreduce<R>(const RowParams<R>&, int, double*, double*, const double*,  \
+                                           int, cudaStream_t);                                           \
+  template cudaError_t launch_field_in<R>(const C2T<R>::type*, C2T<R>::type*, int, const C2T<R>::type*, \
+                                          int, int, int, cudaStream_t);                                  \
+  template cudaError_t launch_field_out<R>(const RowParams<R>&, int, C2T<R>::type*, cudaStream_t);      \
+  template cudaError_t launch_dht_simt<R>(const R*, const R*, R*, int, int, int, const PropParams<R>&,  \
+                                          DevCtl*, int, cudaStream_t);
+INST(float)
+INST(double)

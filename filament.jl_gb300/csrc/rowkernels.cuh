@@ -1,0 +1,445 @@
+// rowkernels.cuh -- kernels that own one transverse point (one time row) per
+// thread block: the fused z-step row kernel, the reduction kernel, field
+// in/out conversions.  Included once by rowkernels.cu.
+//
+// Data layout in HBM: the field lives in the frequency domain as the
+// analytic half spectrum S[p][k], p = transverse point (Nr for RT, Nx*Ny for
+// XYT), k = 0 .. Nt/2-1 (FFTW order, non-negative frequencies), contiguous in
+// k.  The time-domain field E(t) = guard * fft(S, zero-padded) exists only in
+// shared memory.
+#pragma once
+#include "common.cuh"
+#include "fft.cuh"
+#include "plasma.cuh"
+
+// Device control block: written by the controller kernel, read by the step
+// kernels (fil_run) or set by the host (fil_step).
+struct DevCtl {
+  double z, dz, zmax;
+  long long steps, nmax, run_steps;
+  int done, status, flags, guard_pending, first, clamp_last, nonlinearity, pad0;
+  unsigned long long imax_acc, rhomax_acc;  // bit patterns of non-negative doubles
+  double imax, rhomax, energy;
+  double dz0, phimax, phik, phip, istop;
+};
+
+#define FIL_FLAG_NAN 1
+#define FIL_FLAG_ISTOP 2
+#define FIL_FLAG_NEWTON 4
+
+template <typename R> struct RowParams {
+  typedef typename C2T<R>::type C;
+  int nrows, n2, geom, ld;
+  const C* tw;                  // twiddles exp(-2 pi i m/N), m < N
+  const R* g1;                  // field guard per transverse point (n1) or x
+  const R* g2;                  // y guard (XYT) or NULL
+  const R* gt;                  // t guard [N]
+  int gt_bug;                   // XYT: t guard indexed by iy (Guards.jl:314)
+  R dt;
+  // nonlinear step
+  int nonlin, has_cubic, has_free, has_losses, cubic_thg, losses_ereal;
+  const C* Cc;                  // i QZ Rnl_cubic * (k ? 2 : 1), [nh]
+  const C* Cf;
+  const C* Cl;
+  int ns;                       // RK stages
+  double A0[4], A1[4], B[4];    // stage input U_s = S0 + dz (A0 k1 + A1 kprev)
+  // plasma
+  int plasma;
+  PlasmaParams pp;
+  R* rho_g;                     // optional full rho / Kdrho rows
+  R* kdrho_g;
+  int store_plasma;
+  double* rho_end;              // rho(t_end) per row
+  // state
+  const C* S_in;
+  C* S_out;
+  DevCtl* ctl;
+};
+
+template <typename R> FIL_DEV R row_guard(const RowParams<R>& P, int row, int* iy) {
+  if (P.g2) {
+    int ix = row / P.n2;
+    *iy = row - ix * P.n2;
+    return P.g1[ix] * P.g2[*iy];
+  }
+  *iy = 0;
+  return P.g1[row];
+}
+
+// ---------------------------------------------------------------------------
+// Load S_in[row] into X (zero upper half), fft to time, apply the pending
+// field guard.  Afterwards X holds E(t).
+template <typename R, int N>
+FIL_DEV void load_time_row(const RowParams<R>& P, typename C2T<R>::type* X, int row, bool guard) {
+  typedef typename C2T<R>::type C;
+  constexpr int T = N / 16, NH = N / 2, EW = NH / T;
+  const int tid = threadIdx.x;
+  const C* src = P.S_in + (size_t)row * P.ld;
+#pragma unroll
+  for (int m = 0; m < EW; ++m) {
+    int k = tid + m * T;
+    X[pad16(k)] = src[k];
+    X[pad16(k + NH)] = mk<R>(0, 0);
+  }
+  filfft::block_fft<C, N, -1>(X, P.tw);
+  if (guard) {
+    int iy;
+    R gs = row_guard(P, row, &iy);
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      int j = tid + m * T;
+      R g = gs * P.gt[P.gt_bug ? iy : j];
+      X[pad16(j)] = g * X[pad16(j)];
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plasma solve on the row in X.  Writes rho[] and kdrho[] (shared), Y is
+// scratch (>= FIL_MAXCOMP*N reals).  Returns max rho (block-uniform).
+template <typename R, int N, int NC>
+FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typename C2T<R>::type* X,
+                     R* rho, R* kdrho, R* ybuf, Aff<R, NC>* ascratch, R* rscratch, int* newton_flag) {
+  typedef typename C2T<R>::type C;
+  const PlasmaParams& pp = P.pp;
+  const int tid = threadIdx.x;
+  const int j0 = tid * 16;
+  const bool ereal = pp.ereal;
+  R u0[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) u0[c] = (R)pp.rho0;
+
+  auto intens = [&](C e) -> R { return ereal ? e.x * e.x : e.x * e.x + e.y * e.y; };
+  auto rates = [&](R I, R (&W)[NC], R (&S)[NC]) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) W[c] = rate_eval<R>(pp, tabs, c, I, &S[c]);
+  };
+  // gather W, ava at the three stage points of step j; W0 carried in
+  auto point_data = [&](int j, R (&W)[3][NC], R (&ava)[3], R (&S0)[NC], bool need_w0) {
+    C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
+    C em = (R)0.5 * (e0 + e1);
+    R Sd[NC];
+    if (need_w0) rates(intens(e0), W[0], S0);
+    rates(intens(em), W[1], Sd);
+    rates(intens(e1), W[2], Sd);
+    ava[0] = e0.x * e0.x;
+    ava[1] = em.x * em.x;
+    ava[2] = e1.x * e1.x;
+  };
+
+  // ---------------- iteration 0: photoionisation only (exact affine scan)
+  {
+    Aff<R, NC> G = aff_identity<R, NC>();
+    R W[3][NC], ava[3], S0[NC];
+    R uz[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) uz[c] = 0;
+    for (int q = 0; q < 16; ++q) {
+      int j = j0 + q;
+      if (j >= N - 1) break;
+      point_data(j, W, ava, S0, true);
+      Aff<R, NC> M = step_map<R, NC>(pp, uz, W, ava, false);
+      G = aff_compose<R, NC>(M, G);
+    }
+    Aff<R, NC> Pin = aff_block_exclusive_scan<R, NC>(G, ascratch);
+    R u[NC];
+    aff_apply<R, NC>(Pin, u0, u);
+    for (int q = 0; q < 16; ++q) {
+      int j = j0 + q;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) ybuf[c * N + j] = u[c];
+      if (j < N - 1) {
+        point_data(j, W, ava, S0, true);
+        Aff<R, NC> M = step_map<R, NC>(pp, uz, W, ava, false);
+        R un[NC];
+        aff_apply<R, NC>(M, u, un);
+        R kd = 0;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          R K = pp.kdep ? S0[c] : (R)pp.kfix[c];
+          kd += K * W[0][c] * ((R)pp.rho_nt[c] - un[c]);
+          u[c] = un[c];
+        }
+        kdrho[j] = kd;
+      } else {
+        kdrho[j] = 0;   // never written by the reference (plasma_equations.jl:63-70)
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---------------- Newton iterations with avalanche
+  if (pp.avalanche) {
+    int it = 0;
+    for (; it < pp.maxit; ++it) {
+      R W[3][NC], ava[3], S0[NC];
+      Aff<R, NC> G = aff_identity<R, NC>();
+      for (int q = 0; q < 16; ++q) {
+        int j = j0 + q;
+        if (j >= N - 1) break;
+        R ul[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) ul[c] = ybuf[c * N + j];
+        point_data(j, W, ava, S0, true);
+        Aff<R, NC> M = step_map<R, NC>(pp, ul, W, ava, true);
+        G = aff_compose<R, NC>(M, G);
+      }
+      Aff<R, NC> Pin = aff_block_exclusive_scan<R, NC>(G, ascratch);
+      R u[NC];
+      aff_apply<R, NC>(Pin, u0, u);
+      R dmax = 0, umax = 0;
+      for (int q = 0; q < 16; ++q) {
+        int j = j0 + q;
+        R ul[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          ul[c] = ybuf[c * N + j];
+          dmax = max(dmax, fabs(u[c] - ul[c]));
+          umax = max(umax, fabs(u[c]));
+          ybuf[c * N + j] = u[c];
+        }
+        if (j < N - 1) {
+          point_data(j, W, ava, S0, true);
+          Aff<R, NC> M = step_map<R, NC>(pp, ul, W, ava, true);
+          R un[NC];
+          aff_apply<R, NC>(M, u, un);
+#pragma unroll
+          for (int c = 0; c < NC; ++c) u[c] = un[c];
+        }
+      }
+      dmax = block_max<R>(dmax, rscratch);
+      umax = block_max<R>(umax, rscratch);
+      if (dmax <= (R)pp.tol * umax) break;
+    }
+    if (it >= pp.maxit && tid == 0) *newton_flag = 1;
+  }
+  // ---------------- rho = sum of species
+  R rmax = 0;
+  for (int q = 0; q < 16; ++q) {
+    int j = j0 + q;
+    R s = 0;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) s += ybuf[c * N + j];
+    rho[j] = s;
+    rmax = max(rmax, s);
+  }
+  __syncthreads();
+  return block_max<R>(rmax, rscratch);
+}
+
+// ---------------------------------------------------------------------------
+// Fused z-step of one row (blockIdx.x = row):
+//   E(t) = guard * fft(S_in)   (guard from the previous step, Models.jl:116-118)
+//   plasma solve on E(t)       (Models.jl:84-89)
+//   S0 = ifft(E)[0:N/2]        (Models.jl:91-96)
+//   RK step of func!            (Models.jl:98-103, nonlinear_propagators.jl:38-74)
+//   S_out = S0 + dz sum b_s k_s
+// mode 1: plasma only (initialisation), no S_out.
+template <typename R, int N, int NC>
+__global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
+  typedef typename C2T<R>::type C;
+  constexpr int T = N / 16, NH = N / 2, EW = NH / T, NP = N + N / 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* X = reinterpret_cast<C*>(smem_raw);
+  C* Y = X + NP;
+  R* rho = reinterpret_cast<R*>(Y + NP);
+  R* kdrho = rho + N;
+  R* rscratch = kdrho + N;                               // 32
+  Aff<R, (NC > 0 ? NC : 1)>* ascratch = reinterpret_cast<Aff<R, (NC > 0 ? NC : 1)>*>(rscratch + 32);
+  PlasmaSmem<R>* tabs = reinterpret_cast<PlasmaSmem<R>*>(ascratch + 32);
+  __shared__ int s_flag;
+
+  DevCtl* ctl = P.ctl;
+  if (ctl->done) return;
+  const int row = blockIdx.x;
+  const int tid = threadIdx.x;
+  const R dz = (R)ctl->dz;
+  const bool guard = ctl->guard_pending != 0;
+  if (tid == 0) s_flag = 0;
+
+  if constexpr (NC > 0) {
+    if (P.plasma) {
+      for (int i = tid; i < FIL_MAXCOMP * FIL_MAXRATE; i += T) {
+        int c = i / FIL_MAXRATE, q = i % FIL_MAXRATE;
+        tabs->lx[c][q] = (R)P.pp.lx[c][q];
+        tabs->ly[c][q] = (R)P.pp.ly[c][q];
+        tabs->sl[c][q] = (R)P.pp.sl[c][q];
+      }
+    }
+  }
+  load_time_row<R, N>(P, X, row, guard);
+
+  // ---- plasma
+  if constexpr (NC > 0) {
+    if (P.plasma) {
+      R rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag);
+      if (tid == 0) {
+        atomic_max_nonneg(&ctl->rhomax_acc, (double)rmax);
+        P.rho_end[row] = (double)rho[N - 1];
+        if (s_flag) atomicOr(&ctl->flags, FIL_FLAG_NEWTON);
+      }
+      if (P.store_plasma) {
+        for (int m = 0; m < 16; ++m) {
+          int j = tid + m * T;
+          P.rho_g[(size_t)row * N + j] = rho[j];
+          P.kdrho_g[(size_t)row * N + j] = kdrho[j];
+        }
+      }
+    }
+  }
+  if (mode == 1) return;
+
+  // ---- t -> w, keep the analytic half
+  filfft::block_fft<C, N, +1>(X, P.tw);
+  const R invN = (R)1 / (R)N;
+  C S0[EW], k1[EW], kp[EW], acc[EW];
+#pragma unroll
+  for (int m = 0; m < EW; ++m) {
+    int k = tid + m * T;
+    S0[m] = invN * X[pad16(k)];
+    acc[m] = mk<R>(0, 0);
+  }
+  if (P.nonlin) {
+    int iy;
+    const R gs = row_guard(P, row, &iy);
+    for (int s = 0; s < P.ns; ++s) {
+      const R a0 = (R)P.A0[s], a1 = (R)P.A1[s];
+      __syncthreads();   // X and Y free
+#pragma unroll
+      for (int m = 0; m < EW; ++m) {
+        int k = tid + m * T;
+        C u = S0[m];
+        if (s > 0) u = u + (dz * a0) * k1[m] + (dz * a1) * kp[m];
+        X[pad16(k)] = u;
+        X[pad16(k + NH)] = mk<R>(0, 0);
+      }
+      filfft::block_fft<C, N, -1>(X, P.tw);            // inverse_transform_time!
+      // responses in the time domain (medium_responses/*.jl), field filter
+#pragma unroll 4
+      for (int m = 0; m < 16; ++m) {
+        int j = tid + m * T;
+        C e = X[pad16(j)];
+        R re = e.x;
+        R I = e.x * e.x + e.y * e.y;
+        R g = gs * P.gt[P.gt_bug ? iy : j];
+        R fc = 0, ff = 0, fl = 0;
+        if (P.has_cubic) fc = P.cubic_thg ? re * re * re : (R)0.75 * I * re;
+        if (NC > 0 && P.has_free) ff = rho[j] * re;
+        if (NC > 0 && P.has_losses) {
+          R Il = P.losses_ereal ? re * re : I;
+          R inv = (Il >= (R)1e-30) ? (R)1 / Il : (R)0;
+          fl = kdrho[j] * inv * re;
+        }
+        X[pad16(j)] = mk<R>(g * fc, g * ff);
+        Y[pad16(j)] = mk<R>(g * fl, 0);
+      }
+      filfft::block_fft<C, N, +1>(X, P.tw);            // rsig2aspec! (two packed)
+      if (P.has_losses) filfft::block_fft<C, N, +1>(Y, P.tw);
+#pragma unroll
+      for (int m = 0; m < EW; ++m) {
+        int k = tid + m * T;
+        C z = X[pad16(k)];
+        C zm = cconj(X[pad16((N - k) & (N - 1))]);
+        // F_c = (z + conj(z_-k))/2, F_f = (z - conj(z_-k))/(2i), both /N
+        C fc = ((R)0.5 * invN) * (z + zm);
+        C dff = z - zm;
+        C ffr = mk<R>(dff.y * (R)0.5 * invN, -dff.x * (R)0.5 * invN);
+        C d = cmul(__ldg(&P.Cc[k]), fc);
+        if (NC > 0 && P.has_free) d = d + cmul(__ldg(&P.Cf[k]), ffr);
+        if (NC > 0 && P.has_losses) d = d + cmul(__ldg(&P.Cl[k]), invN * Y[pad16(k)]);
+        if (s == 0) k1[m] = d;
+        kp[m] = d;
+        acc[m] = acc[m] + (R)P.B[s] * d;
+      }
+    }
+  }
+  C* dst = P.S_out + (size_t)row * P.ld;
+#pragma unroll
+  for (int m = 0; m < EW; ++m) {
+    int k = tid + m * T;
+    dst[k] = S0[m] + dz * acc[m];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Reductions over the current field (FieldAnalyzers.jl:166-215): Imax,
+// fluence per row F = sum_t |E|^2 dt (FP64), optional power per t
+// P[t] += w_row |E|^2.  Flags non-finite values.
+template <typename R, int N>
+__global__ void __launch_bounds__(N / 16) k_rowreduce(RowParams<R> P, double* fluence, double* power,
+                                                      const double* pw, int check_done) {
+  typedef typename C2T<R>::type C;
+  constexpr int T = N / 16, NP = N + N / 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* X = reinterpret_cast<C*>(smem_raw);
+  double* dscratch = reinterpret_cast<double*>(X + NP);
+  DevCtl* ctl = P.ctl;
+  if (check_done && ctl->done) return;
+  const int row = blockIdx.x, tid = threadIdx.x;
+  load_time_row<R, N>(P, X, row, ctl->guard_pending != 0);
+  double s = 0;
+  R mx = 0;
+  const double w = power ? pw[row] : 0.0;
+#pragma unroll 4
+  for (int m = 0; m < 16; ++m) {
+    int j = tid + m * T;
+    C e = X[pad16(j)];
+    R I = e.x * e.x + e.y * e.y;
+    s += (double)I;
+    mx = max(mx, I);
+    if (power) atomicAdd(&power[j], w * (double)I);
+  }
+  double tot = block_sum<double>(s, dscratch);
+  double bm = block_max<double>((double)mx, dscratch);
+  if (tid == 0) {
+    fluence[row] = tot * (double)P.dt;
+    if (!isfinite(tot)) atomicOr(&ctl->flags, FIL_FLAG_NAN);
+    else atomic_max_nonneg(&ctl->imax_acc, bm);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Field in: rows of E(t) (R complex, row-major) -> S = c_k ifft(E)[k], k < N/2
+// with c_0 = 1, c_k = 2 (rsig2asig!, Fields.jl:115) or c_k = 1 (analytic).
+template <typename R, int N>
+__global__ void __launch_bounds__(N / 16) k_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S,
+                                                     int ld, const typename C2T<R>::type* tw, int analytic) {
+  typedef typename C2T<R>::type C;
+  constexpr int T = N / 16, NH = N / 2, EW = NH / T, NP = N + N / 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* X = reinterpret_cast<C*>(smem_raw);
+  (void)NP;
+  const int row = blockIdx.x, tid = threadIdx.x;
+  const C* src = E + (size_t)row * N;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) {
+    int j = tid + m * T;
+    X[pad16(j)] = src[j];
+  }
+  filfft::block_fft<C, N, +1>(X, tw);
+  const R invN = (R)1 / (R)N;
+#pragma unroll
+  for (int m = 0; m < EW; ++m) {
+    int k = tid + m * T;
+    R c = (analytic || k == 0) ? invN : (R)2 * invN;
+    S[(size_t)row * ld + k] = c * X[pad16(k)];
+  }
+}
+
+// Field out: E(t) = guard * fft(S), rows row-major.
+template <typename R, int N>
+__global__ void __launch_bounds__(N / 16) k_field_out(RowParams<R> P, typename C2T<R>::type* E) {
+  typedef typename C2T<R>::type C;
+  constexpr int T = N / 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* X = reinterpret_cast<C*>(smem_raw);
+  const int row = blockIdx.x, tid = threadIdx.x;
+  load_time_row<R, N>(P, X, row, P.ctl->guard_pending != 0);
+  C* dst = E + (size_t)row * N;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) {
+    int j = tid + m * T;
+    dst[j] = X[pad16(j)];
+  }
+}

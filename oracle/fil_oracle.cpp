@@ -1,0 +1,793 @@
+// fil_oracle.cpp -- CPU FP64 restatement of Filament.jl's per-z-step loop.
+//
+// TEST INFRASTRUCTURE ONLY.  This is the checker that the CUDA library is
+// compared against (and the timed CPU baseline); it is never linked into or
+// called by the product.  It exports the C ABI of include/filament_gb.h under
+// the prefix "filo_" and follows the reference literally:
+//
+//   Models.zstep                  src/modules/Models.jl:75-121
+//   t <-> w transforms            src/modules/Models.jl:152-171 (t->w = ifft)
+//   linear propagator             src/modules/linear_propagators/spectral.jl:16-26
+//   KZ                            src/modules/linear_propagators/spectral.jl:78-184
+//   nonlinear RHS func!           src/modules/nonlinear_propagators.jl:38-67
+//   update_dE!                    src/modules/nonlinear_propagators.jl:246-283
+//   responses                     src/modules/medium_responses/cubic.jl:33-54,
+//                                 current_free.jl:31-37, current_losses.jl:36-83,
+//                                 raman.jl:46-111
+//   plasma solve                  src/modules/plasma_equations.jl:1-72
+//   plasma RHS                    src/modules/plasma_equations/photoionization_avalanche.jl:119-205
+//   guards                        src/modules/Guards.jl:199-318
+//   adaptive dz                   src/modules/AdaptiveSteps.jl:91-107
+//   main loop                     src/Filament.jl:123-172
+//   analyzer reductions           src/modules/FieldAnalyzers.jl:120-215, 272-353
+//
+// Choices where the reference relies on un-vendored dependencies:
+//   * QDHT (HankelTransforms): E <- diag(1/s) T D T diag(s) E on the first
+//     half(Nt) = Nt/2 frequency columns (Fields.jl:108-110); the columns
+//     above stay in r-space but still receive the KZ and guard multiply,
+//     exactly as the reference's full-array broadcast (spectral.jl:22).
+//   * Analytic spectrum (AnalyticSignals.rsig2aspec!): ifft, bin 0 kept,
+//     bins 1..Nt/2-1 doubled, bins Nt/2..Nt-1 zeroed.
+//   * RK tableaux (ODEIntegrators): RK2 midpoint, RK3 Kutta, RK4 classic.
+//   * Rates (TabulatedFunctions): log-log linear interpolation, tfpower =
+//     segment slope; linterp = linear interpolation between time samples.
+//   * FFT sizes: powers of two.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../include/filament_gb.h"
+
+typedef std::complex<double> cd;
+
+namespace {
+
+thread_local std::string g_err;
+
+// ------------------------------------------------------------------ FFT --
+struct FFTPlan {
+  int n = 0, logn = 0;
+  std::vector<cd> tw;       // exp(-2 pi i k / n), k < n/2
+  std::vector<int> rev;
+  void init(int n_) {
+    n = n_;
+    logn = 0;
+    while ((1 << logn) < n) ++logn;
+    tw.resize(std::max(1, n / 2));
+    for (int k = 0; k < n / 2; ++k) {
+      double a = -2.0 * M_PI * (double)k / (double)n;
+      tw[k] = cd(std::cos(a), std::sin(a));
+    }
+    rev.resize(n);
+    for (int i = 0; i < n; ++i) {
+      int r = 0;
+      for (int b = 0; b < logn; ++b)
+        if (i & (1 << b)) r |= 1 << (logn - 1 - b);
+      rev[i] = r;
+    }
+  }
+  // sign = -1: fft (unscaled, exp(-i...)), sign = +1: ifft (scaled 1/n).
+  // x is accessed with a stride.
+  void run(cd* x, long stride, int sign, cd* work) const {
+    if (n == 1) return;
+    for (int i = 0; i < n; ++i) work[rev[i]] = x[(long)i * stride];
+    for (int len = 2; len <= n; len <<= 1) {
+      int half = len >> 1, step = n / len;
+      for (int i = 0; i < n; i += len)
+        for (int j = 0; j < half; ++j) {
+          cd w = tw[j * step];
+          if (sign > 0) w = std::conj(w);
+          cd u = work[i + j], v = work[i + j + half] * w;
+          work[i + j] = u + v;
+          work[i + j + half] = u - v;
+        }
+    }
+    double sc = sign > 0 ? 1.0 / n : 1.0;
+    for (int i = 0; i < n; ++i) x[(long)i * stride] = work[i] * sc;
+  }
+};
+
+static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// ----------------------------------------------------------- RK tableaux --
+struct Tableau {
+  int s;
+  double a[4][4];
+  double b[4];
+  double c[4];
+};
+static Tableau tableau(int alg) {
+  Tableau t;
+  std::memset(&t, 0, sizeof t);
+  if (alg == FIL_ALG_RK2) {          // midpoint
+    t.s = 2;
+    t.a[1][0] = 0.5;
+    t.b[0] = 0.0; t.b[1] = 1.0;
+    t.c[1] = 0.5;
+  } else if (alg == FIL_ALG_RK3) {   // Kutta third order
+    t.s = 3;
+    t.a[1][0] = 0.5;
+    t.a[2][0] = -1.0; t.a[2][1] = 2.0;
+    t.b[0] = 1.0 / 6.0; t.b[1] = 4.0 / 6.0; t.b[2] = 1.0 / 6.0;
+    t.c[1] = 0.5; t.c[2] = 1.0;
+  } else {                           // classic RK4
+    t.s = 4;
+    t.a[1][0] = 0.5; t.a[2][1] = 0.5; t.a[3][2] = 1.0;
+    t.b[0] = 1.0 / 6.0; t.b[1] = 1.0 / 3.0; t.b[2] = 1.0 / 3.0; t.b[3] = 1.0 / 6.0;
+    t.c[1] = 0.5; t.c[2] = 0.5; t.c[3] = 1.0;
+  }
+  return t;
+}
+
+static std::vector<double> copyv(const double* p, size_t n, double fill) {
+  std::vector<double> v(n, fill);
+  if (p) std::copy(p, p + n, v.begin());
+  return v;
+}
+static std::vector<cd> copyc(const double* p, size_t n) {
+  std::vector<cd> v(n, cd(0, 0));
+  if (p)
+    for (size_t i = 0; i < n; ++i) v[i] = cd(p[2 * i], p[2 * i + 1]);
+  return v;
+}
+
+}  // namespace
+
+struct fil_handle {
+  fil_config cfg;
+  std::string err;
+  int geom, n1, n2, nt, nh;
+  long ntr;                    // transverse points n1*n2
+  bool has_t, spatial_nl;
+  // tables
+  std::vector<double> kt1, kt2, g1, g2, gt, sg1, sg2, kmax, wg, dht, dht_s, rdr;
+  std::vector<cd> beta, dfr, qz, rnl_c, rnl_f, rnl_l, rnl_r, ramh;
+  std::vector<double> rho_nt, rava, kfix, rlx, rly;
+  Tableau tab_nl, tab_pl;
+  FFTPlan pt, px, py;
+  // state: E in row layout (transverse-major, t fastest): E[p*nt + j]
+  std::vector<cd> E;
+  std::vector<double> rho, kdrho;
+  bool field_set = false;
+  bool bugcompat = false, clamp_last = false;
+  double z = 0, dz_last = 0;
+  long steps = 0;
+  double imax = 0, rhomax = 0;
+  int status = 0;
+};
+
+namespace {
+
+int fail(fil_handle* h, int code, const std::string& m) {
+  if (h) h->err = m; else g_err = m;
+  return code;
+}
+
+// ---------------------------------------------------------- transforms ---
+// t -> w: ifft along t for every transverse point (Models.jl:162-165)
+void t_to_w(fil_handle* h, std::vector<cd>& A) {
+  if (!h->has_t) return;
+#pragma omp parallel
+  {
+    std::vector<cd> work(h->nt);
+#pragma omp for schedule(static)
+    for (long p = 0; p < h->ntr; ++p) h->pt.run(&A[p * h->nt], 1, +1, work.data());
+  }
+}
+// w -> t: fft (Models.jl:168-171)
+void w_to_t(fil_handle* h, std::vector<cd>& A) {
+  if (!h->has_t) return;
+#pragma omp parallel
+  {
+    std::vector<cd> work(h->nt);
+#pragma omp for schedule(static)
+    for (long p = 0; p < h->ntr; ++p) h->pt.run(&A[p * h->nt], 1, -1, work.data());
+  }
+}
+
+// 2-D FFT over (x, y) for every t column; sign -1 = forward (P * E).
+void xy_fft(fil_handle* h, std::vector<cd>& A, int sign) {
+  int nx = h->n1, ny = h->n2, nt = h->nt;
+  // along y (index p = ix*ny + iy): stride nt
+#pragma omp parallel
+  {
+    std::vector<cd> work(std::max(nx, ny));
+#pragma omp for collapse(2) schedule(static)
+    for (int ix = 0; ix < nx; ++ix)
+      for (int j = 0; j < nt; ++j)
+        h->py.run(&A[((long)ix * ny) * nt + j], nt, sign, work.data());
+#pragma omp for collapse(2) schedule(static)
+    for (int iy = 0; iy < ny; ++iy)
+      for (int j = 0; j < nt; ++j)
+        h->px.run(&A[((long)iy) * nt + j], (long)ny * nt, sign, work.data());
+  }
+}
+
+// QDHT propagation on the first ncol frequency columns: C <- T * C, rows.
+void dht_apply(fil_handle* h, std::vector<cd>& A, int ncol, bool scale_in, bool scale_out) {
+  int N = h->n1, nt = h->nt;
+  const int JB = 64;
+  std::vector<cd> out((size_t)N * ncol);
+#pragma omp parallel
+  {
+    std::vector<cd> xin((size_t)N * JB), acc(JB);
+#pragma omp for schedule(dynamic)
+    for (int j0 = 0; j0 < ncol; j0 += JB) {
+      int jn = std::min(JB, ncol - j0);
+      for (int k = 0; k < N; ++k) {
+        double s = scale_in ? h->dht_s[k] : 1.0;
+        for (int jj = 0; jj < jn; ++jj) xin[(size_t)k * JB + jj] = A[(size_t)k * nt + j0 + jj] * s;
+      }
+      for (int i = 0; i < N; ++i) {
+        for (int jj = 0; jj < jn; ++jj) acc[jj] = 0;
+        const double* Ti = &h->dht[(size_t)i * N];
+        for (int k = 0; k < N; ++k) {
+          double t = Ti[k];
+          const cd* xr = &xin[(size_t)k * JB];
+          for (int jj = 0; jj < jn; ++jj) acc[jj] += t * xr[jj];
+        }
+        double so = scale_out ? 1.0 / h->dht_s[i] : 1.0;
+        for (int jj = 0; jj < jn; ++jj) out[(size_t)i * ncol + j0 + jj] = acc[jj] * so;
+      }
+    }
+  }
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < ncol; ++j) A[(size_t)i * nt + j] = out[(size_t)i * ncol + j];
+}
+
+// KZ (spectral.jl:160-184) in zu units from the tables.
+cd kz_value(const fil_handle* h, double kt2, int j) {
+  cd b = h->beta[j];
+  cd frame = h->dfr[j] - b;   // -w/vf*zu
+  cd K;
+  if (h->cfg.kparaxial) {
+    K = (b != cd(0, 0)) ? b - kt2 / (2.0 * b) : cd(0, 0);
+  } else {
+    // sqrt(beta^2 - kt^2 + 0im): adding complex zero turns a -0.0 imaginary
+    // part into +0.0, which selects the decaying branch for kt > beta.
+    K = std::sqrt(b * b - kt2 + cd(0.0, 0.0));
+  }
+  return K + frame;
+}
+
+double kguard_value(const fil_handle* h, double kt2, int j) {
+  if (h->kmax.empty()) return 1.0;
+  double km = h->kmax[j];
+  if (km == 0.0) return 0.0;
+  double q = kt2 / (km * km);
+  return std::exp(-std::pow(q, 20));
+}
+
+// spectral.jl:16-26: forward transverse transform, E *= exp(i KZ dz),
+// spectral guard, inverse transform.  A is in the w-domain (t geometries).
+void linear_step(fil_handle* h, std::vector<cd>& A, double dz) {
+  int nt = h->nt;
+  if (h->geom == FIL_GEOM_R || h->geom == FIL_GEOM_RT) {
+    int ncol = h->geom == FIL_GEOM_RT ? h->nh : 1;
+    if (h->n1 > 1) dht_apply(h, A, ncol, true, false);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < h->n1; ++i) {
+      double k2 = h->kt1[i] * h->kt1[i];
+      for (int j = 0; j < nt; ++j) {
+        cd kz = kz_value(h, k2, j);
+        double g = kguard_value(h, k2, j) * (h->wg.empty() ? 1.0 : h->wg[j]);
+        A[(size_t)i * nt + j] *= std::exp(cd(0, 1) * kz * dz) * g;
+      }
+    }
+    if (h->n1 > 1) dht_apply(h, A, ncol, false, true);
+  } else if (h->geom == FIL_GEOM_T) {
+    for (int j = 0; j < nt; ++j) {
+      cd kz = kz_value(h, 0.0, j);
+      A[j] *= std::exp(cd(0, 1) * kz * dz) * (h->wg.empty() ? 1.0 : h->wg[j]);
+    }
+  } else {  // XY, XYT
+    xy_fft(h, A, -1);
+    int nx = h->n1, ny = h->n2;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int ix = 0; ix < nx; ++ix)
+      for (int iy = 0; iy < ny; ++iy) {
+        double k2 = h->kt1[ix] * h->kt1[ix] + h->kt2[iy] * h->kt2[iy];
+        double sg = h->sg1[ix] * h->sg2[iy];
+        size_t base = ((size_t)ix * ny + iy) * nt;
+        for (int j = 0; j < nt; ++j) {
+          cd kz = kz_value(h, k2, j);
+          int jw = (h->bugcompat && h->geom == FIL_GEOM_XYT) ? iy : j;  // Guards.jl:314
+          double g = sg * (h->wg.empty() ? 1.0 : h->wg[jw]);
+          A[base + j] *= std::exp(cd(0, 1) * kz * dz) * g;
+        }
+      }
+    xy_fft(h, A, +1);
+  }
+}
+
+// field guard (Guards.jl:199-229, 265-318), in the time/space domain
+void field_guard(fil_handle* h, std::vector<cd>& A) {
+  int nt = h->nt;
+#pragma omp parallel for schedule(static)
+  for (long p = 0; p < h->ntr; ++p) {
+    double gs;
+    int iy = 0;
+    if (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_XYT) {
+      int ix = (int)(p / h->n2);
+      iy = (int)(p % h->n2);
+      gs = h->g1[ix] * h->g2[iy];
+    } else {
+      gs = h->g1[p];
+    }
+    for (int j = 0; j < nt; ++j) {
+      double g = gs;
+      if (h->has_t) {
+        int jt = (h->bugcompat && h->geom == FIL_GEOM_XYT) ? iy : j;
+        g *= h->gt[jt];
+      }
+      A[(size_t)p * nt + j] *= g;
+    }
+  }
+}
+
+// ------------------------------------------------------ tabulated rates --
+struct Rate {
+  const double* lx;
+  const double* ly;
+  int n;
+  int seg(double l) const {
+    int i = (int)(std::upper_bound(lx, lx + n, l) - lx) - 1;
+    return std::min(std::max(i, 0), n - 2);
+  }
+  double operator()(double x) const {
+    if (x <= 0) return 0.0;
+    double l = std::log(x);
+    int i = seg(l);
+    double s = (ly[i + 1] - ly[i]) / (lx[i + 1] - lx[i]);
+    return std::exp(ly[i] + (l - lx[i]) * s);
+  }
+  double power(double x) const {
+    double l = x > 0 ? std::log(x) : -HUGE_VAL;
+    int i = seg(l);
+    return (ly[i + 1] - ly[i]) / (lx[i + 1] - lx[i]);
+  }
+};
+
+// plasma_equations.jl:46-72 for one transverse point
+void plasma_row(fil_handle* h, const cd* Er, double* rho, double* kdrho) {
+  const int nc = h->cfg.plasma_ncomp, nt = h->nt;
+  const bool ereal = h->cfg.plasma_ereal, kdep = h->cfg.plasma_kdep;
+  const Tableau& T = h->tab_pl;
+  const double dt = h->cfg.dt;
+  Rate rates[4];
+  for (int c = 0; c < nc; ++c)
+    rates[c] = Rate{&h->rlx[(size_t)c * h->cfg.rate_n], &h->rly[(size_t)c * h->cfg.rate_n], h->cfg.rate_n};
+  double u[4], up[4];
+  for (int c = 0; c < nc; ++c) u[c] = up[c] = h->cfg.rho0;
+  auto sum = [&](const double* v) { double s = 0; for (int c = 0; c < nc; ++c) s += v[c]; return s; };
+  rho[0] = sum(u);
+  auto field_at = [&](int j, double frac) {   // TabulatedFunctions.linterp
+    if (frac == 0.0) return Er[j];
+    int j1 = std::min(j + 1, nt - 1);
+    return Er[j] + frac * (Er[j1] - Er[j]);
+  };
+  for (int j = 0; j < nt - 1; ++j) {
+    // --- full equation (photoionization_avalanche.jl:119-147)
+    double k[4][4], U[4];
+    for (int s = 0; s < T.s; ++s) {
+      for (int c = 0; c < nc; ++c) {
+        U[c] = u[c];
+        for (int l = 0; l < s; ++l) U[c] += dt * T.a[s][l] * k[l][c];
+      }
+      cd E = field_at(j, T.c[s]);
+      double I = ereal ? E.real() * E.real() : std::norm(E);
+      double E2 = E.real() * E.real();
+      double S = sum(U);
+      for (int c = 0; c < nc; ++c) {
+        double R1 = rates[c](I);
+        double R2 = h->rava[c] * E2;
+        double fr = h->rho_nt[c];
+        k[s][c] = R1 * (fr - U[c]) + R2 * (fr - U[c]) / fr * S;
+      }
+    }
+    for (int c = 0; c < nc; ++c)
+      for (int s = 0; s < T.s; ++s) u[c] += dt * T.b[s] * k[s][c];
+    rho[j + 1] = sum(u);
+    // --- photoionisation only (photoionization_avalanche.jl:150-173)
+    for (int s = 0; s < T.s; ++s) {
+      for (int c = 0; c < nc; ++c) {
+        U[c] = up[c];
+        for (int l = 0; l < s; ++l) U[c] += dt * T.a[s][l] * k[l][c];
+      }
+      cd E = field_at(j, T.c[s]);
+      double I = ereal ? E.real() * E.real() : std::norm(E);
+      for (int c = 0; c < nc; ++c) k[s][c] = rates[c](I) * (h->rho_nt[c] - U[c]);
+    }
+    for (int c = 0; c < nc; ++c)
+      for (int s = 0; s < T.s; ++s) up[c] += dt * T.b[s] * k[s][c];
+    // --- kdrho_func (photoionization_avalanche.jl:176-205) at t[j]
+    cd E = Er[j];
+    double I = ereal ? E.real() * E.real() : std::norm(E);
+    double kd = 0;
+    for (int c = 0; c < nc; ++c) {
+      double R1 = rates[c](I);
+      double K = kdep ? rates[c].power(I) : h->kfix[c];
+      kd += K * R1 * (h->rho_nt[c] - up[c]);
+    }
+    kdrho[j] = kd;
+  }
+  // kdrho[nt-1] is never written by the reference and stays zero
+}
+
+void plasma_solve(fil_handle* h) {
+#pragma omp parallel for schedule(dynamic, 4)
+  for (long p = 0; p < h->ntr; ++p)
+    plasma_row(h, &h->E[(size_t)p * h->nt], &h->rho[(size_t)p * h->nt], &h->kdrho[(size_t)p * h->nt]);
+  double m = 0;
+  for (double v : h->rho) m = std::max(m, v);
+  h->rhomax = m;
+}
+
+// ---------------------------------------------------------- func! -------
+// dE = i QZ sum_resp Rnl(w) aspec(guard * calc(E)).  U is in the w-domain
+// (t geometries) or space domain (R, XY).
+void nl_rhs(fil_handle* h, const std::vector<cd>& U, std::vector<cd>& dE) {
+  const int nt = h->nt, nh = h->nh;
+  std::vector<cd> Et = U;
+  w_to_t(h, Et);                                  // inverse_transform_time!
+  std::fill(dE.begin(), dE.end(), cd(0, 0));
+  const unsigned mask = h->cfg.resp_mask;
+  int chans[4] = {(int)FIL_RESP_CUBIC, (int)FIL_RESP_RAMAN, (int)FIL_RESP_FREE, (int)FIL_RESP_LOSSES};
+#pragma omp parallel
+  {
+    std::vector<cd> F(nt), work(nt);
+#pragma omp for schedule(static)
+    for (long p = 0; p < h->ntr; ++p) {
+      const cd* Er = &Et[(size_t)p * nt];
+      cd* dr = &dE[(size_t)p * nt];
+      double gs;
+      int iy = 0;
+      if (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_XYT) {
+        iy = (int)(p % h->n2);
+        gs = h->g1[p / h->n2] * h->g2[iy];
+      } else {
+        gs = h->g1[p];
+      }
+      for (int ch : chans) {
+        if (!(mask & (unsigned)ch)) continue;
+        const std::vector<cd>* R = nullptr;
+        for (int j = 0; j < nt; ++j) {
+          cd E = Er[j];
+          double re = E.real();
+          cd f;
+          if (ch == FIL_RESP_CUBIC) {
+            if (h->spatial_nl) f = 0.75 * std::norm(E) * E;              // cubic.jl:49-54
+            else if (h->cfg.cubic_thg) f = re * re * re;                 // cubic.jl:33-38
+            else f = 0.75 * std::norm(E) * re;                           // cubic.jl:41-46
+          } else if (ch == FIL_RESP_FREE) {
+            f = h->rho[(size_t)p * nt + j] * re;                         // current_free.jl:31-37
+          } else if (ch == FIL_RESP_LOSSES) {
+            double I = h->cfg.losses_ereal ? re * re : std::norm(E);    // current_losses.jl:36-44
+            double inv = (I >= 1e-30) ? 1.0 / I : 0.0;
+            f = h->kdrho[(size_t)p * nt + j] * inv * re;
+          } else {  // raman: x = Re(E)^2 or 3/4|E|^2, filled below
+            f = h->cfg.raman_thg ? re * re : 0.75 * std::norm(E);
+          }
+          F[j] = f;
+        }
+        if (ch == FIL_RESP_RAMAN) {                                      // raman.jl:80-98
+          h->pt.run(F.data(), 1, +1, work.data());
+          for (int j = 0; j < nt; ++j) F[j] *= h->ramh[j];
+          h->pt.run(F.data(), 1, -1, work.data());
+          for (int j = 0; j < nt; ++j) F[j] *= Er[j].real();
+        }
+        // field filter (nonlinear_propagators.jl:51)
+        for (int j = 0; j < nt; ++j) {
+          double g = gs;
+          if (h->has_t) {
+            int jt = (h->bugcompat && h->geom == FIL_GEOM_XYT) ? iy : j;
+            g *= h->gt[jt];
+          }
+          F[j] *= g;
+        }
+        if (h->has_t) {                                                   // rsig2aspec!
+          h->pt.run(F.data(), 1, +1, work.data());
+          for (int j = 1; j < nh; ++j) F[j] *= 2.0;
+          for (int j = nh; j < nt; ++j) F[j] = 0.0;
+        }
+        if (ch == FIL_RESP_CUBIC) R = &h->rnl_c;
+        else if (ch == FIL_RESP_FREE) R = &h->rnl_f;
+        else if (ch == FIL_RESP_LOSSES) R = &h->rnl_l;
+        else R = &h->rnl_r;
+        for (int j = 0; j < nt; ++j) dr[j] += (*R)[j] * F[j];          // update_dE!
+      }
+      for (int j = 0; j < nt; ++j) dr[j] = cd(0, 1) * h->qz[j] * dr[j];  // QPARAXIAL
+    }
+  }
+}
+
+void nl_step(fil_handle* h, std::vector<cd>& u, double dz) {
+  const Tableau& T = h->tab_nl;
+  size_t n = u.size();
+  std::vector<std::vector<cd>> k(T.s, std::vector<cd>(n));
+  std::vector<cd> U(n);
+  for (int s = 0; s < T.s; ++s) {
+    for (size_t i = 0; i < n; ++i) {
+      cd v = u[i];
+      for (int l = 0; l < s; ++l)
+        if (T.a[s][l] != 0.0) v += dz * T.a[s][l] * k[l][i];
+      U[i] = v;
+    }
+    nl_rhs(h, U, k[s]);
+  }
+  for (size_t i = 0; i < n; ++i) {
+    cd v = 0;
+    for (int s = 0; s < T.s; ++s)
+      if (T.b[s] != 0.0) v += T.b[s] * k[s][i];
+    u[i] += dz * v;
+  }
+}
+
+void zstep(fil_handle* h, double dz) {
+  if (h->cfg.plasma) plasma_solve(h);      // Models.jl:84-89
+  t_to_w(h, h->E);                         // Models.jl:91-96
+  if (h->cfg.nonlinearity) nl_step(h, h->E, dz);  // Models.jl:98-103
+  linear_step(h, h->E, dz);                // Models.jl:105-108
+  w_to_t(h, h->E);                         // Models.jl:110-114
+  field_guard(h, h->E);                    // Models.jl:116-119
+}
+
+double current_imax(const fil_handle* h) {
+  double m = 0;
+  for (const cd& e : h->E) m = std::max(m, std::norm(e));
+  return m;
+}
+
+}  // namespace
+
+// =================================================================== ABI ==
+extern "C" {
+
+int filo_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power, double* rho_end);
+int filo_get_stats(fil_handle* h, fil_stats* st);
+
+const char* filo_last_error(const fil_handle* h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+int filo_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
+  if (!cfg || !t || !out) return fail(nullptr, FIL_ERR_ARG, "null argument");
+  if (cfg->abi_version != FIL_ABI_VERSION) return fail(nullptr, FIL_ERR_ARG, "ABI version mismatch");
+  fil_handle* h = new fil_handle();
+  h->cfg = *cfg;
+  h->geom = cfg->geometry;
+  h->n1 = cfg->n1; h->n2 = cfg->n2; h->nt = cfg->nt;
+  h->ntr = (long)h->n1 * h->n2;
+  h->has_t = (h->geom == FIL_GEOM_T || h->geom == FIL_GEOM_RT || h->geom == FIL_GEOM_XYT);
+  h->spatial_nl = (h->geom == FIL_GEOM_R || h->geom == FIL_GEOM_XY);
+  h->nh = h->has_t ? h->nt / 2 : 1;
+  if (h->has_t && !is_pow2(h->nt)) { delete h; return fail(nullptr, FIL_ERR_UNSUPPORTED, "nt must be a power of two"); }
+  if ((h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_XYT) && (!is_pow2(h->n1) || !is_pow2(h->n2))) {
+    delete h; return fail(nullptr, FIL_ERR_UNSUPPORTED, "nx, ny must be powers of two");
+  }
+  if (cfg->nonlinearity && !cfg->qparaxial) { delete h; return fail(nullptr, FIL_ERR_UNSUPPORTED, "QPARAXIAL=false"); }
+  int n1 = h->n1, n2 = h->n2, nt = h->nt;
+  h->kt1 = copyv(t->kt1, n1, 0.0);
+  h->kt2 = copyv(t->kt2, n2, 0.0);
+  h->g1 = copyv(t->guard1, n1, 1.0);
+  h->g2 = copyv(t->guard2, n2, 1.0);
+  h->gt = copyv(t->guardt, nt, 1.0);
+  h->sg1 = copyv(t->sguard1, n1, 1.0);
+  h->sg2 = copyv(t->sguard2, n2, 1.0);
+  if (t->kmax) h->kmax = copyv(t->kmax, nt, 0.0);
+  if (t->wguard) h->wg = copyv(t->wguard, nt, 1.0);
+  h->beta = copyc(t->beta, nt);
+  h->dfr = copyc(t->dfr, nt);
+  h->qz = copyc(t->qz, nt);
+  h->rnl_c = copyc(t->rnl_cubic, nt);
+  h->rnl_f = copyc(t->rnl_free, nt);
+  h->rnl_l = copyc(t->rnl_losses, nt);
+  h->rnl_r = copyc(t->rnl_raman, nt);
+  h->ramh = copyc(t->raman_h, nt);
+  if (h->geom == FIL_GEOM_R || h->geom == FIL_GEOM_RT) {
+    if (!t->dht || !t->dht_s) { delete h; return fail(nullptr, FIL_ERR_ARG, "missing DHT tables"); }
+    h->dht = copyv(t->dht, (size_t)n1 * n1, 0.0);
+    h->dht_s = copyv(t->dht_s, n1, 1.0);
+  }
+  h->rdr = copyv(t->rdr, n1, 0.0);
+  if (cfg->plasma) {
+    int nc = cfg->plasma_ncomp;
+    if (nc < 1 || nc > 4 || cfg->rate_n < 2) { delete h; return fail(nullptr, FIL_ERR_ARG, "bad plasma config"); }
+    h->rho_nt = copyv(t->rho_nt, nc, 0.0);
+    h->rava = copyv(t->rava, nc, 0.0);
+    h->kfix = copyv(t->kfix, nc, 0.0);
+    h->rlx = copyv(t->rate_lx, (size_t)nc * cfg->rate_n, 0.0);
+    h->rly = copyv(t->rate_ly, (size_t)nc * cfg->rate_n, 0.0);
+    h->tab_pl = tableau(cfg->plasma_alg);
+  }
+  h->tab_nl = tableau(cfg->alg);
+  if (h->has_t) h->pt.init(nt);
+  if (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_XYT) { h->px.init(n1); h->py.init(n2); }
+  h->E.assign((size_t)h->ntr * nt, cd(0, 0));
+  h->rho.assign((size_t)h->ntr * nt, 0.0);
+  h->kdrho.assign((size_t)h->ntr * nt, 0.0);
+  *out = h;
+  return FIL_OK;
+}
+
+int filo_destroy(fil_handle* h) { delete h; return FIL_OK; }
+
+int filo_set_option(fil_handle* h, int opt, int64_t v) {
+  if (!h) return fail(nullptr, FIL_ERR_ARG, "null handle");
+  if (opt == FIL_OPT_XYT_GUARD_BUGCOMPAT) h->bugcompat = v != 0;
+  else if (opt == FIL_OPT_CLAMP_LAST_DZ) h->clamp_last = v != 0;
+  return FIL_OK;
+}
+
+static void layout_in(const fil_handle* h, const void* src, int dtype, int layout, std::vector<cd>& dst) {
+  long ntr = h->ntr, nt = h->nt;
+  for (long p = 0; p < ntr; ++p)
+    for (long j = 0; j < nt; ++j) {
+      long s = layout == FIL_LAYOUT_ROWMAJOR ? p * nt + j : j * ntr + (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_XYT ? ((p % h->n2) * h->n1 + p / h->n2) : p);
+      cd v;
+      if (dtype == FIL_DTYPE_C128) v = cd(((const double*)src)[2 * s], ((const double*)src)[2 * s + 1]);
+      else v = cd(((const float*)src)[2 * s], ((const float*)src)[2 * s + 1]);
+      dst[p * nt + j] = v;
+    }
+}
+
+int filo_set_field(fil_handle* h, const void* E, int dtype, int layout, int analytic) {
+  if (!h || !E) return fail(h, FIL_ERR_ARG, "null argument");
+  layout_in(h, E, dtype, layout, h->E);
+  if (h->has_t && !analytic) {             // AnalyticSignals.rsig2asig!
+    t_to_w(h, h->E);
+    for (long p = 0; p < h->ntr; ++p) {
+      cd* r = &h->E[(size_t)p * h->nt];
+      for (int j = 1; j < h->nh; ++j) r[j] *= 2.0;
+      for (int j = h->nh; j < h->nt; ++j) r[j] = 0.0;
+    }
+    w_to_t(h, h->E);
+  }
+  std::fill(h->rho.begin(), h->rho.end(), 0.0);
+  std::fill(h->kdrho.begin(), h->kdrho.end(), 0.0);
+  h->rhomax = 0;
+  if (h->cfg.plasma) plasma_solve(h);       // Models.jl:66
+  h->field_set = true;
+  h->imax = current_imax(h);
+  h->steps = 0;
+  return FIL_OK;
+}
+
+int filo_get_field(fil_handle* h, void* out, int dtype, int layout) {
+  if (!h || !out) return fail(h, FIL_ERR_ARG, "null argument");
+  long ntr = h->ntr, nt = h->nt;
+  for (long p = 0; p < ntr; ++p)
+    for (long j = 0; j < nt; ++j) {
+      long s = layout == FIL_LAYOUT_ROWMAJOR ? p * nt + j : j * ntr + (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_XYT ? ((p % h->n2) * h->n1 + p / h->n2) : p);
+      cd v = h->E[p * nt + j];
+      if (dtype == FIL_DTYPE_C128) { ((double*)out)[2 * s] = v.real(); ((double*)out)[2 * s + 1] = v.imag(); }
+      else { ((float*)out)[2 * s] = (float)v.real(); ((float*)out)[2 * s + 1] = (float)v.imag(); }
+    }
+  return FIL_OK;
+}
+
+int filo_get_plasma(fil_handle* h, int which, void* out, int dtype, int layout) {
+  if (!h || !out) return fail(h, FIL_ERR_ARG, "null argument");
+  const std::vector<double>& src = which == 0 ? h->rho : h->kdrho;
+  long ntr = h->ntr, nt = h->nt;
+  for (long p = 0; p < ntr; ++p)
+    for (long j = 0; j < nt; ++j) {
+      long s = layout == FIL_LAYOUT_ROWMAJOR ? p * nt + j : j * ntr + (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_XYT ? ((p % h->n2) * h->n1 + p / h->n2) : p);
+      if (dtype == FIL_DTYPE_F64) ((double*)out)[s] = src[p * nt + j];
+      else ((float*)out)[s] = (float)src[p * nt + j];
+    }
+  return FIL_OK;
+}
+
+int filo_step(fil_handle* h, double z, double dz) {
+  if (!h) return fail(nullptr, FIL_ERR_ARG, "null handle");
+  if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
+  zstep(h, dz);
+  h->z = z;
+  h->dz_last = dz;
+  h->steps += 1;
+  h->imax = current_imax(h);
+  return FIL_OK;
+}
+
+static double controller_dz(const fil_handle* h) {  // AdaptiveSteps.jl:96-107
+  const fil_config& c = h->cfg;
+  if (!c.nonlinearity) return c.dz0;
+  double dz = c.dz0;
+  double dzk = c.phimax / (c.phik * h->imax);
+  dz = std::min(dz, dzk);
+  if (c.phip > 0) {
+    double dzp = c.phimax / (c.phip * h->rhomax);
+    dz = std::min(dz, dzp);
+  }
+  return dz;
+}
+
+int filo_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* st) {
+  if (!h) return fail(nullptr, FIL_ERR_ARG, "null handle");
+  if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
+  double z = z0;
+  int code = FIL_STOP_NMAX;
+  int64_t n = 0;
+  while (true) {
+    if (!(z < zmax)) { code = FIL_STOP_ZMAX; break; }
+    if (n >= nmax) { code = FIL_STOP_NMAX; break; }
+    double dz = controller_dz(h);
+    if (h->clamp_last && z + dz > zmax) dz = zmax - z;
+    z += dz;
+    zstep(h, dz);
+    h->z = z;
+    h->dz_last = dz;
+    h->steps += 1;
+    ++n;
+    h->imax = current_imax(h);
+    if (!std::isfinite(h->imax)) { h->status = FIL_ERR_NAN; return fail(h, FIL_ERR_NAN, "non-finite field"); }
+    if (h->imax > h->cfg.istop) { code = FIL_STOP_ISTOP; break; }
+  }
+  h->status = code;
+  if (st) filo_get_stats(h, st);
+  return code;
+}
+
+int filo_get_stats(fil_handle* h, fil_stats* st) {
+  if (!h || !st) return fail(h, FIL_ERR_ARG, "null argument");
+  filo_analyze(h, st, nullptr, nullptr, nullptr);
+  st->imax = h->imax;
+  return FIL_OK;
+}
+
+int filo_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power, double* rho_end) {
+  if (!h) return fail(nullptr, FIL_ERR_ARG, "null handle");
+  long ntr = h->ntr;
+  int nt = h->nt;
+  double dt = h->cfg.dt;
+  std::vector<double> F(ntr, 0.0), P(h->has_t ? nt : 1, 0.0);
+  double imax = 0;
+  for (long p = 0; p < ntr; ++p) {
+    double s = 0;
+    for (int j = 0; j < nt; ++j) {
+      double I = std::norm(h->E[(size_t)p * nt + j]);
+      imax = std::max(imax, I);
+      s += I;
+    }
+    F[p] = h->has_t ? s * dt : s;
+  }
+  // transverse weights
+  auto wgt = [&](long p) {
+    if (h->geom == FIL_GEOM_R || h->geom == FIL_GEOM_RT) return 2.0 * M_PI * h->rdr[p];
+    if (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_XYT) return h->cfg.dxdy;
+    return 1.0;
+  };
+  if (h->has_t) {
+    for (int j = 0; j < nt; ++j) {
+      double s = 0;
+      for (long p = 0; p < ntr; ++p) s += std::norm(h->E[(size_t)p * nt + j]) * wgt(p);
+      P[j] = s;
+    }
+  } else {
+    double s = 0;
+    for (long p = 0; p < ntr; ++p) s += F[p] * wgt(p);
+    P[0] = s;
+  }
+  double energy = 0;
+  for (long p = 0; p < ntr; ++p) energy += F[p] * wgt(p);
+  if (fluence) std::copy(F.begin(), F.end(), fluence);
+  if (power) std::copy(P.begin(), P.end(), power);
+  if (rho_end)
+    for (long p = 0; p < ntr; ++p) rho_end[p] = h->rho[(size_t)p * nt + nt - 1];
+  if (st) {
+    st->z = h->z; st->dz = h->dz_last; st->imax = imax; st->rhomax = h->rhomax;
+    st->energy = energy; st->steps = h->steps; st->status = h->status; st->flags = 0;
+  }
+  return FIL_OK;
+}
+
+int filo_kernel_times(fil_handle* h, double* ms, int n) {
+  (void)h;
+  for (int i = 0; i < n; ++i) ms[i] = 0;
+  return FIL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,60 @@
+"""The C-ABI library builds, loads without a GPU, exports every function
+declared in include/filament_gb.h, and refuses work loudly without one."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "filament_gb.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fil_[a-z_]+)\s*\(", src)))
+
+
+def test_header_declares_the_abi():
+    names = declared_functions()
+    for n in ("fil_create", "fil_destroy", "fil_set_field", "fil_get_field", "fil_step",
+              "fil_run", "fil_analyze", "fil_last_error"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol():
+    import build as b
+    lib = ctypes.CDLL(b.build())
+    for n in declared_functions():
+        assert hasattr(lib, n), n
+
+
+def test_oracle_exports_same_abi(oracle_binding):
+    import oracle
+    lib = ctypes.CDLL(oracle.LIB)
+    for n in declared_functions():
+        assert hasattr(lib, "filo_" + n[4:]), n
+
+
+def test_create_rejects_bad_config_before_touching_the_device():
+    import filament_gb._abi as abi
+    import build as b
+    bd = abi.Binding(b.build(), "fil_")
+    cfg = abi.fil_config()
+    cfg.abi_version = 999
+    tab = abi.fil_tables()
+    h = ctypes.c_void_p()
+    rc = bd.create(ctypes.byref(cfg), ctypes.byref(tab), ctypes.byref(h))
+    assert rc == abi.FIL_ERR_ARG
+    assert b"version" in bd.last_error(None)
+
+
+def test_product_has_no_cpu_fallback(monkeypatch):
+    """Without the library the host package raises instead of computing."""
+    import filament_gb.backend as be
+    monkeypatch.setattr(be, "LIB_PATH", "/nonexistent/libfilament_gb.so")
+    monkeypatch.setattr(be, "_binding", None)
+    with pytest.raises(RuntimeError):
+        be.load_library()

@@ -1,0 +1,101 @@
+"""CUDA path vs the FP64 oracle on the same seeded inputs, through the C ABI.
+
+Tolerances: the plain FP64 form must agree to rounding (1e-10 relative L2);
+the mixed form (complex FP32 field) within 1e-5 relative L2 after a few
+steps, the accuracy budget of a single FP32 z-step chain.  The acceptance
+bound for whole runs is 1e-4 relative L2 field error and 1e-3 fluence error.
+"""
+import numpy as np
+import pytest
+
+from gpu_helpers import pair, rel_l2, rt_input, step_both, two_species_rates
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"mixed": 1e-5, "fp64": 1e-10}
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_field_upload_is_the_analytic_signal(gpu_lib, precision):
+    inp = rt_input(PLASMA=False)
+    g, r = pair(inp, precision)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL[precision] / 10
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_linear_step(gpu_lib, precision):
+    inp = rt_input(NONLINEARITY=False, PLASMA=False)
+    g, r = pair(inp, precision)
+    step_both(g, r, 5, 2e-3)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("alg", ["RK2", "RK3", "RK4"])
+def test_kerr_step(gpu_lib, precision, alg):
+    inp = rt_input(PLASMA=False, ALG=alg, PPcr=30.0)
+    g, r = pair(inp, precision)
+    step_both(g, r, 3, 2e-3)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("species", [1, 2])
+def test_plasma_density(gpu_lib, precision, species):
+    """rho(t) and Kdrho(t) of the parallel scan vs the sequential RK solve."""
+    kw = dict(PPcr=150.0)
+    inp = rt_input(**kw)
+    if species == 2:
+        inp["p_model"][1]["components"] = two_species_rates()
+    g, r = pair(inp, precision, store_plasma=True)
+    rho_g, rho_r = g.handle.get_plasma(0), r.handle.get_plasma(0)
+    kd_g, kd_r = g.handle.get_plasma(1), r.handle.get_plasma(1)
+    assert np.max(rho_r) > 1e-6          # ionisation actually happened
+    tol = 1e-5 if precision == "mixed" else 1e-10
+    assert rel_l2(rho_g, rho_r) < tol
+    assert rel_l2(kd_g, kd_r) < tol
+    st_g, st_r = g.handle.analyze(), r.handle.analyze()
+    assert st_g["rhomax"] == pytest.approx(st_r["rhomax"], rel=tol)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_full_step_with_plasma(gpu_lib, precision):
+    inp = rt_input(PPcr=150.0, ALG="RK4")
+    g, r = pair(inp, precision)
+    step_both(g, r, 3, 1e-3)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL[precision]
+    ag, ar = g.handle.analyze(), r.handle.analyze()
+    assert rel_l2(ag["fluence"], ar["fluence"]) < TOL[precision]
+    assert ag["energy"] == pytest.approx(ar["energy"], rel=TOL[precision])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_device_loop_matches_oracle_loop(gpu_lib, precision):
+    """fil_run: on-device adaptive dz, stop at zmax (Filament.jl:123-172)."""
+    import math
+    inp = rt_input(PPcr=60.0, ALG="RK4", dzphimax=0.1, dz_initial=1e-2, zmax=0.03)
+    g, r = pair(inp, precision)
+    code_g, st_g = g.handle.run(0.0, inp["zmax"], 10 ** 6)
+    code_r, st_r = r.handle.run(0.0, inp["zmax"], 10 ** 6)
+    assert code_g == code_r == 1
+    assert st_g["steps"] == st_r["steps"]
+    assert st_g["z"] == pytest.approx(st_r["z"], rel=1e-6)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < 10 * TOL[precision]
+    assert st_g["energy"] == pytest.approx(r.handle.analyze()["energy"], rel=1e-5)
+
+
+def test_device_loop_istop(gpu_lib):
+    """Imax > Istop ends the loop after the step that exceeded it."""
+    inp = rt_input(PLASMA=False, PPcr=30.0, Istop=1.0, dz_initial=2e-3)
+    g, r = pair(inp, "mixed")
+    code_g, st_g = g.handle.run(0.0, 1.0, 10 ** 6)
+    code_r, st_r = r.handle.run(0.0, 1.0, 10 ** 6)
+    assert code_g == code_r == 2
+    assert st_g["steps"] == st_r["steps"] == 1
+
+
+def test_run_nmax(gpu_lib):
+    inp = rt_input(PLASMA=False)
+    g, _ = pair(inp, "mixed")
+    code, st = g.handle.run(0.0, 10.0, 5)
+    assert code == 3 and st["steps"] == 5
