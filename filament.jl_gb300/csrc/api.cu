@@ -10,6 +10,7 @@
 //   k_dht (x2)                   Hankel transform, propagator, inverse
 // fil_run captures a few steps into a CUDA graph and replays it until the
 // on-device controller raises its done flag.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -55,6 +56,7 @@ struct fil_handle {
   PlasmaParams pp;
   int ns;
   double A0[4], A1[4], B[4];
+  double sc = 1, sf = 1, sl = 1;   // response channel pre-scales
   bool field_set = false, store_plasma = false;
   int bugcompat = 0, clamp_last = 0, timing = 0;
   cudaGraphExec_t graph = nullptr;
@@ -127,20 +129,42 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     if (t->guardt) gtt.assign(t->guardt, t->guardt + nt);
     if (upload<R>(h, &h->g1, g) || upload<R>(h, &h->gt, gtt)) return FIL_ERR_CUDA;
   }
-  // nonlinear coefficients C_ch[k] = i QZ Rnl_ch (k ? 2 : 1), k < nh
+  // nonlinear coefficients C_ch[k] = i QZ Rnl_ch (k ? 2 : 1) / s_ch, k < nh.
+  // The row kernel multiplies response ch by s_ch, the median of |C_ch| over
+  // the band, so that channels sharing a complex FFT have comparable size
+  // (any positive constant gives the same result in exact arithmetic).
   {
-    auto comb = [&](const double* rnl, void** dst) -> int {
+    auto coef = [&](const double* rnl, int k) {
+      cd q(t->qz[2 * k], t->qz[2 * k + 1]), r(rnl[2 * k], rnl[2 * k + 1]);
+      return cd(0, 1) * q * r * (k ? 2.0 : 1.0);
+    };
+    auto scale = [&](const double* rnl) {
+      if (!rnl || !t->qz || nh < 2) return 1.0;
+      std::vector<double> a;
+      for (int k = 1; k < nh; ++k) {
+        double v = std::abs(coef(rnl, k));
+        if (v > 0 && std::isfinite(v)) a.push_back(v);
+      }
+      if (a.empty()) return 1.0;
+      std::nth_element(a.begin(), a.begin() + a.size() / 2, a.end());
+      return a[a.size() / 2];
+    };
+    h->sc = scale(t->rnl_cubic);
+    h->sf = scale(t->rnl_free);
+    h->sl = scale(t->rnl_losses);
+    auto comb = [&](const double* rnl, double sch, void** dst) -> int {
       std::vector<double> v(2 * nh, 0.0);
       if (rnl && t->qz)
         for (int k = 0; k < nh; ++k) {
-          cd q(t->qz[2 * k], t->qz[2 * k + 1]), r(rnl[2 * k], rnl[2 * k + 1]);
-          cd x = cd(0, 1) * q * r * (k ? 2.0 : 1.0);
+          cd x = coef(rnl, k) / sch;
           v[2 * k] = x.real();
           v[2 * k + 1] = x.imag();
         }
       return upload<R>(h, dst, v);
     };
-    if (comb(t->rnl_cubic, &h->Cc) || comb(t->rnl_free, &h->Cf) || comb(t->rnl_losses, &h->Cl)) return FIL_ERR_CUDA;
+    if (comb(t->rnl_cubic, h->sc, &h->Cc) || comb(t->rnl_free, h->sf, &h->Cf) ||
+        comb(t->rnl_losses, h->sl, &h->Cl))
+      return FIL_ERR_CUDA;
   }
   // propagator tables
   {
@@ -244,6 +268,9 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
   P.Cc = (const C*)h->Cc;
   P.Cf = (const C*)h->Cf;
   P.Cl = (const C*)h->Cl;
+  P.sc = h->sc;
+  P.sf = h->sf;
+  P.sl = h->sl;
   P.ns = h->ns;
   for (int s = 0; s < 4; ++s) { P.A0[s] = h->A0[s]; P.A1[s] = h->A1[s]; P.B[s] = h->B[s]; }
   P.plasma = c.plasma;
@@ -500,9 +527,12 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
     h->bugcompat = value != 0;
   } else if (option == FIL_OPT_CLAMP_LAST_DZ) {
     h->clamp_last = value != 0;
-  } else if (option == 4) {  // per-kernel timing of fil_step (diagnostic)
+  } else if (option == FIL_OPT_TIMING) {
     h->timing = value != 0;
-  } else {
+  } else if (option == FIL_OPT_ANALYTIC_PROJECTION) {
+    // the field state is the analytic half spectrum: always projected
+  }
+  else {
     return fail(h, FIL_ERR_ARG, "unknown option");
   }
   if (h->graph) {           // parameters baked into the graph changed

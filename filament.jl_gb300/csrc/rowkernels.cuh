@@ -41,6 +41,7 @@ template <typename R> struct RowParams {
   const C* Cc;                  // i QZ Rnl_cubic * (k ? 2 : 1), [nh]
   const C* Cf;
   const C* Cl;
+  double sc, sf, sl;            // channel pre-scales (C tables are divided by them)
   int ns;                       // RK stages
   double A0[4], A1[4], B[4];    // stage input U_s = S0 + dz (A0 k1 + A1 kprev)
   // plasma
@@ -315,7 +316,11 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
         X[pad16(k + NH)] = mk<R>(0, 0);
       }
       filfft::block_fft<C, N, -1>(X, P.tw);            // inverse_transform_time!
-      // responses in the time domain (medium_responses/*.jl), field filter
+      // responses in the time domain (medium_responses/*.jl) times the field
+      // filter.  Channels are packed two per complex FFT by scale: X holds
+      // the Kerr response, Y the two plasma responses (free current in the
+      // real part, losses in the imaginary part); each channel is pre-scaled
+      // by |C_ch| at the carrier so packed partners have comparable size.
 #pragma unroll 4
       for (int m = 0; m < 16; ++m) {
         int j = tid + m * T;
@@ -331,23 +336,30 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
           R inv = (Il >= (R)1e-30) ? (R)1 / Il : (R)0;
           fl = kdrho[j] * inv * re;
         }
-        X[pad16(j)] = mk<R>(g * fc, g * ff);
-        Y[pad16(j)] = mk<R>(g * fl, 0);
+        X[pad16(j)] = mk<R>(g * (R)P.sc * fc, 0);
+        Y[pad16(j)] = mk<R>(g * (R)P.sf * ff, g * (R)P.sl * fl);
       }
-      filfft::block_fft<C, N, +1>(X, P.tw);            // rsig2aspec! (two packed)
-      if (P.has_losses) filfft::block_fft<C, N, +1>(Y, P.tw);
+      const bool plas = NC > 0 && (P.has_free || P.has_losses);
+      if (P.has_cubic) filfft::block_fft<C, N, +1>(X, P.tw);   // rsig2aspec!
+      if (plas) filfft::block_fft<C, N, +1>(Y, P.tw);
+      __syncthreads();
 #pragma unroll
       for (int m = 0; m < EW; ++m) {
         int k = tid + m * T;
-        C z = X[pad16(k)];
-        C zm = cconj(X[pad16((N - k) & (N - 1))]);
-        // F_c = (z + conj(z_-k))/2, F_f = (z - conj(z_-k))/(2i), both /N
-        C fc = ((R)0.5 * invN) * (z + zm);
-        C dff = z - zm;
-        C ffr = mk<R>(dff.y * (R)0.5 * invN, -dff.x * (R)0.5 * invN);
-        C d = cmul(__ldg(&P.Cc[k]), fc);
-        if (NC > 0 && P.has_free) d = d + cmul(__ldg(&P.Cf[k]), ffr);
-        if (NC > 0 && P.has_losses) d = d + cmul(__ldg(&P.Cl[k]), invN * Y[pad16(k)]);
+        const int km = (N - k) & (N - 1);
+        C d = mk<R>(0, 0);
+        if (P.has_cubic) {
+          C z = X[pad16(k)], zm = cconj(X[pad16(km)]);
+          d = cmul(__ldg(&P.Cc[k]), ((R)0.5 * invN) * (z + zm));
+        }
+        if (plas) {
+          C z = Y[pad16(k)], zm = cconj(Y[pad16(km)]);
+          C ffr = ((R)0.5 * invN) * (z + zm);                 // (z + conj z_-k)/2
+          C dl = z - zm;
+          C flr = mk<R>(dl.y * (R)0.5 * invN, -dl.x * (R)0.5 * invN);  // (z - conj z_-k)/(2i)
+          if (P.has_free) d = d + cmul(__ldg(&P.Cf[k]), ffr);
+          if (P.has_losses) d = d + cmul(__ldg(&P.Cl[k]), flr);
+        }
         if (s == 0) k1[m] = d;
         kp[m] = d;
         acc[m] = acc[m] + (R)P.B[s] * d;

@@ -37,6 +37,8 @@ LAYOUT_ROWMAJOR = 1
 OPT_STORE_PLASMA = 1
 OPT_XYT_GUARD_BUGCOMPAT = 2
 OPT_CLAMP_LAST_DZ = 3
+OPT_TIMING = 4
+OPT_ANALYTIC_PROJECTION = 5
 
 _dp = C.POINTER(C.c_double)
 

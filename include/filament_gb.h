@@ -92,6 +92,14 @@ extern "C" {
                                   indexed by the y index) in XYT           */
 #define FIL_OPT_CLAMP_LAST_DZ 3 /* fil_run shortens the last step so that z
                                   lands on zmax exactly (off = reference)  */
+#define FIL_OPT_TIMING 4       /* fil_step records per-kernel device times
+                                  (fil_kernel_times)                        */
+#define FIL_OPT_ANALYTIC_PROJECTION 5 /* drop negative frequencies after
+                                  every t->w transform.  The library's field
+                                  state is the analytic half spectrum, so
+                                  this is always on there; an implementation
+                                  that keeps the full spectrum (as the
+                                  reference does) can switch it on to match */
 
 typedef struct fil_config {
   int32_t abi_version;   /* FIL_ABI_VERSION                                  */

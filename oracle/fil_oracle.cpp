@@ -153,7 +153,7 @@ struct fil_handle {
   std::vector<cd> E;
   std::vector<double> rho, kdrho;
   bool field_set = false;
-  bool bugcompat = false, clamp_last = false;
+  bool bugcompat = false, clamp_last = false, project = false;
   double z = 0, dz_last = 0;
   long steps = 0;
   double imax = 0, rhomax = 0;
@@ -530,6 +530,9 @@ void nl_step(fil_handle* h, std::vector<cd>& u, double dz) {
 void zstep(fil_handle* h, double dz) {
   if (h->cfg.plasma) plasma_solve(h);      // Models.jl:84-89
   t_to_w(h, h->E);                         // Models.jl:91-96
+  if (h->project && h->has_t)              // checker option, see filament_gb.h
+    for (long p = 0; p < h->ntr; ++p)
+      for (int j = h->nh; j < h->nt; ++j) h->E[(size_t)p * h->nt + j] = 0.0;
   if (h->cfg.nonlinearity) nl_step(h, h->E, dz);  // Models.jl:98-103
   linear_step(h, h->E, dz);                // Models.jl:105-108
   w_to_t(h, h->E);                         // Models.jl:110-114
@@ -618,6 +621,7 @@ int filo_set_option(fil_handle* h, int opt, int64_t v) {
   if (!h) return fail(nullptr, FIL_ERR_ARG, "null handle");
   if (opt == FIL_OPT_XYT_GUARD_BUGCOMPAT) h->bugcompat = v != 0;
   else if (opt == FIL_OPT_CLAMP_LAST_DZ) h->clamp_last = v != 0;
+  else if (opt == FIL_OPT_ANALYTIC_PROJECTION) h->project = v != 0;
   return FIL_OK;
 }
 

@@ -27,11 +27,18 @@ def two_species_rates():
     return [n2, o2]
 
 
-def pair(inp, precision="mixed", store_plasma=False):
+def pair(inp, precision="mixed", store_plasma=False, project=True):
+    """(CUDA simulation, oracle simulation) on the same input.  With
+    project=True the oracle drops negative frequencies after each t->w
+    transform, as the library's half-spectrum state does, so that the two
+    differ by arithmetic only."""
     import filament_gb as fg
     import oracle
+    from filament_gb import _abi
     g = fg.Simulation(inp, precision=precision)
     r = fg.Simulation(inp, binding=oracle.binding())
+    if project:
+        r.handle.set_option(_abi.OPT_ANALYTIC_PROJECTION, 1)
     if store_plasma:
         from filament_gb import _abi
         g.handle.set_option(_abi.OPT_STORE_PLASMA, 1)
