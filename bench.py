@@ -1,0 +1,308 @@
+"""Benchmark: RT filamentation z-steps/s on one GB300 (replicas for N > 1).
+
+Workload (the 1000 x 4096 RT configuration): Nr = 1000 Hankel points to
+R = 5 mm, Nt = 4096 over +-200 fs, 5 Pcr Gaussian beam (1/e intensity radius
+1 mm) x 35 fs FWHM pulse at 800 nm in air (Peck-Reeder dispersion,
+n2 = 1e-23, one-species sigma_8 I^8 multiphoton ionisation with avalanche,
+Drude free current and multiphoton losses), RK4 nonlinear step, adaptive dz
+with max nonlinear phase 0.1 rad, z_end = 3 m.  Synthetic input (seedless
+analytic Gaussian pulse; the reference ships no dataset).
+
+A "step" is one z-step of the device loop (fil_run): reductions + dz
+controller + fused row kernel (plasma, t<->w FFTs, RK4 stages) + Hankel
+transform, propagator, inverse transform.  The timed steps run one at a time
+with a 512 MB buffer written before each step (L2 flushed, outside the timed
+events), device time from CUDA events on the library's stream.
+
+--impl reference times the project's FP64 CPU oracle of the same loop on the
+host cores (the reference itself is Julia + CUDA.jl, absent on this machine).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "filament.jl_gb300")
+DECK = os.path.join(PKG, "decks", "filament_RT", "input.py")
+
+WORKLOAD = dict(Nr=1000, Nt=4096, rmax=5.0, tmin=-200.0, tmax=200.0, PPcr=5.0, ALG="RK4",
+                dzphimax=0.1, dz_initial=1e-2, zmax=3.0)
+WORKLOAD_NAME = "RT filamentation Nr=1000 x Nt=4096, RK4, 5 Pcr, adaptive dz (phimax 0.1 rad), z_end 3 m"
+
+
+def _env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def _config(args, extra=None):
+    c = {"workload": WORKLOAD_NAME, "Nr": WORKLOAD["Nr"], "Nt": WORKLOAD["Nt"], "alg": "RK4",
+         "z_end_m": WORKLOAD["zmax"], "l2": "512 MB buffer written before every timed step",
+         "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower().startswith("active"):
+                    reasons.add(n)
+        sm_sorted = sorted(sm)
+        return {"sm_mhz": sm_sorted[len(sm_sorted) // 2] if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def _prepare(**over):
+    import filament_gb as fg
+    kw = dict(WORKLOAD)
+    kw.update(over)
+    return fg.prepare(DECK, **kw)
+
+
+def time_device_loop(precision, warmup, steps, load_seconds=0.0):
+    """Warm-up in graph mode, then `steps` timed steps (flushed L2), then
+    the same steps in graph mode (warm L2, for information); with
+    load_seconds > 0 the graph-mode loop continues that long so the clock
+    sampler sees the kernels under sustained load."""
+    import filament_gb as fg
+    from filament_gb import _abi
+    inp = _prepare()
+    sim = fg.Simulation(inp, precision=precision)
+    h = sim.handle
+    code, st = h.run(0.0, inp["zmax"], warmup)
+    h.set_option(_abi.OPT_TIMING, 1)
+    t0 = time.perf_counter()
+    code, st2 = h.run(st["z"], inp["zmax"], steps)
+    wall = time.perf_counter() - t0
+    kt = h.kernel_times(6)
+    h.set_option(_abi.OPT_TIMING, 0)
+    # warm (graph) throughput for information
+    t1 = time.perf_counter()
+    code3, st3 = h.run(st2["z"], inp["zmax"], steps)
+    graph_wall = time.perf_counter() - t1
+    t2 = time.perf_counter()
+    z = st3["z"]
+    while time.perf_counter() - t2 < load_seconds and z < inp["zmax"]:
+        _, stl = h.run(z, inp["zmax"], 200)
+        z = stl["z"]
+    res = {"ms_per_step": kt[4], "row_ms": kt[0], "dht_fwd_ms": kt[1], "dht_inv_ms": kt[2],
+           "reduce_ms": kt[3], "timed_steps": int(kt[5]), "wall_s": wall,
+           "graph_steps_per_s": (st3["steps"] - st2["steps"]) / graph_wall if graph_wall > 0 else None,
+           "z_after": st3["z"]}
+    sim.close()
+    return res
+
+
+def accuracy_run(zend, nmax):
+    """Mixed form vs plain FP64 form from the same field to the same z
+    (dz clamped on the last step), relative L2 of the field and fluence."""
+    import numpy as np
+    import filament_gb as fg
+    from filament_gb import _abi
+    inp = _prepare(zmax=zend)
+    out = {}
+    fields = {}
+    for prec in ("mixed", "fp64"):
+        sim = fg.Simulation(inp, precision=prec)
+        sim.handle.set_option(_abi.OPT_CLAMP_LAST_DZ, 1)
+        t0 = time.perf_counter()
+        code, st = sim.handle.run(0.0, zend, nmax)
+        out[prec + "_wall_s"] = time.perf_counter() - t0
+        out[prec + "_steps"] = st["steps"]
+        out[prec + "_z"] = st["z"]
+        a = sim.handle.analyze()
+        fields[prec] = (sim.handle.get_field(), a["fluence"], a["imax"])
+        sim.close()
+    Em, Fm, Im = fields["mixed"]
+    Ed, Fd, Id = fields["fp64"]
+    out["rel_l2_field"] = float(np.linalg.norm(Em - Ed) / np.linalg.norm(Ed))
+    out["rel_l2_fluence"] = float(np.linalg.norm(Fm - Fd) / np.linalg.norm(Fd))
+    out["imax_end"] = Id
+    out["z_end"] = zend
+    return out
+
+
+def e2e_host_loop(steps):
+    """The reference's main loop through the public API: per step the host
+    dz (AdaptiveSteps), fil_step, and fil_analyze (device reductions copied
+    to the host: fluence[Nr], power[Nt], rho_end[Nr], stats).  The initial
+    field upload and the final field download are inside the timed region."""
+    import numpy as np
+    import filament_gb as fg
+    from filament_gb.filament import AStep
+    inp = _prepare()
+    E0 = None
+    t0 = time.perf_counter()
+    sim = fg.Simulation(inp, precision="mixed")          # H2D of the field
+    z = 0.0
+    for _ in range(steps):
+        dz = sim.dzadaptive(sim.analyzer)
+        z += dz
+        sim.handle.step(z, dz)
+        sim.analyzer.analyze(z)                           # D2H of reductions
+    E = sim.handle.get_field()                            # D2H of the field
+    wall = time.perf_counter() - t0
+    nr, nt = WORKLOAD["Nr"], WORKLOAD["Nt"]
+    field_bytes = nr * nt * 16
+    sim.close()
+    return {"value": steps / wall, "unit": "z-steps/s",
+            "h2d_bytes_per_step": int(field_bytes / steps + 16),
+            "d2h_bytes_per_step": int((2 * nr + nt) * 8 + 64 + field_bytes / steps)}
+
+
+def cpu_oracle(steps):
+    import filament_gb as fg
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    inp = _prepare()
+    sim = fg.Simulation(inp, binding=oracle.binding())
+    t0 = time.perf_counter()
+    code, st = sim.handle.run(0.0, inp["zmax"], steps)
+    wall = time.perf_counter() - t0
+    sim.close()
+    return st["steps"] / wall, wall
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=30)
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--accuracy-zend", type=float, default=WORKLOAD["zmax"])
+    args = ap.parse_args()
+    rank, local_rank, world = _env_rank()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
+    sys.path.insert(0, PKG)
+    sys.path.insert(0, ROOT)
+    args.warmup = max(args.warmup, 3)
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sps, wall = cpu_oracle(args.cpu_steps)
+        cores = os.cpu_count()
+        line = {"metric": "RT z-steps/s", "value": sps, "unit": "z-steps/s", "n_gpus": args.gpus,
+                "steps": args.cpu_steps, "warmup": 0, "ms_per_step": 1000.0 / sps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "impl": "reference", "config": _config(args),
+                "cpu_baseline": {"value": sps, "unit": "z-steps/s", "cores": cores, "kind": "port",
+                                 "sample": "%d z-steps of the workload from z=0 (%.1f s) with the "
+                                           "OpenMP FP64 oracle on all host threads" % (args.cpu_steps, wall)},
+                "e2e": {"value": sps, "unit": "z-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import build as _b
+    _b.build()
+    sampler = ClockSampler(0)
+    if dist is not None:
+        dist.barrier()
+    sampler.start()
+    mixed = time_device_loop("mixed", args.warmup, args.steps, load_seconds=3.0)
+    clocks = sampler.stop()
+    fp64 = time_device_loop("fp64", args.warmup, max(3, args.steps // 10))
+    t_local = mixed["ms_per_step"]
+    if dist is not None:
+        import torch
+        t = torch.tensor([t_local], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_local = float(t[0])
+    value = world * 1000.0 / t_local
+    if rank != 0:
+        return
+    e2e = e2e_host_loop(max(10, args.steps // 2))
+    acc = None if args.no_accuracy else accuracy_run(args.accuracy_zend, 200000)
+    sps_cpu, cpu_wall = cpu_oracle(args.cpu_steps)
+    hbm, bf16, src = _peaks()
+    nr, nt, s = WORKLOAD["Nr"], WORKLOAD["Nt"], 4
+    # algorithmic bytes of the row kernel per launch (complex 8 B, real 4 B):
+    # plasma (read E, write rho, Kdrho) + t->w (r+w) + s stages (read base and
+    # previous k, read rho and Kdrho, write k) + RK combine (read E, k1..ks,
+    # write E) = c(4s+5) + q(2s+2) per grid point
+    b_row = nr * nt * (8 * (4 * s + 5) + 4 * (2 * s + 2))
+    achieved = b_row / (mixed["row_ms"] * 1e-3) / 1e9
+    line = {
+        "metric": "RT z-steps/s", "value": value, "unit": "z-steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_local,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic", "config": _config(args),
+        "forms": {"mixed": mixed, "fp64": fp64,
+                  "speedup_mixed_over_fp64": fp64["ms_per_step"] / mixed["ms_per_step"]},
+        "accuracy": acc,
+        "roofline": {"kernel": "k_rowstep (plasma + RK4 nonlinear step, fused)", "bound": "hbm",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": src, "traffic": None,
+                     "algorithmic_bytes_per_launch": b_row},
+        "cpu_baseline": {"value": sps_cpu, "unit": "z-steps/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "%d z-steps of the workload from z=0 (%.1f s), FP64 OpenMP oracle"
+                                   % (args.cpu_steps, cpu_wall)},
+        "e2e": e2e,
+        "clocks": clocks,
+        "gpu_launches": 6 * args.steps,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

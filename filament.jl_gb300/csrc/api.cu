@@ -61,8 +61,10 @@ struct fil_handle {
   int bugcompat = 0, clamp_last = 0, timing = 0;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev[8];
-  double tsum[3] = {0, 0, 0};
+  double tsum[5] = {0, 0, 0, 0, 0};   // row, dht fwd, dht inv, reduce+control, whole step
   long tcount = 0;
+  void* flushbuf = nullptr;            // > L2, benchmark timing only
+  size_t flushbytes = 0;
 };
 
 static int fail(fil_handle* h, int code, const std::string& m) {
@@ -303,13 +305,13 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   P.S_out = (typename C2T<R>::type*)h->W1;
   PropParams<R> pp = prop_params<R>(h);
   const int Nc = 2 * h->nh;
-  if (timed) CK(cudaEventRecord(h->ev[0], h->st));
-  CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
-  CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 1, h->st));
+  CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
   if (timed) CK(cudaEventRecord(h->ev[2], h->st));
-  CK(launch_dht_simt<R>((const R*)h->M2, (const R*)h->W2, (R*)h->S, h->mpad, Nc, h->mpad, pp, h->ctl, 2, h->st));
+  CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 1, h->st));
   if (timed) CK(cudaEventRecord(h->ev[3], h->st));
+  CK(launch_dht_simt<R>((const R*)h->M2, (const R*)h->W2, (R*)h->S, h->mpad, Nc, h->mpad, pp, h->ctl, 2, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[4], h->st));
   return 0;
 }
 
@@ -336,7 +338,7 @@ static int read_ctl(fil_handle* h) {
 static void free_all(fil_handle* h) {
   void* bufs[] = {h->S, h->W1, h->W2, h->M1, h->M2, h->tw, h->g1, h->g2, h->gt, h->Cc, h->Cf, h->Cl,
                   h->kt2, h->beta, h->dfr, h->kmax2, h->wg, h->rho_g, h->kdrho_g, h->stage,
-                  h->fluence, h->power, h->pw, h->rho_end, h->ctl};
+                  h->fluence, h->power, h->pw, h->rho_end, h->ctl, h->flushbuf};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -529,6 +531,8 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
     h->clamp_last = value != 0;
   } else if (option == FIL_OPT_TIMING) {
     h->timing = value != 0;
+    for (int i = 0; i < 5; ++i) h->tsum[i] = 0;
+    h->tcount = 0;
   } else if (option == FIL_OPT_ANALYTIC_PROJECTION) {
     // the field state is the analytic half spectrum: always projected
   }
@@ -582,17 +586,9 @@ int fil_step(fil_handle* h, double z, double dz) {
   if (!h) return fail(h, FIL_ERR_ARG, "null handle");
   if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
   CK(launch_setdz(h->ctl, z, dz, h->st));
-  int rc = zstep(h, h->timing != 0);
+  int rc = zstep(h, false);
   if (rc) return rc;
   CK(cudaStreamSynchronize(h->st));
-  if (h->timing) {
-    float ms;
-    for (int i = 0; i < 3; ++i) {
-      CK(cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]));
-      h->tsum[i] += ms;
-    }
-    h->tcount += 1;
-  }
   return FIL_OK;
 }
 
@@ -640,6 +636,35 @@ int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stat
   c.clamp_last = h->clamp_last;
   c.imax_acc = 0;
   CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
+  if (h->timing) {
+    // benchmark path: one step at a time, L2 flushed before each step
+    // (outside the timed events), device time of each kernel accumulated
+    if (!h->flushbuf) {
+      h->flushbytes = (size_t)512 << 20;
+      CK(cudaMalloc(&h->flushbuf, h->flushbytes));
+    }
+    for (;;) {
+      CK(launch_flush(h->flushbuf, h->flushbytes, h->st));
+      CK(cudaEventRecord(h->ev[0], h->st));
+      int rc = reduce(h, nullptr, 1);
+      if (rc) return rc;
+      CK(launch_control(h->ctl, h->fluence, h->pw, h->nrows, h->st));
+      rc = zstep(h, true);
+      if (rc) return rc;
+      rc = read_ctl(h);
+      if (rc) return rc;
+      if (h->ctl_host->done) break;
+      float t[4], tot;
+      for (int i = 0; i < 4; ++i) CK(cudaEventElapsedTime(&t[i], h->ev[i], h->ev[i + 1]));
+      CK(cudaEventElapsedTime(&tot, h->ev[0], h->ev[4]));
+      h->tsum[0] += t[1];
+      h->tsum[1] += t[2];
+      h->tsum[2] += t[3];
+      h->tsum[3] += t[0];
+      h->tsum[4] += tot;
+      h->tcount += 1;
+    }
+  } else {
   if (!h->graph) {
     int rc = build_graph(h);
     if (rc) return rc;
@@ -649,6 +674,7 @@ int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stat
     int rc = read_ctl(h);
     if (rc) return rc;
     if (h->ctl_host->done) break;
+  }
   }
   const DevCtl& r = *h->ctl_host;
   if (stats) {
@@ -721,7 +747,8 @@ int fil_get_stats(fil_handle* h, fil_stats* st) {
 
 int fil_kernel_times(fil_handle* h, double* ms, int n) {
   if (!h || !ms) return fail(h, FIL_ERR_ARG, "null argument");
-  for (int i = 0; i < n; ++i) ms[i] = (i < 3 && h->tcount) ? h->tsum[i] / h->tcount : 0.0;
+  for (int i = 0; i < n; ++i) ms[i] = (i < 5 && h->tcount) ? h->tsum[i] / h->tcount : 0.0;
+  if (n > 5) ms[5] = (double)h->tcount;
   return FIL_OK;
 }
 

@@ -22,4 +22,5 @@ template <typename R>
 cudaError_t launch_dht_simt(const R* A, const R* B, R* C, int M, int N, int K, const PropParams<R>& pp,
                             DevCtl* ctl, int epi, cudaStream_t st);
 cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
+cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);

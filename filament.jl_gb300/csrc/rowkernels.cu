@@ -165,6 +165,17 @@ cudaError_t launch_control(DevCtl* c, const double* fl, const double* w, int nro
   k_control<<<1, 256, 0, st>>>(c, fl, w, nrows);
   return cudaGetLastError();
 }
+// Writes a buffer larger than L2 so the next step starts with a cold cache
+// (benchmark timing only).
+__global__ void k_flush(float4* buf, size_t n, float v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    buf[i] = make_float4(v, v, v, v);
+}
+cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st) {
+  k_flush<<<152 * 8, 256, 0, st>>>((float4*)buf, bytes / sizeof(float4), 0.0f);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st) {
   k_setdz<<<1, 1, 0, st>>>(c, z, dz);
   return cudaGetLastError();

@@ -92,8 +92,10 @@ extern "C" {
                                   indexed by the y index) in XYT           */
 #define FIL_OPT_CLAMP_LAST_DZ 3 /* fil_run shortens the last step so that z
                                   lands on zmax exactly (off = reference)  */
-#define FIL_OPT_TIMING 4       /* fil_step records per-kernel device times
-                                  (fil_kernel_times)                        */
+#define FIL_OPT_TIMING 4       /* benchmark mode: fil_run runs steps one at
+                                  a time, writes a buffer larger than L2
+                                  before each step and records per-kernel
+                                  device times (fil_kernel_times)          */
 #define FIL_OPT_ANALYTIC_PROJECTION 5 /* drop negative frequencies after
                                   every t->w transform.  The library's field
                                   state is the analytic half spectrum, so
@@ -241,8 +243,10 @@ int fil_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power,
 /* Current controller state without launching work beyond a copy. */
 int fil_get_stats(fil_handle* h, fil_stats* st);
 
-/* Average device time per kernel family of the last fil_run, in ms
- * (index 0: row kernel, 1: forward transverse transform, 2: inverse).      */
+/* Average device time per step of each kernel family over the timed steps
+ * since FIL_OPT_TIMING was set, in ms: 0 row kernel (plasma + nonlinear
+ * step), 1 forward transverse transform + propagator, 2 inverse transform,
+ * 3 reductions + controller, 4 whole step; ms[5] = number of timed steps. */
 int fil_kernel_times(fil_handle* h, double* ms, int n);
 
 #ifdef __cplusplus
