@@ -221,7 +221,8 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     P.dt = c.dt;
     P.rho0 = c.rho0;
     P.maxit = 8;
-    P.tol = h->fp64 ? 1e-13 : 1e-6;
+    P.tol = h->fp64 ? 1e-26 : 1e-8;
+    P.skip = h->fp64 ? 1e-250 : 1e-30;
     bool pl = true;
     for (int i = 0; i < nc; ++i) {
       P.rho_nt[i] = t->rho_nt[i];
@@ -685,7 +686,7 @@ int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stat
     stats->energy = r.energy;
     stats->steps = r.steps;
     stats->status = r.status;
-    stats->flags = r.flags;
+    stats->flags = r.flags | (std::min(r.newton_max, 255) << 8);
   }
   if (r.status < 0) return fail(h, r.status, "non-finite field during fil_run");
   return r.status;
@@ -741,7 +742,7 @@ int fil_get_stats(fil_handle* h, fil_stats* st) {
   st->energy = c.energy;
   st->steps = c.steps;
   st->status = c.status;
-  st->flags = c.flags;
+  st->flags = c.flags | (std::min(c.newton_max, 255) << 8);
   return FIL_OK;
 }
 

@@ -40,7 +40,8 @@ struct PlasmaParams {
   double lx[FIL_MAXCOMP][FIL_MAXRATE], ly[FIL_MAXCOMP][FIL_MAXRATE], sl[FIL_MAXCOMP][FIL_MAXRATE];
   int avalanche;          // any rava != 0
   int maxit;              // Newton iteration cap
-  double tol;             // Newton relative tolerance
+  double tol;             // Newton: stop when update^2 <= tol |u|^2
+  double skip;            // rows with max W * window below this keep rho0
 };
 
 template <typename R> struct PlasmaSmem {
@@ -158,7 +159,9 @@ FIL_DEV Aff<R, NC> step_map(const PlasmaParams& P, const R* u, const R (&W)[3][N
                             bool aval) {
   R k[4][NC], dk[4][NC][NC];
   const R dt = (R)P.dt;
-  for (int s = 0; s < P.ns; ++s) {
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    if (s >= P.ns) break;
     R U[NC], dU[NC][NC];
 #pragma unroll
     for (int i = 0; i < NC; ++i) {
@@ -166,6 +169,7 @@ FIL_DEV Aff<R, NC> step_map(const PlasmaParams& P, const R* u, const R (&W)[3][N
 #pragma unroll
       for (int l = 0; l < NC; ++l) dU[i][l] = (i == l) ? (R)1 : (R)0;
     }
+#pragma unroll
     for (int l = 0; l < s; ++l) {
       R al = (R)P.a[s][l];
       if (al != (R)0) {
@@ -207,7 +211,9 @@ FIL_DEV Aff<R, NC> step_map(const PlasmaParams& P, const R* u, const R (&W)[3][N
     R Lrow[NC];
 #pragma unroll
     for (int l = 0; l < NC; ++l) Lrow[l] = 0;
-    for (int s = 0; s < P.ns; ++s) {
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      if (s >= P.ns) break;
       R bs = (R)P.b[s];
       inc += bs * k[s][i];
 #pragma unroll

@@ -56,7 +56,7 @@ template <typename R, int N, int NC>
 static size_t rowstep_smem() {
   typedef typename C2T<R>::type C;
   constexpr int NP = N + N / 16;
-  return 2 * NP * sizeof(C) + 2 * N * sizeof(R) + 32 * sizeof(R) + 32 * sizeof(Aff<R, (NC > 0 ? NC : 1)>) +
+  return 2 * NP * sizeof(C) + 2 * NP * sizeof(R) + 32 * sizeof(R) + 32 * sizeof(Aff<R, (NC > 0 ? NC : 1)>) +
          sizeof(PlasmaSmem<R>);
 }
 template <typename R, int N> static size_t x_smem() {

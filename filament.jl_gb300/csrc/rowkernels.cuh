@@ -17,7 +17,7 @@
 struct DevCtl {
   double z, dz, zmax;
   long long steps, nmax, run_steps;
-  int done, status, flags, guard_pending, first, clamp_last, nonlinearity, pad0;
+  int done, status, flags, guard_pending, first, clamp_last, nonlinearity, newton_max;
   unsigned long long imax_acc, rhomax_acc;  // bit patterns of non-negative doubles
   double imax, rhomax, energy;
   double dz0, phimax, phik, phip, istop;
@@ -97,16 +97,29 @@ FIL_DEV void load_time_row(const RowParams<R>& P, typename C2T<R>::type* X, int 
 }
 
 // ---------------------------------------------------------------------------
-// Plasma solve on the row in X.  Writes rho[] and kdrho[] (shared), Y is
-// scratch (>= FIL_MAXCOMP*N reals).  Returns max rho (block-uniform).
+// Plasma solve on the row in X.  Writes rho[] and kdrho[] (shared, indexed
+// with pad16), Y is scratch (2*(N + N/16) reals).  Returns max rho
+// (block-uniform).
+//
+// Work split: thread t owns the 16 consecutive time steps j = 16t .. 16t+15.
+// Single-species power-law rates (the common case) are evaluated once per
+// time point and midpoint into Y; otherwise they are re-evaluated per use.
+// A row whose largest rate times the window length is below `skip` keeps
+// rho = rho0 exactly to the working precision and needs no scan.
 template <typename R, int N, int NC>
 FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typename C2T<R>::type* X,
-                     R* rho, R* kdrho, R* ybuf, Aff<R, NC>* ascratch, R* rscratch, int* newton_flag) {
+                     R* rho, R* kdrho, R* Y, Aff<R, NC>* ascratch, R* rscratch, int* newton_flag) {
   typedef typename C2T<R>::type C;
+  constexpr int NP = N + N / 16;
   const PlasmaParams& pp = P.pp;
   const int tid = threadIdx.x;
   const int j0 = tid * 16;
   const bool ereal = pp.ereal;
+  const bool cached = (NC == 1) && pp.powerlaw;
+  // iterate storage: species c at ub[c*NP + pad16(j)]; rho itself for NC = 1
+  R* ub = (NC == 1) ? rho : Y;
+  R* Wp = Y;          // cached W(I_j)      (NC = 1, power law)
+  R* Wm = Y + NP;     // cached W(I_{j+1/2})
   R u0[NC];
 #pragma unroll
   for (int c = 0; c < NC; ++c) u0[c] = (R)pp.rho0;
@@ -116,21 +129,116 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 #pragma unroll
     for (int c = 0; c < NC; ++c) W[c] = rate_eval<R>(pp, tabs, c, I, &S[c]);
   };
-  // gather W, ava at the three stage points of step j; W0 carried in
-  auto point_data = [&](int j, R (&W)[3][NC], R (&ava)[3], R (&S0)[NC], bool need_w0) {
+  // W and E^2 at the three stage points of step j, slope at t_j in S0
+  auto point_data = [&](int j, R (&W)[3][NC], R (&ava)[3], R (&S0)[NC]) {
     C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
     C em = (R)0.5 * (e0 + e1);
-    R Sd[NC];
-    if (need_w0) rates(intens(e0), W[0], S0);
-    rates(intens(em), W[1], Sd);
-    rates(intens(e1), W[2], Sd);
+    if (cached) {
+      W[0][0] = Wp[pad16(j)];
+      W[1][0] = Wm[pad16(j)];
+      W[2][0] = Wp[pad16(j + 1)];
+      S0[0] = tabs.sl[0][0];
+    } else {
+      R Sd[NC];
+      rates(intens(e0), W[0], S0);
+      rates(intens(em), W[1], Sd);
+      rates(intens(e1), W[2], Sd);
+    }
     ava[0] = e0.x * e0.x;
     ava[1] = em.x * em.x;
     ava[2] = e1.x * e1.x;
   };
 
+  // ---------------- rate cache and the negligible-row test
+  R wmax = 0;
+  if (cached) {
+    for (int q = 0; q < 16; ++q) {
+      int j = j0 + q;
+      R sl;
+      R w0 = rate_eval<R>(pp, tabs, 0, intens(X[pad16(j)]), &sl);
+      Wp[pad16(j)] = w0;
+      wmax = max(wmax, w0);
+      if (j < N - 1) {
+        C em = (R)0.5 * (X[pad16(j)] + X[pad16(j + 1)]);
+        R wm = rate_eval<R>(pp, tabs, 0, intens(em), &sl);
+        Wm[pad16(j)] = wm;
+        wmax = max(wmax, wm);
+      }
+    }
+  } else {
+    for (int q = 0; q < 16; ++q) {
+      int j = j0 + q;
+      R W[NC], S[NC];
+      rates(intens(X[pad16(j)]), W, S);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) wmax = max(wmax, W[c]);
+    }
+  }
+  wmax = block_max<R>(wmax, rscratch);
+  if (wmax * (R)(pp.dt * (N - 1)) < (R)pp.skip) {
+    // rho stays rho0; Kdrho = sum K W (rho_nt - rho0) to the same precision
+    for (int q = 0; q < 16; ++q) {
+      int j = j0 + q;
+      R kd = 0;
+      if (j < N - 1) {
+        R W[NC], S[NC];
+        if (cached) { W[0] = Wp[pad16(j)]; S[0] = tabs.sl[0][0]; }
+        else rates(intens(X[pad16(j)]), W, S);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          R K = pp.kdep ? S[c] : (R)pp.kfix[c];
+          kd += K * W[c] * ((R)pp.rho_nt[c] - u0[c]);
+        }
+      }
+      kdrho[pad16(j)] = kd;
+      R r = 0;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) r += u0[c];
+      rho[pad16(j)] = r;
+    }
+    __syncthreads();
+    R r0 = 0;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) r0 += u0[c];
+    return r0;
+  }
+
   // ---------------- iteration 0: photoionisation only (exact affine scan)
-  {
+  if constexpr (NC == 1) {
+    // one pass: the 16 local prefix maps stay in registers
+    Aff<R, 1> Pq[16];
+    R W[3][1], ava[3], S0[1], uz[1] = {0};
+    Aff<R, 1> G = aff_identity<R, 1>();
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      int j = j0 + q;
+      if (j < N - 1) {
+        point_data(j, W, ava, S0);
+        G = aff_compose<R, 1>(step_map<R, 1>(pp, uz, W, ava, false), G);
+      }
+      Pq[q] = G;
+    }
+    Aff<R, 1> Pin = aff_block_exclusive_scan<R, 1>(G, ascratch);
+    R v[1];
+    aff_apply<R, 1>(Pin, u0, v);
+    const R K = pp.kdep ? tabs.sl[0][0] : (R)pp.kfix[0];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      int j = j0 + q;
+      R un[1];
+      if (q == 0) ub[pad16(j)] = v[0];
+      aff_apply<R, 1>(Pq[q], v, un);
+      if (j < N - 1) {
+        if (q < 15) ub[pad16(j + 1)] = un[0];
+        R w0, sl0;
+        if (cached) { w0 = Wp[pad16(j)]; sl0 = tabs.sl[0][0]; }
+        else w0 = rate_eval<R>(pp, tabs, 0, intens(X[pad16(j)]), &sl0);
+        kdrho[pad16(j)] = (pp.kdep ? sl0 : K) * w0 * ((R)pp.rho_nt[0] - un[0]);
+      } else {
+        kdrho[pad16(j)] = 0;   // never written by the reference (plasma_equations.jl:63-70)
+      }
+    }
+  } else {
     Aff<R, NC> G = aff_identity<R, NC>();
     R W[3][NC], ava[3], S0[NC];
     R uz[NC];
@@ -139,7 +247,7 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
     for (int q = 0; q < 16; ++q) {
       int j = j0 + q;
       if (j >= N - 1) break;
-      point_data(j, W, ava, S0, true);
+      point_data(j, W, ava, S0);
       Aff<R, NC> M = step_map<R, NC>(pp, uz, W, ava, false);
       G = aff_compose<R, NC>(M, G);
     }
@@ -149,9 +257,9 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
     for (int q = 0; q < 16; ++q) {
       int j = j0 + q;
 #pragma unroll
-      for (int c = 0; c < NC; ++c) ybuf[c * N + j] = u[c];
+      for (int c = 0; c < NC; ++c) ub[c * NP + pad16(j)] = u[c];
       if (j < N - 1) {
-        point_data(j, W, ava, S0, true);
+        point_data(j, W, ava, S0);
         Aff<R, NC> M = step_map<R, NC>(pp, uz, W, ava, false);
         R un[NC];
         aff_apply<R, NC>(M, u, un);
@@ -162,68 +270,108 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
           kd += K * W[0][c] * ((R)pp.rho_nt[c] - un[c]);
           u[c] = un[c];
         }
-        kdrho[j] = kd;
+        kdrho[pad16(j)] = kd;
       } else {
-        kdrho[j] = 0;   // never written by the reference (plasma_equations.jl:63-70)
+        kdrho[pad16(j)] = 0;   // never written by the reference (plasma_equations.jl:63-70)
       }
     }
   }
   __syncthreads();
 
-  // ---------------- Newton iterations with avalanche
+  // ---------------- Newton iterations with avalanche.  The update d of
+  // iteration m estimates the error of iteration m-1; Newton's quadratic
+  // convergence leaves an error ~ d^2/|u| after it, so iteration stops when
+  // d^2 <= tol |u|^2.
   if (pp.avalanche) {
     int it = 0;
+    bool conv = false;
     for (; it < pp.maxit; ++it) {
-      R W[3][NC], ava[3], S0[NC];
-      Aff<R, NC> G = aff_identity<R, NC>();
-      for (int q = 0; q < 16; ++q) {
-        int j = j0 + q;
-        if (j >= N - 1) break;
-        R ul[NC];
-#pragma unroll
-        for (int c = 0; c < NC; ++c) ul[c] = ybuf[c * N + j];
-        point_data(j, W, ava, S0, true);
-        Aff<R, NC> M = step_map<R, NC>(pp, ul, W, ava, true);
-        G = aff_compose<R, NC>(M, G);
-      }
-      Aff<R, NC> Pin = aff_block_exclusive_scan<R, NC>(G, ascratch);
-      R u[NC];
-      aff_apply<R, NC>(Pin, u0, u);
       R dmax = 0, umax = 0;
-      for (int q = 0; q < 16; ++q) {
-        int j = j0 + q;
-        R ul[NC];
+      if constexpr (NC == 1) {
+        Aff<R, 1> Pq[16];
+        R ul[16];
+        R W[3][1], ava[3], S0[1];
+        Aff<R, 1> G = aff_identity<R, 1>();
 #pragma unroll
-        for (int c = 0; c < NC; ++c) {
-          ul[c] = ybuf[c * N + j];
-          dmax = max(dmax, fabs(u[c] - ul[c]));
-          umax = max(umax, fabs(u[c]));
-          ybuf[c * N + j] = u[c];
+        for (int q = 0; q < 16; ++q) {
+          int j = j0 + q;
+          ul[q] = ub[pad16(j)];
+          if (j < N - 1) {
+            point_data(j, W, ava, S0);
+            G = aff_compose<R, 1>(step_map<R, 1>(pp, &ul[q], W, ava, true), G);
+          }
+          Pq[q] = G;
         }
-        if (j < N - 1) {
-          point_data(j, W, ava, S0, true);
-          Aff<R, NC> M = step_map<R, NC>(pp, ul, W, ava, true);
-          R un[NC];
-          aff_apply<R, NC>(M, u, un);
+        Aff<R, 1> Pin = aff_block_exclusive_scan<R, 1>(G, ascratch);  // syncs: old values all read
+        R v[1];
+        aff_apply<R, 1>(Pin, u0, v);
 #pragma unroll
-          for (int c = 0; c < NC; ++c) u[c] = un[c];
+        for (int q = 0; q < 16; ++q) {
+          int j = j0 + q;
+          R un;
+          if (q == 0) {
+            un = v[0];
+          } else {
+            R t[1];
+            aff_apply<R, 1>(Pq[q - 1], v, t);
+            un = t[0];
+          }
+          dmax = max(dmax, fabs(un - ul[q]));
+          umax = max(umax, fabs(un));
+          ub[pad16(j)] = un;
+        }
+      } else {
+        R W[3][NC], ava[3], S0[NC];
+        Aff<R, NC> G = aff_identity<R, NC>();
+        for (int q = 0; q < 16; ++q) {
+          int j = j0 + q;
+          if (j >= N - 1) break;
+          R ul[NC];
+#pragma unroll
+          for (int c = 0; c < NC; ++c) ul[c] = ub[c * NP + pad16(j)];
+          point_data(j, W, ava, S0);
+          Aff<R, NC> M = step_map<R, NC>(pp, ul, W, ava, true);
+          G = aff_compose<R, NC>(M, G);
+        }
+        Aff<R, NC> Pin = aff_block_exclusive_scan<R, NC>(G, ascratch);
+        R u[NC];
+        aff_apply<R, NC>(Pin, u0, u);
+        for (int q = 0; q < 16; ++q) {
+          int j = j0 + q;
+          R ul[NC];
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            ul[c] = ub[c * NP + pad16(j)];
+            dmax = max(dmax, fabs(u[c] - ul[c]));
+            umax = max(umax, fabs(u[c]));
+            ub[c * NP + pad16(j)] = u[c];
+          }
+          if (j < N - 1) {
+            point_data(j, W, ava, S0);
+            Aff<R, NC> M = step_map<R, NC>(pp, ul, W, ava, true);
+            R un[NC];
+            aff_apply<R, NC>(M, u, un);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) u[c] = un[c];
+          }
         }
       }
       dmax = block_max<R>(dmax, rscratch);
       umax = block_max<R>(umax, rscratch);
-      if (dmax <= (R)pp.tol * umax) break;
+      if (dmax * dmax <= (R)pp.tol * umax * umax) { conv = true; break; }
     }
-    if (it >= pp.maxit && tid == 0) *newton_flag = 1;
+    if (!conv && tid == 0) *newton_flag = 1;
+    if (tid == 0) atomicMax(&P.ctl->newton_max, it + 1);
   }
   // ---------------- rho = sum of species
   R rmax = 0;
   for (int q = 0; q < 16; ++q) {
     int j = j0 + q;
-    R s = 0;
+    R sm = 0;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) s += ybuf[c * N + j];
-    rho[j] = s;
-    rmax = max(rmax, s);
+    for (int c = 0; c < NC; ++c) sm += ub[c * NP + pad16(j)];
+    if (NC > 1) rho[pad16(j)] = sm;
+    rmax = max(rmax, sm);
   }
   __syncthreads();
   return block_max<R>(rmax, rscratch);
@@ -244,9 +392,9 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* X = reinterpret_cast<C*>(smem_raw);
   C* Y = X + NP;
-  R* rho = reinterpret_cast<R*>(Y + NP);
-  R* kdrho = rho + N;
-  R* rscratch = kdrho + N;                               // 32
+  R* rho = reinterpret_cast<R*>(Y + NP);                 // [NP], pad16 index
+  R* kdrho = rho + NP;
+  R* rscratch = kdrho + NP;                              // 32
   Aff<R, (NC > 0 ? NC : 1)>* ascratch = reinterpret_cast<Aff<R, (NC > 0 ? NC : 1)>*>(rscratch + 32);
   PlasmaSmem<R>* tabs = reinterpret_cast<PlasmaSmem<R>*>(ascratch + 32);
   __shared__ int s_flag;
@@ -277,14 +425,14 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
       R rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag);
       if (tid == 0) {
         atomic_max_nonneg(&ctl->rhomax_acc, (double)rmax);
-        P.rho_end[row] = (double)rho[N - 1];
+        P.rho_end[row] = (double)rho[pad16(N - 1)];
         if (s_flag) atomicOr(&ctl->flags, FIL_FLAG_NEWTON);
       }
       if (P.store_plasma) {
         for (int m = 0; m < 16; ++m) {
           int j = tid + m * T;
-          P.rho_g[(size_t)row * N + j] = rho[j];
-          P.kdrho_g[(size_t)row * N + j] = kdrho[j];
+          P.rho_g[(size_t)row * N + j] = rho[pad16(j)];
+          P.kdrho_g[(size_t)row * N + j] = kdrho[pad16(j)];
         }
       }
     }
@@ -330,11 +478,11 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
         R g = gs * P.gt[P.gt_bug ? iy : j];
         R fc = 0, ff = 0, fl = 0;
         if (P.has_cubic) fc = P.cubic_thg ? re * re * re : (R)0.75 * I * re;
-        if (NC > 0 && P.has_free) ff = rho[j] * re;
+        if (NC > 0 && P.has_free) ff = rho[pad16(j)] * re;
         if (NC > 0 && P.has_losses) {
           R Il = P.losses_ereal ? re * re : I;
           R inv = (Il >= (R)1e-30) ? (R)1 / Il : (R)0;
-          fl = kdrho[j] * inv * re;
+          fl = kdrho[pad16(j)] * inv * re;
         }
         X[pad16(j)] = mk<R>(g * (R)P.sc * fc, 0);
         Y[pad16(j)] = mk<R>(g * (R)P.sf * ff, g * (R)P.sl * fl);

@@ -41,9 +41,12 @@ def test_kerr_step(gpu_lib, precision, alg):
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 @pytest.mark.parametrize("species", [1, 2])
-def test_plasma_density(gpu_lib, precision, species):
-    """rho(t) and Kdrho(t) of the parallel scan vs the sequential RK solve."""
-    kw = dict(PPcr=150.0)
+@pytest.mark.parametrize("rmax", [2.0, 5.0])
+def test_plasma_density(gpu_lib, precision, species, rmax):
+    """rho(t) and Kdrho(t) of the parallel scan vs the sequential RK solve.
+    rmax = 5 mm puts the outer rows below the rate cut-off where the row is
+    left at rho0 without a scan."""
+    kw = dict(PPcr=150.0, rmax=rmax)
     inp = rt_input(**kw)
     if species == 2:
         inp["p_model"][1]["components"] = two_species_rates()
