@@ -32,7 +32,15 @@ DECK = os.path.join(PKG, "decks", "filament_RT", "input.py")
 
 WORKLOAD = dict(Nr=1000, Nt=4096, rmax=5.0, tmin=-200.0, tmax=200.0, PPcr=5.0, ALG="RK4",
                 dzphimax=0.1, dz_initial=1e-2, zmax=3.0)
-WORKLOAD_NAME = "RT filamentation Nr=1000 x Nt=4096, RK4, 5 Pcr, adaptive dz (phimax 0.1 rad), z_end 3 m"
+# The explicit RK nonlinear step of the reference becomes unstable in this
+# workload near z = 2.29 m (the Drude free-current term grows like 1/w at the
+# lowest frequency bins and leaves the RK4 stability region once the
+# filament's plasma forms); both precision forms diverge at the same step.
+# Accuracy is compared at z = 2.25 m, after the collapse, with the intensity
+# clamped by the plasma; throughput loops stay below STABLE_Z.
+ACCURACY_ZEND = 2.25
+STABLE_Z = 2.2
+WORKLOAD_NAME = "RT filamentation Nr=1000 x Nt=4096, RK4, 5 Pcr, adaptive dz (phimax 0.1 rad)"
 
 
 def _env_rank():
@@ -42,7 +50,7 @@ def _env_rank():
 
 def _config(args, extra=None):
     c = {"workload": WORKLOAD_NAME, "Nr": WORKLOAD["Nr"], "Nt": WORKLOAD["Nt"], "alg": "RK4",
-         "z_end_m": WORKLOAD["zmax"], "l2": "512 MB buffer written before every timed step",
+         "timed_range_m": [0.0, args.accuracy_zend], "l2": "512 MB buffer written before every timed step",
          "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
     if extra:
         c.update(extra)
@@ -111,36 +119,36 @@ def _prepare(**over):
     return fg.prepare(DECK, **kw)
 
 
-def time_device_loop(precision, warmup, steps, load_seconds=0.0):
-    """Warm-up in graph mode, then `steps` timed steps (flushed L2), then
-    the same steps in graph mode (warm L2, for information); with
-    load_seconds > 0 the graph-mode loop continues that long so the clock
+def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0):
+    """Warm-up steps in graph mode, then the timed steps from z = 0 (the
+    field re-uploaded) up to `steps` steps or z = zend, one at a time with L2
+    flushed, then the same range in graph mode (warm L2, for information);
+    with load_seconds > 0 graph-mode runs continue that long so the clock
     sampler sees the kernels under sustained load."""
     import filament_gb as fg
     from filament_gb import _abi
     inp = _prepare()
     sim = fg.Simulation(inp, precision=precision)
     h = sim.handle
-    code, st = h.run(0.0, inp["zmax"], warmup)
+    h.run(0.0, zend, warmup)
+    h.set_field(sim.field.E0, analytic=False)
     h.set_option(_abi.OPT_TIMING, 1)
     t0 = time.perf_counter()
-    code, st2 = h.run(st["z"], inp["zmax"], steps)
+    code, st2 = h.run(0.0, zend, steps)
     wall = time.perf_counter() - t0
     kt = h.kernel_times(6)
     h.set_option(_abi.OPT_TIMING, 0)
-    # warm (graph) throughput for information
+    h.set_field(sim.field.E0, analytic=False)
     t1 = time.perf_counter()
-    code3, st3 = h.run(st2["z"], inp["zmax"], steps)
+    code3, st3 = h.run(0.0, zend, steps)
     graph_wall = time.perf_counter() - t1
     t2 = time.perf_counter()
-    z = st3["z"]
-    while time.perf_counter() - t2 < load_seconds and z < inp["zmax"]:
-        _, stl = h.run(z, inp["zmax"], 200)
-        z = stl["z"]
+    while time.perf_counter() - t2 < load_seconds:
+        h.set_field(sim.field.E0, analytic=False)
+        h.run(0.0, STABLE_Z, 10 ** 9)
     res = {"ms_per_step": kt[4], "row_ms": kt[0], "dht_fwd_ms": kt[1], "dht_inv_ms": kt[2],
-           "reduce_ms": kt[3], "timed_steps": int(kt[5]), "wall_s": wall,
-           "graph_steps_per_s": (st3["steps"] - st2["steps"]) / graph_wall if graph_wall > 0 else None,
-           "z_after": st3["z"]}
+           "reduce_ms": kt[3], "timed_steps": int(kt[5]), "z_end": st2["z"], "wall_s": wall,
+           "graph_steps_per_s": st3["steps"] / graph_wall if graph_wall > 0 else None}
     sim.close()
     return res
 
@@ -218,12 +226,13 @@ def cpu_oracle(steps):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000000,
+                    help="timed z-steps (default: the whole run to the accuracy z_end)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=30)
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--accuracy-zend", type=float, default=WORKLOAD["zmax"])
+    ap.add_argument("--accuracy-zend", type=float, default=ACCURACY_ZEND)
     args = ap.parse_args()
     rank, local_rank, world = _env_rank()
     if world > 1:
@@ -259,9 +268,9 @@ def main():
     if dist is not None:
         dist.barrier()
     sampler.start()
-    mixed = time_device_loop("mixed", args.warmup, args.steps, load_seconds=3.0)
+    mixed = time_device_loop("mixed", args.warmup, args.steps, args.accuracy_zend, load_seconds=3.0)
     clocks = sampler.stop()
-    fp64 = time_device_loop("fp64", args.warmup, max(3, args.steps // 10))
+    fp64 = time_device_loop("fp64", args.warmup, args.steps, args.accuracy_zend)
     t_local = mixed["ms_per_step"]
     if dist is not None:
         import torch
@@ -271,7 +280,7 @@ def main():
     value = world * 1000.0 / t_local
     if rank != 0:
         return
-    e2e = e2e_host_loop(max(10, args.steps // 2))
+    e2e = e2e_host_loop(max(10, min(300, mixed["timed_steps"])))
     acc = None if args.no_accuracy else accuracy_run(args.accuracy_zend, 200000)
     sps_cpu, cpu_wall = cpu_oracle(args.cpu_steps)
     hbm, bf16, src = _peaks()
@@ -284,7 +293,7 @@ def main():
     achieved = b_row / (mixed["row_ms"] * 1e-3) / 1e9
     line = {
         "metric": "RT z-steps/s", "value": value, "unit": "z-steps/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_local,
+        "steps": mixed["timed_steps"], "warmup": args.warmup, "ms_per_step": t_local,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
         "data": "synthetic", "config": _config(args),
         "forms": {"mixed": mixed, "fp64": fp64,
@@ -299,7 +308,7 @@ def main():
                                    % (args.cpu_steps, cpu_wall)},
         "e2e": e2e,
         "clocks": clocks,
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": 6 * mixed["timed_steps"],
     }
     print(json.dumps(line))
 
