@@ -1,0 +1,46 @@
+# FilamentGB.jl -- ccall binding of libfilament_gb.so for Filament.jl.
+# Mirrors include/filament_gb.h; see INTEGRATION.md for the replacement of
+# Filament.main_loop (src/Filament.jl:111-184).  Not executed in this
+# environment (no Julia); the Python binding filament_gb/_abi.py is the
+# tested twin.
+module FilamentGB
+const LIB = joinpath(@__DIR__, "..", "_build", "libfilament_gb.so")
+
+# mirrors fil_config / fil_tables / fil_stats of include/filament_gb.h field by field
+struct FilConfig
+    abi_version::Int32; geometry::Int32; precision::Int32; alg::Int32
+    n1::Int32; n2::Int32; nt::Int32
+    nonlinearity::Int32; plasma::Int32; kparaxial::Int32; qparaxial::Int32
+    resp_mask::UInt32; cubic_thg::Int32; losses_ereal::Int32; raman_thg::Int32
+    plasma_alg::Int32; plasma_ereal::Int32; plasma_kdep::Int32; plasma_ncomp::Int32
+    rate_n::Int32; reserved_i::NTuple{8,Int32}
+    dt::Float64; dz0::Float64; phimax::Float64; phik::Float64; phip::Float64
+    istop::Float64; rho0::Float64; dxdy::Float64; reserved_d::NTuple{8,Float64}
+end
+struct FilTables            # 25 pointers, in header order; C_NULL for absent tables
+    p::NTuple{25,Ptr{Float64}}
+end
+struct FilStats
+    z::Float64; dz::Float64; imax::Float64; rhomax::Float64; energy::Float64
+    steps::Int64; status::Int32; flags::Int32
+end
+
+function create(cfg::FilConfig, tab::FilTables)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:fil_create, LIB), Cint, (Ref{FilConfig}, Ref{FilTables}, Ref{Ptr{Cvoid}}), cfg, tab, h)
+    rc < 0 && error(unsafe_string(ccall((:fil_last_error, LIB), Cstring, (Ptr{Cvoid},), C_NULL)))
+    return h[]
+end
+set_field(h, E::Array{ComplexF64}) =                      # column-major E[Nr, Nt], real signal
+    ccall((:fil_set_field, LIB), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}, Cint, Cint, Cint), h, E, 1, 0, 0)
+zstep(h, z, dz) = ccall((:fil_step, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cdouble), h, z, dz)
+function run!(h, z0, zmax, nmax)
+    st = Ref{FilStats}()
+    rc = ccall((:fil_run, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cdouble, Int64, Ref{FilStats}), h, z0, zmax, nmax, st)
+    return rc, st[]
+end
+analyze(h, F, P, rho_end) = ccall((:fil_analyze, LIB), Cint,
+    (Ptr{Cvoid}, Ptr{FilStats}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), h, C_NULL, F, P, rho_end)
+get_field!(h, E::Array{ComplexF64}) =
+    ccall((:fil_get_field, LIB), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}, Cint, Cint), h, E, 1, 0)
+end

@@ -21,6 +21,16 @@
 //   main loop                     src/Filament.jl:123-172
 //   analyzer reductions           src/modules/FieldAnalyzers.jl:120-215, 272-353
 //
+// Pinning: the linear path (QDHT, KZ, t-FFT, analytic signal, guards) is
+// pinned by the reference's five closed-form physics tests
+// (test/test_diffraction_r.jl, test_diffraction_rt.jl, test_diffraction_xy.jl,
+// test_dispersion_t.jl, test_dispersion_rt.jl), run against this oracle in
+// tests/test_oracle_known_answers.py with the reference's tolerances.  The
+// nonlinear responses, the plasma equation, the RK tableaux and the adaptive
+// step have no reference test and no runnable reference here (Julia is
+// absent): for those parts parity is unpinned; they follow the cited source
+// lines.
+//
 // Choices where the reference relies on un-vendored dependencies:
 //   * QDHT (HankelTransforms): E <- diag(1/s) T D T diag(s) E on the first
 //     half(Nt) = Nt/2 frequency columns (Fields.jl:108-110); the columns
