@@ -67,6 +67,8 @@ struct fil_handle {
   size_t flushbytes = 0;
 };
 
+void fil_set_global_error(const std::string& m) { g_err = m; }
+
 static int fail(fil_handle* h, int code, const std::string& m) {
   if (h) h->err = m; else g_err = m;
   return code;

@@ -2,7 +2,12 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "common.cuh"
+
+// sets the message that fil_last_error(NULL) returns
+void fil_set_global_error(const std::string& m);
 
 struct DevCtl;
 template <typename R> struct RowParams;

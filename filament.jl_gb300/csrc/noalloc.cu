@@ -1,0 +1,98 @@
+// noalloc.cu -- the linear propagator of an RT z-step on caller-owned device
+// buffers, without any device allocation.
+//
+// Some callers cannot allocate device memory at the point where they need
+// the propagator: code that runs inside a region where cudaMalloc is not
+// allowed (for example while the caller itself is capturing a CUDA graph, or
+// in a host that pre-reserves all device memory and hands out fixed pools),
+// or a caller that must not grow the process's memory footprint after start-
+// up.  fil_hankel_propagate_noalloc serves them: the caller passes every
+// input and the output; the one intermediate (the Hankel-transformed,
+// propagated spectrum) lives in a file-scope __device__ array of fixed size
+// that every GPU loading this library holds until the process exits.
+#include <mutex>
+#include <string>
+
+#include "../../include/filament_gb.h"
+#include "launch.h"
+#include "rowkernels.cuh"
+#include "dht_simt.cuh"
+
+// 4 Mi floats = 16 MiB: one [128-padded Nr][Nt] real view of the half
+// spectrum up to Nr <= 1024, Nt <= 4096.
+#define FIL_NOALLOC_MAX_FLOATS (4u << 20)
+#define FIL_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) float g_noalloc_scratch[FIL_NOALLOC_MAX_FLOATS];
+static __device__ DevCtl g_noalloc_ctl;
+
+namespace {
+std::mutex g_mu;
+float* g_scratch[FIL_NOALLOC_MAX_DEVICES];
+DevCtl* g_ctl[FIL_NOALLOC_MAX_DEVICES];
+
+// the message is read back with fil_last_error(NULL)
+int noalloc_fail(int code, const std::string& m) {
+  fil_set_global_error(m);
+  return code;
+}
+
+__global__ void k_noalloc_arm(DevCtl* c, double dz) {
+  c->done = 0;
+  c->dz = dz;
+}
+}  // namespace
+
+extern "C" int fil_hankel_propagate_noalloc(const float* m1, const float* m2, const float* kt2, const float* beta,
+                                            const float* dfr, const float* kmax2, const float* wg, int kparaxial,
+                                            const float* in, float* out, int mpad, int nh, double dz,
+                                            void* stream) {
+  if (!m1 || !m2 || !kt2 || !beta || !dfr || !in || !out) return noalloc_fail(FIL_ERR_ARG, "null pointer argument");
+  if (mpad <= 0 || mpad % 128 != 0) return noalloc_fail(FIL_ERR_ARG, "mpad must be a positive multiple of 128");
+  if (nh <= 0 || (2 * nh) % 128 != 0) return noalloc_fail(FIL_ERR_ARG, "2*nh must be a positive multiple of 128");
+  const unsigned long long need = (unsigned long long)mpad * (unsigned long long)(2 * nh);
+  if (need > FIL_NOALLOC_MAX_FLOATS)
+    return noalloc_fail(FIL_ERR_ARG, "mpad * 2 * nh = " + std::to_string(need) +
+                                         " exceeds the fixed scratch of " + std::to_string(FIL_NOALLOC_MAX_FLOATS) +
+                                         " floats (16 MiB)");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return noalloc_fail(FIL_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= FIL_NOALLOC_MAX_DEVICES) return noalloc_fail(FIL_ERR_ARG, "device index out of range");
+  float* scratch;
+  DevCtl* ctl;
+  {
+    // one-time set-up per device, with that device current: the device
+    // addresses of the static arrays (the host-side names are not device
+    // addresses)
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_scratch[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess)
+        return noalloc_fail(FIL_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+      void* q = nullptr;
+      e = cudaGetSymbolAddress(&q, g_noalloc_ctl);
+      if (e != cudaSuccess)
+        return noalloc_fail(FIL_ERR_CUDA, std::string("cudaGetSymbolAddress(ctl): ") + cudaGetErrorString(e));
+      g_scratch[dev] = (float*)p;
+      g_ctl[dev] = (DevCtl*)q;
+    }
+    scratch = g_scratch[dev];
+    ctl = g_ctl[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  PropParams<float> pp;
+  pp.kt2 = kt2;
+  pp.beta = (const float2*)beta;
+  pp.dfr = (const float2*)dfr;
+  pp.kmax2 = kmax2;
+  pp.wg = wg;
+  pp.kparaxial = kparaxial;
+  k_noalloc_arm<<<1, 1, 0, st>>>(ctl, dz);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_dht_simt<float>(m1, in, scratch, mpad, 2 * nh, mpad, pp, ctl, 1, st);
+  if (e == cudaSuccess) e = launch_dht_simt<float>(m2, scratch, out, mpad, 2 * nh, mpad, pp, ctl, 2, st);
+  if (e != cudaSuccess) return noalloc_fail(FIL_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  return FIL_OK;
+}

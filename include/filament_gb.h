@@ -250,6 +250,29 @@ int fil_get_stats(fil_handle* h, fil_stats* st);
  * 3 reductions + controller, 4 whole step; ms[5] = number of timed steps. */
 int fil_kernel_times(fil_handle* h, double* ms, int n);
 
+/* ---- linear propagator without device allocation ----------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory where they need the step (inside a region where cudaMalloc is not
+ * allowed, or a host that hands out fixed device pools): applies the linear
+ * propagator of an RT z-step, out = M2 P M1 in, to caller-owned FP32 device
+ * buffers, where M1 = T diag(s) and M2 = diag(1/s) T are the Hankel pair
+ * ([mpad][mpad], row-major, zero padded), `in`/`out` are the half spectrum
+ * [mpad][nh] complex (interleaved), and P = exp(i KZ dz) * guard is built from
+ * kt2[mpad] (kt^2, zu units), beta[2*nh], dfr[2*nh] (interleaved complex),
+ * kmax2[nh] and wg[nh] (NULL = no guard), with KPARAXIAL as kparaxial.
+ * mpad and 2*nh must be multiples of 128 and mpad*2*nh <= 4194304.
+ * The one intermediate lives in a fixed 16 MiB __device__ array that every
+ * GPU loading this library holds until exit; the call allocates and frees
+ * nothing.  The first call on a device looks up that array's device address
+ * (do it before any stream capture).  All calls share the array: calls that
+ * overlap on the GPU (different streams or threads) race.  Runs on `stream`
+ * (NULL = default stream) and returns without synchronising; errors go to
+ * fil_last_error(NULL).                                                     */
+int fil_hankel_propagate_noalloc(const float* m1, const float* m2, const float* kt2,
+                                 const float* beta, const float* dfr, const float* kmax2,
+                                 const float* wg, int kparaxial, const float* in, float* out,
+                                 int mpad, int nh, double dz, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,9 +32,13 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_oracle_exports_same_abi(oracle_binding):
+    """The oracle mirrors the problem-handle ABI; the handle-free device
+    buffer entry point has no CPU counterpart."""
     import oracle
     lib = ctypes.CDLL(oracle.LIB)
     for n in declared_functions():
+        if n == "fil_hankel_propagate_noalloc":
+            continue
         assert hasattr(lib, "filo_" + n[4:]), n
 
 
