@@ -22,6 +22,8 @@
 #include "launch.h"
 #include "rowkernels.cuh"
 #include "dht_simt.cuh"
+#include "dht_tc.cuh"
+#include "tc_host.h"
 
 namespace {
 thread_local std::string g_err;
@@ -65,6 +67,13 @@ struct fil_handle {
   long tcount = 0;
   void* flushbuf = nullptr;            // > L2, benchmark timing only
   size_t flushbytes = 0;
+  // tensor-core Hankel path (mixed form)
+  bool use_tc = false;
+  void* Th = nullptr; void* Tl = nullptr;      // [mpad][mpad] TF32 head / remainder of T
+  void* kzt = nullptr; void* gdt = nullptr;    // [mpad][nh] KZ (float2), guard (float)
+  void* s_row = nullptr; void* inv_s = nullptr;
+  int* tc_err = nullptr;
+  CUtensorMap tm_th, tm_tl, tm_w1, tm_w2;
 };
 
 void fil_set_global_error(const std::string& m) { g_err = m; }
@@ -116,13 +125,30 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
   const fil_config& c = h->cfg;
   const int n1 = h->n1, nt = h->nt, nh = h->nh, mp = h->mpad, nr = h->nrows;
   typedef std::complex<double> cd;
-  // twiddles exp(-2 pi i m / nt)
+  // twiddles exp(-2 pi i m / nt); in single precision each entry is the
+  // pair of FP32 neighbours of (cos, sin) whose magnitude is closest to 1,
+  // so that the table carries no systematic gain
   {
     std::vector<double> v(2 * nt);
     for (int m = 0; m < nt; ++m) {
       double a = -2.0 * M_PI * (double)m / (double)nt;
-      v[2 * m] = std::cos(a);
-      v[2 * m + 1] = std::sin(a);
+      double c = std::cos(a), sn = std::sin(a);
+      v[2 * m] = c;
+      v[2 * m + 1] = sn;
+      if (sizeof(R) == 4) {
+        float cf = (float)c, sf = (float)sn, bc = cf, bs = sf;
+        double best = 1e300;
+        for (int dc = -1; dc <= 1; ++dc)
+          for (int ds = -1; ds <= 1; ++ds) {
+            float cc = cf, ss = sf;
+            if (dc) cc = std::nextafter(cf, dc > 0 ? 2.0f : -2.0f);
+            if (ds) ss = std::nextafter(sf, ds > 0 ? 2.0f : -2.0f);
+            double err = std::fabs((double)cc * cc + (double)ss * ss - 1.0);
+            if (err < best) { best = err; bc = cc; bs = ss; }
+          }
+        v[2 * m] = bc;
+        v[2 * m + 1] = bs;
+      }
     }
     if (upload<R>(h, &h->tw, v)) return FIL_ERR_CUDA;
   }
@@ -249,6 +275,67 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
   return 0;
 }
 
+// Tables of the tensor-core Hankel path: T split into an exact TF32 head and
+// the nearest-TF32 remainder, the propagator's KZ and guard per (r, w), the
+// row scales s and 1/s, and the TMA maps of the operands.
+static uint32_t f_bits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+static float bits_f(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+static int create_tc(fil_handle* h, const fil_tables* t) {
+  typedef std::complex<double> cd;
+  const int n1 = h->n1, nh = h->nh, mp = h->mpad;
+  std::vector<float> th((size_t)mp * mp, 0.f), tl((size_t)mp * mp, 0.f);
+  for (int i = 0; i < n1; ++i)
+    for (int k = 0; k < n1; ++k) {
+      double T = t->dht[(size_t)i * n1 + k];
+      float hd = bits_f(f_bits((float)T) & 0xFFFFE000u);
+      float lo = (float)(T - (double)hd);
+      lo = bits_f((f_bits(lo) + 0x1000u) & 0xFFFFE000u);
+      th[(size_t)i * mp + k] = hd;
+      tl[(size_t)i * mp + k] = lo;
+    }
+  std::vector<float> kz((size_t)mp * nh * 2, 0.f), gd((size_t)mp * nh, 0.f), sr(mp, 0.f), is(mp, 0.f);
+  for (int i = 0; i < n1; ++i) {
+    double kt2 = t->kt1[i] * t->kt1[i];
+    sr[i] = (float)t->dht_s[i];
+    is[i] = (float)(1.0 / t->dht_s[i]);
+    for (int j = 0; j < nh; ++j) {
+      cd b(t->beta[2 * j], t->beta[2 * j + 1]), d(t->dfr[2 * j], t->dfr[2 * j + 1]);
+      cd K = d;
+      if (h->cfg.kparaxial) {
+        if (b != cd(0, 0)) K = d - kt2 / (2.0 * b);
+      } else {
+        cd den = b + std::sqrt(b * b - kt2 + cd(0.0, 0.0));
+        if (den != cd(0, 0)) K = d - kt2 / den;
+      }
+      double g = 1.0;
+      if (t->kmax) {
+        double km = t->kmax[j];
+        g = (km == 0.0) ? 0.0 : std::exp(-std::pow(kt2 / (km * km), 20));
+      }
+      if (t->wguard) g *= t->wguard[j];
+      kz[((size_t)i * nh + j) * 2] = (float)K.real();
+      kz[((size_t)i * nh + j) * 2 + 1] = (float)K.imag();
+      gd[(size_t)i * nh + j] = (float)g;
+    }
+  }
+  auto up = [&](void** dst, const std::vector<float>& v) -> int {
+    CK(cudaMalloc(dst, v.size() * sizeof(float)));
+    CK(cudaMemcpy(*dst, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return 0;
+  };
+  if (up(&h->Th, th) || up(&h->Tl, tl) || up(&h->kzt, kz) || up(&h->gdt, gd) || up(&h->s_row, sr) ||
+      up(&h->inv_s, is))
+    return FIL_ERR_CUDA;
+  CK(cudaMalloc(&h->tc_err, sizeof(int)));
+  CK(cudaMemset(h->tc_err, 0, sizeof(int)));
+  if (tc_make_map(&h->tm_th, (const float*)h->Th, mp, mp, 32, 128) ||
+      tc_make_map(&h->tm_tl, (const float*)h->Tl, mp, mp, 32, 128) ||
+      tc_make_map(&h->tm_w1, (const float*)h->W1, mp, 2 * nh, 32, 128) ||
+      tc_make_map(&h->tm_w2, (const float*)h->W2, mp, 2 * nh, 32, 128))
+    return fail(h, FIL_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return 0;
+}
+
 template <typename R> static RowParams<R> row_params(fil_handle* h) {
   typedef typename C2T<R>::type C;
   RowParams<R> P;
@@ -285,6 +372,8 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
   P.store_plasma = h->store_plasma ? 1 : 0;
   P.rho_end = h->rho_end;
   P.ctl = h->ctl;
+  P.out_T = 0;
+  P.ldT = h->mpad;
   return P;
 }
 
@@ -308,12 +397,42 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   P.S_out = (typename C2T<R>::type*)h->W1;
   PropParams<R> pp = prop_params<R>(h);
   const int Nc = 2 * h->nh;
+  const bool tcp = h->use_tc && sizeof(R) == 4;
+  if (tcp) {
+    P.out_T = 1;
+    P.out_scale = (const R*)h->s_row;
+  }
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
   CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
   if (timed) CK(cudaEventRecord(h->ev[2], h->st));
-  CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 1, h->st));
-  if (timed) CK(cudaEventRecord(h->ev[3], h->st));
-  CK(launch_dht_simt<R>((const R*)h->M2, (const R*)h->W2, (R*)h->S, h->mpad, Nc, h->mpad, pp, h->ctl, 2, h->st));
+  if (tcp) {
+    TcGemmParams p1;
+    std::memset(&p1, 0, sizeof p1);
+    p1.out = (float*)h->W2;
+    p1.ldo = h->mpad;
+    p1.K = h->mpad;
+    p1.mode = 1;
+    p1.kz = (const float2*)h->kzt;
+    p1.gd = (const float*)h->gdt;
+    p1.nh = h->nh;
+    p1.ctl = h->ctl;
+    p1.err = h->tc_err;
+    // expected value of the round-toward-zero error of each chunk result:
+    // ~ -2^-23 relative for log-uniformly distributed mantissas
+    p1.rz_fix = 1.0f + 1.1920928955078125e-07f;
+    CK(launch_dht_tc2(h->tm_th, h->tm_tl, h->tm_w1, p1, h->mpad, Nc, h->st));
+    if (timed) CK(cudaEventRecord(h->ev[3], h->st));
+    TcGemmParams p2 = p1;
+    p2.out = (float*)h->S;
+    p2.ldo = Nc;
+    p2.mode = 2;
+    p2.inv_s = (const float*)h->inv_s;
+    CK(launch_dht_tc2(h->tm_th, h->tm_tl, h->tm_w2, p2, h->mpad, Nc, h->st));
+  } else {
+    CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 1, h->st));
+    if (timed) CK(cudaEventRecord(h->ev[3], h->st));
+    CK(launch_dht_simt<R>((const R*)h->M2, (const R*)h->W2, (R*)h->S, h->mpad, Nc, h->mpad, pp, h->ctl, 2, h->st));
+  }
   if (timed) CK(cudaEventRecord(h->ev[4], h->st));
   return 0;
 }
@@ -332,6 +451,15 @@ static int reduce(fil_handle* h, double* power, int check_done) {
   return h->fp64 ? enqueue_reduce<double>(h, power, check_done) : enqueue_reduce<float>(h, power, check_done);
 }
 
+static int check_tc(fil_handle* h) {
+  if (!h->tc_err) return 0;
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (e) return fail(h, FIL_ERR_TIMEOUT, "a tensor-core pipeline wait timed out");
+  return 0;
+}
+
 static int read_ctl(fil_handle* h) {
   CK(cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -341,7 +469,8 @@ static int read_ctl(fil_handle* h) {
 static void free_all(fil_handle* h) {
   void* bufs[] = {h->S, h->W1, h->W2, h->M1, h->M2, h->tw, h->g1, h->g2, h->gt, h->Cc, h->Cf, h->Cl,
                   h->kt2, h->beta, h->dfr, h->kmax2, h->wg, h->rho_g, h->kdrho_g, h->stage,
-                  h->fluence, h->power, h->pw, h->rho_end, h->ctl, h->flushbuf};
+                  h->fluence, h->power, h->pw, h->rho_end, h->ctl, h->flushbuf,
+                  h->Th, h->Tl, h->kzt, h->gdt, h->s_row, h->inv_s, h->tc_err};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -506,6 +635,10 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   CKC(cudaMemset(h->ctl, 0, sizeof(DevCtl)));
   CKC(cudaMallocHost(&h->ctl_host, sizeof(DevCtl)));
   rc = h->fp64 ? create_tables<double>(h, t) : create_tables<float>(h, t);
+  if (!rc && !h->fp64 && h->nh * 2 % 128 == 0) {
+    rc = create_tc(h, t);
+    h->use_tc = (rc == 0);
+  }
   if (rc) {
     g_err = h->err;
     free_all(h);
@@ -536,6 +669,8 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
     h->timing = value != 0;
     for (int i = 0; i < 5; ++i) h->tsum[i] = 0;
     h->tcount = 0;
+  } else if (option == FIL_OPT_DHT_SIMT) {
+    if (!h->fp64) h->use_tc = (value == 0) && h->Th != nullptr;
   } else if (option == FIL_OPT_ANALYTIC_PROJECTION) {
     // the field state is the analytic half spectrum: always projected
   }
@@ -592,6 +727,8 @@ int fil_step(fil_handle* h, double z, double dz) {
   int rc = zstep(h, false);
   if (rc) return rc;
   CK(cudaStreamSynchronize(h->st));
+  rc = check_tc(h);
+  if (rc) return rc;
   return FIL_OK;
 }
 
@@ -678,6 +815,10 @@ int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stat
     if (rc) return rc;
     if (h->ctl_host->done) break;
   }
+  }
+  {
+    int rc = check_tc(h);
+    if (rc) return rc;
   }
   const DevCtl& r = *h->ctl_host;
   if (stats) {

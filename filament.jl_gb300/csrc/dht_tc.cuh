@@ -47,7 +47,19 @@ struct TcGemmParams {
   DevCtl* ctl;       // NULL: no controller (dz = dz_fixed)
   float dz_fixed;
   int* err;          // set to 1 on a timed-out wait
+  float rz_fix;      // factor applied to each chunk of the head product as it
+                     // is summed (de-biasing of round-toward-zero), see dht_tc2.cuh
 };
+
+// nearest TF32 value (ties away from zero); exact TF32 operands are not
+// altered by the tensor core's conversion, so rounding here keeps the
+// remainder terms unbiased
+__device__ __forceinline__ float tf32_round1(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+__device__ __forceinline__ float4 tf32_round(float4 v) {
+  return make_float4(tf32_round1(v.x), tf32_round1(v.y), tf32_round1(v.z), tf32_round1(v.w));
+}
 
 __device__ __forceinline__ float4 tf32_head(float4 v) {
   const unsigned m = 0xFFFFE000u;
@@ -55,7 +67,7 @@ __device__ __forceinline__ float4 tf32_head(float4 v) {
                      __uint_as_float(__float_as_uint(v.z) & m), __uint_as_float(__float_as_uint(v.w) & m));
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
+static __global__ void __launch_bounds__(TC_THREADS, 1)
     k_dht_tc(const __grid_constant__ CUtensorMap tTh, const __grid_constant__ CUtensorMap tTl,
              const __grid_constant__ CUtensorMap tB, TcGemmParams p) {
   extern __shared__ __align__(1024) uint8_t tc_smem[];

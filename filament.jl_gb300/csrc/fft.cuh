@@ -36,16 +36,44 @@ template <typename C, int SIGN> FIL_DEV void dft4(C* v) {
   v[3] = a1 - b1;
 }
 
+// Multiplication by exp(SIGN i K pi/8), K = 1, 2, 3.  In single precision
+// the constants are applied as head + remainder: the nearest FP32 values of
+// cos(pi/8), sin(pi/8) and sqrt(2)/2 all lie below the true values
+// (|w|^2 - 1 = -5.7e-8 and -3.4e-8), which would shrink the field by ~2e-8
+// per butterfly and, over six radix-16 passes per time<->frequency round
+// trip, damp the energy by ~1.5e-7 every z-step.  The split form keeps the
+// rotation's magnitude exact to ~2^-48.
+template <int SIGN, int K> FIL_DEV float2 rot8(float2 v) {
+  // K=1: (c1, s1), K=2: (c2, c2), K=3: (s1, c1); head + remainder
+  const float c1h = 0.92387950420379638671875f, c1l = 2.8307490243e-08f;
+  const float s1h = 0.3826834261417388916015625f, s1l = 6.2233508e-09f;
+  const float c2h = 0.707106769084930419921875f, c2l = 1.2101617e-08f;
+  float ch, cl, sh, sl;
+  if (K == 1) { ch = c1h; cl = c1l; sh = s1h; sl = s1l; }
+  else if (K == 2) { ch = c2h; cl = c2l; sh = c2h; sl = c2l; }
+  else { ch = s1h; cl = s1l; sh = c1h; sl = c1l; }
+  // re = x c - SIGN y s, im = y c + SIGN x s
+  const float ys = fmaf(v.y, sh, v.y * sl), xs = fmaf(v.x, sh, v.x * sl);
+  const float re = fmaf(v.x, ch, fmaf(v.x, cl, -(float)SIGN * ys));
+  const float im = fmaf(v.y, ch, fmaf(v.y, cl, (float)SIGN * xs));
+  return make_float2(re, im);
+}
+template <int SIGN, int K> FIL_DEV double2 rot8(double2 v) {
+  const double c1 = 0.92387953251128675613, s1 = 0.38268343236508977173, c2 = 0.70710678118654752440;
+  double c, s;
+  if (K == 1) { c = c1; s = s1; }
+  else if (K == 2) { c = c2; s = c2; }
+  else { c = s1; s = c1; }
+  return make_double2(v.x * c - SIGN * v.y * s, v.y * c + SIGN * v.x * s);
+}
+
 template <typename C, int SIGN> FIL_DEV void dft8(C* v) {
-  typedef decltype(C().x) R;
-  const R h = (R)0.70710678118654752440;
   C e[4] = {v[0], v[2], v[4], v[6]};
   C o[4] = {v[1], v[3], v[5], v[7]};
   dft4<C, SIGN>(e);
   dft4<C, SIGN>(o);
-  // W8^k = exp(SIGN 2 pi i k / 8)
-  C w1 = mk<R>(h, SIGN * h), w3 = mk<R>(-h, SIGN * h);
-  C t0 = o[0], t1 = cmul(o[1], w1), t2 = mul_si<C, SIGN>(o[2]), t3 = cmul(o[3], w3);
+  // W8^1 = exp(SIGN i pi/4), W8^2 = SIGN i, W8^3 = SIGN i W8^1
+  C t0 = o[0], t1 = rot8<SIGN, 2>(o[1]), t2 = mul_si<C, SIGN>(o[2]), t3 = mul_si<C, SIGN>(rot8<SIGN, 2>(o[3]));
   v[0] = e[0] + t0; v[4] = e[0] - t0;
   v[1] = e[1] + t1; v[5] = e[1] - t1;
   v[2] = e[2] + t2; v[6] = e[2] - t2;
@@ -53,24 +81,21 @@ template <typename C, int SIGN> FIL_DEV void dft8(C* v) {
 }
 
 template <typename C, int SIGN> FIL_DEV void dft16(C* v) {
-  typedef decltype(C().x) R;
-  // cos(k pi/8), sin(k pi/8), k = 0..7
-  const R c1 = (R)0.92387953251128675613, s1 = (R)0.38268343236508977173;
-  const R c2 = (R)0.70710678118654752440;
   C e[8], o[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) { e[i] = v[2 * i]; o[i] = v[2 * i + 1]; }
   dft8<C, SIGN>(e);
   dft8<C, SIGN>(o);
+  // W16^k = exp(SIGN i k pi/8); W16^(k+4) = SIGN i W16^k
   C t[8];
   t[0] = o[0];
-  t[1] = cmul(o[1], mk<R>(c1, SIGN * s1));
-  t[2] = cmul(o[2], mk<R>(c2, SIGN * c2));
-  t[3] = cmul(o[3], mk<R>(s1, SIGN * c1));
+  t[1] = rot8<SIGN, 1>(o[1]);
+  t[2] = rot8<SIGN, 2>(o[2]);
+  t[3] = rot8<SIGN, 3>(o[3]);
   t[4] = mul_si<C, SIGN>(o[4]);
-  t[5] = cmul(o[5], mk<R>(-s1, SIGN * c1));
-  t[6] = cmul(o[6], mk<R>(-c2, SIGN * c2));
-  t[7] = cmul(o[7], mk<R>(-c1, SIGN * s1));
+  t[5] = mul_si<C, SIGN>(rot8<SIGN, 1>(o[5]));
+  t[6] = mul_si<C, SIGN>(rot8<SIGN, 2>(o[6]));
+  t[7] = mul_si<C, SIGN>(rot8<SIGN, 3>(o[7]));
 #pragma unroll
   for (int k = 0; k < 8; ++k) { v[k] = e[k] + t[k]; v[k + 8] = e[k] - t[k]; }
 }

@@ -54,6 +54,9 @@ template <typename R> struct RowParams {
   // state
   const C* S_in;
   C* S_out;
+  int out_T;                    // 1: write s_row * S transposed, [2k + re/im][ldT]
+  const R* out_scale;           // s_row (out_T)
+  int ldT;
   DevCtl* ctl;
 };
 
@@ -514,11 +517,25 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
       }
     }
   }
-  C* dst = P.S_out + (size_t)row * P.ld;
+  if (P.out_T) {
+    // operand layout of the tensor-core Hankel GEMM: real column 2k + c,
+    // transverse index contiguous, scaled by s_row
+    R* base = reinterpret_cast<R*>(P.S_out);
+    const R sc = P.out_scale[row];
 #pragma unroll
-  for (int m = 0; m < EW; ++m) {
-    int k = tid + m * T;
-    dst[k] = S0[m] + dz * acc[m];
+    for (int m = 0; m < EW; ++m) {
+      int k = tid + m * T;
+      C v = S0[m] + dz * acc[m];
+      base[(size_t)(2 * k) * P.ldT + row] = sc * v.x;
+      base[(size_t)(2 * k + 1) * P.ldT + row] = sc * v.y;
+    }
+  } else {
+    C* dst = P.S_out + (size_t)row * P.ld;
+#pragma unroll
+    for (int m = 0; m < EW; ++m) {
+      int k = tid + m * T;
+      dst[k] = S0[m] + dz * acc[m];
+    }
   }
 }
 

@@ -96,6 +96,9 @@ extern "C" {
                                   a time, writes a buffer larger than L2
                                   before each step and records per-kernel
                                   device times (fil_kernel_times)          */
+#define FIL_OPT_DHT_SIMT 6      /* mixed form: run the Hankel transforms as
+                                  FP32 CUDA-core GEMMs instead of the
+                                  tensor-core (tcgen05) GEMMs              */
 #define FIL_OPT_ANALYTIC_PROJECTION 5 /* drop negative frequencies after
                                   every t->w transform.  The library's field
                                   state is the analytic half spectrum, so
