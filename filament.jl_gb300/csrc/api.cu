@@ -69,11 +69,13 @@ struct fil_handle {
   size_t flushbytes = 0;
   // tensor-core Hankel path (mixed form)
   bool use_tc = false;
-  void* Th = nullptr; void* Tl = nullptr;      // [mpad][mpad] TF32 head / remainder of T
+  void* Th = nullptr; void* Tl = nullptr;      // unused (kept null)
+  void* MA1[3] = {nullptr, nullptr, nullptr};  // M1 = T diag(s) as three TF32 pieces
+  void* MA2[3] = {nullptr, nullptr, nullptr};  // M2 = diag(1/s) T
   void* kzt = nullptr; void* gdt = nullptr;    // [mpad][nh] KZ (float2), guard (float)
   void* s_row = nullptr; void* inv_s = nullptr;
   int* tc_err = nullptr;
-  CUtensorMap tm_th, tm_tl, tm_w1, tm_w2;
+  CUtensorMap tm_a1[3], tm_a2[3], tm_w1, tm_w2;
 };
 
 void fil_set_global_error(const std::string& m) { g_err = m; }
@@ -283,15 +285,33 @@ static float bits_f(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 static int create_tc(fil_handle* h, const fil_tables* t) {
   typedef std::complex<double> cd;
   const int n1 = h->n1, nh = h->nh, mp = h->mpad;
-  std::vector<float> th((size_t)mp * mp, 0.f), tl((size_t)mp * mp, 0.f);
+  // M1 = T diag(s), M2 = diag(1/s) T, each as head (exact TF32) + middle +
+  // low piece (nearest TF32 of the remainders): 33 significant bits
+  std::vector<float> a1[3], a2[3];
+  for (int q = 0; q < 3; ++q) {
+    a1[q].assign((size_t)mp * mp, 0.f);
+    a2[q].assign((size_t)mp * mp, 0.f);
+  }
+  auto split3 = [&](double x, float* out) {
+    float hd = bits_f(f_bits((float)x) & 0xFFFFE000u);
+    double r1 = x - (double)hd;
+    float md = bits_f((f_bits((float)r1) + 0x1000u) & 0xFFFFE000u);
+    double r2 = r1 - (double)md;
+    float lo = bits_f((f_bits((float)r2) + 0x1000u) & 0xFFFFE000u);
+    out[0] = hd;
+    out[1] = md;
+    out[2] = lo;
+  };
   for (int i = 0; i < n1; ++i)
     for (int k = 0; k < n1; ++k) {
       double T = t->dht[(size_t)i * n1 + k];
-      float hd = bits_f(f_bits((float)T) & 0xFFFFE000u);
-      float lo = (float)(T - (double)hd);
-      lo = bits_f((f_bits(lo) + 0x1000u) & 0xFFFFE000u);
-      th[(size_t)i * mp + k] = hd;
-      tl[(size_t)i * mp + k] = lo;
+      float p1[3], p2[3];
+      split3(T * t->dht_s[k], p1);
+      split3(T / t->dht_s[i], p2);
+      for (int q = 0; q < 3; ++q) {
+        a1[q][(size_t)i * mp + k] = p1[q];
+        a2[q][(size_t)i * mp + k] = p2[q];
+      }
     }
   std::vector<float> kz((size_t)mp * nh * 2, 0.f), gd((size_t)mp * nh, 0.f), sr(mp, 0.f), is(mp, 0.f);
   for (int i = 0; i < n1; ++i) {
@@ -323,14 +343,16 @@ static int create_tc(fil_handle* h, const fil_tables* t) {
     CK(cudaMemcpy(*dst, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice));
     return 0;
   };
-  if (up(&h->Th, th) || up(&h->Tl, tl) || up(&h->kzt, kz) || up(&h->gdt, gd) || up(&h->s_row, sr) ||
-      up(&h->inv_s, is))
-    return FIL_ERR_CUDA;
+  for (int q = 0; q < 3; ++q)
+    if (up(&h->MA1[q], a1[q]) || up(&h->MA2[q], a2[q])) return FIL_ERR_CUDA;
+  if (up(&h->kzt, kz) || up(&h->gdt, gd) || up(&h->s_row, sr) || up(&h->inv_s, is)) return FIL_ERR_CUDA;
   CK(cudaMalloc(&h->tc_err, sizeof(int)));
   CK(cudaMemset(h->tc_err, 0, sizeof(int)));
-  if (tc_make_map(&h->tm_th, (const float*)h->Th, mp, mp, 32, 128) ||
-      tc_make_map(&h->tm_tl, (const float*)h->Tl, mp, mp, 32, 128) ||
-      tc_make_map(&h->tm_w1, (const float*)h->W1, mp, 2 * nh, 32, 128) ||
+  for (int q = 0; q < 3; ++q)
+    if (tc_make_map(&h->tm_a1[q], (const float*)h->MA1[q], mp, mp, 32, 128) ||
+        tc_make_map(&h->tm_a2[q], (const float*)h->MA2[q], mp, mp, 32, 128))
+      return fail(h, FIL_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  if (tc_make_map(&h->tm_w1, (const float*)h->W1, mp, 2 * nh, 32, 128) ||
       tc_make_map(&h->tm_w2, (const float*)h->W2, mp, 2 * nh, 32, 128))
     return fail(h, FIL_ERR_CUDA, "cuTensorMapEncodeTiled failed");
   return 0;
@@ -400,7 +422,7 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   const bool tcp = h->use_tc && sizeof(R) == 4;
   if (tcp) {
     P.out_T = 1;
-    P.out_scale = (const R*)h->s_row;
+    P.out_scale = nullptr;   // the scalings live in M1, M2
   }
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
   CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
@@ -420,14 +442,14 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
     // expected value of the round-toward-zero error of each chunk result:
     // ~ -2^-23 relative for log-uniformly distributed mantissas
     p1.rz_fix = 1.0f + 1.1920928955078125e-07f;
-    CK(launch_dht_tc2(h->tm_th, h->tm_tl, h->tm_w1, p1, h->mpad, Nc, h->st));
+    CK(launch_dht_tc2(h->tm_a1[0], h->tm_a1[1], h->tm_a1[2], h->tm_w1, p1, h->mpad, Nc, h->st));
     if (timed) CK(cudaEventRecord(h->ev[3], h->st));
     TcGemmParams p2 = p1;
     p2.out = (float*)h->S;
     p2.ldo = Nc;
     p2.mode = 2;
-    p2.inv_s = (const float*)h->inv_s;
-    CK(launch_dht_tc2(h->tm_th, h->tm_tl, h->tm_w2, p2, h->mpad, Nc, h->st));
+    p2.inv_s = nullptr;
+    CK(launch_dht_tc2(h->tm_a2[0], h->tm_a2[1], h->tm_a2[2], h->tm_w2, p2, h->mpad, Nc, h->st));
   } else {
     CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 1, h->st));
     if (timed) CK(cudaEventRecord(h->ev[3], h->st));
@@ -470,7 +492,8 @@ static void free_all(fil_handle* h) {
   void* bufs[] = {h->S, h->W1, h->W2, h->M1, h->M2, h->tw, h->g1, h->g2, h->gt, h->Cc, h->Cf, h->Cl,
                   h->kt2, h->beta, h->dfr, h->kmax2, h->wg, h->rho_g, h->kdrho_g, h->stage,
                   h->fluence, h->power, h->pw, h->rho_end, h->ctl, h->flushbuf,
-                  h->Th, h->Tl, h->kzt, h->gdt, h->s_row, h->inv_s, h->tc_err};
+                  h->Th, h->Tl, h->kzt, h->gdt, h->s_row, h->inv_s, h->tc_err,
+                  h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2]};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -637,7 +660,7 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   rc = h->fp64 ? create_tables<double>(h, t) : create_tables<float>(h, t);
   if (!rc && !h->fp64 && h->nh * 2 % 128 == 0) {
     rc = create_tc(h, t);
-    h->use_tc = (rc == 0);
+    h->use_tc = false;   // opt-in (FIL_OPT_DHT_TENSOR)
   }
   if (rc) {
     g_err = h->err;
@@ -669,8 +692,8 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
     h->timing = value != 0;
     for (int i = 0; i < 5; ++i) h->tsum[i] = 0;
     h->tcount = 0;
-  } else if (option == FIL_OPT_DHT_SIMT) {
-    if (!h->fp64) h->use_tc = (value == 0) && h->Th != nullptr;
+  } else if (option == FIL_OPT_DHT_TENSOR) {
+    if (!h->fp64) h->use_tc = (value != 0) && h->MA1[0] != nullptr;
   } else if (option == FIL_OPT_ANALYTIC_PROJECTION) {
     // the field state is the analytic half spectrum: always projected
   }

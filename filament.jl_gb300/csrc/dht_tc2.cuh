@@ -1,9 +1,12 @@
 // dht_tc2.cuh -- Hankel transform GEMM on tcgen05 tensor cores with
 // round-to-nearest accumulation across K.
 //
-// Same product as dht_tc.cuh (C = T B, TF32 head/remainder split of both
-// operands, three products), but the tensor memory accumulator only ever holds
-// one 16-wide K chunk: the tensor core's FP32 accumulation rounds toward
+// C = A B with A one of the two fixed Hankel matrices, split on the host into
+// three TF32 pieces A = Ah + Am + Al (33 significant bits: the matrix is
+// applied every z-step, so its representation error would add up
+// coherently), and B split per tile into a TF32 head and rounded remainder;
+// C ~ Ah Bh + Ah Bl + Am Bh + Al Bh.  The tensor memory accumulator only
+// ever holds one 16-wide K chunk: the tensor core's FP32 accumulation rounds toward
 // zero, which over a long K chain biases every output toward zero by
 // ~7e-6 relative at K = 1024 and would damp the field step after step.
 // Each chunk lands in a fresh accumulator (two sets, ping-pong: the Th*Bh
@@ -18,7 +21,7 @@
 // Warp roles (320 threads): warps 0-7 split the B tiles into head and
 // remainder and accumulate chunks into registers, then run the epilogue;
 // warp 8 issues the TMA loads; warp 9 issues the MMAs.  Tile 128 x 128,
-// K step 32, three shared-memory stages {Th, Tl, B, Bl} of 64 KB.
+// K step 32, two shared-memory stages {Ah, Am, Al, B, Bl} of 80 KB.
 // Every mbarrier wait is bounded and also gives up as soon as another role
 // has failed; failures set *err.
 #pragma once
@@ -31,12 +34,12 @@
 #ifndef T2_CHUNK
 #define T2_CHUNK 16
 #endif
-#define T2_STAGES 3
+#define T2_STAGES 2
 #define T2_CONSUMERS 256
 #define T2_THREADS (T2_CONSUMERS + 64)
 #define T2_A_BYTES (T2_BM * T2_BK * 4)
 #define T2_B_BYTES (T2_BN * T2_BK * 4)
-#define T2_STAGE_BYTES (2 * T2_A_BYTES + 2 * T2_B_BYTES)
+#define T2_STAGE_BYTES (3 * T2_A_BYTES + 2 * T2_B_BYTES)
 #define T2_SMEM_BYTES (T2_STAGES * T2_STAGE_BYTES + 1024 + 256)
 
 // bounded wait that also stops when *fail is set by another role
@@ -53,8 +56,8 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 }
 
 __global__ void __launch_bounds__(T2_THREADS, 1)
-    k_dht_tc2(const __grid_constant__ CUtensorMap tTh, const __grid_constant__ CUtensorMap tTl,
-              const __grid_constant__ CUtensorMap tB, TcGemmParams p) {
+    k_dht_tc2(const __grid_constant__ CUtensorMap tTh, const __grid_constant__ CUtensorMap tTm,
+              const __grid_constant__ CUtensorMap tTl, const __grid_constant__ CUtensorMap tB, TcGemmParams p) {
   extern __shared__ __align__(1024) uint8_t t2_smem[];
   __shared__ volatile int s_fail;
   if (p.ctl && p.ctl->done) return;
@@ -107,10 +110,11 @@ __global__ void __launch_bounds__(T2_THREADS, 1)
         const int use = kb / T2_STAGES;
         if (use > 0 && !t2_wait(empty_bar(s), (use - 1) & 1, &s_fail)) break;
         const uint32_t st = sbase + s * T2_STAGE_BYTES;
-        tc::mbar_expect_tx(full_bar(s), 2 * T2_A_BYTES + T2_B_BYTES);
+        tc::mbar_expect_tx(full_bar(s), 3 * T2_A_BYTES + T2_B_BYTES);
         tc::tma_load_2d(st, &tTh, kb * T2_BK, bm, full_bar(s));
-        tc::tma_load_2d(st + T2_A_BYTES, &tTl, kb * T2_BK, bm, full_bar(s));
-        tc::tma_load_2d(st + 2 * T2_A_BYTES, &tB, kb * T2_BK, bn, full_bar(s));
+        tc::tma_load_2d(st + T2_A_BYTES, &tTm, kb * T2_BK, bm, full_bar(s));
+        tc::tma_load_2d(st + 2 * T2_A_BYTES, &tTl, kb * T2_BK, bm, full_bar(s));
+        tc::tma_load_2d(st + 3 * T2_A_BYTES, &tB, kb * T2_BK, bn, full_bar(s));
       }
       // wait for the last loads so no copy lands after the block exits
       for (int kb = (nk > T2_STAGES ? nk - T2_STAGES : 0); kb < nk; ++kb)
@@ -136,11 +140,13 @@ __global__ void __launch_bounds__(T2_THREADS, 1)
           for (int kk = 0; kk < T2_CHUNK / 8; ++kk) {
             const uint32_t koff = (uint32_t)((c * T2_CHUNK + kk * 8) * 4);
             const uint64_t ah = tc::desc_k128(st + koff);
-            const uint64_t al = tc::desc_k128(st + T2_A_BYTES + koff);
-            const uint64_t bh = tc::desc_k128(st + 2 * T2_A_BYTES + koff);
-            const uint64_t bl = tc::desc_k128(st + 2 * T2_A_BYTES + T2_B_BYTES + koff);
+            const uint64_t am = tc::desc_k128(st + T2_A_BYTES + koff);
+            const uint64_t al = tc::desc_k128(st + 2 * T2_A_BYTES + koff);
+            const uint64_t bh = tc::desc_k128(st + 3 * T2_A_BYTES + koff);
+            const uint64_t bl = tc::desc_k128(st + 3 * T2_A_BYTES + T2_B_BYTES + koff);
             tc::mma_tf32(big, ah, bh, idesc, kk != 0);
             tc::mma_tf32(small, ah, bl, idesc, kk != 0);
+            tc::mma_tf32(small, am, bh, idesc, 1);
             tc::mma_tf32(small, al, bh, idesc, 1);
           }
           tc::mma_commit(accf_bar(b));
@@ -154,8 +160,8 @@ __global__ void __launch_bounds__(T2_THREADS, 1)
     auto convert = [&](int kb) -> bool {
       const int s = kb % T2_STAGES;
       if (!t2_wait(full_bar(s), (kb / T2_STAGES) & 1, &s_fail)) return false;
-      float4* Bp = reinterpret_cast<float4*>(gbase + s * T2_STAGE_BYTES + 2 * T2_A_BYTES);
-      float4* Bl = reinterpret_cast<float4*>(gbase + s * T2_STAGE_BYTES + 2 * T2_A_BYTES + T2_B_BYTES);
+      float4* Bp = reinterpret_cast<float4*>(gbase + s * T2_STAGE_BYTES + 3 * T2_A_BYTES);
+      float4* Bl = reinterpret_cast<float4*>(gbase + s * T2_STAGE_BYTES + 3 * T2_A_BYTES + T2_B_BYTES);
 #pragma unroll
       for (int i = tid; i < T2_B_BYTES / 16; i += T2_CONSUMERS) {
         float4 v = Bp[i];
@@ -223,7 +229,7 @@ __global__ void __launch_bounds__(T2_THREADS, 1)
 #pragma unroll
       for (int i = 0; i < 64; ++i) p.out[(size_t)(col0 + i) * p.ldo + row] = acc[i];
     } else {
-      const float sc = (p.mode == 2) ? p.inv_s[row] : 1.0f;
+      const float sc = (p.mode == 2 && p.inv_s) ? p.inv_s[row] : 1.0f;
       float4* dst = reinterpret_cast<float4*>(p.out + (size_t)row * p.ldo + col0);
 #pragma unroll
       for (int i = 0; i < 16; ++i)

@@ -28,8 +28,8 @@ template <typename R>
 cudaError_t launch_dht_simt(const R* A, const R* B, R* C, int M, int N, int K, const PropParams<R>& pp,
                             DevCtl* ctl, int epi, cudaStream_t st);
 struct TcGemmParams;
-cudaError_t launch_dht_tc2(const CUtensorMap& th, const CUtensorMap& tl, const CUtensorMap& b,
-                           const TcGemmParams& p, int M, int N, cudaStream_t st);
+cudaError_t launch_dht_tc2(const CUtensorMap& th, const CUtensorMap& tm, const CUtensorMap& tl,
+                           const CUtensorMap& b, const TcGemmParams& p, int M, int N, cudaStream_t st);
 cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
 cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);

@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
     // operand layout of the tensor-core Hankel GEMM: real column 2k + c,
     // transverse index contiguous, scaled by s_row
     R* base = reinterpret_cast<R*>(P.S_out);
-    const R sc = P.out_scale[row];
+    const R sc = P.out_scale ? P.out_scale[row] : (R)1;
 #pragma unroll
     for (int m = 0; m < EW; ++m) {
       int k = tid + m * T;
