@@ -299,6 +299,10 @@ def main():
     # previous k, read rho and Kdrho, write k) + RK combine (read E, k1..ks,
     # write E) = c(4s+5) + q(2s+2) per grid point
     b_row = nr * nt * (8 * (4 * s + 5) + 4 * (2 * s + 2))
+    # DRAM bytes (read + write) of one k_rowstep launch of this workload,
+    # from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); the
+    # 16 MB spectrum it writes stays in L2 within the launch
+    row_traffic = 16.80e6 + 0.0
     achieved = b_row / (mixed["row_ms"] * 1e-3) / 1e9
     # tensor-core Hankel transform: 2 Mpad^2 Nt FLOP per transform (FP32
     # product), executed as three TF32 products
@@ -315,7 +319,8 @@ def main():
         "accuracy": acc,
         "roofline": {"kernel": "k_rowstep (plasma + RK4 nonlinear step, fused)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src, "traffic": None,
+                     "peak_source": src, "traffic": row_traffic,
+                     "traffic_source": "ncu, one k_rowstep launch of this workload",
                      "algorithmic_bytes_per_launch": b_row,
                      "dht_tensor": {"kernel": "k_dht_tc2 (tcgen05 kind::tf32, 4 products, opt-in)",
                                     "achieved_tflops_tf32": dht_tf,
