@@ -119,7 +119,7 @@ def _prepare(**over):
     return fg.prepare(DECK, **kw)
 
 
-def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, tensor_dht=False):
+def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, simt_dht=False):
     """Warm-up steps in graph mode, then the timed steps from z = 0 (the
     field re-uploaded) up to `steps` steps or z = zend, one at a time with L2
     flushed, then the same range in graph mode (warm L2, for information);
@@ -130,8 +130,8 @@ def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, tensor_dh
     inp = _prepare()
     sim = fg.Simulation(inp, precision=precision)
     h = sim.handle
-    if tensor_dht:
-        h.set_option(_abi.OPT_DHT_TENSOR, 1)
+    if simt_dht:
+        h.set_option(_abi.OPT_DHT_SIMT, 1)
     h.run(0.0, zend, warmup)
     h.set_field(sim.field.E0, analytic=False)
     h.set_option(_abi.OPT_TIMING, 1)
@@ -165,10 +165,10 @@ def accuracy_run(zend, nmax):
     inp = _prepare(zmax=zend)
     out = {}
     fields = {}
-    for prec in ("mixed", "mixed_tensor", "fp64"):
+    for prec in ("mixed", "mixed_simt", "fp64"):
         sim = fg.Simulation(inp, precision="fp64" if prec == "fp64" else "mixed")
-        if prec == "mixed_tensor":
-            sim.handle.set_option(_abi.OPT_DHT_TENSOR, 1)
+        if prec == "mixed_simt":
+            sim.handle.set_option(_abi.OPT_DHT_SIMT, 1)
         sim.handle.set_option(_abi.OPT_CLAMP_LAST_DZ, 1)
         t0 = time.perf_counter()
         code, st = sim.handle.run(0.0, zend, nmax)
@@ -180,42 +180,48 @@ def accuracy_run(zend, nmax):
         sim.close()
     Em, Fm, Im = fields["mixed"]
     Ed, Fd, Id = fields["fp64"]
-    Es, Fs, Is = fields["mixed_tensor"]
+    Es, Fs, Is = fields["mixed_simt"]
     out["rel_l2_field"] = float(np.linalg.norm(Em - Ed) / np.linalg.norm(Ed))
     out["rel_l2_fluence"] = float(np.linalg.norm(Fm - Fd) / np.linalg.norm(Fd))
-    out["tensor_dht_rel_l2_field"] = float(np.linalg.norm(Es - Ed) / np.linalg.norm(Ed))
-    out["tensor_dht_rel_l2_fluence"] = float(np.linalg.norm(Fs - Fd) / np.linalg.norm(Fd))
+    out["cuda_core_dht_rel_l2_field"] = float(np.linalg.norm(Es - Ed) / np.linalg.norm(Ed))
+    out["cuda_core_dht_rel_l2_fluence"] = float(np.linalg.norm(Fs - Fd) / np.linalg.norm(Fd))
     out["imax_end"] = Id
     out["z_end"] = zend
     return out
 
 
 def e2e_host_loop(steps):
-    """The reference's main loop through the public API: per step the host
-    dz (AdaptiveSteps), fil_step, and fil_analyze (device reductions copied
-    to the host: fluence[Nr], power[Nt], rho_end[Nr], stats).  The initial
-    field upload and the final field download are inside the timed region."""
+    """The reference's main loop through the public API, timed from host
+    buffers: the upload of the initial field (host complex128 E(r, t)),
+    then per step the host dz (AdaptiveSteps), fil_step and fil_analyze
+    (device reductions copied to the host: fluence[Nr], power[Nt],
+    rho_end[Nr], stats), and the download of the final field.  The problem
+    tables (grids, DHT matrix, responses) are built before the timed region,
+    as the reference builds them before its loop."""
     import numpy as np
     import filament_gb as fg
-    from filament_gb.filament import AStep
     inp = _prepare()
-    E0 = None
+    sim = fg.Simulation(inp, precision="mixed")
+    E0 = np.ascontiguousarray(np.asarray(sim.field.E0, dtype=np.complex128))
+    sim.handle.step(0.0, 1e-9)                             # warm the kernels once
     t0 = time.perf_counter()
-    sim = fg.Simulation(inp, precision="mixed")          # H2D of the field
+    sim.handle.set_field(E0)                               # H2D of the field
+    sim.analyzer.analyze(0.0)
     z = 0.0
     for _ in range(steps):
         dz = sim.dzadaptive(sim.analyzer)
         z += dz
         sim.handle.step(z, dz)
-        sim.analyzer.analyze(z)                           # D2H of reductions
-    E = sim.handle.get_field()                            # D2H of the field
+        sim.analyzer.analyze(z)                            # D2H of reductions
+    E = sim.handle.get_field()                             # D2H of the field
     wall = time.perf_counter() - t0
     nr, nt = WORKLOAD["Nr"], WORKLOAD["Nt"]
-    field_bytes = nr * nt * 16
+    field_bytes = E0.nbytes
+    assert E.nbytes == field_bytes
     sim.close()
     return {"value": steps / wall, "unit": "z-steps/s",
             "h2d_bytes_per_step": int(field_bytes / steps + 16),
-            "d2h_bytes_per_step": int((2 * nr + nt) * 8 + 64 + field_bytes / steps)}
+            "d2h_bytes_per_step": int((3 * nr + nt) * 8 + 64 + field_bytes / steps)}
 
 
 def cpu_oracle(steps):
@@ -279,7 +285,7 @@ def main():
     mixed = time_device_loop("mixed", args.warmup, args.steps, args.accuracy_zend, load_seconds=3.0)
     clocks = sampler.stop()
     fp64 = time_device_loop("fp64", args.warmup, args.steps, args.accuracy_zend)
-    mixed_tc = time_device_loop("mixed", args.warmup, args.steps, args.accuracy_zend, tensor_dht=True)
+    mixed_simt = time_device_loop("mixed", args.warmup, args.steps, args.accuracy_zend, simt_dht=True)
     t_local = mixed["ms_per_step"]
     if dist is not None:
         import torch
@@ -305,16 +311,16 @@ def main():
     row_traffic = 16.80e6 + 0.0
     achieved = b_row / (mixed["row_ms"] * 1e-3) / 1e9
     # tensor-core Hankel transform: 2 Mpad^2 Nt FLOP per transform (FP32
-    # product), executed as three TF32 products
+    # product), executed as six FP16 slice products
     mpad = (nr + 127) // 128 * 128
     f_dht = 2.0 * mpad * mpad * nt
-    dht_tf = 4 * f_dht / (mixed_tc["dht_fwd_ms"] * 1e-3) / 1e12
+    dht_tf = 6 * f_dht / (mixed["dht_inv_ms"] * 1e-3) / 1e12
     line = {
         "metric": "RT z-steps/s", "value": value, "unit": "z-steps/s", "n_gpus": args.gpus,
         "steps": mixed["timed_steps"], "warmup": args.warmup, "ms_per_step": t_local,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
         "data": "synthetic", "config": _config(args),
-        "forms": {"mixed": mixed, "mixed_tensor_core_dht": mixed_tc, "fp64": fp64,
+        "forms": {"mixed": mixed, "mixed_cuda_core_dht": mixed_simt, "fp64": fp64,
                   "speedup_mixed_over_fp64": fp64["ms_per_step"] / mixed["ms_per_step"]},
         "accuracy": acc,
         "roofline": {"kernel": "k_rowstep (plasma + RK4 nonlinear step, fused)", "bound": "hbm",
@@ -322,9 +328,9 @@ def main():
                      "peak_source": src, "traffic": row_traffic,
                      "traffic_source": "ncu, one k_rowstep launch of this workload",
                      "algorithmic_bytes_per_launch": b_row,
-                     "dht_tensor": {"kernel": "k_dht_tc2 (tcgen05 kind::tf32, 4 products, opt-in)",
-                                    "achieved_tflops_tf32": dht_tf,
-                                    "ms_per_launch": mixed_tc["dht_fwd_ms"]}},
+                     "dht_tensor": {"kernel": "k_dht_tc (tcgen05 kind::f16, 6 slice products), inverse transform",
+                                    "achieved_tflops_f16": dht_tf,
+                                    "ms_per_launch": mixed["dht_inv_ms"]}},
         "cpu_baseline": {"value": sps_cpu, "unit": "z-steps/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": "%d z-steps of the workload from z=0 (%.1f s), FP64 OpenMP oracle"
                                    % (args.cpu_steps, cpu_wall)},

@@ -22,7 +22,8 @@
 #include "launch.h"
 #include "rowkernels.cuh"
 #include "dht_simt.cuh"
-#include "dht_tc.cuh"
+#include "tc_params.h"
+#include <cuda_fp16.h>
 #include "tc_host.h"
 
 namespace {
@@ -55,7 +56,8 @@ struct fil_handle {
   double* rho_end = nullptr;   // [nrows]
   DevCtl* ctl = nullptr;
   DevCtl* ctl_host = nullptr;  // pinned
-  PlasmaParams pp;
+  double* an_host = nullptr;   // pinned: fluence[nrows], power[nt], rho_end[nrows], w[nrows]
+  PlasmaParams<double> pp;
   int ns;
   double A0[4], A1[4], B[4];
   double sc = 1, sf = 1, sl = 1;   // response channel pre-scales
@@ -69,11 +71,11 @@ struct fil_handle {
   size_t flushbytes = 0;
   // tensor-core Hankel path (mixed form)
   bool use_tc = false;
-  void* Th = nullptr; void* Tl = nullptr;      // unused (kept null)
-  void* MA1[3] = {nullptr, nullptr, nullptr};  // M1 = T diag(s) as three TF32 pieces
+  void* MA1[3] = {nullptr, nullptr, nullptr};  // M1 = T diag(s): FP16 slices a0, a1, a2
   void* MA2[3] = {nullptr, nullptr, nullptr};  // M2 = diag(1/s) T
+  void* qa1 = nullptr; void* qa2 = nullptr;    // [mpad] row scales of M1, M2
+  void* cm1 = nullptr; void* cm2 = nullptr;    // [2 nh] column maxima of W1, W2 (float bits)
   void* kzt = nullptr; void* gdt = nullptr;    // [mpad][nh] KZ (float2), guard (float)
-  void* s_row = nullptr; void* inv_s = nullptr;
   int* tc_err = nullptr;
   CUtensorMap tm_a1[3], tm_a2[3], tm_w1, tm_w2;
 };
@@ -234,7 +236,7 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
   }
   // plasma
   if (c.plasma) {
-    PlasmaParams& P = h->pp;
+    PlasmaParams<double>& P = h->pp;
     std::memset(&P, 0, sizeof P);
     int nc = c.plasma_ncomp, n = c.rate_n;
     P.nc = nc;
@@ -277,47 +279,56 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
   return 0;
 }
 
-// Tables of the tensor-core Hankel path: T split into an exact TF32 head and
-// the nearest-TF32 remainder, the propagator's KZ and guard per (r, w), the
-// row scales s and 1/s, and the TMA maps of the operands.
-static uint32_t f_bits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
-static float bits_f(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+// Slices of a fixed Hankel matrix for the tensor-core GEMM: per row i a
+// power-of-two scale q_i = 2^(E_i - 9), 2^E_i <= max_k |x_ik| < 2^(E_i + 1),
+// and x_ik = q_i (a0 + a1 + a2) with a0 = round(x/q_i) (|a0| <= 1024) and
+// a1, a2 the FP16 roundings of the remainders: 32 significant bits relative
+// to the row maximum.
+static void slice_rows(const std::vector<double>& x, int n, int mp, std::vector<__half> (&a)[3],
+                       std::vector<float>& q) {
+  for (int k = 0; k < 3; ++k) a[k].assign((size_t)mp * mp, __float2half_rn(0.f));
+  q.assign(mp, 0.f);
+  for (int i = 0; i < n; ++i) {
+    double m = 0;
+    for (int k = 0; k < n; ++k) m = std::max(m, std::fabs(x[(size_t)i * n + k]));
+    if (m == 0) continue;
+    int e;
+    std::frexp(m, &e);                      // m = f 2^e, f in [1/2, 1)
+    const double qi = std::ldexp(1.0, e - 1 - 9);
+    q[i] = (float)qi;
+    for (int k = 0; k < n; ++k) {
+      const double y = x[(size_t)i * n + k] / qi;
+      const double a0 = std::nearbyint(y);
+      const double r = y - a0;
+      const __half a1 = __float2half_rn((float)r);
+      const double r2 = r - (double)__half2float(a1);
+      a[0][(size_t)i * mp + k] = __float2half_rn((float)a0);
+      a[1][(size_t)i * mp + k] = a1;
+      a[2][(size_t)i * mp + k] = __float2half_rn((float)r2);
+    }
+  }
+}
+
+// Tables of the tensor-core Hankel path: the slices of M1 = T diag(s) and
+// M2 = diag(1/s) T with their row scales, the propagator's KZ and guard per
+// (r, w), the column-maximum arrays and the TMA maps of the operands.
 static int create_tc(fil_handle* h, const fil_tables* t) {
   typedef std::complex<double> cd;
   const int n1 = h->n1, nh = h->nh, mp = h->mpad;
-  // M1 = T diag(s), M2 = diag(1/s) T, each as head (exact TF32) + middle +
-  // low piece (nearest TF32 of the remainders): 33 significant bits
-  std::vector<float> a1[3], a2[3];
-  for (int q = 0; q < 3; ++q) {
-    a1[q].assign((size_t)mp * mp, 0.f);
-    a2[q].assign((size_t)mp * mp, 0.f);
-  }
-  auto split3 = [&](double x, float* out) {
-    float hd = bits_f(f_bits((float)x) & 0xFFFFE000u);
-    double r1 = x - (double)hd;
-    float md = bits_f((f_bits((float)r1) + 0x1000u) & 0xFFFFE000u);
-    double r2 = r1 - (double)md;
-    float lo = bits_f((f_bits((float)r2) + 0x1000u) & 0xFFFFE000u);
-    out[0] = hd;
-    out[1] = md;
-    out[2] = lo;
-  };
+  std::vector<double> m1((size_t)n1 * n1), m2((size_t)n1 * n1);
   for (int i = 0; i < n1; ++i)
     for (int k = 0; k < n1; ++k) {
-      double T = t->dht[(size_t)i * n1 + k];
-      float p1[3], p2[3];
-      split3(T * t->dht_s[k], p1);
-      split3(T / t->dht_s[i], p2);
-      for (int q = 0; q < 3; ++q) {
-        a1[q][(size_t)i * mp + k] = p1[q];
-        a2[q][(size_t)i * mp + k] = p2[q];
-      }
+      const double T = t->dht[(size_t)i * n1 + k];
+      m1[(size_t)i * n1 + k] = T * t->dht_s[k];
+      m2[(size_t)i * n1 + k] = T / t->dht_s[i];
     }
-  std::vector<float> kz((size_t)mp * nh * 2, 0.f), gd((size_t)mp * nh, 0.f), sr(mp, 0.f), is(mp, 0.f);
+  std::vector<__half> a1[3], a2[3];
+  std::vector<float> q1, q2;
+  slice_rows(m1, n1, mp, a1, q1);
+  slice_rows(m2, n1, mp, a2, q2);
+  std::vector<float> kz((size_t)mp * nh * 2, 0.f), gd((size_t)mp * nh, 0.f);
   for (int i = 0; i < n1; ++i) {
     double kt2 = t->kt1[i] * t->kt1[i];
-    sr[i] = (float)t->dht_s[i];
-    is[i] = (float)(1.0 / t->dht_s[i]);
     for (int j = 0; j < nh; ++j) {
       cd b(t->beta[2 * j], t->beta[2 * j + 1]), d(t->dfr[2 * j], t->dfr[2 * j + 1]);
       cd K = d;
@@ -338,22 +349,28 @@ static int create_tc(fil_handle* h, const fil_tables* t) {
       gd[(size_t)i * nh + j] = (float)g;
     }
   }
-  auto up = [&](void** dst, const std::vector<float>& v) -> int {
-    CK(cudaMalloc(dst, v.size() * sizeof(float)));
-    CK(cudaMemcpy(*dst, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice));
+  auto up = [&](void** dst, const void* src, size_t bytes) -> int {
+    CK(cudaMalloc(dst, bytes));
+    CK(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
     return 0;
   };
-  for (int q = 0; q < 3; ++q)
-    if (up(&h->MA1[q], a1[q]) || up(&h->MA2[q], a2[q])) return FIL_ERR_CUDA;
-  if (up(&h->kzt, kz) || up(&h->gdt, gd) || up(&h->s_row, sr) || up(&h->inv_s, is)) return FIL_ERR_CUDA;
+  const size_t sb = (size_t)mp * mp * sizeof(__half);
+  for (int k = 0; k < 3; ++k)
+    if (up(&h->MA1[k], a1[k].data(), sb) || up(&h->MA2[k], a2[k].data(), sb)) return FIL_ERR_CUDA;
+  if (up(&h->qa1, q1.data(), mp * sizeof(float)) || up(&h->qa2, q2.data(), mp * sizeof(float)) ||
+      up(&h->kzt, kz.data(), kz.size() * sizeof(float)) || up(&h->gdt, gd.data(), gd.size() * sizeof(float)))
+    return FIL_ERR_CUDA;
+  CK(cudaMalloc(&h->cm1, 2 * nh * sizeof(unsigned)));
+  CK(cudaMalloc(&h->cm2, 2 * nh * sizeof(unsigned)));
+  CK(cudaMemset(h->cm1, 0, 2 * nh * sizeof(unsigned)));
+  CK(cudaMemset(h->cm2, 0, 2 * nh * sizeof(unsigned)));
   CK(cudaMalloc(&h->tc_err, sizeof(int)));
   CK(cudaMemset(h->tc_err, 0, sizeof(int)));
-  for (int q = 0; q < 3; ++q)
-    if (tc_make_map(&h->tm_a1[q], (const float*)h->MA1[q], mp, mp, 32, 128) ||
-        tc_make_map(&h->tm_a2[q], (const float*)h->MA2[q], mp, mp, 32, 128))
+  for (int k = 0; k < 3; ++k)
+    if (tc_make_map(&h->tm_a1[k], h->MA1[k], 2, mp, mp, 32, 128) ||
+        tc_make_map(&h->tm_a2[k], h->MA2[k], 2, mp, mp, 32, 128))
       return fail(h, FIL_ERR_CUDA, "cuTensorMapEncodeTiled failed");
-  if (tc_make_map(&h->tm_w1, (const float*)h->W1, mp, 2 * nh, 32, 128) ||
-      tc_make_map(&h->tm_w2, (const float*)h->W2, mp, 2 * nh, 32, 128))
+  if (tc_make_map(&h->tm_w1, h->W1, 4, mp, 2 * nh, 32, 128) || tc_make_map(&h->tm_w2, h->W2, 4, mp, 2 * nh, 32, 128))
     return fail(h, FIL_ERR_CUDA, "cuTensorMapEncodeTiled failed");
   return 0;
 }
@@ -382,13 +399,17 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
   P.Cc = (const C*)h->Cc;
   P.Cf = (const C*)h->Cf;
   P.Cl = (const C*)h->Cl;
-  P.sc = h->sc;
-  P.sf = h->sf;
-  P.sl = h->sl;
+  P.sc = (R)h->sc;
+  P.sf = (R)h->sf;
+  P.sl = (R)h->sl;
   P.ns = h->ns;
-  for (int s = 0; s < 4; ++s) { P.A0[s] = h->A0[s]; P.A1[s] = h->A1[s]; P.B[s] = h->B[s]; }
+  for (int s = 0; s < 4; ++s) {
+    P.A0[s] = (R)h->A0[s];
+    P.A1[s] = (R)h->A1[s];
+    P.B[s] = (R)h->B[s];
+  }
   P.plasma = c.plasma;
-  P.pp = h->pp;
+  P.pp = plasma_params_as<R>(h->pp);
   P.rho_g = (R*)h->rho_g;
   P.kdrho_g = (R*)h->kdrho_g;
   P.store_plasma = h->store_plasma ? 1 : 0;
@@ -423,6 +444,9 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   if (tcp) {
     P.out_T = 1;
     P.out_scale = nullptr;   // the scalings live in M1, M2
+    P.cm_out = (unsigned*)h->cm1;
+    P.cm_clear = (unsigned*)h->cm2;
+    P.ncols = Nc;
   }
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
   CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
@@ -437,19 +461,22 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
     p1.kz = (const float2*)h->kzt;
     p1.gd = (const float*)h->gdt;
     p1.nh = h->nh;
+    p1.qa = (const float*)h->qa1;
+    p1.cm_in = (const unsigned*)h->cm1;
+    p1.cm_out = (unsigned*)h->cm2;
     p1.ctl = h->ctl;
     p1.err = h->tc_err;
-    // expected value of the round-toward-zero error of each chunk result:
-    // ~ -2^-23 relative for log-uniformly distributed mantissas
-    p1.rz_fix = 1.0f + 1.1920928955078125e-07f;
-    CK(launch_dht_tc2(h->tm_a1[0], h->tm_a1[1], h->tm_a1[2], h->tm_w1, p1, h->mpad, Nc, h->st));
+    CK(launch_dht_tc(h->tm_a1[0], h->tm_a1[1], h->tm_a1[2], h->tm_w1, p1, h->mpad, Nc, h->st));
     if (timed) CK(cudaEventRecord(h->ev[3], h->st));
     TcGemmParams p2 = p1;
     p2.out = (float*)h->S;
     p2.ldo = Nc;
     p2.mode = 2;
-    p2.inv_s = nullptr;
-    CK(launch_dht_tc2(h->tm_a2[0], h->tm_a2[1], h->tm_a2[2], h->tm_w2, p2, h->mpad, Nc, h->st));
+    p2.qa = (const float*)h->qa2;
+    p2.cm_in = (const unsigned*)h->cm2;
+    p2.cm_out = nullptr;
+    p2.cm_clear = (unsigned*)h->cm1;
+    CK(launch_dht_tc(h->tm_a2[0], h->tm_a2[1], h->tm_a2[2], h->tm_w2, p2, h->mpad, Nc, h->st));
   } else {
     CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 1, h->st));
     if (timed) CK(cudaEventRecord(h->ev[3], h->st));
@@ -459,10 +486,15 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   return 0;
 }
 
+// Imax and fluence of the current field; with `power`, also
+// power[t] = sum_row w_row |E|^2 (the intensities pass through the staging
+// buffer)
 template <typename R> static int enqueue_reduce(fil_handle* h, double* power, int check_done) {
   RowParams<R> P = row_params<R>(h);
   P.S_in = (const typename C2T<R>::type*)h->S;
-  CK(launch_rowreduce<R>(P, h->nt, h->fluence, power, h->pw, check_done, h->st));
+  R* I = power ? (R*)h->stage : nullptr;
+  CK(launch_rowreduce<R>(P, h->nt, h->fluence, I, check_done, h->st));
+  if (power) CK(launch_colsum<R>(I, h->pw, power, h->nrows, h->nt, h->st));
   return 0;
 }
 
@@ -492,11 +524,12 @@ static void free_all(fil_handle* h) {
   void* bufs[] = {h->S, h->W1, h->W2, h->M1, h->M2, h->tw, h->g1, h->g2, h->gt, h->Cc, h->Cf, h->Cl,
                   h->kt2, h->beta, h->dfr, h->kmax2, h->wg, h->rho_g, h->kdrho_g, h->stage,
                   h->fluence, h->power, h->pw, h->rho_end, h->ctl, h->flushbuf,
-                  h->Th, h->Tl, h->kzt, h->gdt, h->s_row, h->inv_s, h->tc_err,
+                  h->qa1, h->qa2, h->cm1, h->cm2, h->kzt, h->gdt, h->tc_err,
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2]};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
+  if (h->an_host) cudaFreeHost(h->an_host);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   for (int i = 0; i < 8; ++i)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
@@ -657,10 +690,11 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   CKC(cudaMalloc(&h->ctl, sizeof(DevCtl)));
   CKC(cudaMemset(h->ctl, 0, sizeof(DevCtl)));
   CKC(cudaMallocHost(&h->ctl_host, sizeof(DevCtl)));
+  CKC(cudaMallocHost(&h->an_host, (3 * (size_t)h->nrows + h->nt) * sizeof(double)));
   rc = h->fp64 ? create_tables<double>(h, t) : create_tables<float>(h, t);
   if (!rc && !h->fp64 && h->nh * 2 % 128 == 0) {
     rc = create_tc(h, t);
-    h->use_tc = false;   // opt-in (FIL_OPT_DHT_TENSOR)
+    h->use_tc = (rc == 0);
   }
   if (rc) {
     g_err = h->err;
@@ -692,8 +726,8 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
     h->timing = value != 0;
     for (int i = 0; i < 5; ++i) h->tsum[i] = 0;
     h->tcount = 0;
-  } else if (option == FIL_OPT_DHT_TENSOR) {
-    if (!h->fp64) h->use_tc = (value != 0) && h->MA1[0] != nullptr;
+  } else if (option == FIL_OPT_DHT_SIMT) {
+    if (!h->fp64) h->use_tc = (value == 0) && h->MA1[0] != nullptr;
   } else if (option == FIL_OPT_ANALYTIC_PROJECTION) {
     // the field state is the analytic half spectrum: always projected
   }
@@ -866,20 +900,26 @@ int fil_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power, do
   CK(cudaMemsetAsync((char*)h->ctl + offsetof(DevCtl, imax_acc), 0, sizeof(unsigned long long), h->st));
   int rc = reduce(h, h->power, 0);
   if (rc) return rc;
-  std::vector<double> F(h->nrows), P(h->nt), re(h->nrows), w(h->nrows);
-  CK(cudaMemcpyAsync(F.data(), h->fluence, h->nrows * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaMemcpyAsync(P.data(), h->power, h->nt * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaMemcpyAsync(re.data(), h->rho_end, h->nrows * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaMemcpyAsync(w.data(), h->pw, h->nrows * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  const int nr = h->nrows;
+  double* F = h->an_host;
+  double* P = F + nr;
+  double* re = P + h->nt;
+  double* w = re + nr;
+  CK(cudaMemcpyAsync(F, h->fluence, nr * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(P, h->power, h->nt * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(re, h->rho_end, nr * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(w, h->pw, nr * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   rc = read_ctl(h);
   if (rc) return rc;
+  rc = check_tc(h);
+  if (rc) return rc;
   const DevCtl& c = *h->ctl_host;
-  if (fluence) std::memcpy(fluence, F.data(), F.size() * sizeof(double));
-  if (power) std::memcpy(power, P.data(), P.size() * sizeof(double));
-  if (rho_end) std::memcpy(rho_end, re.data(), re.size() * sizeof(double));
+  if (fluence) std::memcpy(fluence, F, nr * sizeof(double));
+  if (power) std::memcpy(power, P, h->nt * sizeof(double));
+  if (rho_end) std::memcpy(rho_end, re, nr * sizeof(double));
   if (st) {
     double e = 0;
-    for (int i = 0; i < h->nrows; ++i) e += F[i] * w[i];
+    for (int i = 0; i < nr; ++i) e += F[i] * w[i];
     st->z = c.z;
     st->dz = c.dz;
     double im, rm;

@@ -17,8 +17,10 @@ template <typename R> struct PropParams;
 template <typename R>
 cudaError_t launch_rowstep(const RowParams<R>& P, int n, int nc, int mode, cudaStream_t st);
 template <typename R>
-cudaError_t launch_rowreduce(const RowParams<R>& P, int n, double* fluence, double* power_out,
-                             const double* power_w, int check_done, cudaStream_t st);
+cudaError_t launch_rowreduce(const RowParams<R>& P, int n, double* fluence, R* Iout, int check_done,
+                             cudaStream_t st);
+template <typename R>
+cudaError_t launch_colsum(const R* I, const double* w, double* power, int nrows, int nt, cudaStream_t st);
 template <typename R>
 cudaError_t launch_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S, int ld,
                             const typename C2T<R>::type* tw, int analytic, int nrows, int n, cudaStream_t st);
@@ -28,8 +30,8 @@ template <typename R>
 cudaError_t launch_dht_simt(const R* A, const R* B, R* C, int M, int N, int K, const PropParams<R>& pp,
                             DevCtl* ctl, int epi, cudaStream_t st);
 struct TcGemmParams;
-cudaError_t launch_dht_tc2(const CUtensorMap& th, const CUtensorMap& tm, const CUtensorMap& tl,
-                           const CUtensorMap& b, const TcGemmParams& p, int M, int N, cudaStream_t st);
+cudaError_t launch_dht_tc(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& a2,
+                          const CUtensorMap& b, const TcGemmParams& p, int M, int N, cudaStream_t st);
 cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
 cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);

@@ -29,20 +29,56 @@
 #define FIL_MAXCOMP 2
 #define FIL_MAXRATE 32
 
-struct PlasmaParams {
+// Scalars in the working precision R: the FP32 kernels then issue no FP64
+// instruction (the FP64 pipe of this part runs at 1/64 of the FP32 rate).
+// The rate tables stay FP64 here and are converted once per block into
+// shared memory.
+template <typename R> struct PlasmaParams {
   int nc;                 // species
   int ns;                 // RK stages
   int kdep, ereal, powerlaw, rate_n;
   int pidx[4];            // stage time: 0 = t_j, 1 = midpoint, 2 = t_{j+1}
-  double a[4][4], b[4];   // RK tableau
-  double dt, rho0;
-  double rho_nt[FIL_MAXCOMP], rava_nt[FIL_MAXCOMP], kfix[FIL_MAXCOMP];
+  R a[4][4], b[4];        // RK tableau
+  R dt, rho0;
+  R rho_nt[FIL_MAXCOMP], rava_nt[FIL_MAXCOMP], kfix[FIL_MAXCOMP];
   double lx[FIL_MAXCOMP][FIL_MAXRATE], ly[FIL_MAXCOMP][FIL_MAXRATE], sl[FIL_MAXCOMP][FIL_MAXRATE];
   int avalanche;          // any rava != 0
   int maxit;              // Newton iteration cap
-  double tol;             // Newton: stop when update^2 <= tol |u|^2
-  double skip;            // rows with max W * window below this keep rho0
+  R tol;                  // Newton: stop when update^2 <= tol |u|^2
+  R skip;                 // rows with max W * window below this keep rho0
 };
+
+template <typename R> inline PlasmaParams<R> plasma_params_as(const PlasmaParams<double>& d) {
+  PlasmaParams<R> r;
+  r.nc = d.nc;
+  r.ns = d.ns;
+  r.kdep = d.kdep;
+  r.ereal = d.ereal;
+  r.powerlaw = d.powerlaw;
+  r.rate_n = d.rate_n;
+  for (int i = 0; i < 4; ++i) {
+    r.pidx[i] = d.pidx[i];
+    r.b[i] = (R)d.b[i];
+    for (int j = 0; j < 4; ++j) r.a[i][j] = (R)d.a[i][j];
+  }
+  r.dt = (R)d.dt;
+  r.rho0 = (R)d.rho0;
+  for (int c = 0; c < FIL_MAXCOMP; ++c) {
+    r.rho_nt[c] = (R)d.rho_nt[c];
+    r.rava_nt[c] = (R)d.rava_nt[c];
+    r.kfix[c] = (R)d.kfix[c];
+    for (int q = 0; q < FIL_MAXRATE; ++q) {
+      r.lx[c][q] = d.lx[c][q];
+      r.ly[c][q] = d.ly[c][q];
+      r.sl[c][q] = d.sl[c][q];
+    }
+  }
+  r.avalanche = d.avalanche;
+  r.maxit = d.maxit;
+  r.tol = (R)d.tol;
+  r.skip = (R)d.skip;
+  return r;
+}
 
 template <typename R> struct PlasmaSmem {
   R lx[FIL_MAXCOMP][FIL_MAXRATE], ly[FIL_MAXCOMP][FIL_MAXRATE], sl[FIL_MAXCOMP][FIL_MAXRATE];
@@ -131,7 +167,7 @@ template <typename R, int NC> FIL_DEV Aff<R, NC> aff_block_exclusive_scan(Aff<R,
 
 // W(I) and its log-log slope (TabulatedFunctions restatement: linear
 // interpolation of ln W over ln I, end segments extended, W(I<=0) = 0).
-template <typename R> FIL_DEV R rate_eval(const PlasmaParams& P, const PlasmaSmem<R>& T, int c, R I, R* slope) {
+template <typename R> FIL_DEV R rate_eval(const PlasmaParams<R>& P, const PlasmaSmem<R>& T, int c, R I, R* slope) {
   int n = P.rate_n;
   if (!(I > (R)0)) {
     *slope = T.sl[c][0];
@@ -155,7 +191,7 @@ template <typename R> FIL_DEV R rate_eval(const PlasmaParams& P, const PlasmaSme
 // equation, linearised at u: returns the affine map (L, B) with
 // Phi(v) ~= (I - L) v + B exact for the affine case.
 template <typename R, int NC>
-FIL_DEV Aff<R, NC> step_map(const PlasmaParams& P, const R* u, const R (&W)[3][NC], const R (&ava)[3],
+FIL_DEV Aff<R, NC> step_map(const PlasmaParams<R>& P, const R* u, const R (&W)[3][NC], const R (&ava)[3],
                             bool aval) {
   R k[4][NC], dk[4][NC][NC];
   const R dt = (R)P.dt;

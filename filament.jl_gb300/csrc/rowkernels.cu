@@ -92,24 +92,28 @@ cudaError_t launch_rowstep(const RowParams<R>& P, int n, int nc, int mode, cudaS
 }
 
 template <typename R, int N>
-static cudaError_t launch_rowreduce_n(const RowParams<R>& P, double* fl, double* pw_out, const double* pw,
-                                      int check_done, cudaStream_t st) {
+static cudaError_t launch_rowreduce_n(const RowParams<R>& P, double* fl, R* Iout, int check_done, cudaStream_t st) {
   size_t sm = x_smem<R, N>();
   cudaError_t e = cudaFuncSetAttribute(k_rowreduce<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k_rowreduce<R, N><<<P.nrows, N / 16, sm, st>>>(P, fl, pw_out, pw, check_done);
+  k_rowreduce<R, N><<<P.nrows, N / 16, sm, st>>>(P, fl, Iout, check_done);
   return cudaGetLastError();
 }
 template <typename R>
-cudaError_t launch_rowreduce(const RowParams<R>& P, int n, double* fl, double* pw_out, const double* pw,
-                             int check_done, cudaStream_t st) {
+cudaError_t launch_rowreduce(const RowParams<R>& P, int n, double* fl, R* Iout, int check_done, cudaStream_t st) {
   switch (n) {
-    case 512: return launch_rowreduce_n<R, 512>(P, fl, pw_out, pw, check_done, st);
-    case 1024: return launch_rowreduce_n<R, 1024>(P, fl, pw_out, pw, check_done, st);
-    case 2048: return launch_rowreduce_n<R, 2048>(P, fl, pw_out, pw, check_done, st);
-    case 4096: return launch_rowreduce_n<R, 4096>(P, fl, pw_out, pw, check_done, st);
+    case 512: return launch_rowreduce_n<R, 512>(P, fl, Iout, check_done, st);
+    case 1024: return launch_rowreduce_n<R, 1024>(P, fl, Iout, check_done, st);
+    case 2048: return launch_rowreduce_n<R, 2048>(P, fl, Iout, check_done, st);
+    case 4096: return launch_rowreduce_n<R, 4096>(P, fl, Iout, check_done, st);
   }
   return cudaErrorInvalidValue;
+}
+template <typename R>
+cudaError_t launch_colsum(const R* I, const double* w, double* power, int nrows, int nt, cudaStream_t st) {
+  dim3 grid((nt + 255) / 256, (nrows + 63) / 64);
+  k_colsum<R><<<grid, 256, 0, st>>>(I, w, power, nrows, nt);
+  return cudaGetLastError();
 }
 
 template <typename R, int N>
@@ -183,8 +187,8 @@ cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st) {
 
 #define INST(R)                                                                                          \
   template cudaError_t launch_rowstep<R>(const RowParams<R>&, int, int, int, cudaStream_t);            \
-  template cudaError_t launch_rowreduce<R>(const RowParams<R>&, int, double*, double*, const double*,  \
-                                           int, cudaStream_t);                                           \
+  template cudaError_t launch_rowreduce<R>(const RowParams<R>&, int, double*, R*, int, cudaStream_t);   \
+  template cudaError_t launch_colsum<R>(const R*, const double*, double*, int, int, cudaStream_t);       \
   template cudaError_t launch_field_in<R>(const C2T<R>::type*, C2T<R>::type*, int, const C2T<R>::type*, \
                                           int, int, int, cudaStream_t);                                  \
   template cudaError_t launch_field_out<R>(const RowParams<R>&, int, C2T<R>::type*, cudaStream_t);      \

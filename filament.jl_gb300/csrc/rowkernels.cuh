@@ -41,12 +41,12 @@ template <typename R> struct RowParams {
   const C* Cc;                  // i QZ Rnl_cubic * (k ? 2 : 1), [nh]
   const C* Cf;
   const C* Cl;
-  double sc, sf, sl;            // channel pre-scales (C tables are divided by them)
+  R sc, sf, sl;                 // channel pre-scales (C tables are divided by them)
   int ns;                       // RK stages
-  double A0[4], A1[4], B[4];    // stage input U_s = S0 + dz (A0 k1 + A1 kprev)
+  R A0[4], A1[4], B[4];         // stage input U_s = S0 + dz (A0 k1 + A1 kprev)
   // plasma
   int plasma;
-  PlasmaParams pp;
+  PlasmaParams<R> pp;
   R* rho_g;                     // optional full rho / Kdrho rows
   R* kdrho_g;
   int store_plasma;
@@ -55,8 +55,11 @@ template <typename R> struct RowParams {
   const C* S_in;
   C* S_out;
   int out_T;                    // 1: write s_row * S transposed, [2k + re/im][ldT]
-  const R* out_scale;           // s_row (out_T)
+  const R* out_scale;           // s_row (out_T), or NULL
   int ldT;
+  unsigned* cm_out;             // out_T: max |value| per transposed row (atomic, float bits), or NULL
+  unsigned* cm_clear;           // [ncols] cleared by the first blocks, or NULL
+  int ncols;
   DevCtl* ctl;
 };
 
@@ -114,7 +117,7 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
                      R* rho, R* kdrho, R* Y, Aff<R, NC>* ascratch, R* rscratch, int* newton_flag) {
   typedef typename C2T<R>::type C;
   constexpr int NP = N + N / 16;
-  const PlasmaParams& pp = P.pp;
+  const PlasmaParams<R>& pp = P.pp;
   const int tid = threadIdx.x;
   const int j0 = tid * 16;
   const bool ereal = pp.ereal;
@@ -519,16 +522,24 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
   }
   if (P.out_T) {
     // operand layout of the tensor-core Hankel GEMM: real column 2k + c,
-    // transverse index contiguous, scaled by s_row
+    // transverse index contiguous, scaled by s_row; column maxima for the
+    // GEMM's operand scaling
     R* base = reinterpret_cast<R*>(P.S_out);
     const R sc = P.out_scale ? P.out_scale[row] : (R)1;
 #pragma unroll
     for (int m = 0; m < EW; ++m) {
       int k = tid + m * T;
       C v = S0[m] + dz * acc[m];
-      base[(size_t)(2 * k) * P.ldT + row] = sc * v.x;
-      base[(size_t)(2 * k + 1) * P.ldT + row] = sc * v.y;
+      const R vx = sc * v.x, vy = sc * v.y;
+      base[(size_t)(2 * k) * P.ldT + row] = vx;
+      base[(size_t)(2 * k + 1) * P.ldT + row] = vy;
+      if (P.cm_out) {
+        atomicMax(&P.cm_out[2 * k], __float_as_uint(fabsf((float)vx)));
+        atomicMax(&P.cm_out[2 * k + 1], __float_as_uint(fabsf((float)vy)));
+      }
     }
+    if (P.cm_clear)
+      for (int i = row * T + tid; i < P.ncols; i += gridDim.x * T) P.cm_clear[i] = 0u;
   } else {
     C* dst = P.S_out + (size_t)row * P.ld;
 #pragma unroll
@@ -541,39 +552,71 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
 
 // ---------------------------------------------------------------------------
 // Reductions over the current field (FieldAnalyzers.jl:166-215): Imax,
-// fluence per row F = sum_t |E|^2 dt (FP64), optional power per t
-// P[t] += w_row |E|^2.  Flags non-finite values.
+// fluence per row F = sum_t |E|^2 dt, optionally |E|^2 itself into
+// Iout[row][t] (for the power P[t] = sum_row w_row |E|^2, k_colsum).  Flags
+// non-finite values.  The per-thread and
+// per-warp sums run in the working precision (a pairwise sum of 4096
+// positive terms: relative error below 1e-6 in FP32), the eight warp
+// partials are joined in FP64.
 template <typename R, int N>
-__global__ void __launch_bounds__(N / 16) k_rowreduce(RowParams<R> P, double* fluence, double* power,
-                                                      const double* pw, int check_done) {
+__global__ void __launch_bounds__(N / 16) k_rowreduce(RowParams<R> P, double* fluence, R* Iout, int check_done) {
   typedef typename C2T<R>::type C;
-  constexpr int T = N / 16, NP = N + N / 16;
+  constexpr int T = N / 16, NP = N + N / 16, NW = T / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* X = reinterpret_cast<C*>(smem_raw);
-  double* dscratch = reinterpret_cast<double*>(X + NP);
+  R* rs = reinterpret_cast<R*>(X + NP);   // [2 * NW]
   DevCtl* ctl = P.ctl;
   if (check_done && ctl->done) return;
-  const int row = blockIdx.x, tid = threadIdx.x;
+  const int row = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   load_time_row<R, N>(P, X, row, ctl->guard_pending != 0);
-  double s = 0;
+  R s[4] = {0, 0, 0, 0};
   R mx = 0;
-  const double w = power ? pw[row] : 0.0;
-#pragma unroll 4
+#pragma unroll
   for (int m = 0; m < 16; ++m) {
     int j = tid + m * T;
     C e = X[pad16(j)];
     R I = e.x * e.x + e.y * e.y;
-    s += (double)I;
+    s[m & 3] += I;
     mx = max(mx, I);
-    if (power) atomicAdd(&power[j], w * (double)I);
+    if (Iout) Iout[(size_t)row * N + j] = I;
   }
-  double tot = block_sum<double>(s, dscratch);
-  double bm = block_max<double>((double)mx, dscratch);
+  R ts = warp_sum<R>((s[0] + s[1]) + (s[2] + s[3]));
+  R tm = warp_max<R>(mx);
+  if (lane == 0) {
+    rs[w] = ts;
+    rs[NW + w] = tm;
+  }
+  __syncthreads();
   if (tid == 0) {
+    double tot = 0, bm = 0;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+      tot += (double)rs[i];
+      bm = fmax(bm, (double)rs[NW + i]);
+    }
     fluence[row] = tot * (double)P.dt;
     if (!isfinite(tot)) atomicOr(&ctl->flags, FIL_FLAG_NAN);
     else atomic_max_nonneg(&ctl->imax_acc, bm);
   }
+}
+
+// Power P[t] = sum_row w_row I[row][t] (FieldAnalyzers.jl:166-215): one
+// thread per column t and block of 64 rows, a working-precision partial sum
+// per block, FP64 atomics across the row blocks (16-way for 1000 rows).
+template <typename R>
+__global__ void __launch_bounds__(256) k_colsum(const R* __restrict__ I, const double* __restrict__ w,
+                                                double* power, int nrows, int nt) {
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  const int r0 = blockIdx.y * 64, r1 = min(r0 + 64, nrows);
+  if (t >= nt) return;
+  R a0 = 0, a1 = 0;
+  int r = r0;
+  for (; r + 1 < r1; r += 2) {
+    a0 += (R)w[r] * I[(size_t)r * nt + t];
+    a1 += (R)w[r + 1] * I[(size_t)(r + 1) * nt + t];
+  }
+  if (r < r1) a0 += (R)w[r] * I[(size_t)r * nt + t];
+  atomicAdd(&power[t], (double)a0 + (double)a1);
 }
 
 // ---------------------------------------------------------------------------

@@ -17,18 +17,25 @@ static inline PFN_cuTensorMapEncodeTiled_v12000 tc_encode_fn() {
   return fn;
 }
 
-// 2-D row-major FP32 tensor [outer][inner], box [box_outer][box_inner] with
-// 128-byte swizzle (box_inner * 4 must be 128).  Returns 0 on success.
-static inline int tc_make_map(CUtensorMap* m, const float* base, unsigned long long inner,
+// 2-D row-major tensor [outer][inner] of FP32 (elem 4) or FP16 (elem 2),
+// box [box_outer][box_inner]; the swizzle span is the box row
+// (box_inner * elem = 128 B: 128-byte swizzle, 64 B: 64-byte swizzle).
+// Returns 0 on success.
+static inline int tc_make_map(CUtensorMap* m, const void* base, int elem, unsigned long long inner,
                               unsigned long long outer, unsigned box_inner, unsigned box_outer) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = tc_encode_fn();
   if (!fn) return -1;
+  const unsigned row = box_inner * (unsigned)elem;
+  CUtensorMapSwizzle sw;
+  if (row == 128) sw = CU_TENSOR_MAP_SWIZZLE_128B;
+  else if (row == 64) sw = CU_TENSOR_MAP_SWIZZLE_64B;
+  else return -2;
   cuuint64_t dims[2] = {inner, outer};
-  cuuint64_t strides[1] = {inner * 4};
+  cuuint64_t strides[1] = {inner * (unsigned long long)elem};
   cuuint32_t box[2] = {box_inner, box_outer};
   cuuint32_t es[2] = {1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUtensorMapDataType dt = (elem == 4) ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+  CUresult r = fn(m, dt, 2, const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : (int)r;
 }

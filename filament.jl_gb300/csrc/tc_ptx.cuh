@@ -77,6 +77,14 @@ __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
 // arrive on an mbarrier when all previously issued MMAs of this thread finish
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
@@ -111,6 +119,20 @@ __device__ __forceinline__ uint64_t desc_k128(uint32_t saddr) {
   d |= (uint64_t)1 << 46;                              // descriptor version
   d |= (uint64_t)2 << 61;                              // 128-byte swizzle
   return d;
+}
+// Same for 64-byte swizzle: rows of 64 B, 8-row core groups 512 B apart.
+__device__ __forceinline__ uint64_t desc_k64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(512 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)4 << 61;                              // 64-byte swizzle
+  return d;
+}
+// Instruction descriptor, kind::f16: D f32, A/B f16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 // Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {

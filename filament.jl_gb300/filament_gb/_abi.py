@@ -39,7 +39,7 @@ OPT_XYT_GUARD_BUGCOMPAT = 2
 OPT_CLAMP_LAST_DZ = 3
 OPT_TIMING = 4
 OPT_ANALYTIC_PROJECTION = 5
-OPT_DHT_TENSOR = 6
+OPT_DHT_SIMT = 6
 
 _dp = C.POINTER(C.c_double)
 

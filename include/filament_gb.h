@@ -96,15 +96,10 @@ extern "C" {
                                   a time, writes a buffer larger than L2
                                   before each step and records per-kernel
                                   device times (fil_kernel_times)          */
-#define FIL_OPT_DHT_TENSOR 6    /* mixed form: run the Hankel transforms on
-                                  the tcgen05 tensor cores (TF32 split
-                                  products) instead of the FP32 CUDA-core
-                                  GEMMs.  ~2x faster transforms; the tensor
-                                  core's round-toward-zero sums leave a
-                                  data-dependent damping of ~7e-8 per
-                                  transform (5e-4 field error after 327
-                                  steps of the 1000 x 4096 filament run,
-                                  against 7e-5 for the default)          */
+#define FIL_OPT_DHT_SIMT 6      /* mixed form: run the Hankel transforms as
+                                  FP32 CUDA-core GEMMs instead of the
+                                  tcgen05 tensor-core GEMMs on exact FP16
+                                  slices (the default)                    */
 #define FIL_OPT_ANALYTIC_PROJECTION 5 /* drop negative frequencies after
                                   every t->w transform.  The library's field
                                   state is the analytic half spectrum, so

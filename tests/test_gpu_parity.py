@@ -117,13 +117,13 @@ def test_half_spectrum_projection_effect_is_small(gpu_lib):
 
 @pytest.mark.parametrize("dht", ["tensor", "simt"])
 def test_hankel_paths_agree_with_oracle(gpu_lib, dht):
-    """Mixed form with the CUDA-core Hankel GEMMs (default) and with the
-    tcgen05 tensor-core GEMMs, full model, RK4."""
+    """Mixed form with the tcgen05 Hankel GEMMs (default) and with the
+    CUDA-core GEMMs, full model, RK4."""
     from filament_gb import _abi
     inp = rt_input(PPcr=150.0, ALG="RK4")
     g, r = pair(inp, "mixed")
-    if dht == "tensor":
-        g.handle.set_option(_abi.OPT_DHT_TENSOR, 1)
+    if dht == "simt":
+        g.handle.set_option(_abi.OPT_DHT_SIMT, 1)
     step_both(g, r, 4, 1e-3)
     assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL["mixed"]
 
@@ -131,15 +131,14 @@ def test_hankel_paths_agree_with_oracle(gpu_lib, dht):
 @pytest.mark.parametrize("dht", ["tensor", "simt"])
 def test_linear_energy_drift_at_fp32_floor(gpu_lib, dht):
     """Linear propagation over 60 steps against the FP64 oracle.  A tensor
-    core accumulating the whole K sum (round toward zero) damps every
-    transform by ~7e-6, i.e. ~8e-4 in energy here; with the chunked register
-    accumulation the tensor-core path stays within 2.5e-5 of the oracle,
-    the CUDA-core path at the FP32 floor of the FFTs."""
+    core summing the whole K range in FP32 (round toward zero) damps every
+    transform by ~7e-6, i.e. ~8e-4 in energy here; the exact-slice GEMM must
+    stay at the FP32 floor of the FFTs, like the CUDA-core GEMM."""
     from filament_gb import _abi
     inp = rt_input(NONLINEARITY=False, PLASMA=False, rguard=0.0, tguard=0.0, kguard=90.0, wguard=1e30)
     g, r = pair(inp, "mixed")
-    if dht == "tensor":
-        g.handle.set_option(_abi.OPT_DHT_TENSOR, 1)
+    if dht == "simt":
+        g.handle.set_option(_abi.OPT_DHT_SIMT, 1)
     e0 = r.handle.analyze()["energy"]
     step_both(g, r, 60, 2e-3)
     eg, er = g.handle.analyze()["energy"], r.handle.analyze()["energy"]
