@@ -74,10 +74,11 @@ struct fil_handle {
   void* MA1[3] = {nullptr, nullptr, nullptr};  // M1 = T diag(s): FP16 slices a0, a1, a2
   void* MA2[3] = {nullptr, nullptr, nullptr};  // M2 = diag(1/s) T
   void* qa1 = nullptr; void* qa2 = nullptr;    // [mpad] row scales of M1, M2
-  void* cm1 = nullptr; void* cm2 = nullptr;    // [2 nh] column maxima of W1, W2 (float bits)
+  void* BS[3] = {nullptr, nullptr, nullptr};   // FP16 slices of the GEMM operand W1 or W2, [2 nh][mpad]
+  void* qb = nullptr;                          // [mpad/64][2 nh] chunk scales of the operand
   void* kzt = nullptr; void* gdt = nullptr;    // [mpad][nh] KZ (float2), guard (float)
   int* tc_err = nullptr;
-  CUtensorMap tm_a1[3], tm_a2[3], tm_w1, tm_w2;
+  CUtensorMap tm_a1[3], tm_a2[3], tm_b[3];
 };
 
 void fil_set_global_error(const std::string& m) { g_err = m; }
@@ -311,7 +312,7 @@ static void slice_rows(const std::vector<double>& x, int n, int mp, std::vector<
 
 // Tables of the tensor-core Hankel path: the slices of M1 = T diag(s) and
 // M2 = diag(1/s) T with their row scales, the propagator's KZ and guard per
-// (r, w), the column-maximum arrays and the TMA maps of the operands.
+// (r, w), the slice buffers of the field operand and the TMA maps.
 static int create_tc(fil_handle* h, const fil_tables* t) {
   typedef std::complex<double> cd;
   const int n1 = h->n1, nh = h->nh, mp = h->mpad;
@@ -360,18 +361,18 @@ static int create_tc(fil_handle* h, const fil_tables* t) {
   if (up(&h->qa1, q1.data(), mp * sizeof(float)) || up(&h->qa2, q2.data(), mp * sizeof(float)) ||
       up(&h->kzt, kz.data(), kz.size() * sizeof(float)) || up(&h->gdt, gd.data(), gd.size() * sizeof(float)))
     return FIL_ERR_CUDA;
-  CK(cudaMalloc(&h->cm1, 2 * nh * sizeof(unsigned)));
-  CK(cudaMalloc(&h->cm2, 2 * nh * sizeof(unsigned)));
-  CK(cudaMemset(h->cm1, 0, 2 * nh * sizeof(unsigned)));
-  CK(cudaMemset(h->cm2, 0, 2 * nh * sizeof(unsigned)));
+  for (int k = 0; k < 3; ++k) {
+    CK(cudaMalloc(&h->BS[k], sb / mp * 2 * nh));
+    CK(cudaMemset(h->BS[k], 0, sb / mp * 2 * nh));
+  }
+  CK(cudaMalloc(&h->qb, (size_t)(mp / 64) * 2 * nh * sizeof(float)));
   CK(cudaMalloc(&h->tc_err, sizeof(int)));
   CK(cudaMemset(h->tc_err, 0, sizeof(int)));
   for (int k = 0; k < 3; ++k)
     if (tc_make_map(&h->tm_a1[k], h->MA1[k], 2, mp, mp, 32, 128) ||
-        tc_make_map(&h->tm_a2[k], h->MA2[k], 2, mp, mp, 32, 128))
+        tc_make_map(&h->tm_a2[k], h->MA2[k], 2, mp, mp, 32, 128) ||
+        tc_make_map(&h->tm_b[k], h->BS[k], 2, mp, 2 * nh, 32, 128))
       return fail(h, FIL_ERR_CUDA, "cuTensorMapEncodeTiled failed");
-  if (tc_make_map(&h->tm_w1, h->W1, 4, mp, 2 * nh, 32, 128) || tc_make_map(&h->tm_w2, h->W2, 4, mp, 2 * nh, 32, 128))
-    return fail(h, FIL_ERR_CUDA, "cuTensorMapEncodeTiled failed");
   return 0;
 }
 
@@ -444,9 +445,6 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   if (tcp) {
     P.out_T = 1;
     P.out_scale = nullptr;   // the scalings live in M1, M2
-    P.cm_out = (unsigned*)h->cm1;
-    P.cm_clear = (unsigned*)h->cm2;
-    P.ncols = Nc;
   }
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
   CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
@@ -462,21 +460,20 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
     p1.gd = (const float*)h->gdt;
     p1.nh = h->nh;
     p1.qa = (const float*)h->qa1;
-    p1.cm_in = (const unsigned*)h->cm1;
-    p1.cm_out = (unsigned*)h->cm2;
+    p1.qb = (const float*)h->qb;
+    p1.ldqb = Nc;
     p1.ctl = h->ctl;
     p1.err = h->tc_err;
-    CK(launch_dht_tc(h->tm_a1[0], h->tm_a1[1], h->tm_a1[2], h->tm_w1, p1, h->mpad, Nc, h->st));
+    CK(launch_slice((const float*)h->W1, h->BS, (float*)h->qb, Nc, h->mpad, h->ctl, h->st));
+    CK(launch_dht_tc(h->tm_a1, h->tm_b, p1, h->mpad, Nc, h->st));
     if (timed) CK(cudaEventRecord(h->ev[3], h->st));
     TcGemmParams p2 = p1;
     p2.out = (float*)h->S;
     p2.ldo = Nc;
     p2.mode = 2;
     p2.qa = (const float*)h->qa2;
-    p2.cm_in = (const unsigned*)h->cm2;
-    p2.cm_out = nullptr;
-    p2.cm_clear = (unsigned*)h->cm1;
-    CK(launch_dht_tc(h->tm_a2[0], h->tm_a2[1], h->tm_a2[2], h->tm_w2, p2, h->mpad, Nc, h->st));
+    CK(launch_slice((const float*)h->W2, h->BS, (float*)h->qb, Nc, h->mpad, h->ctl, h->st));
+    CK(launch_dht_tc(h->tm_a2, h->tm_b, p2, h->mpad, Nc, h->st));
   } else {
     CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 1, h->st));
     if (timed) CK(cudaEventRecord(h->ev[3], h->st));
@@ -524,7 +521,7 @@ static void free_all(fil_handle* h) {
   void* bufs[] = {h->S, h->W1, h->W2, h->M1, h->M2, h->tw, h->g1, h->g2, h->gt, h->Cc, h->Cf, h->Cl,
                   h->kt2, h->beta, h->dfr, h->kmax2, h->wg, h->rho_g, h->kdrho_g, h->stage,
                   h->fluence, h->power, h->pw, h->rho_end, h->ctl, h->flushbuf,
-                  h->qa1, h->qa2, h->cm1, h->cm2, h->kzt, h->gdt, h->tc_err,
+                  h->qa1, h->qa2, h->BS[0], h->BS[1], h->BS[2], h->qb, h->kzt, h->gdt, h->tc_err,
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2]};
   for (void* p : bufs)
     if (p) cudaFree(p);

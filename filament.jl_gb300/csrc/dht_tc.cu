@@ -1,16 +1,26 @@
-// dht_tc.cu -- launch wrapper of the tcgen05 Hankel GEMM (dht_tc.cuh).
+// dht_tc.cu -- launch wrappers of the tensor-core Hankel GEMM and its
+// operand slicer (dht_tc.cuh).
 #include "launch.h"
 #include "dht_tc.cuh"
 
-cudaError_t launch_dht_tc(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& a2,
-                          const CUtensorMap& b, const TcGemmParams& p, int M, int N, cudaStream_t st) {
+cudaError_t launch_dht_tc(const CUtensorMap (&a)[3], const CUtensorMap (&b)[3], const TcGemmParams& p, int M,
+                          int N, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_dht_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
     if (e != cudaSuccess) return e;
     attr = true;
   }
+  if (M % TC_BM || N % TC_BN || p.K % TC_CHUNK) return cudaErrorInvalidValue;
   dim3 grid(N / TC_BN, M / TC_BM);
-  k_dht_tc<<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(a0, a1, a2, b, p);
+  k_dht_tc<<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(a[0], a[1], a[2], b[0], b[1], b[2], p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_slice(const float* B, void* const (&s)[3], float* qb, int N, int K, const DevCtl* ctl,
+                         cudaStream_t st) {
+  if (K % TC_CHUNK) return cudaErrorInvalidValue;
+  const int warps = N * (K / TC_CHUNK);
+  k_slice<<<(warps + 7) / 8, 256, 0, st>>>(B, (__half2*)s[0], (__half2*)s[1], (__half2*)s[2], qb, N, K, ctl);
   return cudaGetLastError();
 }

@@ -13,31 +13,30 @@
 // Numerics.  The tensor core adds FP32 products rounding toward zero; summed
 // over K = 1024 that biases every output by ~ -7e-6 relative, and the field
 // would be damped step after step.  Here the dominant product is exact:
-//   A[i][k] = qa_i (a0 + a1 + a2),  a0 integer, |a0| <= 1024,
-//   B[k][j] = qb_j (b0 + b1 + b2),  b0 integer, |b0| <= 256,
-// a1 = fp16(rest), a2 = fp16(rest - a1), likewise b1, b2; qa_i and qb_j are
-// powers of two from the row maximum of A and the column maximum of B.  All
-// slices are exact FP16 values.  Over one 32-wide K chunk the head sum
-// sum_k a0 b0 is an integer below 2^23, which the tensor core computes
-// exactly.  The five correction products a0 b1 + a1 b0 + a1 b1 + a0 b2 + a2 b0
-// (together below 2^-9 of the head) go to a second accumulator; its
-// round-toward-zero error is ~2^-30 of the result, and the dropped products
-// a1 b2, a2 b1, a2 b2 are below 2^-31.  The consumer warps add each chunk's
-// two accumulators into FP32 registers (round to nearest) and apply
-// qa_i qb_j in the epilogue.
+//   A[i][k] = qa_i (a0 + a1 + a2),     a0 integer, |a0| <= 1024,
+//   B[k][j] = qb_cj (b0 + b1 + b2),    b0 integer, |b0| <= 128,
+// a1 = fp16(rest), a2 = fp16(rest - a1), likewise b1, b2; qa_i is a power of
+// two from the row maximum of A, qb_cj one from the maximum of column j over
+// the 64-wide K chunk c.  All slices are exact FP16 values.  Over one chunk
+// the head sum sum_k a0 b0 is an integer below 2^23, which the tensor core
+// computes exactly.  The five correction products
+// a0 b1 + a1 b0 + a1 b1 + a0 b2 + a2 b0 (together below 2^-8 of the head) go
+// to a second accumulator, whose round-toward-zero error is ~2^-28 of the
+// result; the dropped products a1 b2, a2 b1, a2 b2 are below 2^-29.  The
+// consumer warps add each chunk's two accumulators times qb_cj into FP32
+// registers (round to nearest) and apply qa_i in the epilogue.
 //
-// Column maxima of B come from the producer of B (the row kernel, or the
-// epilogue of the forward transform) through atomicMax on the bit patterns of
-// |value|; the inverse transform clears the row kernel's array for the next
-// step, the row kernel clears the forward transform's.
+// k_slice cuts the FP32 operand B (written by the row kernel, or by the
+// epilogue of the forward transform) into its slices and chunk scales once,
+// so the GEMM streams FP16 tiles with TMA only.
 //
-// Roles (320 threads): warps 0-7 convert each stage's FP32 B tile into its
-// three slices, drain the accumulators and run the epilogue; warp 8 issues
-// the TMA loads (three A slices and the FP32 B tile); warp 9 issues the MMAs.
-// Tile 128 x 128, K chunk 32, three shared-memory stages of
-// {B fp32, a0, a1, a2, b0, b1, b2} = 64 KB, two accumulator pairs in 512
+// GEMM roles (320 threads): warps 0-7 drain the accumulators and run the
+// epilogue; warp 8 issues the TMA loads; warp 9 issues the MMAs.  Tile
+// 128 x 128, K stage 32 (four stages of six 8 KB slice tiles, 64-byte
+// swizzle), accumulation chunk 64, two accumulator pairs in 512
 // tensor-memory columns (ping-pong between chunks).  Every mbarrier wait is
-// bounded and also gives up once another role has failed; a failure sets *err.
+// bounded and also gives up once another role has failed; a failure sets
+// *err.
 #pragma once
 #include <cuda_fp16.h>
 #include "tc_ptx.cuh"
@@ -46,19 +45,17 @@
 
 #define TC_BM 128
 #define TC_BN 128
-#define TC_BK 32
-#define TC_STAGES 3
+#define TC_BK 32                               // K per shared-memory stage
+#define TC_CHUNK 64                            // K per exact chunk (scale block of B)
+#define TC_STAGES 4
 #define TC_CONSUMERS 256
 #define TC_THREADS (TC_CONSUMERS + 64)
-#define TC_RAW_BYTES (TC_BN * TC_BK * 4)       // FP32 B tile, 128-byte swizzle
 #define TC_SLICE_BYTES (TC_BM * TC_BK * 2)     // one FP16 slice tile, 64-byte swizzle
-#define TC_STAGE_BYTES (TC_RAW_BYTES + 6 * TC_SLICE_BYTES)
-#define TC_SMEM_BYTES (TC_STAGES * TC_STAGE_BYTES + 1024 + 256 + 2 * TC_BN * 4)
+#define TC_STAGE_BYTES (6 * TC_SLICE_BYTES)
+#define TC_SMEM_BYTES (TC_STAGES * TC_STAGE_BYTES + 1024 + 256)
 #define TC_WAIT_LIMIT (1u << 26)
-// byte offsets inside a stage
-#define TC_OFF_A(s) (TC_RAW_BYTES + (s) * TC_SLICE_BYTES)
-#define TC_OFF_B(s) (TC_RAW_BYTES + (3 + (s)) * TC_SLICE_BYTES)
-
+#define TC_OFF_A(s) ((s) * TC_SLICE_BYTES)
+#define TC_OFF_B(s) ((3 + (s)) * TC_SLICE_BYTES)
 
 // bounded wait that also stops when *fail is set by another role
 __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile int* fail) {
@@ -73,20 +70,51 @@ __device__ __forceinline__ void tc_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// column scale qb = 2^(E-7) for a column maximum m = f 2^E (|B / qb| < 256);
-// returns 1/qb, or 0 for an all-zero column
-__device__ __forceinline__ float tc_inv_scale(unsigned mbits, float* qb) {
-  int e = (int)((mbits >> 23) & 0xFFu) - 127;
-  if ((mbits & 0x7FFFFFFFu) == 0u) { *qb = 0.f; return 0.f; }
-  e = max(e, -100);
-  e = min(e, 120);
-  *qb = __uint_as_float((unsigned)(e - 7 + 127) << 23);
-  return __uint_as_float((unsigned)(7 - e + 127) << 23);
+// ---------------------------------------------------------------------------
+// B [N][K] FP32 (K contiguous) -> slices b0, b1, b2 [N][K] FP16 and chunk
+// scales qb [K/64][N].  One warp per (column n, chunk c); lane l holds
+// k = 64c + 2l, 2l + 1.  qb = 2^(E-6) for a chunk maximum f 2^E, so
+// |B / qb| < 128.
+__global__ void __launch_bounds__(256) k_slice(const float* __restrict__ B, __half2* b0, __half2* b1, __half2* b2,
+                                               float* qb, int N, int K, const DevCtl* ctl) {
+  if (ctl && ctl->done) return;
+  const int lane = threadIdx.x & 31;
+  const int g = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int nch = K / TC_CHUNK;
+  if (g >= N * nch) return;
+  const int n = g / nch, c = g - n * nch;
+  const size_t e2 = ((size_t)n * K + (size_t)c * TC_CHUNK) / 2 + lane;   // half2 / float2 index
+  const float2 v = reinterpret_cast<const float2*>(B)[e2];
+  const unsigned m = __reduce_max_sync(0xffffffffu, max(__float_as_uint(fabsf(v.x)), __float_as_uint(fabsf(v.y))));
+  float q = 0.f, iq = 0.f;
+  if (m != 0u) {
+    int e = (int)((m >> 23) & 0xFFu) - 127;
+    e = min(max(e, -100), 120);
+    q = __uint_as_float((unsigned)(e - 6 + 127) << 23);
+    iq = __uint_as_float((unsigned)(6 - e + 127) << 23);
+  }
+  float hd[2], m1[2], m2[2];
+  const float x[2] = {v.x * iq, v.y * iq};
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const float i0 = rintf(x[i]);                 // |i0| <= 128, exact
+    const float r = x[i] - i0;                    // exact, |r| <= 1/2
+    const float r1 = __half2float(__float2half_rn(r));
+    hd[i] = i0;
+    m1[i] = r1;
+    m2[i] = r - r1;                               // exact
+  }
+  b0[e2] = __floats2half2_rn(hd[0], hd[1]);
+  b1[e2] = __floats2half2_rn(m1[0], m1[1]);
+  b2[e2] = __floats2half2_rn(m2[0], m2[1]);
+  if (lane == 0) qb[(size_t)c * N + n] = q;
 }
 
+// ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_dht_tc(const __grid_constant__ CUtensorMap tA0, const __grid_constant__ CUtensorMap tA1,
-             const __grid_constant__ CUtensorMap tA2, const __grid_constant__ CUtensorMap tB, TcGemmParams p) {
+             const __grid_constant__ CUtensorMap tA2, const __grid_constant__ CUtensorMap tB0,
+             const __grid_constant__ CUtensorMap tB1, const __grid_constant__ CUtensorMap tB2, TcGemmParams p) {
   extern __shared__ __align__(1024) uint8_t tc_smem[];
   __shared__ volatile int s_fail;
   if (p.ctl && p.ctl->done) return;
@@ -95,26 +123,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t sbase = (raw + 1023u) & ~1023u;
   uint8_t* gbase = tc_smem + (sbase - raw);
   const uint32_t bars = sbase + TC_STAGES * TC_STAGE_BYTES;
-  // barrier block: full[3] conv[3] empty[3] accf[2] acce[2] tmem_slot done
+  // barrier block: full[4] empty[4] accf[2] acce[2] done tmem_slot
   auto full_bar = [&](int s) { return bars + 8u * s; };
-  auto conv_bar = [&](int s) { return bars + 24u + 8u * s; };
-  auto empty_bar = [&](int s) { return bars + 48u + 8u * s; };
-  auto accf_bar = [&](int b) { return bars + 72u + 8u * b; };
-  auto acce_bar = [&](int b) { return bars + 88u + 8u * b; };
+  auto empty_bar = [&](int s) { return bars + 32u + 8u * s; };
+  auto accf_bar = [&](int b) { return bars + 64u + 8u * b; };
+  auto acce_bar = [&](int b) { return bars + 80u + 8u * b; };
+  const uint32_t done_bar = bars + 96u;   // all issued MMAs complete
   const uint32_t tmem_slot = bars + 104u;
-  const uint32_t done_bar = bars + 112u;   // all issued MMAs complete
   volatile uint32_t* tmem_slot_g = reinterpret_cast<volatile uint32_t*>(gbase + TC_STAGES * TC_STAGE_BYTES + 104);
-  float* qb_s = reinterpret_cast<float*>(gbase + TC_STAGES * TC_STAGE_BYTES + 256);
-  float* iqb_s = qb_s + TC_BN;
 
   const int bm = blockIdx.y * TC_BM, bn = blockIdx.x * TC_BN;
   if (tid == 0) s_fail = 0;
-  if (tid < TC_BN) iqb_s[tid] = tc_inv_scale(p.cm_in[bn + tid], &qb_s[tid]);
   if (warp == 0) tc::tmem_alloc(tmem_slot, 512);
   if (tid == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
       tc::mbar_init(full_bar(s), 1);
-      tc::mbar_init(conv_bar(s), 8);
       tc::mbar_init(empty_bar(s), 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -128,7 +151,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot_g;
-  const int nk = p.K / TC_BK;
+  const int nk = p.K / TC_BK;              // stages; two per chunk
+  const int nc = p.K / TC_CHUNK;
 
   float acc[64];
 #pragma unroll
@@ -142,11 +166,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int use = kb / TC_STAGES;
         if (use > 0 && !tc_wait(empty_bar(s), (use - 1) & 1, &s_fail)) break;
         const uint32_t st = sbase + s * TC_STAGE_BYTES;
-        tc::mbar_expect_tx(full_bar(s), TC_RAW_BYTES + 3 * TC_SLICE_BYTES);
-        tc::tma_load_2d(st, &tB, kb * TC_BK, bn, full_bar(s));
+        tc::mbar_expect_tx(full_bar(s), TC_STAGE_BYTES);
         tc::tma_load_2d(st + TC_OFF_A(0), &tA0, kb * TC_BK, bm, full_bar(s));
         tc::tma_load_2d(st + TC_OFF_A(1), &tA1, kb * TC_BK, bm, full_bar(s));
         tc::tma_load_2d(st + TC_OFF_A(2), &tA2, kb * TC_BK, bm, full_bar(s));
+        tc::tma_load_2d(st + TC_OFF_B(0), &tB0, kb * TC_BK, bn, full_bar(s));
+        tc::tma_load_2d(st + TC_OFF_B(1), &tB1, kb * TC_BK, bn, full_bar(s));
+        tc::tma_load_2d(st + TC_OFF_B(2), &tB2, kb * TC_BK, bn, full_bar(s));
       }
       // wait for the last loads so no copy lands after the block exits
       for (int kb = (nk > TC_STAGES ? nk - TC_STAGES : 0); kb < nk; ++kb)
@@ -158,10 +184,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const uint32_t idesc = tc::idesc_f16(TC_BM, TC_BN);
       for (int kb = 0; kb < nk && !s_fail; ++kb) {
         const int s = kb % TC_STAGES;
-        if (!tc_wait(conv_bar(s), (kb / TC_STAGES) & 1, &s_fail)) break;
-        const int b = kb & 1;
-        const int use = kb >> 1;
-        if (use > 0 && !tc_wait(acce_bar(b), (use - 1) & 1, &s_fail)) break;
+        if (!tc_wait(full_bar(s), (kb / TC_STAGES) & 1, &s_fail)) break;
+        const int c = kb >> 1, b = c & 1;
+        const bool first = (kb & 1) == 0;
+        if (first && (c >> 1) > 0 && !tc_wait(acce_bar(b), ((c >> 1) - 1) & 1, &s_fail)) break;
         tc::tc_fence_after();
         const uint32_t st = sbase + s * TC_STAGE_BYTES;
         const uint32_t big = tmem + (uint32_t)(b * 256), small = big + 128u;
@@ -172,15 +198,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                          a2 = tc::desc_k64(st + TC_OFF_A(2) + ko);
           const uint64_t b0 = tc::desc_k64(st + TC_OFF_B(0) + ko), b1 = tc::desc_k64(st + TC_OFF_B(1) + ko),
                          b2 = tc::desc_k64(st + TC_OFF_B(2) + ko);
-          tc::mma_f16(big, a0, b0, idesc, kk != 0);
-          tc::mma_f16(small, a0, b1, idesc, kk != 0);
+          const uint32_t accum = (first && kk == 0) ? 0u : 1u;
+          tc::mma_f16(big, a0, b0, idesc, accum);
+          tc::mma_f16(small, a0, b1, idesc, accum);
           tc::mma_f16(small, a1, b0, idesc, 1);
           tc::mma_f16(small, a1, b1, idesc, 1);
           tc::mma_f16(small, a0, b2, idesc, 1);
           tc::mma_f16(small, a2, b0, idesc, 1);
         }
-        tc::mma_commit(accf_bar(b));
         tc::mma_commit(empty_bar(s));
+        if (!first) tc::mma_commit(accf_bar(b));
       }
       // no MMA may still write tensor memory when it is released, also after
       // a failure
@@ -188,73 +215,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       tc::mbar_wait(done_bar, 0, TC_WAIT_LIMIT);
     }
   } else {
-    // ---------------- consumers
+    // ---------------- consumers: chunk accumulators -> FP32 registers
     const int q = warp & 3, hcol = warp >> 2;
-    // thread -> (B^T row n = output column, half h of the 32-wide chunk)
-    const int n = tid >> 1, h = tid & 1;
-    const float iq = iqb_s[n];
-    auto convert = [&](int kb) -> bool {
-      const int s = kb % TC_STAGES;
-      if (!tc_wait(full_bar(s), (kb / TC_STAGES) & 1, &s_fail)) return false;
-      uint8_t* st = gbase + s * TC_STAGE_BYTES;
-      float y[16];
+    const float* qcol = p.qb + bn + 64 * hcol;
+    for (int c = 0; c < nc; ++c) {
+      const int b = c & 1;
+      const float4* qv = reinterpret_cast<const float4*>(qcol + (size_t)c * p.ldqb);
+      float4 sc[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        // 128-byte swizzle: 16-byte unit u of row n sits at unit u ^ (n & 7)
-        const int u = (4 * h + j) ^ (n & 7);
-        const float4 v = *reinterpret_cast<const float4*>(st + n * 128 + u * 16);
-        y[4 * j] = v.x * iq;
-        y[4 * j + 1] = v.y * iq;
-        y[4 * j + 2] = v.z * iq;
-        y[4 * j + 3] = v.w * iq;
-      }
-      __half2 s0[8], s1[8], s2[8];
-#pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        float hd[2], m1[2], m2[2];
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-          const float x = y[2 * e + c];
-          const float i0 = rintf(x);                 // |i0| <= 256, exact
-          const float r = x - i0;                    // exact, |r| <= 1/2
-          const float r1 = __half2float(__float2half_rn(r));
-          hd[c] = i0;
-          m1[c] = r1;
-          m2[c] = r - r1;                            // exact
-        }
-        s0[e] = __floats2half2_rn(hd[0], hd[1]);
-        s1[e] = __floats2half2_rn(m1[0], m1[1]);
-        s2[e] = __floats2half2_rn(m2[0], m2[1]);
-      }
-#pragma unroll
-      for (int w = 0; w < 2; ++w) {
-        // 64-byte swizzle: 16-byte unit u of row n sits at unit u ^ ((n >> 1) & 3)
-        const int u = (2 * h + w) ^ ((n >> 1) & 3);
-        const int off = n * 64 + u * 16;
-        *reinterpret_cast<uint4*>(st + TC_OFF_B(0) + off) = *reinterpret_cast<const uint4*>(&s0[4 * w]);
-        *reinterpret_cast<uint4*>(st + TC_OFF_B(1) + off) = *reinterpret_cast<const uint4*>(&s1[4 * w]);
-        *reinterpret_cast<uint4*>(st + TC_OFF_B(2) + off) = *reinterpret_cast<const uint4*>(&s2[4 * w]);
-      }
-      tc::fence_proxy_async_smem();
-      __syncwarp();
-      if (lane == 0) tc_arrive(conv_bar(s));
-      return true;
-    };
-    bool ok = convert(0);
-    for (int kb = 0; kb < nk && ok; ++kb) {
-      if (kb + 1 < nk) ok = convert(kb + 1);
-      if (!ok) break;
-      const int b = kb & 1;
-      if (!tc_wait(accf_bar(b), (kb >> 1) & 1, &s_fail)) { ok = false; break; }
+      for (int i = 0; i < 4; ++i) sc[i] = __ldg(qv + i);
+      if (!tc_wait(accf_bar(b), (c >> 1) & 1, &s_fail)) break;
       tc::tc_fence_after();
       const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * 256 + 64 * hcol);
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        float vb[32], vs[32];
-        tc::tmem_ld32(taddr + 32u * half, vb);
-        tc::tmem_ld32(taddr + 128u + 32u * half, vs);
+      for (int qq = 0; qq < 4; ++qq) {
+        uint32_t rb[16], rs[16];
+        tc::tmem_ld16_async(taddr + 16u * qq, rb);
+        tc::tmem_ld16_async(taddr + 128u + 16u * qq, rs);
+        tc::tmem_wait_ld16(rb, rs);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) acc[32 * half + i] += vb[i] + vs[i];
+        for (int i = 0; i < 4; ++i) {
+          const float sq[4] = {sc[i].x, sc[i].y, sc[i].z, sc[i].w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int j = 4 * i + e;
+            acc[16 * qq + j] = fmaf(__uint_as_float(rb[j]) + __uint_as_float(rs[j]), sq[e], acc[16 * qq + j]);
+          }
+        }
+        if (qq < 3) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) sc[i] = __ldg(qv + 4 * (qq + 1) + i);
+        }
       }
       tc::tc_fence_before();
       __syncwarp();
@@ -266,11 +257,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (warp < 8 && !s_fail) {
     const int q = warp & 3, hcol = warp >> 2;
     const int row = bm + 32 * q + lane;
-    const int c0 = 64 * hcol;
+    const int col0 = bn + 64 * hcol;
     const float sa = p.qa[row];
 #pragma unroll
-    for (int i = 0; i < 64; ++i) acc[i] *= sa * qb_s[c0 + i];
-    const int col0 = bn + c0;
+    for (int i = 0; i < 64; ++i) acc[i] *= sa;
     if (p.mode == 1) {
       const float dz = p.ctl ? (float)p.ctl->dz : p.dz_fixed;
       const int w0 = col0 >> 1;
@@ -287,13 +277,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         acc[2 * i + 1] = amp * (re * sn + im * cs);
       }
 #pragma unroll
-      for (int i = 0; i < 64; ++i) {
-        p.out[(size_t)(col0 + i) * p.ldo + row] = acc[i];
-        if (p.cm_out) {
-          const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(acc[i])));
-          if (lane == 0) atomicMax(&p.cm_out[col0 + i], m);
-        }
-      }
+      for (int i = 0; i < 64; ++i) p.out[(size_t)(col0 + i) * p.ldo + row] = acc[i];
     } else {
       float4* dst = reinterpret_cast<float4*>(p.out + (size_t)row * p.ldo + col0);
 #pragma unroll
@@ -307,7 +291,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc::tmem_dealloc(tmem, 512);
   }
   if (s_fail && tid == 0) atomicExch(p.err, 1);
-  if (!s_fail && p.cm_clear && blockIdx.y == 0 && tid < TC_BN) p.cm_clear[bn + tid] = 0u;
   if (p.mode == 2 && p.ctl && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0 && !s_fail)
     p.ctl->guard_pending = 1;
 }

@@ -30,8 +30,10 @@ template <typename R>
 cudaError_t launch_dht_simt(const R* A, const R* B, R* C, int M, int N, int K, const PropParams<R>& pp,
                             DevCtl* ctl, int epi, cudaStream_t st);
 struct TcGemmParams;
-cudaError_t launch_dht_tc(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& a2,
-                          const CUtensorMap& b, const TcGemmParams& p, int M, int N, cudaStream_t st);
+cudaError_t launch_dht_tc(const CUtensorMap (&a)[3], const CUtensorMap (&b)[3], const TcGemmParams& p, int M,
+                          int N, cudaStream_t st);
+cudaError_t launch_slice(const float* B, void* const (&s)[3], float* qb, int N, int K, const DevCtl* ctl,
+                         cudaStream_t st);
 cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
 cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);

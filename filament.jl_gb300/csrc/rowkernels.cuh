@@ -57,9 +57,6 @@ template <typename R> struct RowParams {
   int out_T;                    // 1: write s_row * S transposed, [2k + re/im][ldT]
   const R* out_scale;           // s_row (out_T), or NULL
   int ldT;
-  unsigned* cm_out;             // out_T: max |value| per transposed row (atomic, float bits), or NULL
-  unsigned* cm_clear;           // [ncols] cleared by the first blocks, or NULL
-  int ncols;
   DevCtl* ctl;
 };
 
@@ -522,24 +519,16 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
   }
   if (P.out_T) {
     // operand layout of the tensor-core Hankel GEMM: real column 2k + c,
-    // transverse index contiguous, scaled by s_row; column maxima for the
-    // GEMM's operand scaling
+    // transverse index contiguous, scaled by s_row
     R* base = reinterpret_cast<R*>(P.S_out);
     const R sc = P.out_scale ? P.out_scale[row] : (R)1;
 #pragma unroll
     for (int m = 0; m < EW; ++m) {
       int k = tid + m * T;
       C v = S0[m] + dz * acc[m];
-      const R vx = sc * v.x, vy = sc * v.y;
-      base[(size_t)(2 * k) * P.ldT + row] = vx;
-      base[(size_t)(2 * k + 1) * P.ldT + row] = vy;
-      if (P.cm_out) {
-        atomicMax(&P.cm_out[2 * k], __float_as_uint(fabsf((float)vx)));
-        atomicMax(&P.cm_out[2 * k + 1], __float_as_uint(fabsf((float)vy)));
-      }
+      base[(size_t)(2 * k) * P.ldT + row] = sc * v.x;
+      base[(size_t)(2 * k + 1) * P.ldT + row] = sc * v.y;
     }
-    if (P.cm_clear)
-      for (int i = row * T + tid; i < P.ncols; i += gridDim.x * T) P.cm_clear[i] = 0u;
   } else {
     C* dst = P.S_out + (size_t)row * P.ld;
 #pragma unroll

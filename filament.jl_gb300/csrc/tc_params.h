@@ -8,15 +8,14 @@ struct DevCtl;
 struct TcGemmParams {
   float* out;
   int ldo;                // leading dimension of out (floats)
-  int K;                  // contraction length, multiple of TC_BK
+  int K;                  // contraction length, multiple of 64
   int mode;               // 1 propagator + transposed store; 2 row-major store (+ guard pending)
   const float2* kz;       // mode 1: [M][nh] KZ in zu units
   const float* gd;        // mode 1: [M][nh] spectral guard
   int nh;
   const float* qa;        // [M] row scales of A (powers of two)
-  const unsigned* cm_in;  // [N] bit patterns of max |B| over each column
-  unsigned* cm_out;       // mode 1: max |out| per column of out (atomic), or NULL
-  unsigned* cm_clear;     // cleared for this block's columns by the blocks of row 0, or NULL
+  const float* qb;        // [K/64][ldqb] chunk scales of B (powers of two)
+  int ldqb;
   DevCtl* ctl;            // NULL: no controller (dz = dz_fixed)
   float dz_fixed;
   int* err;               // set to 1 on a timed-out wait
