@@ -46,6 +46,10 @@ template <typename R> struct PlasmaParams {
   int maxit;              // Newton iteration cap
   R tol;                  // Newton: stop when update^2 <= tol |u|^2
   R skip;                 // rows with max W * window below this keep rho0
+  // power law with an integer order m (multiphoton rate sigma_m I^m):
+  // W(I) = (wscale I)^m by repeated squaring instead of exp/log; 0 = no
+  int ipow[FIL_MAXCOMP];
+  R wscale[FIL_MAXCOMP];
 };
 
 template <typename R> inline PlasmaParams<R> plasma_params_as(const PlasmaParams<double>& d) {
@@ -77,6 +81,10 @@ template <typename R> inline PlasmaParams<R> plasma_params_as(const PlasmaParams
   r.maxit = d.maxit;
   r.tol = (R)d.tol;
   r.skip = (R)d.skip;
+  for (int c = 0; c < FIL_MAXCOMP; ++c) {
+    r.ipow[c] = d.ipow[c];
+    r.wscale[c] = (R)d.wscale[c];
+  }
   return r;
 }
 
@@ -172,6 +180,19 @@ template <typename R> FIL_DEV R rate_eval(const PlasmaParams<R>& P, const Plasma
   if (!(I > (R)0)) {
     *slope = T.sl[c][0];
     return (R)0;
+  }
+  if (P.ipow[c] > 0) {
+    // exp(ly + (ln I - lx) m) = (exp((ly - m lx)/m) I)^m
+    *slope = T.sl[c][0];
+    R b = I * P.wscale[c], r = (R)1;
+    int m = P.ipow[c];
+#pragma unroll 1
+    while (m) {
+      if (m & 1) r *= b;
+      m >>= 1;
+      if (m) b *= b;
+    }
+    return r;
   }
   R l = log(I);
   int i = 0;
