@@ -76,7 +76,7 @@ struct fil_handle {
   void* qa1 = nullptr; void* qa2 = nullptr;    // [mpad] row scales of M1, M2
   void* BS[3] = {nullptr, nullptr, nullptr};   // FP16 slices of the GEMM operand W1 or W2, [2 nh][mpad]
   void* qb = nullptr;                          // [mpad/64][2 nh] chunk scales of the operand
-  void* kzt = nullptr; void* gdt = nullptr;    // [nh][mpad] KZ (float2), guard (float)
+  void* kzt = nullptr; void* gdt = nullptr;    // [mpad][nh] KZ (float2), guard (float)
   int* tc_err = nullptr;
   CUtensorMap tm_a1[3], tm_a2[3], tm_b[3];
 };
@@ -353,9 +353,9 @@ static int create_tc(fil_handle* h, const fil_tables* t) {
         g = (km == 0.0) ? 0.0 : std::exp(-std::pow(kt2 / (km * km), 20));
       }
       if (t->wguard) g *= t->wguard[j];
-      kz[((size_t)j * mp + i) * 2] = (float)K.real();
-      kz[((size_t)j * mp + i) * 2 + 1] = (float)K.imag();
-      gd[(size_t)j * mp + i] = (float)g;
+      kz[((size_t)i * nh + j) * 2] = (float)K.real();
+      kz[((size_t)i * nh + j) * 2 + 1] = (float)K.imag();
+      gd[(size_t)i * nh + j] = (float)g;
     }
   }
   auto up = [&](void** dst, const void* src, size_t bytes) -> int {

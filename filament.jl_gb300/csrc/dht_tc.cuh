@@ -264,13 +264,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (p.mode == 1) {
       const float dz = p.ctl ? (float)p.ctl->dz : p.dz_fixed;
       const int w0 = col0 >> 1;
-      const int M = gridDim.y * TC_BM;
-      const float2* kzr = p.kz + (size_t)w0 * M + row;
-      const float* gr = p.gd + (size_t)w0 * M + row;
+      const float2* kzr = p.kz + (size_t)row * p.nh + w0;
+      const float* gr = p.gd + (size_t)row * p.nh + w0;
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
-        float2 k = kzr[(size_t)i * M];
-        float amp = gr[(size_t)i * M] * expf(-k.y * dz);
+        float2 k = kzr[i];
+        float amp = gr[i] * expf(-k.y * dz);
         float sn, cs;
         sincosf(k.x * dz, &sn, &cs);
         float re = acc[2 * i], im = acc[2 * i + 1];

@@ -10,8 +10,8 @@ struct TcGemmParams {
   int ldo;                // leading dimension of out (floats)
   int K;                  // contraction length, multiple of 64
   int mode;               // 1 propagator + transposed store; 2 row-major store (+ guard pending)
-  const float2* kz;       // mode 1: [nh][M] KZ in zu units (row index contiguous)
-  const float* gd;        // mode 1: [nh][M] spectral guard
+  const float2* kz;       // mode 1: [M][nh] KZ in zu units
+  const float* gd;        // mode 1: [M][nh] spectral guard
   int nh;
   const float* qa;        // [M] row scales of A (powers of two)
   const float* qb;        // [K/64][ldqb] chunk scales of B (powers of two)
