@@ -44,7 +44,7 @@ struct fil_handle {
   void* W2 = nullptr;     // DHT intermediate
   void* M1 = nullptr;     // [mpad][mpad]
   void* M2 = nullptr;
-  void* tw = nullptr;     // [nt] complex
+  void* tw = nullptr;     // [nt] complex, per-pass twiddle layout of fft.cuh
   void* g1 = nullptr; void* g2 = nullptr; void* gt = nullptr;
   void* Cc = nullptr; void* Cf = nullptr; void* Cl = nullptr;
   void* kt2 = nullptr; void* beta = nullptr; void* dfr = nullptr; void* kmax2 = nullptr; void* wg = nullptr;
@@ -155,7 +155,24 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
         v[2 * m + 1] = bs;
       }
     }
-    if (upload<R>(h, &h->tw, v)) return FIL_ERR_CUDA;
+    // per-pass layout of the block FFT (fft.cuh): for each radix-16 pass of
+    // stride NS > 1, entries (r - 1) NS + k = w^(k r nt / (16 NS)),
+    // r = 1..15, k < NS
+    std::vector<double> p(2 * nt, 0.0);
+    int lg = 0;
+    while ((1 << lg) < nt) ++lg;
+    size_t o = 0;
+    for (int ns = 1 << (lg % 4); ns < nt; ns *= 16) {
+      if (ns == 1) continue;
+      for (int r = 1; r < 16; ++r)
+        for (int k = 0; k < ns; ++k) {
+          const size_t m = (size_t)k * r * (nt / (16 * ns));
+          p[2 * o] = v[2 * m];
+          p[2 * o + 1] = v[2 * m + 1];
+          ++o;
+        }
+    }
+    if (upload<R>(h, &h->tw, p)) return FIL_ERR_CUDA;
   }
   // guards
   {
