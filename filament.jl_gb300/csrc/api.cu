@@ -273,12 +273,18 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     P.maxit = 8;
     P.tol = h->fp64 ? 1e-26 : 1e-8;
     P.skip = h->fp64 ? 1e-250 : 1e-30;
+    // single precision: rows whose density rise stays below 2^-30 of the
+    // previous maximum are left at rho0 (their free-current contribution is
+    // far below the FP32 resolution of the step); FP64 solves every row
+    P.skip_rel = h->fp64 ? 0.0 : std::ldexp(1.0, -30);
     bool pl = true;
     for (int i = 0; i < nc; ++i) {
       P.rho_nt[i] = t->rho_nt[i];
       P.rava_nt[i] = t->rava[i] / t->rho_nt[i];
       P.kfix[i] = t->kfix[i];
       if (t->rava[i] != 0.0) P.avalanche = 1;
+      P.rhont_sum += t->rho_nt[i];
+      P.rava_sum += std::fabs(t->rava[i]);
       double s0 = 0;
       for (int q = 0; q < n; ++q) {
         P.lx[i][q] = t->rate_lx[i * n + q];

@@ -46,6 +46,13 @@ template <typename R> struct PlasmaParams {
   int maxit;              // Newton iteration cap
   R tol;                  // Newton: stop when update^2 <= tol |u|^2
   R skip;                 // rows with max W * window below this keep rho0
+  // relative skip (0: off): a row whose density rise is bounded by
+  // skip_rel * (largest density of the previous solve) keeps rho0.  With
+  // g = rava_sum * max E^2 * window the rise is bounded (Gronwall) by
+  // (max W * window * rhont_sum + nc * rho0 * g) * exp(g): photoionisation at
+  // the largest rate plus avalanche of the initial density, amplified by the
+  // largest avalanche growth.
+  R skip_rel, rhont_sum, rava_sum;
   // power law with an integer order m (multiphoton rate sigma_m I^m):
   // W(I) = (wscale I)^m by repeated squaring instead of exp/log; 0 = no
   int ipow[FIL_MAXCOMP];
@@ -85,6 +92,9 @@ template <typename R> inline PlasmaParams<R> plasma_params_as(const PlasmaParams
     r.ipow[c] = d.ipow[c];
     r.wscale[c] = (R)d.wscale[c];
   }
+  r.skip_rel = (R)d.skip_rel;
+  r.rhont_sum = (R)d.rhont_sum;
+  r.rava_sum = (R)d.rava_sum;
   return r;
 }
 

@@ -111,7 +111,7 @@ FIL_DEV void load_time_row(const RowParams<R>& P, typename C2T<R>::type* X, int 
 // rho = rho0 exactly to the working precision and needs no scan.
 template <typename R, int N, int NC>
 FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typename C2T<R>::type* X,
-                     R* rho, R* kdrho, R* Y, Aff<R, NC>* ascratch, R* rscratch, int* newton_flag) {
+                     R* rho, R* kdrho, R* Y, Aff<R, NC>* ascratch, R* rscratch, int* newton_flag, R rho_prev) {
   typedef typename C2T<R>::type C;
   constexpr int NP = N + N / 16;
   const PlasmaParams<R>& pp = P.pp;
@@ -153,16 +153,18 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
   };
 
   // ---------------- rate cache and the negligible-row test
-  R wmax = 0;
+  R wmax = 0, e2max = 0;
   if (cached) {
     for (int q = 0; q < 16; ++q) {
       int j = j0 + q;
       R sl;
-      R w0 = rate_eval<R>(pp, tabs, 0, intens(X[pad16(j)]), &sl);
+      const C e = X[pad16(j)];
+      R w0 = rate_eval<R>(pp, tabs, 0, intens(e), &sl);
       Wp[pad16(j)] = w0;
       wmax = max(wmax, w0);
+      e2max = max(e2max, e.x * e.x);
       if (j < N - 1) {
-        C em = (R)0.5 * (X[pad16(j)] + X[pad16(j + 1)]);
+        C em = (R)0.5 * (e + X[pad16(j + 1)]);
         R wm = rate_eval<R>(pp, tabs, 0, intens(em), &sl);
         Wm[pad16(j)] = wm;
         wmax = max(wmax, wm);
@@ -172,13 +174,25 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
     for (int q = 0; q < 16; ++q) {
       int j = j0 + q;
       R W[NC], S[NC];
-      rates(intens(X[pad16(j)]), W, S);
+      const C e = X[pad16(j)];
+      rates(intens(e), W, S);
+      e2max = max(e2max, e.x * e.x);
 #pragma unroll
       for (int c = 0; c < NC; ++c) wmax = max(wmax, W[c]);
     }
   }
   wmax = block_max<R>(wmax, rscratch);
-  if (wmax * (R)(pp.dt * (N - 1)) < (R)pp.skip) {
+  const R window = pp.dt * (R)(N - 1);
+  bool skip = wmax * window < pp.skip;
+  if (!skip && pp.skip_rel > (R)0 && rho_prev > (R)0) {
+    // the midpoint intensities do not exceed the larger end-point one, so
+    // e2max over the points bounds E^2 at every stage time
+    e2max = block_max<R>(e2max, rscratch);
+    const R g = pp.rava_sum * e2max * window;
+    if (g < (R)40)
+      skip = (wmax * window * pp.rhont_sum + (R)NC * pp.rho0 * g) * exp(g) < pp.skip_rel * rho_prev;
+  }
+  if (skip) {
     // rho stays rho0; Kdrho = sum K W (rho_nt - rho0) to the same precision
     for (int q = 0; q < 16; ++q) {
       int j = j0 + q;
@@ -425,7 +439,8 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
   // ---- plasma
   if constexpr (NC > 0) {
     if (P.plasma) {
-      R rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag);
+      R rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag,
+                                    mode == 0 ? (R)ctl->rhomax : (R)0);
       if (tid == 0) {
         atomic_max_nonneg(&ctl->rhomax_acc, (double)rmax);
         P.rho_end[row] = (double)rho[pad16(N - 1)];
