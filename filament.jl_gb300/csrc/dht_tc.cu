@@ -20,7 +20,10 @@ cudaError_t launch_dht_tc(const CUtensorMap (&a)[3], const CUtensorMap (&b)[3], 
 cudaError_t launch_slice(const float* B, void* const (&s)[3], float* qb, int N, int K, const DevCtl* ctl,
                          cudaStream_t st) {
   if (K % TC_CHUNK) return cudaErrorInvalidValue;
-  const int warps = N * (K / TC_CHUNK);
-  k_slice<<<(warps + 7) / 8, 256, 0, st>>>(B, (__half2*)s[0], (__half2*)s[1], (__half2*)s[2], qb, N, K, ctl);
+  const int nch = K / TC_CHUNK;
+  __half2 *s0 = (__half2*)s[0], *s1 = (__half2*)s[1], *s2 = (__half2*)s[2];
+  if (nch % 4 == 0) k_slice<4><<<(N * (nch / 4) + 7) / 8, 256, 0, st>>>(B, s0, s1, s2, qb, N, K, ctl);
+  else if (nch % 2 == 0) k_slice<2><<<(N * (nch / 2) + 7) / 8, 256, 0, st>>>(B, s0, s1, s2, qb, N, K, ctl);
+  else k_slice<1><<<(N * nch + 7) / 8, 256, 0, st>>>(B, s0, s1, s2, qb, N, K, ctl);
   return cudaGetLastError();
 }

@@ -72,42 +72,51 @@ __device__ __forceinline__ void tc_arrive(uint32_t bar) {
 
 // ---------------------------------------------------------------------------
 // B [N][K] FP32 (K contiguous) -> slices b0, b1, b2 [N][K] FP16 and chunk
-// scales qb [K/64][N].  One warp per (column n, chunk c); lane l holds
-// k = 64c + 2l, 2l + 1.  qb = 2^(E-6) for a chunk maximum f 2^E, so
-// |B / qb| < 128.
+// scales qb [K/64][N].  One warp per (column n, CH consecutive chunks);
+// lane l holds k = 64c + 2l, 2l + 1 of each chunk c.  All loads of a warp
+// are issued before the first use.  qb = 2^(E-6) for a chunk maximum f 2^E,
+// so |B / qb| < 128.
+template <int CH>
 __global__ void __launch_bounds__(256) k_slice(const float* __restrict__ B, __half2* b0, __half2* b1, __half2* b2,
                                                float* qb, int N, int K, const DevCtl* ctl) {
   if (ctl && ctl->done) return;
   const int lane = threadIdx.x & 31;
   const int g = blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int nch = K / TC_CHUNK;
-  if (g >= N * nch) return;
-  const int n = g / nch, c = g - n * nch;
-  const size_t e2 = ((size_t)n * K + (size_t)c * TC_CHUNK) / 2 + lane;   // half2 / float2 index
-  const float2 v = reinterpret_cast<const float2*>(B)[e2];
-  const unsigned m = __reduce_max_sync(0xffffffffu, max(__float_as_uint(fabsf(v.x)), __float_as_uint(fabsf(v.y))));
-  float q = 0.f, iq = 0.f;
-  if (m != 0u) {
-    int e = (int)((m >> 23) & 0xFFu) - 127;
-    e = min(max(e, -100), 120);
-    q = __uint_as_float((unsigned)(e - 6 + 127) << 23);
-    iq = __uint_as_float((unsigned)(6 - e + 127) << 23);
-  }
-  float hd[2], m1[2], m2[2];
-  const float x[2] = {v.x * iq, v.y * iq};
+  const int nch = K / TC_CHUNK, ngrp = nch / CH;
+  if (g >= N * ngrp) return;
+  const int n = g / ngrp, c0 = (g - n * ngrp) * CH;
+  const size_t base = ((size_t)n * K + (size_t)c0 * TC_CHUNK) / 2 + lane;   // half2 / float2 index
+  float2 v[CH];
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    const float i0 = rintf(x[i]);                 // |i0| <= 128, exact
-    const float r = x[i] - i0;                    // exact, |r| <= 1/2
-    const float r1 = __half2float(__float2half_rn(r));
-    hd[i] = i0;
-    m1[i] = r1;
-    m2[i] = r - r1;                               // exact
+  for (int u = 0; u < CH; ++u) v[u] = __ldg(reinterpret_cast<const float2*>(B) + base + u * (TC_CHUNK / 2));
+#pragma unroll
+  for (int u = 0; u < CH; ++u) {
+    const unsigned m =
+        __reduce_max_sync(0xffffffffu, max(__float_as_uint(fabsf(v[u].x)), __float_as_uint(fabsf(v[u].y))));
+    float q = 0.f, iq = 0.f;
+    if (m != 0u) {
+      int e = (int)((m >> 23) & 0xFFu) - 127;
+      e = min(max(e, -100), 120);
+      q = __uint_as_float((unsigned)(e - 6 + 127) << 23);
+      iq = __uint_as_float((unsigned)(6 - e + 127) << 23);
+    }
+    float hd[2], m1[2], m2[2];
+    const float x[2] = {v[u].x * iq, v[u].y * iq};
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const float i0 = rintf(x[i]);               // |i0| <= 128, exact
+      const float r = x[i] - i0;                  // exact, |r| <= 1/2
+      const float r1 = __half2float(__float2half_rn(r));
+      hd[i] = i0;
+      m1[i] = r1;
+      m2[i] = r - r1;                             // exact
+    }
+    const size_t e2 = base + u * (TC_CHUNK / 2);
+    b0[e2] = __floats2half2_rn(hd[0], hd[1]);
+    b1[e2] = __floats2half2_rn(m1[0], m1[1]);
+    b2[e2] = __floats2half2_rn(m2[0], m2[1]);
+    if (lane == 0) qb[(size_t)(c0 + u) * N + n] = q;
   }
-  b0[e2] = __floats2half2_rn(hd[0], hd[1]);
-  b1[e2] = __floats2half2_rn(m1[0], m1[1]);
-  b2[e2] = __floats2half2_rn(m2[0], m2[1]);
-  if (lane == 0) qb[(size_t)c * N + n] = q;
 }
 
 // ---------------------------------------------------------------------------
