@@ -76,7 +76,7 @@ struct fil_handle {
   void* qa1 = nullptr; void* qa2 = nullptr;    // [mpad] row scales of M1, M2
   void* BS[3] = {nullptr, nullptr, nullptr};   // FP16 slices of the GEMM operand W1 or W2, [2 nh][mpad]
   void* qb = nullptr;                          // [mpad/64][2 nh] chunk scales of the operand
-  void* kzt = nullptr; void* gdt = nullptr;    // [mpad][nh] KZ (float2), guard (float)
+  void* kzt = nullptr; void* gdt = nullptr;    // [nh][mpad] KZ (float2), guard (float)
   int* tc_err = nullptr;
   CUtensorMap tm_a1[3], tm_a2[3], tm_b[3];
 };
@@ -299,6 +299,25 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
       P.sl[i][n - 1] = P.sl[i][n - 2];
     }
     P.powerlaw = pl ? 1 : 0;
+    {
+      // plasma-channel skip bound (plasma.cuh): power-law rates of order
+      // >= 1/2, |E|^2 losses, rho0 = 0, single precision
+      bool ok = !h->fp64 && pl && !c.losses_ereal && c.rho0 == 0.0;
+      double kmax = 0;
+      for (int i = 0; i < nc && ok; ++i) {
+        if (P.sl[i][0] < 0.5) ok = false;
+        kmax = std::max(kmax, c.plasma_kdep ? P.sl[i][0] : std::fabs(t->kfix[i]));
+      }
+      double clmax = 0;
+      if (ok && t->rnl_losses && t->qz)
+        for (int k = 0; k < nh; ++k) {
+          cd q(t->qz[2 * k], t->qz[2 * k + 1]), r(t->rnl_losses[2 * k], t->rnl_losses[2 * k + 1]);
+          clmax = std::max(clmax, std::abs(q * r) * (k ? 2.0 : 1.0));
+        }
+      double rnt = 0;
+      for (int i = 0; i < nc; ++i) rnt += t->rho_nt[i];
+      P.ychan_coef = ok ? std::max(clmax * kmax * rnt * nh, 1e-300) : 0.0;
+    }
     for (int i = 0; i < nc && pl; ++i) {
       // an integer multiphoton order: rate by repeated squaring
       const double s0 = P.sl[i][0], m = std::nearbyint(s0);
@@ -376,9 +395,9 @@ static int create_tc(fil_handle* h, const fil_tables* t) {
         g = (km == 0.0) ? 0.0 : std::exp(-std::pow(kt2 / (km * km), 20));
       }
       if (t->wguard) g *= t->wguard[j];
-      kz[((size_t)i * nh + j) * 2] = (float)K.real();
-      kz[((size_t)i * nh + j) * 2 + 1] = (float)K.imag();
-      gd[(size_t)i * nh + j] = (float)g;
+      kz[((size_t)j * mp + i) * 2] = (float)K.real();
+      kz[((size_t)j * mp + i) * 2 + 1] = (float)K.imag();
+      gd[(size_t)j * mp + i] = (float)g;
     }
   }
   auto up = [&](void** dst, const void* src, size_t bytes) -> int {
@@ -487,9 +506,6 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
     p1.ldo = h->mpad;
     p1.K = h->mpad;
     p1.mode = 1;
-    p1.kz = (const float2*)h->kzt;
-    p1.gd = (const float*)h->gdt;
-    p1.nh = h->nh;
     p1.qa = (const float*)h->qa1;
     p1.qb = (const float*)h->qb;
     p1.ldqb = Nc;
@@ -503,7 +519,8 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
     p2.ldo = Nc;
     p2.mode = 2;
     p2.qa = (const float*)h->qa2;
-    CK(launch_slice((const float*)h->W2, h->BS, (float*)h->qb, Nc, h->mpad, h->ctl, h->st));
+    CK(launch_slice_prop((const float*)h->W2, (const float2*)h->kzt, (const float*)h->gdt, h->BS, (float*)h->qb,
+                         h->nh, h->mpad, h->ctl, h->st));
     CK(launch_dht_tc(h->tm_a2, h->tm_b, p2, h->mpad, Nc, h->st));
   } else {
     CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 1, h->st));

@@ -26,9 +26,10 @@
 // consumer warps add each chunk's two accumulators times qb_cj into FP32
 // registers (round to nearest) and apply qa_i in the epilogue.
 //
-// k_slice cuts the FP32 operand B (written by the row kernel, or by the
-// epilogue of the forward transform) into its slices and chunk scales once,
-// so the GEMM streams FP16 tiles with TMA only.
+// k_slice cuts the FP32 operand B (written by the row kernel) into its
+// slices and chunk scales once, so the GEMM streams FP16 tiles with TMA
+// only; k_slice_prop does the same for the forward transform's output after
+// applying the linear propagator exp(i KZ dz) * guard.
 //
 // GEMM roles (320 threads): warps 0-7 drain the accumulators and run the
 // epilogue; warp 8 issues the TMA loads; warp 9 issues the MMAs.  Tile
@@ -116,6 +117,84 @@ __global__ void __launch_bounds__(256) k_slice(const float* __restrict__ B, __ha
     b1[e2] = __floats2half2_rn(m1[0], m1[1]);
     b2[e2] = __floats2half2_rn(m2[0], m2[1]);
     if (lane == 0) qb[(size_t)(c0 + u) * N + n] = q;
+  }
+}
+
+// The same for the output of the forward transform, with the linear
+// propagator applied first (spectral.jl:21-24: E .*= exp(i KZ dz), spectral
+// guard): W [2 nh][K] holds (re, im) of frequency w in rows 2w, 2w + 1; kz, gd
+// are [nh][K] (radial index contiguous).  One warp per (frequency w,
+// CH consecutive chunks); both rows of w are sliced with their own chunk
+// scales.
+template <int CH>
+__global__ void __launch_bounds__(256) k_slice_prop(const float* __restrict__ W, const float2* __restrict__ kz,
+                                                    const float* __restrict__ gd, __half2* b0, __half2* b1,
+                                                    __half2* b2, float* qb, int nh, int K, const DevCtl* ctl,
+                                                    float dz_fixed) {
+  if (ctl && ctl->done) return;
+  const int lane = threadIdx.x & 31;
+  const int g = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int nch = K / TC_CHUNK, ngrp = nch / CH;
+  if (g >= nh * ngrp) return;
+  const int w = g / ngrp, c0 = (g - w * ngrp) * CH;
+  const float dz = ctl ? (float)ctl->dz : dz_fixed;
+  const size_t kb = (size_t)c0 * TC_CHUNK / 2 + lane;                   // float2 index inside a row
+  const float2* re = reinterpret_cast<const float2*>(W + (size_t)(2 * w) * K) + kb;
+  const float2* im = reinterpret_cast<const float2*>(W + (size_t)(2 * w + 1) * K) + kb;
+  const float4* kq = reinterpret_cast<const float4*>(kz + (size_t)w * K) + kb;
+  const float2* gq = reinterpret_cast<const float2*>(gd + (size_t)w * K) + kb;
+  float2 vr[CH], vi[CH], gg[CH];
+  float4 kk[CH];
+#pragma unroll
+  for (int u = 0; u < CH; ++u) {
+    vr[u] = __ldg(re + u * (TC_CHUNK / 2));
+    vi[u] = __ldg(im + u * (TC_CHUNK / 2));
+    kk[u] = __ldg(kq + u * (TC_CHUNK / 2));
+    gg[u] = __ldg(gq + u * (TC_CHUNK / 2));
+  }
+#pragma unroll
+  for (int u = 0; u < CH; ++u) {
+    // two radial points per lane: (vr.x, vi.x) and (vr.y, vi.y)
+    float xr[2], xi[2];
+    const float kx[2] = {kk[u].x, kk[u].z}, ky[2] = {kk[u].y, kk[u].w}, gv[2] = {gg[u].x, gg[u].y};
+    const float ar[2] = {vr[u].x, vr[u].y}, ai[2] = {vi[u].x, vi[u].y};
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const float amp = gv[i] * expf(-ky[i] * dz);
+      float sn, cs;
+      sincosf(kx[i] * dz, &sn, &cs);
+      xr[i] = amp * (ar[i] * cs - ai[i] * sn);
+      xi[i] = amp * (ar[i] * sn + ai[i] * cs);
+    }
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+      const float* x = part ? xi : xr;
+      const unsigned m = __reduce_max_sync(0xffffffffu, max(__float_as_uint(fabsf(x[0])), __float_as_uint(fabsf(x[1]))));
+      float q = 0.f, iq = 0.f;
+      if (m != 0u) {
+        int e = (int)((m >> 23) & 0xFFu) - 127;
+        e = min(max(e, -100), 120);
+        q = __uint_as_float((unsigned)(e - 6 + 127) << 23);
+        iq = __uint_as_float((unsigned)(6 - e + 127) << 23);
+      }
+      float hd[2], m1[2], m2[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const float y = x[i] * iq;
+        const float i0 = rintf(y);
+        const float r = y - i0;
+        const float r1 = __half2float(__float2half_rn(r));
+        hd[i] = i0;
+        m1[i] = r1;
+        m2[i] = r - r1;
+      }
+      const int n = 2 * w + part;
+      const size_t e2 = ((size_t)n * K) / 2 + kb + u * (TC_CHUNK / 2);
+      b0[e2] = __floats2half2_rn(hd[0], hd[1]);
+      b1[e2] = __floats2half2_rn(m1[0], m1[1]);
+      b2[e2] = __floats2half2_rn(m2[0], m2[1]);
+      if (lane == 0) qb[(size_t)(c0 + u) * (2 * nh) + n] = q;
+    }
   }
 }
 
@@ -271,20 +350,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
     for (int i = 0; i < 64; ++i) acc[i] *= sa;
     if (p.mode == 1) {
-      const float dz = p.ctl ? (float)p.ctl->dz : p.dz_fixed;
-      const int w0 = col0 >> 1;
-      const float2* kzr = p.kz + (size_t)row * p.nh + w0;
-      const float* gr = p.gd + (size_t)row * p.nh + w0;
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        float2 k = kzr[i];
-        float amp = gr[i] * expf(-k.y * dz);
-        float sn, cs;
-        sincosf(k.x * dz, &sn, &cs);
-        float re = acc[2 * i], im = acc[2 * i + 1];
-        acc[2 * i] = amp * (re * cs - im * sn);
-        acc[2 * i + 1] = amp * (re * sn + im * cs);
-      }
 #pragma unroll
       for (int i = 0; i < 64; ++i) p.out[(size_t)(col0 + i) * p.ldo + row] = acc[i];
     } else {

@@ -34,6 +34,8 @@ cudaError_t launch_dht_tc(const CUtensorMap (&a)[3], const CUtensorMap (&b)[3], 
                           int N, cudaStream_t st);
 cudaError_t launch_slice(const float* B, void* const (&s)[3], float* qb, int N, int K, const DevCtl* ctl,
                          cudaStream_t st);
+cudaError_t launch_slice_prop(const float* W, const float2* kz, const float* gd, void* const (&s)[3], float* qb, int nh,
+                              int K, const DevCtl* ctl, cudaStream_t st);
 cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
 cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);

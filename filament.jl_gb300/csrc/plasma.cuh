@@ -53,6 +53,14 @@ template <typename R> struct PlasmaParams {
   // the largest rate plus avalanche of the initial density, amplified by the
   // largest avalanche growth.
   R skip_rel, rhont_sum, rava_sum;
+  // plasma-channel skip of a row left at rho0 = 0: its losses response
+  // |Kdrho E / |E|^2| <= K rho_nt W(Imax) / sqrt(Imax) changes the step by at
+  // most dz * max|C_losses| * that, and the row's spectrum is at least
+  // sqrt(Imax) / (Nt/2); the channel is dropped when
+  // dz * ychan_coef * max W <= 2^-30 Imax, ychan_coef = max|C_losses| K
+  // rho_nt (Nt/2).  0: never (FP64, rho0 != 0, tabulated or sub-linear rates,
+  // E_real losses).
+  R ychan_coef;
   // power law with an integer order m (multiphoton rate sigma_m I^m):
   // W(I) = (wscale I)^m by repeated squaring instead of exp/log; 0 = no
   int ipow[FIL_MAXCOMP];
@@ -93,6 +101,7 @@ template <typename R> inline PlasmaParams<R> plasma_params_as(const PlasmaParams
     r.wscale[c] = (R)d.wscale[c];
   }
   r.skip_rel = (R)d.skip_rel;
+  r.ychan_coef = (R)d.ychan_coef;
   r.rhont_sum = (R)d.rhont_sum;
   r.rava_sum = (R)d.rava_sum;
   return r;

@@ -111,7 +111,8 @@ FIL_DEV void load_time_row(const RowParams<R>& P, typename C2T<R>::type* X, int 
 // rho = rho0 exactly to the working precision and needs no scan.
 template <typename R, int N, int NC>
 FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typename C2T<R>::type* X,
-                     R* rho, R* kdrho, R* Y, Aff<R, NC>* ascratch, R* rscratch, int* newton_flag, R rho_prev) {
+                     R* rho, R* kdrho, R* Y, Aff<R, NC>* ascratch, R* rscratch, int* newton_flag, R rho_prev,
+                     R dz, bool* ychan) {
   typedef typename C2T<R>::type C;
   constexpr int NP = N + N / 16;
   const PlasmaParams<R>& pp = P.pp;
@@ -153,7 +154,8 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
   };
 
   // ---------------- rate cache and the negligible-row test
-  R wmax = 0, e2max = 0;
+  R wmax = 0, e2max = 0, i2max = 0;
+  *ychan = true;
   if (cached) {
     for (int q = 0; q < 16; ++q) {
       int j = j0 + q;
@@ -163,6 +165,7 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
       Wp[pad16(j)] = w0;
       wmax = max(wmax, w0);
       e2max = max(e2max, e.x * e.x);
+      i2max = max(i2max, e.x * e.x + e.y * e.y);
       if (j < N - 1) {
         C em = (R)0.5 * (e + X[pad16(j + 1)]);
         R wm = rate_eval<R>(pp, tabs, 0, intens(em), &sl);
@@ -177,6 +180,7 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
       const C e = X[pad16(j)];
       rates(intens(e), W, S);
       e2max = max(e2max, e.x * e.x);
+      i2max = max(i2max, e.x * e.x + e.y * e.y);
 #pragma unroll
       for (int c = 0; c < NC; ++c) wmax = max(wmax, W[c]);
     }
@@ -191,6 +195,10 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
     const R g = pp.rava_sum * e2max * window;
     if (g < (R)40)
       skip = (wmax * window * pp.rhont_sum + (R)NC * pp.rho0 * g) * exp(g) < pp.skip_rel * rho_prev;
+  }
+  if (skip && pp.ychan_coef > (R)0) {
+    i2max = block_max<R>(i2max, rscratch);
+    *ychan = !(dz * pp.ychan_coef * wmax <= (R)9.313225746154785e-10 * i2max);   // 2^-30
   }
   if (skip) {
     // rho stays rho0; Kdrho = sum K W (rho_nt - rho0) to the same precision
@@ -415,6 +423,7 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
   Aff<R, (NC > 0 ? NC : 1)>* ascratch = reinterpret_cast<Aff<R, (NC > 0 ? NC : 1)>*>(rscratch + 32);
   PlasmaSmem<R>* tabs = reinterpret_cast<PlasmaSmem<R>*>(ascratch + 32);
   __shared__ int s_flag;
+  bool ych = true;   // the plasma channels (Y) carry a response for this row
 
   DevCtl* ctl = P.ctl;
   if (ctl->done) return;
@@ -440,7 +449,7 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
   if constexpr (NC > 0) {
     if (P.plasma) {
       R rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag,
-                                    mode == 0 ? (R)ctl->rhomax : (R)0);
+                                    mode == 0 ? (R)ctl->rhomax : (R)0, dz, &ych);
       if (tid == 0) {
         atomic_max_nonneg(&ctl->rhomax_acc, (double)rmax);
         P.rho_end[row] = (double)rho[pad16(N - 1)];
@@ -505,7 +514,7 @@ __global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
         X[pad16(j)] = mk<R>(g * (R)P.sc * fc, 0);
         Y[pad16(j)] = mk<R>(g * (R)P.sf * ff, g * (R)P.sl * fl);
       }
-      const bool plas = NC > 0 && (P.has_free || P.has_losses);
+      const bool plas = NC > 0 && (P.has_free || P.has_losses) && ych;
       if (P.has_cubic) filfft::block_fft<C, N, +1>(X, P.tw);   // rsig2aspec!
       if (plas) filfft::block_fft<C, N, +1>(Y, P.tw);
       __syncthreads();

@@ -9,10 +9,7 @@ struct TcGemmParams {
   float* out;
   int ldo;                // leading dimension of out (floats)
   int K;                  // contraction length, multiple of 64
-  int mode;               // 1 propagator + transposed store; 2 row-major store (+ guard pending)
-  const float2* kz;       // mode 1: [M][nh] KZ in zu units
-  const float* gd;        // mode 1: [M][nh] spectral guard
-  int nh;
+  int mode;               // 1 transposed store; 2 row-major store (+ guard pending)
   const float* qa;        // [M] row scales of A (powers of two)
   const float* qb;        // [K/64][ldqb] chunk scales of B (powers of two)
   int ldqb;
