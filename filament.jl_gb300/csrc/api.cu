@@ -25,6 +25,7 @@
 #include "tc_params.h"
 #include <cuda_fp16.h>
 #include "tc_host.h"
+#include "xyfft.h"
 
 namespace {
 thread_local std::string g_err;
@@ -69,6 +70,9 @@ struct fil_handle {
   long tcount = 0;
   void* flushbuf = nullptr;            // > L2, benchmark timing only
   size_t flushbytes = 0;
+  // XYT transverse transform (xyfft.cu)
+  void* kx2 = nullptr; void* ky2 = nullptr; void* sg1 = nullptr; void* sg2 = nullptr;
+  void* twx = nullptr; void* twy = nullptr;
   // tensor-core Hankel path (mixed form)
   bool use_tc = false;
   void* MA1[3] = {nullptr, nullptr, nullptr};  // M1 = T diag(s): FP16 slices a0, a1, a2
@@ -125,61 +129,67 @@ static void rk_tableau(int alg, int* s, double a[4][4], double b[4], double c[4]
   }
 }
 
+// Twiddles of the block FFT of length n (fft.cuh), laid out per pass: for
+// each radix-16 pass of stride NS > 1, entries (r - 1) NS + k = w^(k r n /
+// (16 NS)), r = 1..15, k < NS, with w^m = exp(-2 pi i m / n).  In single
+// precision each value is the pair of FP32 neighbours of (cos, sin) whose
+// magnitude is closest to 1, so that the table carries no systematic gain.
+static std::vector<double> fft_twiddles(int n, bool fp32) {
+  std::vector<double> v(2 * n);
+  for (int m = 0; m < n; ++m) {
+    double a = -2.0 * M_PI * (double)m / (double)n;
+    double c = std::cos(a), sn = std::sin(a);
+    v[2 * m] = c;
+    v[2 * m + 1] = sn;
+    if (fp32) {
+      float cf = (float)c, sf = (float)sn, bc = cf, bs = sf;
+      double best = 1e300;
+      for (int dc = -1; dc <= 1; ++dc)
+        for (int ds = -1; ds <= 1; ++ds) {
+          float cc = cf, ss = sf;
+          if (dc) cc = std::nextafter(cf, dc > 0 ? 2.0f : -2.0f);
+          if (ds) ss = std::nextafter(sf, ds > 0 ? 2.0f : -2.0f);
+          double err = std::fabs((double)cc * cc + (double)ss * ss - 1.0);
+          if (err < best) { best = err; bc = cc; bs = ss; }
+        }
+      v[2 * m] = bc;
+      v[2 * m + 1] = bs;
+    }
+  }
+  std::vector<double> p(2 * n, 0.0);
+  int lg = 0;
+  while ((1 << lg) < n) ++lg;
+  size_t o = 0;
+  for (int ns = 1 << (lg % 4); ns < n; ns *= 16) {
+    if (ns == 1) continue;
+    for (int r = 1; r < 16; ++r)
+      for (int k = 0; k < ns; ++k) {
+        const size_t m = (size_t)k * r * (n / (16 * ns));
+        p[2 * o] = v[2 * m];
+        p[2 * o + 1] = v[2 * m + 1];
+        ++o;
+      }
+  }
+  return p;
+}
+
 template <typename R>
 static int create_tables(fil_handle* h, const fil_tables* t) {
   const fil_config& c = h->cfg;
   const int n1 = h->n1, nt = h->nt, nh = h->nh, mp = h->mpad, nr = h->nrows;
   typedef std::complex<double> cd;
-  // twiddles exp(-2 pi i m / nt); in single precision each entry is the
-  // pair of FP32 neighbours of (cos, sin) whose magnitude is closest to 1,
-  // so that the table carries no systematic gain
-  {
-    std::vector<double> v(2 * nt);
-    for (int m = 0; m < nt; ++m) {
-      double a = -2.0 * M_PI * (double)m / (double)nt;
-      double c = std::cos(a), sn = std::sin(a);
-      v[2 * m] = c;
-      v[2 * m + 1] = sn;
-      if (sizeof(R) == 4) {
-        float cf = (float)c, sf = (float)sn, bc = cf, bs = sf;
-        double best = 1e300;
-        for (int dc = -1; dc <= 1; ++dc)
-          for (int ds = -1; ds <= 1; ++ds) {
-            float cc = cf, ss = sf;
-            if (dc) cc = std::nextafter(cf, dc > 0 ? 2.0f : -2.0f);
-            if (ds) ss = std::nextafter(sf, ds > 0 ? 2.0f : -2.0f);
-            double err = std::fabs((double)cc * cc + (double)ss * ss - 1.0);
-            if (err < best) { best = err; bc = cc; bs = ss; }
-          }
-        v[2 * m] = bc;
-        v[2 * m + 1] = bs;
-      }
-    }
-    // per-pass layout of the block FFT (fft.cuh): for each radix-16 pass of
-    // stride NS > 1, entries (r - 1) NS + k = w^(k r nt / (16 NS)),
-    // r = 1..15, k < NS
-    std::vector<double> p(2 * nt, 0.0);
-    int lg = 0;
-    while ((1 << lg) < nt) ++lg;
-    size_t o = 0;
-    for (int ns = 1 << (lg % 4); ns < nt; ns *= 16) {
-      if (ns == 1) continue;
-      for (int r = 1; r < 16; ++r)
-        for (int k = 0; k < ns; ++k) {
-          const size_t m = (size_t)k * r * (nt / (16 * ns));
-          p[2 * o] = v[2 * m];
-          p[2 * o + 1] = v[2 * m + 1];
-          ++o;
-        }
-    }
-    if (upload<R>(h, &h->tw, p)) return FIL_ERR_CUDA;
-  }
+  if (upload<R>(h, &h->tw, fft_twiddles(nt, sizeof(R) == 4))) return FIL_ERR_CUDA;
   // guards
   {
     std::vector<double> g(n1, 1.0), gtt(nt, 1.0);
     if (t->guard1) g.assign(t->guard1, t->guard1 + n1);
     if (t->guardt) gtt.assign(t->guardt, t->guardt + nt);
     if (upload<R>(h, &h->g1, g) || upload<R>(h, &h->gt, gtt)) return FIL_ERR_CUDA;
+    if (h->geom == FIL_GEOM_XYT) {
+      std::vector<double> g2(h->n2, 1.0);
+      if (t->guard2) g2.assign(t->guard2, t->guard2 + h->n2);
+      if (upload<R>(h, &h->g2, g2)) return FIL_ERR_CUDA;
+    }
   }
   // nonlinear coefficients C_ch[k] = i QZ Rnl_ch (k ? 2 : 1) / s_ch, k < nh.
   // The row kernel multiplies response ch by s_ch, the median of |C_ch| over
@@ -234,8 +244,21 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
       if (upload<R>(h, &h->wg, w)) return FIL_ERR_CUDA;
     }
   }
+  if (h->geom == FIL_GEOM_XYT) {
+    // transverse 2-D transform tables (xyfft.cu)
+    const int nx = h->n1, ny = h->n2;
+    std::vector<double> kx2(nx), ky2(ny), s1(nx, 1.0), s2(ny, 1.0);
+    for (int i = 0; i < nx; ++i) kx2[i] = t->kt1[i] * t->kt1[i];
+    for (int i = 0; i < ny; ++i) ky2[i] = t->kt2[i] * t->kt2[i];
+    if (t->sguard1) s1.assign(t->sguard1, t->sguard1 + nx);
+    if (t->sguard2) s2.assign(t->sguard2, t->sguard2 + ny);
+    if (upload<R>(h, &h->kx2, kx2) || upload<R>(h, &h->ky2, ky2) || upload<R>(h, &h->sg1, s1) ||
+        upload<R>(h, &h->sg2, s2) || upload<R>(h, &h->twx, fft_twiddles(nx, sizeof(R) == 4)) ||
+        upload<R>(h, &h->twy, fft_twiddles(ny, sizeof(R) == 4)))
+      return FIL_ERR_CUDA;
+  }
   // Hankel matrices M1 = T diag(s), M2 = diag(1/s) T, zero padded
-  {
+  if (h->geom == FIL_GEOM_RT) {
     std::vector<double> m1((size_t)mp * mp, 0.0), m2((size_t)mp * mp, 0.0);
     for (int i = 0; i < n1; ++i)
       for (int k = 0; k < n1; ++k) {
@@ -248,7 +271,8 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
   // transverse weights 2 pi r dr
   {
     std::vector<double> w(nr);
-    for (int i = 0; i < nr; ++i) w[i] = 2.0 * M_PI * (t->rdr ? t->rdr[i] : 0.0);
+    for (int i = 0; i < nr; ++i)
+      w[i] = h->geom == FIL_GEOM_XYT ? c.dxdy : 2.0 * M_PI * (t->rdr ? t->rdr[i] : 0.0);
     CK(cudaMalloc(&h->pw, nr * sizeof(double)));
     CK(cudaMemcpy(h->pw, w.data(), nr * sizeof(double), cudaMemcpyHostToDevice));
   }
@@ -485,7 +509,54 @@ template <typename R> static PropParams<R> prop_params(fil_handle* h) {
 
 // one z-step: row kernel (W1 <- S), DHT forward + propagator (W2 <- W1),
 // inverse (S <- W2)
+// XYT: row kernel (W1 <- S, row-major), fft along y, fft along x with the
+// propagator and the inverse along x, inverse along y (S <- W1)
+template <typename R> static int enqueue_zstep_xyt(fil_handle* h, bool timed) {
+  typedef typename C2T<R>::type C;
+  RowParams<R> P = row_params<R>(h);
+  P.S_in = (const C*)h->S;
+  P.S_out = (C*)h->W1;
+  if (timed) CK(cudaEventRecord(h->ev[1], h->st));
+  CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[2], h->st));
+  const int nx = h->n1, ny = h->n2, nh = h->nh;
+  XyParams<R> q;
+  std::memset(&q, 0, sizeof q);
+  q.in = (const C*)h->W1;
+  q.out = (C*)h->W1;
+  q.ctl = h->ctl;
+  // along y: lines p = ix*ny + iy
+  q.line_stride = nh;
+  q.outer_stride = (size_t)ny * nh;
+  q.tw = (const C*)h->twy;
+  q.scale = (R)1;
+  CK(launch_xylines<R>(q, ny, 0, nh, nx, h->st));
+  // along x, propagator, back along x
+  XyParams<R> qx = q;
+  qx.line_stride = (size_t)ny * nh;
+  qx.outer_stride = nh;
+  qx.tw = (const C*)h->twx;
+  qx.scale = (R)1 / (R)nx;
+  qx.pp = prop_params<R>(h);
+  qx.pp.kmax2 = nullptr;
+  qx.wg = (const R*)h->wg;
+  qx.wg_bug = h->bugcompat;
+  qx.kt2_line = (const R*)h->kx2;
+  qx.kt2_outer = (const R*)h->ky2;
+  qx.sg_line = (const R*)h->sg1;
+  qx.sg_outer = (const R*)h->sg2;
+  CK(launch_xylines<R>(qx, nx, 1, nh, ny, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[3], h->st));
+  XyParams<R> qi = q;
+  qi.out = (C*)h->S;
+  qi.scale = (R)1 / (R)ny;
+  CK(launch_xylines<R>(qi, ny, 2, nh, nx, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[4], h->st));
+  return 0;
+}
+
 template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
+  if (h->geom == FIL_GEOM_XYT) return enqueue_zstep_xyt<R>(h, timed);
   RowParams<R> P = row_params<R>(h);
   P.S_in = (const typename C2T<R>::type*)h->S;
   P.S_out = (typename C2T<R>::type*)h->W1;
@@ -570,6 +641,7 @@ static void free_all(fil_handle* h) {
                   h->kt2, h->beta, h->dfr, h->kmax2, h->wg, h->rho_g, h->kdrho_g, h->stage,
                   h->fluence, h->power, h->pw, h->rho_end, h->ctl, h->flushbuf,
                   h->qa1, h->qa2, h->BS[0], h->BS[1], h->BS[2], h->qb, h->kzt, h->gdt, h->tc_err,
+                  h->kx2, h->ky2, h->sg1, h->sg2, h->twx, h->twy,
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2]};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -666,8 +738,11 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (!cfg || !t || !out) return fail(h, FIL_ERR_ARG, "null argument");
   *out = nullptr;
   if (cfg->abi_version != FIL_ABI_VERSION) return fail(h, FIL_ERR_ARG, "ABI version mismatch");
-  if (cfg->geometry != FIL_GEOM_RT)
-    return fail(h, FIL_ERR_UNSUPPORTED, "this build runs the RT geometry on the GPU");
+  if (cfg->geometry != FIL_GEOM_RT && cfg->geometry != FIL_GEOM_XYT)
+    return fail(h, FIL_ERR_UNSUPPORTED, "this build runs the RT and XYT geometries on the GPU");
+  if (cfg->geometry == FIL_GEOM_XYT &&
+      (!is_pow2(cfg->n1) || !is_pow2(cfg->n2) || cfg->n1 < 64 || cfg->n1 > 1024 || cfg->n2 < 64 || cfg->n2 > 1024))
+    return fail(h, FIL_ERR_UNSUPPORTED, "XYT: nx and ny must be powers of two in [64, 1024]");
   if (!is_pow2(cfg->nt) || cfg->nt < 512 || cfg->nt > 4096)
     return fail(h, FIL_ERR_UNSUPPORTED, "nt must be a power of two in [512, 4096]");
   if (cfg->n1 < 1 || cfg->n1 > 65536) return fail(h, FIL_ERR_ARG, "bad n1");
@@ -679,8 +754,9 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
     return fail(h, FIL_ERR_UNSUPPORTED, "plasma_ncomp must be 1 or 2");
   if (cfg->plasma && (cfg->rate_n < 2 || cfg->rate_n > FIL_MAXRATE))
     return fail(h, FIL_ERR_ARG, "rate_n must be in [2, 32]");
-  if (!t->kt1 || !t->beta || !t->dfr || !t->dht || !t->dht_s)
-    return fail(h, FIL_ERR_ARG, "missing propagator or DHT tables");
+  if (!t->kt1 || !t->beta || !t->dfr) return fail(h, FIL_ERR_ARG, "missing propagator tables");
+  if (cfg->geometry == FIL_GEOM_RT && (!t->dht || !t->dht_s)) return fail(h, FIL_ERR_ARG, "missing DHT tables");
+  if (cfg->geometry == FIL_GEOM_XYT && !t->kt2) return fail(h, FIL_ERR_ARG, "missing ky table");
   if (cfg->nonlinearity && !t->qz) return fail(h, FIL_ERR_ARG, "missing QZ table");
   if (cfg->plasma && (!t->rho_nt || !t->rava || !t->kfix || !t->rate_lx || !t->rate_ly))
     return fail(h, FIL_ERR_ARG, "missing plasma tables");
@@ -737,7 +813,7 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   CKC(cudaMallocHost(&h->ctl_host, sizeof(DevCtl)));
   CKC(cudaMallocHost(&h->an_host, (3 * (size_t)h->nrows + h->nt) * sizeof(double)));
   rc = h->fp64 ? create_tables<double>(h, t) : create_tables<float>(h, t);
-  if (!rc && !h->fp64 && h->nh * 2 % 128 == 0) {
+  if (!rc && !h->fp64 && h->geom == FIL_GEOM_RT && h->nh * 2 % 128 == 0) {
     rc = create_tc(h, t);
     h->use_tc = (rc == 0);
   }

@@ -1,6 +1,6 @@
 // fft.cuh -- block-level Stockham FFT of one row held in shared memory.
 //
-// N = 2^L points, N/16 threads, 16 elements per thread.  Passes: one
+// N = 2^L points (N >= 16), N/16 threads, 16 elements per thread.  Passes: one
 // radix-(2^(L mod 4)) pass (if L is not a multiple of 4) followed by radix-16
 // passes; each pass loads all of a thread's elements into registers, syncs,
 // and stores them in Stockham (auto-sorted) order, so the transform is
@@ -113,12 +113,11 @@ template <typename C, int RD, int SIGN> FIL_DEV void dft(C* v) {
 }
 
 template <typename C, int N, int RD, int NS, int SIGN>
-FIL_DEV void pass(C* s, const C* __restrict__ tp) {
+FIL_DEV void pass(C* s, const C* __restrict__ tp, int tid) {
   constexpr int T = N / 16;
   constexpr int NB = N / RD;
   constexpr int Q = NB / T;
   C v[Q][RD];
-  const int tid = threadIdx.x;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int b = tid + q * T;
@@ -147,30 +146,38 @@ FIL_DEV void pass(C* s, const C* __restrict__ tp) {
 }
 
 template <typename C, int N, int NS, int SIGN>
-FIL_DEV void passes16(C* s, const C* __restrict__ tp) {
+FIL_DEV void passes16(C* s, const C* __restrict__ tp, int tid) {
   if constexpr (NS < N) {
-    pass<C, N, 16, NS, SIGN>(s, tp);
-    passes16<C, N, NS * 16, SIGN>(s, tp + (NS > 1 ? 15 * NS : 0));
+    pass<C, N, 16, NS, SIGN>(s, tp, tid);
+    passes16<C, N, NS * 16, SIGN>(s, tp + (NS > 1 ? 15 * NS : 0), tid);
   }
 }
 
 
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
 
-// In-place FFT of s[pad16(0..N-1)] by the first N/16 threads of the block
-// (blockDim.x must equal N/16).  Synchronises on entry and exit.
+// In-place FFT of s[pad16(0..N-1)] by a group of N/16 threads; `tid` is the
+// thread's index in its group.  Several groups may run side by side on
+// their own arrays: every thread of the block must call it (the passes
+// synchronise the whole block), all with the same N and SIGN.
 template <typename C, int N, int SIGN>
-FIL_DEV void block_fft(C* s, const C* __restrict__ tw) {
-  static_assert(N >= 256 && (N & (N - 1)) == 0, "N must be a power of two >= 256");
+FIL_DEV void group_fft(C* s, const C* __restrict__ tw, int tid) {
+  static_assert(N >= 16 && (N & (N - 1)) == 0, "N must be a power of two >= 16");
   constexpr int L = ilog2(N);
   constexpr int R0 = 1 << (L % 4);
   __syncthreads();
   if constexpr (R0 > 1) {
-    pass<C, N, R0, 1, SIGN>(s, tw);
-    passes16<C, N, R0, SIGN>(s, tw);
+    pass<C, N, R0, 1, SIGN>(s, tw, tid);
+    passes16<C, N, R0, SIGN>(s, tw, tid);
   } else {
-    passes16<C, N, 1, SIGN>(s, tw);
+    passes16<C, N, 1, SIGN>(s, tw, tid);
   }
+}
+
+// In-place FFT of s[pad16(0..N-1)] by the N/16 threads of the block.
+template <typename C, int N, int SIGN>
+FIL_DEV void block_fft(C* s, const C* __restrict__ tw) {
+  group_fft<C, N, SIGN>(s, tw, threadIdx.x);
 }
 
 }  // namespace filfft

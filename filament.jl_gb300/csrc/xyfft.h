@@ -1,0 +1,26 @@
+// xyfft.h -- launch parameters of the XYT transverse transform (xyfft.cu).
+#pragma once
+#include "dht_simt.cuh"
+
+template <typename R> struct XyParams {
+  typedef typename C2T<R>::type C;
+  const C* in;
+  C* out;                 // may equal in
+  size_t line_stride;     // elements between consecutive points of a line
+  size_t outer_stride;    // elements between consecutive lines
+  const C* tw;            // per-pass FFT twiddles of the line length
+  R scale;                // applied on store
+  // propagator (x pass)
+  PropParams<R> pp;       // beta, dfr, kparaxial (kmax2, wg unused here)
+  const R* wg;            // frequency guard [nh] or NULL
+  int wg_bug;             // XYT: frequency guard indexed by iy (Guards.jl:314)
+  const R* kt2_line;      // kx^2 along the line
+  const R* kt2_outer;     // ky^2 of the line
+  const R* sg_line;       // spectral guard along the line
+  const R* sg_outer;
+  DevCtl* ctl;
+  R dz_fixed;
+};
+
+template <typename R>
+cudaError_t launch_xylines(const XyParams<R>& p, int nl, int mode, int nh, int nouter, cudaStream_t st);

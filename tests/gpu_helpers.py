@@ -7,6 +7,7 @@ import numpy as np
 from conftest import PKG_DECKS
 
 FIL_DECK = os.path.join(PKG_DECKS, "filament_RT", "input.py")
+XYT_DECK = os.path.join(PKG_DECKS, "filament_XYT", "input.py")
 
 
 def rt_input(**kw):
@@ -14,6 +15,14 @@ def rt_input(**kw):
     base = dict(Nr=64, Nt=512, rmax=2.0, tmin=-100.0, tmax=100.0, zmax=0.02, ALG="RK3")
     base.update(kw)
     return fg.prepare(FIL_DECK, **base)
+
+
+def xyt_input(**kw):
+    """The XYT multifilamentation deck on a small grid (64 x 64 x 512)."""
+    import filament_gb as fg
+    base = dict(Nx=64, Ny=64, Nt=512, zmax=0.02)
+    base.update(kw)
+    return fg.prepare(XYT_DECK, **base)
 
 
 def two_species_rates():
