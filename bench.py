@@ -155,6 +155,35 @@ def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, simt_dht=
     return res
 
 
+XYT_DECK = os.path.join(PKG, "decks", "filament_XYT", "input.py")
+
+
+def time_xyt(steps, warmup=3):
+    """The 512 x 512 x 512 XYT multifilamentation deck (order-4 super-Gaussian,
+    w0 = 3 mm, 50 fs, 20 Pcr, 5 % seeded amplitude noise, RK3): warm-up steps,
+    then `steps` steps one at a time with the L2 flushed (CUDA events), both
+    precision forms.  Per step: reduce, control, row kernel (262144 rows of
+    512 points), y pass, x pass with the propagator, inverse y pass."""
+    import filament_gb as fg
+    from filament_gb import _abi
+    inp = fg.prepare(XYT_DECK)
+    out = {"workload": "XYT 512x512x512, RK3, 20 Pcr super-Gaussian + 5% noise, adaptive dz"}
+    for prec in ("mixed", "fp64"):
+        sim = fg.Simulation(inp, precision=prec)
+        h = sim.handle
+        h.run(0.0, inp["zmax"], warmup)
+        h.set_field(sim.field.E0, analytic=False)
+        h.set_option(_abi.OPT_TIMING, 1)
+        code, st = h.run(0.0, inp["zmax"], steps)
+        kt = h.kernel_times(6)
+        out[prec] = {"ms_per_step": kt[4], "z_steps_per_s": 1000.0 / kt[4], "row_ms": kt[0],
+                     "xy_transform_ms": kt[1] + kt[2], "reduce_ms": kt[3], "timed_steps": int(kt[5]),
+                     "z_end": st["z"]}
+        sim.close()
+    out["speedup_mixed_over_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    return out
+
+
 def accuracy_run(zend, nmax):
     """Mixed form (tensor-core and CUDA-core Hankel transforms) vs the plain
     FP64 form from the same field to the same z (dz clamped on the last
@@ -247,6 +276,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=30)
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--accuracy-zend", type=float, default=ACCURACY_ZEND)
+    ap.add_argument("--no-xyt", action="store_true", help="skip the 512^3 XYT measurement")
+    ap.add_argument("--xyt-steps", type=int, default=10)
     args = ap.parse_args()
     rank, local_rank, world = _env_rank()
     if world > 1:
@@ -296,6 +327,7 @@ def main():
     if rank != 0:
         return
     e2e = e2e_host_loop(max(10, min(300, mixed["timed_steps"])))
+    xyt = None if args.no_xyt else time_xyt(args.xyt_steps)
     acc = None if args.no_accuracy else accuracy_run(args.accuracy_zend, 200000)
     sps_cpu, cpu_wall = cpu_oracle(args.cpu_steps)
     hbm, bf16, src = _peaks()
@@ -323,6 +355,7 @@ def main():
         "forms": {"mixed": mixed, "mixed_cuda_core_dht": mixed_simt, "fp64": fp64,
                   "speedup_mixed_over_fp64": fp64["ms_per_step"] / mixed["ms_per_step"]},
         "accuracy": acc,
+        "xyt_512": xyt,
         "roofline": {"kernel": "k_rowstep (plasma + RK4 nonlinear step, fused)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": src, "traffic": row_traffic,

@@ -410,8 +410,10 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 //   RK step of func!            (Models.jl:98-103, nonlinear_propagators.jl:38-74)
 //   S_out = S0 + dz sum b_s k_s
 // mode 1: plasma only (initialisation), no S_out.
+// Rows of up to 1024 points (32-64 threads per block, the XYT geometry) are
+// held to 128 registers so that 8-16 blocks share an SM.
 template <typename R, int N, int NC>
-__global__ void __launch_bounds__(N / 16) k_rowstep(RowParams<R> P, int mode) {
+__global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 1) k_rowstep(RowParams<R> P, int mode) {
   typedef typename C2T<R>::type C;
   constexpr int T = N / 16, NH = N / 2, EW = NH / T, NP = N + N / 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
