@@ -47,7 +47,7 @@ struct fil_handle {
   void* M2 = nullptr;
   void* tw = nullptr;     // [nt] complex, per-pass twiddle layout of fft.cuh
   void* g1 = nullptr; void* g2 = nullptr; void* gt = nullptr;
-  void* Cc = nullptr; void* Cf = nullptr; void* Cl = nullptr;
+  void* Cc = nullptr; void* Cf = nullptr; void* Cl = nullptr; void* Cr = nullptr; void* ramh = nullptr;
   void* kt2 = nullptr; void* beta = nullptr; void* dfr = nullptr; void* kmax2 = nullptr; void* wg = nullptr;
   void* rho_g = nullptr; void* kdrho_g = nullptr;
   void* stage = nullptr;  // field staging [nrows][nt] complex
@@ -61,7 +61,7 @@ struct fil_handle {
   PlasmaParams<double> pp;
   int ns;
   double A0[4], A1[4], B[4];
-  double sc = 1, sf = 1, sl = 1;   // response channel pre-scales
+  double sc = 1, sf = 1, sl = 1, sr = 1;   // response channel pre-scales
   bool field_set = false, store_plasma = false;
   int bugcompat = 0, clamp_last = 0, timing = 0;
   cudaGraphExec_t graph = nullptr;
@@ -214,6 +214,7 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     h->sc = scale(t->rnl_cubic);
     h->sf = scale(t->rnl_free);
     h->sl = scale(t->rnl_losses);
+    h->sr = scale(t->rnl_raman);
     auto comb = [&](const double* rnl, double sch, void** dst) -> int {
       std::vector<double> v(2 * nh, 0.0);
       if (rnl && t->qz)
@@ -225,8 +226,12 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
       return upload<R>(h, dst, v);
     };
     if (comb(t->rnl_cubic, h->sc, &h->Cc) || comb(t->rnl_free, h->sf, &h->Cf) ||
-        comb(t->rnl_losses, h->sl, &h->Cl))
+        comb(t->rnl_losses, h->sl, &h->Cl) || comb(t->rnl_raman, h->sr, &h->Cr))
       return FIL_ERR_CUDA;
+    if (t->raman_h) {
+      std::vector<double> v(t->raman_h, t->raman_h + 2 * nt);
+      if (upload<R>(h, &h->ramh, v)) return FIL_ERR_CUDA;
+    }
   }
   // propagator tables
   {
@@ -474,6 +479,11 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
   P.Cc = (const C*)h->Cc;
   P.Cf = (const C*)h->Cf;
   P.Cl = (const C*)h->Cl;
+  P.Cr = (const C*)h->Cr;
+  P.sr = (R)h->sr;
+  P.has_raman = (c.resp_mask & FIL_RESP_RAMAN) && h->ramh ? 1 : 0;
+  P.raman_thg = c.raman_thg;
+  P.ramh = (const C*)h->ramh;
   P.sc = (R)h->sc;
   P.sf = (R)h->sf;
   P.sl = (R)h->sl;
@@ -637,7 +647,7 @@ static int read_ctl(fil_handle* h) {
 }
 
 static void free_all(fil_handle* h) {
-  void* bufs[] = {h->S, h->W1, h->W2, h->M1, h->M2, h->tw, h->g1, h->g2, h->gt, h->Cc, h->Cf, h->Cl,
+  void* bufs[] = {h->S, h->W1, h->W2, h->M1, h->M2, h->tw, h->g1, h->g2, h->gt, h->Cc, h->Cf, h->Cl, h->Cr, h->ramh,
                   h->kt2, h->beta, h->dfr, h->kmax2, h->wg, h->rho_g, h->kdrho_g, h->stage,
                   h->fluence, h->power, h->pw, h->rho_end, h->ctl, h->flushbuf,
                   h->qa1, h->qa2, h->BS[0], h->BS[1], h->BS[2], h->qb, h->kzt, h->gdt, h->tc_err,
@@ -748,8 +758,8 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (cfg->n1 < 1 || cfg->n1 > 65536) return fail(h, FIL_ERR_ARG, "bad n1");
   if (cfg->nonlinearity && !cfg->qparaxial)
     return fail(h, FIL_ERR_UNSUPPORTED, "QPARAXIAL=false is not built");
-  if (cfg->nonlinearity && (cfg->resp_mask & FIL_RESP_RAMAN))
-    return fail(h, FIL_ERR_UNSUPPORTED, "the Raman response is not built");
+  if (cfg->nonlinearity && (cfg->resp_mask & FIL_RESP_RAMAN) && !t->raman_h)
+    return fail(h, FIL_ERR_ARG, "missing Raman response table");
   if (cfg->plasma && (cfg->plasma_ncomp < 1 || cfg->plasma_ncomp > FIL_MAXCOMP))
     return fail(h, FIL_ERR_UNSUPPORTED, "plasma_ncomp must be 1 or 2");
   if (cfg->plasma && (cfg->rate_n < 2 || cfg->rate_n > FIL_MAXRATE))

@@ -5,6 +5,7 @@
 #include "launch.h"
 #include "rowkernels.cuh"
 #include "dht_simt.cuh"
+#include "rowstep_launch.h"
 
 // ---------------------------------------------------------------------------
 // Controller (AdaptiveSteps.jl:96-107, Filament.jl:123-164): one block.
@@ -52,32 +53,17 @@ __global__ void k_setdz(DevCtl* c, double z, double dz) {
 }
 
 // ---------------------------------------------------------------------------
-template <typename R, int N, int NC>
-static size_t rowstep_smem() {
-  typedef typename C2T<R>::type C;
-  constexpr int NP = N + N / 16;
-  return 2 * NP * sizeof(C) + 2 * NP * sizeof(R) + 32 * sizeof(R) + 32 * sizeof(Aff<R, (NC > 0 ? NC : 1)>) +
-         sizeof(PlasmaSmem<R>);
-}
 template <typename R, int N> static size_t x_smem() {
   typedef typename C2T<R>::type C;
   return (N + N / 16) * sizeof(C) + 64 * sizeof(double);
 }
 
-template <typename R, int N, int NC>
-static cudaError_t launch_rowstep_t(const RowParams<R>& P, int mode, cudaStream_t st) {
-  size_t sm = rowstep_smem<R, N, NC>();
-  cudaError_t e = cudaFuncSetAttribute(k_rowstep<R, N, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  k_rowstep<R, N, NC><<<P.nrows, N / 16, sm, st>>>(P, mode);
-  return cudaGetLastError();
-}
-
 template <typename R, int N>
 static cudaError_t launch_rowstep_n(const RowParams<R>& P, int nc, int mode, cudaStream_t st) {
-  if (nc == 0) return launch_rowstep_t<R, N, 0>(P, mode, st);
-  if (nc == 1) return launch_rowstep_t<R, N, 1>(P, mode, st);
-  return launch_rowstep_t<R, N, 2>(P, mode, st);
+  const bool ram = P.has_raman != 0;
+  if (nc == 0) return ram ? launch_rowstep_t<R, N, 0, true>(P, mode, st) : launch_rowstep_t<R, N, 0, false>(P, mode, st);
+  if (nc == 1) return ram ? launch_rowstep_t<R, N, 1, true>(P, mode, st) : launch_rowstep_t<R, N, 1, false>(P, mode, st);
+  return ram ? launch_rowstep_t<R, N, 2, true>(P, mode, st) : launch_rowstep_t<R, N, 2, false>(P, mode, st);
 }
 
 template <typename R>

@@ -41,7 +41,10 @@ template <typename R> struct RowParams {
   const C* Cc;                  // i QZ Rnl_cubic * (k ? 2 : 1), [nh]
   const C* Cf;
   const C* Cl;
-  R sc, sf, sl;                 // channel pre-scales (C tables are divided by them)
+  const C* Cr;                  // Raman
+  R sc, sf, sl, sr;             // channel pre-scales (C tables are divided by them)
+  int has_raman, raman_thg;
+  const C* ramh;                // Raman response H(w) [N] (raman.jl:21-31)
   int ns;                       // RK stages
   R A0[4], A1[4], B[4];         // stage input U_s = S0 + dz (A0 k1 + A1 kprev)
   // plasma
@@ -409,11 +412,12 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 //   S0 = ifft(E)[0:N/2]        (Models.jl:91-96)
 //   RK step of func!            (Models.jl:98-103, nonlinear_propagators.jl:38-74)
 //   S_out = S0 + dz sum b_s k_s
-// mode 1: plasma only (initialisation), no S_out.
-// Rows of up to 1024 points (32-64 threads per block, the XYT geometry) are
-// held to 128 registers so that 8-16 blocks share an SM.
-template <typename R, int N, int NC>
-__global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 1) k_rowstep(RowParams<R> P, int mode) {
+// mode 1: plasma only (initialisation), no S_out.  RAM: the Raman channel
+// (compiled only where used, it costs registers).  Blocks are held to 128
+// registers so that two (4096-point rows) to sixteen (512-point rows, the
+// XYT geometry) share an SM.
+template <typename R, int N, int NC, bool RAM>
+__global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(RowParams<R> P, int mode) {
   typedef typename C2T<R>::type C;
   constexpr int T = N / 16, NH = N / 2, EW = NH / T, NP = N + N / 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -493,11 +497,30 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 1) k_rowstep(Ro
         X[pad16(k + NH)] = mk<R>(0, 0);
       }
       filfft::block_fft<C, N, -1>(X, P.tw);            // inverse_transform_time!
+      if (RAM) {
+        // raman.jl:80-98: conv = fft(H * ifft(x)), x = Re(E)^2 or 3/4 |E|^2,
+        // in Y (free until the responses below are written)
+#pragma unroll 4
+        for (int m = 0; m < 16; ++m) {
+          int j = tid + m * T;
+          C e = X[pad16(j)];
+          R x = P.raman_thg ? e.x * e.x : (R)0.75 * (e.x * e.x + e.y * e.y);
+          Y[pad16(j)] = mk<R>(x, 0);
+        }
+        filfft::block_fft<C, N, +1>(Y, P.tw);
+#pragma unroll 4
+        for (int m = 0; m < 16; ++m) {
+          int j = tid + m * T;
+          Y[pad16(j)] = invN * cmul(Y[pad16(j)], __ldg(&P.ramh[j]));
+        }
+        filfft::block_fft<C, N, -1>(Y, P.tw);
+      }
       // responses in the time domain (medium_responses/*.jl) times the field
       // filter.  Channels are packed two per complex FFT by scale: X holds
-      // the Kerr response, Y the two plasma responses (free current in the
-      // real part, losses in the imaginary part); each channel is pre-scaled
-      // by |C_ch| at the carrier so packed partners have comparable size.
+      // the Kerr response (real part) and the Raman response (imaginary
+      // part), Y the two plasma responses (free current in the real part,
+      // losses in the imaginary part); each channel is pre-scaled by |C_ch|
+      // at the carrier so packed partners have comparable size.
 #pragma unroll 4
       for (int m = 0; m < 16; ++m) {
         int j = tid + m * T;
@@ -505,19 +528,20 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 1) k_rowstep(Ro
         R re = e.x;
         R I = e.x * e.x + e.y * e.y;
         R g = gs * P.gt[P.gt_bug ? iy : j];
-        R fc = 0, ff = 0, fl = 0;
+        R fc = 0, ff = 0, fl = 0, fr = 0;
         if (P.has_cubic) fc = P.cubic_thg ? re * re * re : (R)0.75 * I * re;
+        if (RAM) fr = Y[pad16(j)].x * re;
         if (NC > 0 && P.has_free) ff = rho[pad16(j)] * re;
         if (NC > 0 && P.has_losses) {
           R Il = P.losses_ereal ? re * re : I;
           R inv = (Il >= (R)1e-30) ? (R)1 / Il : (R)0;
           fl = kdrho[pad16(j)] * inv * re;
         }
-        X[pad16(j)] = mk<R>(g * (R)P.sc * fc, 0);
+        X[pad16(j)] = mk<R>(g * (R)P.sc * fc, RAM ? g * P.sr * fr : (R)0);
         Y[pad16(j)] = mk<R>(g * (R)P.sf * ff, g * (R)P.sl * fl);
       }
       const bool plas = NC > 0 && (P.has_free || P.has_losses) && ych;
-      if (P.has_cubic) filfft::block_fft<C, N, +1>(X, P.tw);   // rsig2aspec!
+      if (P.has_cubic || RAM) filfft::block_fft<C, N, +1>(X, P.tw);   // rsig2aspec!
       if (plas) filfft::block_fft<C, N, +1>(Y, P.tw);
       __syncthreads();
 #pragma unroll
@@ -525,9 +549,13 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 1) k_rowstep(Ro
         int k = tid + m * T;
         const int km = (N - k) & (N - 1);
         C d = mk<R>(0, 0);
-        if (P.has_cubic) {
+        if (P.has_cubic || RAM) {
           C z = X[pad16(k)], zm = cconj(X[pad16(km)]);
-          d = cmul(__ldg(&P.Cc[k]), ((R)0.5 * invN) * (z + zm));
+          if (P.has_cubic) d = cmul(__ldg(&P.Cc[k]), ((R)0.5 * invN) * (z + zm));
+          if (RAM) {
+            C dl = z - zm;
+            d = d + cmul(__ldg(&P.Cr[k]), mk<R>(dl.y * (R)0.5 * invN, -dl.x * (R)0.5 * invN));
+          }
         }
         if (plas) {
           C z = Y[pad16(k)], zm = cconj(Y[pad16(km)]);

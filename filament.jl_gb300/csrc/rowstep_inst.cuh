@@ -1,0 +1,36 @@
+// rowstep_inst.cuh -- definition of the row-kernel launchers; included by
+// the rowstep_*.cu translation units, each instantiating one share.
+#pragma once
+#include "rowstep_launch.h"
+
+template <typename R, int N, int NC>
+static size_t rowstep_smem() {
+  typedef typename C2T<R>::type C;
+  constexpr int NP = N + N / 16;
+  return 2 * NP * sizeof(C) + 2 * NP * sizeof(R) + 32 * sizeof(R) + 32 * sizeof(Aff<R, (NC > 0 ? NC : 1)>) +
+         sizeof(PlasmaSmem<R>);
+}
+
+template <typename R, int N, int NC, bool RAM>
+cudaError_t launch_rowstep_t(const RowParams<R>& P, int mode, cudaStream_t st) {
+  size_t sm = rowstep_smem<R, N, NC>();
+  cudaError_t e =
+      cudaFuncSetAttribute(k_rowstep<R, N, NC, RAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_rowstep<R, N, NC, RAM><<<P.nrows, N / 16, sm, st>>>(P, mode);
+  return cudaGetLastError();
+}
+
+#define FIL_ROWSTEP_INST(R, RAM)                                                                   \
+  template cudaError_t launch_rowstep_t<R, 512, 0, RAM>(const RowParams<R>&, int, cudaStream_t);  \
+  template cudaError_t launch_rowstep_t<R, 512, 1, RAM>(const RowParams<R>&, int, cudaStream_t);  \
+  template cudaError_t launch_rowstep_t<R, 512, 2, RAM>(const RowParams<R>&, int, cudaStream_t);  \
+  template cudaError_t launch_rowstep_t<R, 1024, 0, RAM>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 1024, 1, RAM>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 1024, 2, RAM>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 2048, 0, RAM>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 2048, 1, RAM>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 2048, 2, RAM>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 4096, 0, RAM>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 4096, 1, RAM>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 4096, 2, RAM>(const RowParams<R>&, int, cudaStream_t);

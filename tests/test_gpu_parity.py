@@ -144,3 +144,23 @@ def test_linear_energy_drift_at_fp32_floor(gpu_lib, dht):
     eg, er = g.handle.analyze()["energy"], r.handle.analyze()["energy"]
     assert abs(eg - er) / e0 < 2.5e-5
     assert rel_l2(g.handle.get_field(), r.handle.get_field()) < 3e-5
+
+
+def _with_raman(inp, thg):
+    from filament_gb.responses import init_raman, raman_response_air
+    responses, plasma, keys = inp["p_model"]
+    raman = {"init": init_raman, "THG": thg, "n2": 0.5e-23, "raman_response": raman_response_air}
+    inp = dict(inp)
+    inp["p_model"] = (list(responses) + [raman], plasma, keys)
+    return inp
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("thg", [True, False])
+def test_raman_step(gpu_lib, precision, thg):
+    """raman.jl: delayed response F = (H * x) Re(E), x = Re(E)^2 (THG) or
+    3/4 |E|^2, packed with the Kerr channel in one FFT."""
+    inp = _with_raman(rt_input(ALG="RK4", PPcr=30.0), thg)
+    g, r = pair(inp, precision)
+    step_both(g, r, 3, 2e-3)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL[precision]
