@@ -62,6 +62,7 @@ struct fil_handle {
   int ns;
   double A0[4], A1[4], B[4];
   double sc = 1, sf = 1, sl = 1, sr = 1;   // response channel pre-scales
+  std::complex<double> c0 = 0.0;           // XY: i QZ(w0) Rnl_cubic(w0)
   bool field_set = false, store_plasma = false;
   int bugcompat = 0, clamp_last = 0, timing = 0;
   cudaGraphExec_t graph = nullptr;
@@ -185,7 +186,7 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     if (t->guard1) g.assign(t->guard1, t->guard1 + n1);
     if (t->guardt) gtt.assign(t->guardt, t->guardt + nt);
     if (upload<R>(h, &h->g1, g) || upload<R>(h, &h->gt, gtt)) return FIL_ERR_CUDA;
-    if (h->geom == FIL_GEOM_XYT) {
+    if (h->geom == FIL_GEOM_XYT || h->geom == FIL_GEOM_XY) {
       std::vector<double> g2(h->n2, 1.0);
       if (t->guard2) g2.assign(t->guard2, t->guard2 + h->n2);
       if (upload<R>(h, &h->g2, g2)) return FIL_ERR_CUDA;
@@ -215,6 +216,7 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     h->sf = scale(t->rnl_free);
     h->sl = scale(t->rnl_losses);
     h->sr = scale(t->rnl_raman);
+    if (h->geom == FIL_GEOM_XY && t->qz && t->rnl_cubic && (c.resp_mask & FIL_RESP_CUBIC)) h->c0 = coef(t->rnl_cubic, 0);
     auto comb = [&](const double* rnl, double sch, void** dst) -> int {
       std::vector<double> v(2 * nh, 0.0);
       if (rnl && t->qz)
@@ -249,7 +251,7 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
       if (upload<R>(h, &h->wg, w)) return FIL_ERR_CUDA;
     }
   }
-  if (h->geom == FIL_GEOM_XYT) {
+  if (h->geom == FIL_GEOM_XYT || h->geom == FIL_GEOM_XY) {
     // transverse 2-D transform tables (xyfft.cu)
     const int nx = h->n1, ny = h->n2;
     std::vector<double> kx2(nx), ky2(ny), s1(nx, 1.0), s2(ny, 1.0);
@@ -277,7 +279,7 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
   {
     std::vector<double> w(nr);
     for (int i = 0; i < nr; ++i)
-      w[i] = h->geom == FIL_GEOM_XYT ? c.dxdy : 2.0 * M_PI * (t->rdr ? t->rdr[i] : 0.0);
+      w[i] = (h->geom == FIL_GEOM_XYT || h->geom == FIL_GEOM_XY) ? c.dxdy : 2.0 * M_PI * (t->rdr ? t->rdr[i] : 0.0);
     CK(cudaMalloc(&h->pw, nr * sizeof(double)));
     CK(cudaMemcpy(h->pw, w.data(), nr * sizeof(double), cudaMemcpyHostToDevice));
   }
@@ -565,8 +567,72 @@ template <typename R> static int enqueue_zstep_xyt(fil_handle* h, bool timed) {
   return 0;
 }
 
+// XY (no time axis): pointwise nonlinear RK step (W1 <- S), fft along y,
+// fft along x with the propagator and the inverse along x, inverse along y
+// times the field guard (S <- W1)
+template <typename R> static int enqueue_zstep_xy(fil_handle* h, bool timed) {
+  typedef typename C2T<R>::type C;
+  const int nx = h->n1, ny = h->n2;
+  const C* src = (const C*)h->S;
+  if (timed) CK(cudaEventRecord(h->ev[1], h->st));
+  if (h->cfg.nonlinearity) {
+    XyNlParams<R> q;
+    std::memset(&q, 0, sizeof q);
+    q.n = (long)nx * ny;
+    q.ny = ny;
+    double a[4][4], b[4], cc[4];
+    rk_tableau(h->cfg.alg, &q.ns, a, b, cc);
+    for (int i = 0; i < 4; ++i) {
+      q.b[i] = (R)b[i];
+      for (int j = 0; j < 4; ++j) q.a[i][j] = (R)a[i][j];
+    }
+    q.c0 = mk<R>((R)h->c0.real(), (R)h->c0.imag());
+    q.g1 = (const R*)h->g1;
+    q.g2 = (const R*)h->g2;
+    q.ctl = h->ctl;
+    CK(launch_xy_nonlinear<R>(src, (C*)h->W1, q, h->st));
+    src = (const C*)h->W1;
+  }
+  if (timed) CK(cudaEventRecord(h->ev[2], h->st));
+  XyParams<R> q;
+  std::memset(&q, 0, sizeof q);
+  q.in = src;
+  q.out = (C*)h->W1;
+  q.ctl = h->ctl;
+  q.line_stride = 1;
+  q.outer_stride = (size_t)ny;
+  q.tw = (const C*)h->twy;
+  q.scale = (R)1;
+  CK(launch_xylines<R>(q, ny, 0, 1, nx, h->st));
+  XyParams<R> qx = q;
+  qx.in = (const C*)h->W1;
+  qx.line_stride = (size_t)ny;
+  qx.outer_stride = 1;
+  qx.tw = (const C*)h->twx;
+  qx.scale = (R)1 / (R)nx;
+  qx.pp = prop_params<R>(h);
+  qx.pp.kmax2 = nullptr;
+  qx.wg = (const R*)h->wg;
+  qx.kt2_line = (const R*)h->kx2;
+  qx.kt2_outer = (const R*)h->ky2;
+  qx.sg_line = (const R*)h->sg1;
+  qx.sg_outer = (const R*)h->sg2;
+  CK(launch_xylines<R>(qx, nx, 1, 1, ny, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[3], h->st));
+  XyParams<R> qi = q;
+  qi.in = (const C*)h->W1;
+  qi.out = (C*)h->S;
+  qi.scale = (R)1 / (R)ny;
+  qi.g_outer = (const R*)h->g1;
+  qi.g_line = (const R*)h->g2;
+  CK(launch_xylines<R>(qi, ny, 3, 1, nx, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[4], h->st));
+  return 0;
+}
+
 template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   if (h->geom == FIL_GEOM_XYT) return enqueue_zstep_xyt<R>(h, timed);
+  if (h->geom == FIL_GEOM_XY) return enqueue_zstep_xy<R>(h, timed);
   RowParams<R> P = row_params<R>(h);
   P.S_in = (const typename C2T<R>::type*)h->S;
   P.S_out = (typename C2T<R>::type*)h->W1;
@@ -616,6 +682,10 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
 // power[t] = sum_row w_row |E|^2 (the intensities pass through the staging
 // buffer)
 template <typename R> static int enqueue_reduce(fil_handle* h, double* power, int check_done) {
+  if (h->geom == FIL_GEOM_XY) {   // power = sum F dxdy, formed on the host (fil_analyze)
+    CK(launch_xy_reduce<R>((const typename C2T<R>::type*)h->S, h->fluence, h->ctl, h->nrows, check_done, h->st));
+    return 0;
+  }
   RowParams<R> P = row_params<R>(h);
   P.S_in = (const typename C2T<R>::type*)h->S;
   R* I = power ? (R*)h->stage : nullptr;
@@ -702,6 +772,15 @@ template <typename R> static int set_field_t(fil_handle* h, const void* E, int d
   typedef typename C2T<R>::type C;
   std::vector<R> rows;
   to_rows<R>(h, E, dtype, layout, rows);
+  if (h->geom == FIL_GEOM_XY) {   // no time axis: the state is the field
+    CK(cudaMemcpyAsync(h->S, rows.data(), rows.size() * sizeof(R), cudaMemcpyHostToDevice, h->st));
+    DevCtl c;
+    std::memset(&c, 0, sizeof c);
+    c.first = 1;
+    CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return 0;
+  }
   CK(cudaMemcpyAsync(h->stage, rows.data(), rows.size() * sizeof(R), cudaMemcpyHostToDevice, h->st));
   CK(launch_field_in<R>((const C*)h->stage, (C*)h->S, h->nh, (const C*)h->tw, analytic, h->nrows, h->nt, h->st));
   // control block: fresh simulation, no pending guard
@@ -721,6 +800,13 @@ template <typename R> static int set_field_t(fil_handle* h, const void* E, int d
 
 template <typename R> static int get_field_t(fil_handle* h, void* E, int dtype, int layout) {
   typedef typename C2T<R>::type C;
+  if (h->geom == FIL_GEOM_XY) {
+    std::vector<R> rows((size_t)h->nrows * 2);
+    CK(cudaMemcpyAsync(rows.data(), h->S, rows.size() * sizeof(R), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    from_rows<R>(h, rows, E, dtype, layout, 2);
+    return 0;
+  }
   RowParams<R> P = row_params<R>(h);
   P.S_in = (const C*)h->S;
   CK(launch_field_out<R>(P, h->nt, (C*)h->stage, h->st));
@@ -748,12 +834,17 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (!cfg || !t || !out) return fail(h, FIL_ERR_ARG, "null argument");
   *out = nullptr;
   if (cfg->abi_version != FIL_ABI_VERSION) return fail(h, FIL_ERR_ARG, "ABI version mismatch");
-  if (cfg->geometry != FIL_GEOM_RT && cfg->geometry != FIL_GEOM_XYT)
-    return fail(h, FIL_ERR_UNSUPPORTED, "this build runs the RT and XYT geometries on the GPU");
+  if (cfg->geometry != FIL_GEOM_RT && cfg->geometry != FIL_GEOM_XYT && cfg->geometry != FIL_GEOM_XY)
+    return fail(h, FIL_ERR_UNSUPPORTED, "this build runs the RT, XY and XYT geometries on the GPU");
+  if (cfg->geometry == FIL_GEOM_XY &&
+      (!is_pow2(cfg->n1) || !is_pow2(cfg->n2) || cfg->n1 < 64 || cfg->n1 > 4096 || cfg->n2 < 64 || cfg->n2 > 4096))
+    return fail(h, FIL_ERR_UNSUPPORTED, "XY: nx and ny must be powers of two in [64, 4096]");
+  if (cfg->geometry == FIL_GEOM_XY && (cfg->nt != 1 || cfg->plasma))
+    return fail(h, FIL_ERR_ARG, "XY: nt must be 1 and the plasma off");
   if (cfg->geometry == FIL_GEOM_XYT &&
       (!is_pow2(cfg->n1) || !is_pow2(cfg->n2) || cfg->n1 < 64 || cfg->n1 > 1024 || cfg->n2 < 64 || cfg->n2 > 1024))
     return fail(h, FIL_ERR_UNSUPPORTED, "XYT: nx and ny must be powers of two in [64, 1024]");
-  if (!is_pow2(cfg->nt) || cfg->nt < 512 || cfg->nt > 4096)
+  if (cfg->geometry != FIL_GEOM_XY && (!is_pow2(cfg->nt) || cfg->nt < 512 || cfg->nt > 4096))
     return fail(h, FIL_ERR_UNSUPPORTED, "nt must be a power of two in [512, 4096]");
   if (cfg->n1 < 1 || cfg->n1 > 65536) return fail(h, FIL_ERR_ARG, "bad n1");
   if (cfg->nonlinearity && !cfg->qparaxial)
@@ -766,7 +857,8 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
     return fail(h, FIL_ERR_ARG, "rate_n must be in [2, 32]");
   if (!t->kt1 || !t->beta || !t->dfr) return fail(h, FIL_ERR_ARG, "missing propagator tables");
   if (cfg->geometry == FIL_GEOM_RT && (!t->dht || !t->dht_s)) return fail(h, FIL_ERR_ARG, "missing DHT tables");
-  if (cfg->geometry == FIL_GEOM_XYT && !t->kt2) return fail(h, FIL_ERR_ARG, "missing ky table");
+  if ((cfg->geometry == FIL_GEOM_XYT || cfg->geometry == FIL_GEOM_XY) && !t->kt2)
+    return fail(h, FIL_ERR_ARG, "missing ky table");
   if (cfg->nonlinearity && !t->qz) return fail(h, FIL_ERR_ARG, "missing QZ table");
   if (cfg->plasma && (!t->rho_nt || !t->rava || !t->kfix || !t->rate_lx || !t->rate_ly))
     return fail(h, FIL_ERR_ARG, "missing plasma tables");
@@ -779,7 +871,7 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   h->n1 = cfg->n1;
   h->n2 = cfg->n2;
   h->nt = cfg->nt;
-  h->nh = cfg->nt / 2;
+  h->nh = cfg->geometry == FIL_GEOM_XY ? 1 : cfg->nt / 2;   // XY: the field itself, one column
   h->nrows = cfg->n1 * cfg->n2;
   h->mpad = (h->nrows + 127) / 128 * 128;
   h->nc = cfg->plasma ? cfg->plasma_ncomp : 0;
@@ -1045,6 +1137,11 @@ int fil_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power, do
   rc = check_tc(h);
   if (rc) return rc;
   const DevCtl& c = *h->ctl_host;
+  if (h->geom == FIL_GEOM_XY) {   // FieldAnalyzers.jl:240-255: P = sum |E|^2 dx dy
+    double sp = 0;
+    for (int i = 0; i < nr; ++i) sp += F[i] * w[i];
+    P[0] = sp;
+  }
   if (fluence) std::memcpy(fluence, F, nr * sizeof(double));
   if (power) std::memcpy(power, P, h->nt * sizeof(double));
   if (rho_end) std::memcpy(rho_end, re, nr * sizeof(double));

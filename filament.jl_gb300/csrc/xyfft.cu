@@ -29,11 +29,12 @@ template <typename R, int NL> constexpr int xy_kt() {
 }
 
 // MODE 0: forward transform.  MODE 1: forward, propagator, inverse (x pass).
-// MODE 2: inverse transform into `out`, marks the field guard pending.
-template <typename R, int NL, int MODE>
-__global__ void __launch_bounds__(xy_kt<R, NL>() * (NL / 16)) k_xylines(XyParams<R> p) {
+// MODE 2: inverse transform into `out`, marks the field guard pending (XYT).
+// MODE 3: inverse transform into `out` times the field guard g1[ix] g2[iy]
+// (XY, whose step ends with the guard, Models.jl:116-118).
+template <typename R, int NL, int KT, int MODE>
+__global__ void __launch_bounds__(KT * (NL / 16)) k_xylines(XyParams<R> p) {
   typedef typename C2T<R>::type C;
-  constexpr int KT = xy_kt<R, NL>();
   constexpr int T = NL / 16, NP = NL + NL / 16, NTH = KT * T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tile = reinterpret_cast<C*>(smem_raw);
@@ -49,7 +50,7 @@ __global__ void __launch_bounds__(xy_kt<R, NL>() * (NL / 16)) k_xylines(XyParams
   }
   const int g = tid / T, gt = tid - g * T;
   C* s = tile + g * NP;
-  if (MODE == 2) {
+  if (MODE >= 2) {
     filfft::group_fft<C, NL, +1>(s, p.tw, gt);
   } else {
     filfft::group_fft<C, NL, -1>(s, p.tw, gt);
@@ -74,31 +75,42 @@ __global__ void __launch_bounds__(xy_kt<R, NL>() * (NL / 16)) k_xylines(XyParams
 #pragma unroll 4
   for (int i = tid; i < NL * KT; i += NTH) {
     const int l = i / KT, c = i - l * KT;
-    p.out[base + (size_t)l * p.line_stride + c] = p.scale * tile[c * NP + pad16(l)];
+    R sc = p.scale;
+    if (MODE == 3) sc *= p.g_outer[o] * p.g_line[l];
+    p.out[base + (size_t)l * p.line_stride + c] = sc * tile[c * NP + pad16(l)];
   }
   if (MODE == 2 && p.ctl && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) p.ctl->guard_pending = 1;
 }
 
+template <typename R, int NL, int KT, int MODE>
+static cudaError_t launch_xy_k(const XyParams<R>& p, int nh, int nouter, cudaStream_t st) {
+  typedef typename C2T<R>::type C;
+  const size_t sm = (size_t)KT * (NL + NL / 16) * sizeof(C);
+  cudaError_t e = cudaFuncSetAttribute(k_xylines<R, NL, KT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  dim3 grid(nh / KT, nouter);
+  k_xylines<R, NL, KT, MODE><<<grid, KT * (NL / 16), sm, st>>>(p);
+  return cudaGetLastError();
+}
+
+// XYT: KT frequency columns per block (nh a multiple of KT); XY (nh = 1):
+// one column, modes 0, 1 and 3
 template <typename R, int NL>
 static cudaError_t launch_xy_n(const XyParams<R>& p, int mode, int nh, int nouter, cudaStream_t st) {
-  typedef typename C2T<R>::type C;
   constexpr int KT = xy_kt<R, NL>();
-  if (nh % KT) return cudaErrorInvalidValue;
-  const size_t sm = (size_t)KT * (NL + NL / 16) * sizeof(C);
-  dim3 grid(nh / KT, nouter);
-  cudaError_t e = cudaSuccess;
-  if (mode == 0) {
-    e = cudaFuncSetAttribute(k_xylines<R, NL, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e == cudaSuccess) k_xylines<R, NL, 0><<<grid, KT * (NL / 16), sm, st>>>(p);
-  } else if (mode == 1) {
-    e = cudaFuncSetAttribute(k_xylines<R, NL, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e == cudaSuccess) k_xylines<R, NL, 1><<<grid, KT * (NL / 16), sm, st>>>(p);
-  } else {
-    e = cudaFuncSetAttribute(k_xylines<R, NL, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e == cudaSuccess) k_xylines<R, NL, 2><<<grid, KT * (NL / 16), sm, st>>>(p);
+  if (nh == 1) {
+    if (mode == 0) return launch_xy_k<R, NL, 1, 0>(p, nh, nouter, st);
+    if (mode == 1) return launch_xy_k<R, NL, 1, 1>(p, nh, nouter, st);
+    if (mode == 3) return launch_xy_k<R, NL, 1, 3>(p, nh, nouter, st);
+    return cudaErrorInvalidValue;
   }
-  if (e != cudaSuccess) return e;
-  return cudaGetLastError();
+  if constexpr (NL <= 1024) {
+    if (nh % KT) return cudaErrorInvalidValue;
+    if (mode == 0) return launch_xy_k<R, NL, KT, 0>(p, nh, nouter, st);
+    if (mode == 1) return launch_xy_k<R, NL, KT, 1>(p, nh, nouter, st);
+    if (mode == 2) return launch_xy_k<R, NL, KT, 2>(p, nh, nouter, st);
+  }
+  return cudaErrorInvalidValue;
 }
 
 template <typename R>
@@ -109,9 +121,78 @@ cudaError_t launch_xylines(const XyParams<R>& p, int nl, int mode, int nh, int n
     case 256: return launch_xy_n<R, 256>(p, mode, nh, nouter, st);
     case 512: return launch_xy_n<R, 512>(p, mode, nh, nouter, st);
     case 1024: return launch_xy_n<R, 1024>(p, mode, nh, nouter, st);
+    case 2048: return launch_xy_n<R, 2048>(p, mode, nh, nouter, st);
+    case 4096: return launch_xy_n<R, 4096>(p, mode, nh, nouter, st);
   }
   return cudaErrorInvalidValue;
 }
 
-template cudaError_t launch_xylines<float>(const XyParams<float>&, int, int, int, int, cudaStream_t);
-template cudaError_t launch_xylines<double>(const XyParams<double>&, int, int, int, int, cudaStream_t);
+// ---------------------------------------------------------------------------
+// XY geometry (no time axis): the state is E(x, y) itself.
+// Nonlinear step (nonlinear_propagators.jl:38-74 with cubic.jl:49-54,
+// F = 3/4 |E|^2 E): dE/dz = C0 * g(x, y) * F(E), C0 = i QZ(w0) Rnl(w0), an
+// explicit RK step per point; writes the result into `out`.
+template <typename R>
+__global__ void __launch_bounds__(256) k_xy_nonlinear(const typename C2T<R>::type* in, typename C2T<R>::type* out,
+                                                      XyNlParams<R> p) {
+  typedef typename C2T<R>::type C;
+  const long i = blockIdx.x * 256L + threadIdx.x;
+  if (p.ctl && p.ctl->done) return;
+  if (i >= p.n) return;
+  const R dz = p.ctl ? (R)p.ctl->dz : p.dz_fixed;
+  const int ix = (int)(i / p.ny), iy = (int)(i - (long)ix * p.ny);
+  const R g = p.g1[ix] * p.g2[iy];
+  const C e0 = in[i];
+  C k[4], acc = mk<R>(0, 0);
+  for (int s = 0; s < p.ns; ++s) {
+    C u = e0;
+    for (int l = 0; l < s; ++l) u = u + (dz * p.a[s][l]) * k[l];
+    const R f = g * (R)0.75 * (u.x * u.x + u.y * u.y);
+    k[s] = cmul(p.c0, mk<R>(f * u.x, f * u.y));
+    acc = acc + p.b[s] * k[s];
+  }
+  out[i] = e0 + dz * acc;
+}
+
+// Reductions of the XY field (FieldAnalyzers.jl:240-255): F = |E|^2 per
+// point, Imax.
+template <typename R>
+__global__ void __launch_bounds__(256) k_xy_reduce(const typename C2T<R>::type* E, double* fluence, DevCtl* ctl,
+                                                   long n, int check_done) {
+  typedef typename C2T<R>::type C;
+  __shared__ double sm[32];
+  if (check_done && ctl->done) return;
+  const long i = blockIdx.x * 256L + threadIdx.x;
+  double I = 0;
+  if (i < n) {
+    const C e = E[i];
+    I = (double)(e.x * e.x + e.y * e.y);
+    fluence[i] = I;
+  }
+  const double m = block_max<double>(I, sm);
+  if (threadIdx.x == 0) {
+    if (!isfinite(m)) atomicOr(&ctl->flags, FIL_FLAG_NAN);
+    else atomic_max_nonneg(&ctl->imax_acc, m);
+  }
+}
+
+template <typename R>
+cudaError_t launch_xy_nonlinear(const typename C2T<R>::type* in, typename C2T<R>::type* out, const XyNlParams<R>& p,
+                                cudaStream_t st) {
+  k_xy_nonlinear<R><<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(in, out, p);
+  return cudaGetLastError();
+}
+template <typename R>
+cudaError_t launch_xy_reduce(const typename C2T<R>::type* E, double* fluence, DevCtl* ctl, long n, int check_done,
+                             cudaStream_t st) {
+  k_xy_reduce<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(E, fluence, ctl, n, check_done);
+  return cudaGetLastError();
+}
+
+#define XY_INST(R)                                                                                              \
+  template cudaError_t launch_xylines<R>(const XyParams<R>&, int, int, int, int, cudaStream_t);              \
+  template cudaError_t launch_xy_nonlinear<R>(const C2T<R>::type*, C2T<R>::type*, const XyNlParams<R>&,     \
+                                              cudaStream_t);                                                 \
+  template cudaError_t launch_xy_reduce<R>(const C2T<R>::type*, double*, DevCtl*, long, int, cudaStream_t);
+XY_INST(float)
+XY_INST(double)

@@ -18,9 +18,30 @@ template <typename R> struct XyParams {
   const R* kt2_outer;     // ky^2 of the line
   const R* sg_line;       // spectral guard along the line
   const R* sg_outer;
+  const R* g_line;        // field guard along the line (mode 3)
+  const R* g_outer;
+  DevCtl* ctl;
+  R dz_fixed;
+};
+
+// XY nonlinear step parameters
+template <typename R> struct XyNlParams {
+  typedef typename C2T<R>::type C;
+  long n;                 // nx * ny
+  int ny, ns;
+  R a[4][4], b[4];        // RK tableau
+  C c0;                   // i QZ(w0) Rnl_cubic(w0)
+  const R* g1;            // field guard along x, y
+  const R* g2;
   DevCtl* ctl;
   R dz_fixed;
 };
 
 template <typename R>
 cudaError_t launch_xylines(const XyParams<R>& p, int nl, int mode, int nh, int nouter, cudaStream_t st);
+template <typename R>
+cudaError_t launch_xy_nonlinear(const typename C2T<R>::type* in, typename C2T<R>::type* out, const XyNlParams<R>& p,
+                                cudaStream_t st);
+template <typename R>
+cudaError_t launch_xy_reduce(const typename C2T<R>::type* E, double* fluence, DevCtl* ctl, long n, int check_done,
+                             cudaStream_t st);

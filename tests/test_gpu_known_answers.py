@@ -43,3 +43,15 @@ def test_dispersion_rt(gpu_lib, tmp_path, precision):
     zd = TAU0 ** 2 / K2
     Ith = TAU0 / (TAU0 * np.sqrt(1 + (z / zd) ** 2))
     assert np.max(np.abs(I - Ith)) <= 1e-3
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_diffraction_xy(gpu_lib, tmp_path, precision):
+    """test/test_diffraction_xy.jl:1-30 on the XY path (2048 x 2048)."""
+    d = _run("diffraction_XY", tmp_path, precision)
+    z, I, ax, ay = d[0], d[1], d[2] * 1e-3, d[3] * 1e-3
+    ath = A0 * np.sqrt(1 + (z / ZD) ** 2)
+    Ith = (A0 / ath) ** 2
+    assert np.max(np.abs(ax - ath)) <= 0.01e-3
+    assert np.max(np.abs(ay - ath)) <= 0.01e-3
+    assert np.max(np.abs(I - Ith)) <= 1e-3
