@@ -24,10 +24,17 @@ def xy_input(**kw):
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 @pytest.mark.parametrize("kparaxial", [False, True])
 def test_xy_linear_step(gpu_lib, precision, kparaxial):
+    """Five 10 cm steps of free diffraction.  The oracle evaluates KZ as the
+    reference writes it, sqrt(beta^2 - k^2) + (dfr - beta), which at
+    beta = 7.9e6 carries an absolute error of ~8e-10 from cancellation
+    (a numpy FFT propagation with the same formula reproduces the oracle);
+    the device uses the equal, cancellation-free dfr - k^2/(beta + sqrt(beta^2 -
+    k^2)).  Over 0.5 m that leaves ~2e-10 between the FP64 forms."""
+    tol = {"mixed": 1e-5, "fp64": 1e-9}[precision]
     g, r = pair(xy_input(KPARAXIAL=kparaxial), precision, project=False)
     assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL[precision] / 10
     step_both(g, r, 5, 0.1)
-    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL[precision]
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < tol
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
