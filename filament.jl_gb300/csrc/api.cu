@@ -84,6 +84,14 @@ struct fil_handle {
   void* kzt = nullptr; void* gdt = nullptr;    // [nh][mpad] KZ (float2), guard (float)
   int* tc_err = nullptr;
   CUtensorMap tm_a1[3], tm_a2[3], tm_b[3];
+  // learned plasma surrogate (fil_set_surrogate): the network (caller-owned)
+  // and its per-step buffers
+  const fil_nn* nn = nullptr;
+  void* nn_feat = nullptr;     // [nrows][2][nt] BF16
+  void* nn_a1 = nullptr;       // [nrows][64][nt] BF16
+  void* nn_a2 = nullptr;
+  float* nn_out = nullptr;     // [nrows][nt]
+  int* nn_slot = nullptr;      // [nrows]
 };
 
 void fil_set_global_error(const std::string& m) { g_err = m; }
@@ -519,6 +527,17 @@ template <typename R> static PropParams<R> prop_params(fil_handle* h) {
   return p;
 }
 
+// Learned plasma surrogate: the network over the rows flagged by this step's
+// reduction (a device count; nothing runs when the controller set it to 0),
+// and the row kernel's view of its output.
+template <typename R> static cudaError_t enqueue_surrogate(fil_handle* h, RowParams<R>& P) {
+  if (!h->nn) return cudaSuccess;
+  P.nn_slot = h->nn_slot;
+  P.nn_out = h->nn_out;
+  return nn_forward_rows(h->nn, h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nt, h->nrows, &h->ctl->nn_rows,
+                         &h->ctl->done, h->st);
+}
+
 // one z-step: row kernel (W1 <- S), DHT forward + propagator (W2 <- W1),
 // inverse (S <- W2)
 // XYT: row kernel (W1 <- S, row-major), fft along y, fft along x with the
@@ -529,6 +548,7 @@ template <typename R> static int enqueue_zstep_xyt(fil_handle* h, bool timed) {
   P.S_in = (const C*)h->S;
   P.S_out = (C*)h->W1;
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
+  CK(enqueue_surrogate<R>(h, P));
   CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
   if (timed) CK(cudaEventRecord(h->ev[2], h->st));
   const int nx = h->n1, ny = h->n2, nh = h->nh;
@@ -644,6 +664,7 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
     P.out_scale = nullptr;   // the scalings live in M1, M2
   }
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
+  CK(enqueue_surrogate<R>(h, P));
   CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
   if (timed) CK(cudaEventRecord(h->ev[2], h->st));
   if (tcp) {
@@ -688,6 +709,10 @@ template <typename R> static int enqueue_reduce(fil_handle* h, double* power, in
   }
   RowParams<R> P = row_params<R>(h);
   P.S_in = (const typename C2T<R>::type*)h->S;
+  if (h->nn && check_done) {   // the stepping loop: flag the rows for the surrogate
+    P.nn_feat = (__nv_bfloat16*)h->nn_feat;
+    P.nn_slot = h->nn_slot;
+  }
   R* I = power ? (R*)h->stage : nullptr;
   CK(launch_rowreduce<R>(P, h->nt, h->fluence, I, check_done, h->st));
   if (power) CK(launch_colsum<R>(I, h->pw, power, h->nrows, h->nt, h->st));
@@ -722,7 +747,8 @@ static void free_all(fil_handle* h) {
                   h->fluence, h->power, h->pw, h->rho_end, h->ctl, h->flushbuf,
                   h->qa1, h->qa2, h->BS[0], h->BS[1], h->BS[2], h->qb, h->kzt, h->gdt, h->tc_err,
                   h->kx2, h->ky2, h->sg1, h->sg2, h->twx, h->twy,
-                  h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2]};
+                  h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
+                  h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -1055,6 +1081,7 @@ int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stat
   c.nonlinearity = h->cfg.nonlinearity;
   c.clamp_last = h->clamp_last;
   c.imax_acc = 0;
+  c.nn_count = 0;
   CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
   if (h->timing) {
     // benchmark path: one step at a time, L2 flushed before each step
@@ -1177,6 +1204,57 @@ int fil_get_stats(fil_handle* h, fil_stats* st) {
   st->steps = c.steps;
   st->status = c.status;
   st->flags = c.flags | (std::min(c.newton_max, 255) << 8);
+  return FIL_OK;
+}
+
+int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
+  if (!h) return fail(h, FIL_ERR_ARG, "null handle");
+  if (nn) {
+    if (!h->cfg.plasma || h->nc < 1 || h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_R)
+      return fail(h, FIL_ERR_UNSUPPORTED, "the surrogate needs a time axis and a plasma equation");
+    if (nn_time_points(nn) != h->nt) return fail(h, FIL_ERR_ARG, "network built for another Nt");
+    if (every < 1 || !(tol > 0)) return fail(h, FIL_ERR_ARG, "every >= 1 and tol > 0 required");
+    if (!h->nn_feat) {
+      const size_t rt = (size_t)h->nrows * h->nt;
+      CK(cudaMalloc(&h->nn_feat, rt * 2 * 2));
+      CK(cudaMalloc(&h->nn_a1, rt * 64 * 2));
+      CK(cudaMalloc(&h->nn_a2, rt * 64 * 2));
+      CK(cudaMalloc((void**)&h->nn_out, rt * sizeof(float)));
+      CK(cudaMalloc((void**)&h->nn_slot, (size_t)h->nrows * sizeof(int)));
+      CK(cudaMemset(h->nn_slot, 0xff, (size_t)h->nrows * sizeof(int)));
+    }
+  }
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  DevCtl c = *h->ctl_host;
+  c.nn_on = nn ? 1 : 0;
+  c.nn_use = 1;
+  c.nn_judge = 0;
+  c.nn_every = nn ? every : 1;
+  c.nn_tol = nn ? tol : 0;
+  c.nn_count = c.nn_rows = 0;
+  c.nn_steps = c.nn_used = c.nn_judged = c.nn_rejected = 0;
+  c.nn_diff_acc = 0;
+  c.nn_err = c.nn_err_max = c.nn_rows_sum = 0;
+  CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->nn = nn;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return FIL_OK;
+}
+
+int fil_get_surrogate_stats(fil_handle* h, double* out, int n) {
+  if (!h || !out) return fail(h, FIL_ERR_ARG, "null argument");
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  const DevCtl& c = *h->ctl_host;
+  const double v[9] = {(double)c.nn_on, (double)c.nn_use, (double)c.nn_steps, (double)c.nn_used,
+                       (double)c.nn_judged, (double)c.nn_rejected, c.nn_err, c.nn_err_max,
+                       c.nn_used ? c.nn_rows_sum / (double)c.nn_used : 0.0};
+  for (int i = 0; i < n; ++i) out[i] = i < 9 ? v[i] : 0.0;
   return FIL_OK;
 }
 

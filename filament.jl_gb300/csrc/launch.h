@@ -39,3 +39,12 @@ cudaError_t launch_slice_prop(const float* W, const float2* kz, const float* gd,
 cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
 cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);
+
+// learned plasma surrogate (surrogate.cu): the network over the rows below
+// *count (device value) of x0 [rows][2][T] (BF16) into out [rows][T];
+// a1, a2: BF16 scratch [rows][64][T]; `stop` non-zero skips the launches
+struct fil_nn;
+int nn_time_points(const fil_nn* n);
+cudaError_t nn_forward_rows(const fil_nn* n, const void* x0, void* a1, void* a2, float* out, int T, int maxrows,
+                            const int* count, const int* stop, cudaStream_t st);
+

@@ -227,6 +227,47 @@ template <typename R> FIL_DEV R rate_eval(const PlasmaParams<R>& P, const Plasma
   return exp(T.ly[c][i] + (l - T.lx[c][i]) * T.sl[c][i]);
 }
 
+// W_c(I) in FP64 from the FP64 tables of the parameter block (one
+// evaluation per row: the activity test of the surrogate).
+template <typename R> FIL_DEV double rate_direct(const PlasmaParams<R>& P, int c, double I) {
+  if (!(I > 0)) return 0;
+  if (P.ipow[c] > 0) {
+    double b = I * (double)P.wscale[c], r = 1;
+    for (int m = P.ipow[c]; m; m >>= 1) {
+      if (m & 1) r *= b;
+      b *= b;
+    }
+    return r;
+  }
+  const double l = log(I);
+  int i = 0;
+  if (!P.powerlaw) {
+    int lo = 0, hi = P.rate_n - 2;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (P.lx[c][mid] <= l) lo = mid; else hi = mid - 1;
+    }
+    i = lo;
+  }
+  return exp(P.ly[c][i] + (l - P.lx[c][i]) * P.sl[c][i]);
+}
+
+// The negligible-row test of the plasma solve (plasma_row) from the row's
+// largest intensity and E^2 (the rates grow with I, so max W = W(max I)).
+template <typename R> FIL_DEV bool plasma_row_negligible(const PlasmaParams<R>& P, double imax, double e2max,
+                                                         double window, double rho_prev) {
+  double wmax = 0;
+  for (int c = 0; c < P.nc; ++c) wmax = fmax(wmax, rate_direct<R>(P, c, imax));
+  bool skip = wmax * window < (double)P.skip;
+  if (!skip && (double)P.skip_rel > 0 && rho_prev > 0) {
+    const double g = (double)P.rava_sum * e2max * window;
+    if (g < 40)
+      skip = (wmax * window * (double)P.rhont_sum + P.nc * (double)P.rho0 * g) * exp(g) <
+             (double)P.skip_rel * rho_prev;
+  }
+  return skip;
+}
+
 // One RK step u -> Phi(u) of the full (aval = true) or photoionisation-only
 // equation, linearised at u: returns the affine map (L, B) with
 // Phi(v) ~= (I - L) v + B exact for the affine case.

@@ -33,6 +33,31 @@ __global__ void k_control(DevCtl* c, const double* __restrict__ fluence, const d
     if (c->phip > 0 && rhomax > 0) dz = fmin(dz, c->phimax / (c->phip * rhomax));
   }
   if (c->clamp_last && c->z + dz > c->zmax) dz = c->zmax - c->z;
+  if (c->nn_on) {
+    // the step just taken was a judge step: every row ran the ODE, rhomax is
+    // its maximum
+    if (c->nn_judge) {
+      const double diff = __longlong_as_double((long long)c->nn_diff_acc);
+      const double err = rhomax > 0 ? diff / rhomax : (diff > 0 ? 1.0 : 0.0);
+      c->nn_err = err;
+      c->nn_err_max = fmax(c->nn_err_max, err);
+      c->nn_judged += 1;
+      c->nn_use = err <= c->nn_tol;
+      if (!c->nn_use) c->nn_rejected += 1;
+      c->nn_diff_acc = 0;
+    }
+    c->nn_judge = (c->nn_steps % c->nn_every) == 0;
+    c->nn_rows = (c->nn_use || c->nn_judge) ? c->nn_count : 0;
+    if (c->nn_use && !c->nn_judge) {
+      c->nn_used += 1;
+      c->nn_rows_sum += c->nn_rows;
+    }
+    c->nn_steps += 1;
+  } else {
+    c->nn_judge = 0;
+    c->nn_rows = 0;
+  }
+  c->nn_count = 0;
   c->z += dz;
   c->dz = dz;
   c->steps += 1;
@@ -44,6 +69,9 @@ __global__ void k_control(DevCtl* c, const double* __restrict__ fluence, const d
 // fil_step: latch the plasma maximum of the previous solve, set z and dz.
 __global__ void k_setdz(DevCtl* c, double z, double dz) {
   c->done = 0;
+  c->nn_judge = 0;   // single steps solve the plasma equation
+  c->nn_rows = 0;
+  c->nn_count = 0;
   c->rhomax = __longlong_as_double((long long)c->rhomax_acc);
   c->rhomax_acc = 0;
   c->z = z;

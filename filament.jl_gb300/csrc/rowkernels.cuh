@@ -8,6 +8,7 @@
 // k.  The time-domain field E(t) = guard * fft(S, zero-padded) exists only in
 // shared memory.
 #pragma once
+#include <cuda_bf16.h>
 #include "common.cuh"
 #include "fft.cuh"
 #include "plasma.cuh"
@@ -21,6 +22,18 @@ struct DevCtl {
   unsigned long long imax_acc, rhomax_acc;  // bit patterns of non-negative doubles
   double imax, rhomax, energy;
   double dz0, phimax, phik, phip, istop;
+  // learned plasma surrogate (surrogate.cuh).  Armed (nn_on) it supplies the
+  // density of the rows the reduction flags; every nn_every-th step is a
+  // judge step on which the ODE solves every row and the largest
+  // |rho_net - rho_ode| / max rho_ode is measured.  The network is used on
+  // the following steps only while that error is at most nn_tol (nn_use).
+  int nn_on, nn_use, nn_judge, nn_every;
+  int nn_count;               // rows flagged by this step's reduction (atomic)
+  int nn_rows;                // rows the network runs on in this step
+  long long nn_steps, nn_used, nn_judged, nn_rejected;
+  unsigned long long nn_diff_acc;   // judge step: max |rho_net - rho_ode| (bits)
+  double nn_tol, nn_err, nn_err_max;
+  double nn_rows_sum;         // sum of nn_rows over the steps that used the network
 };
 
 #define FIL_FLAG_NAN 1
@@ -61,6 +74,12 @@ template <typename R> struct RowParams {
   const R* out_scale;           // s_row (out_T), or NULL
   int ldT;
   DevCtl* ctl;
+  // learned plasma surrogate: network inputs of the flagged rows
+  // [slot][2][N] (BF16), slot of each row (-1: not flagged), network output
+  // d(t) = ln w - ln W(I) [slot][N]
+  __nv_bfloat16* nn_feat;
+  int* nn_slot;
+  const float* nn_out;
 };
 
 template <typename R> FIL_DEV R row_guard(const RowParams<R>& P, int row, int* iy) {
@@ -406,6 +425,79 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 }
 
 // ---------------------------------------------------------------------------
+// Density of the row in X from the surrogate output d[j] (surrogate.cuh):
+// effective rate w_j = Wb(I_j) e^{d_j} with the base rate
+// Wb = sum_c W_c rho_nt,c / rho_nt (exact, pointwise), cumulative sum
+// S_j = dt sum_{i<j} w_i (block scan), rho_j = rho_a + (rho_nt - rho_a)(1 - e^{-S_j})
+// with rho_a = nc rho0 the initial density, and the loss term
+// Kdrho_j = sum_c K_c W_c(I_j) (rho_nt,c - rho_{j+1} rho_nt,c / rho_nt), 0 at the
+// last point (the photoionisation-only density of plasma_equations.jl:63-70
+// approximated by rho).  Thread t owns j = 16t .. 16t+15 as in plasma_row.
+// judge: compare with the density in rho[] instead of writing it; returns
+// max |difference|.  Otherwise writes rho[], kdrho[] and returns max rho.
+template <typename R, int N, int NC>
+FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typename C2T<R>::type* X,
+                     const float* __restrict__ d, R* rho, R* kdrho, Aff<R, 1>* ascratch, R* rscratch, bool judge) {
+  typedef typename C2T<R>::type C;
+  const PlasmaParams<R>& pp = P.pp;
+  const int j0 = threadIdx.x * 16;
+  const R rnt = pp.rhont_sum, ra = (R)NC * pp.rho0, dt = pp.dt;
+  R wl[16];
+  R tsum = 0;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int j = j0 + q;
+    const C e = X[pad16(j)];
+    const R I = pp.ereal ? e.x * e.x : e.x * e.x + e.y * e.y;
+    R wb = 0;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      R sl;
+      wb += rate_eval<R>(pp, tabs, c, I, &sl) * pp.rho_nt[c];
+    }
+    wb = wb / rnt;
+    const R w = (j < N - 1 && wb > (R)0) ? wb * exp((R)__ldg(&d[j])) * dt : (R)0;
+    wl[q] = w;
+    tsum += w;
+  }
+  Aff<R, 1> G;
+  G.L[0][0] = 0;
+  G.B[0] = tsum;
+  const Aff<R, 1> Pin = aff_block_exclusive_scan<R, 1>(G, ascratch);
+  R S = Pin.B[0];
+  R out = 0;
+  R rcur = ra + (rnt - ra) * -expm1(-S);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int j = j0 + q;
+    S += wl[q];
+    const R rnext = ra + (rnt - ra) * -expm1(-S);
+    if (judge) {
+      out = max(out, fabs(rcur - rho[pad16(j)]));
+    } else {
+      rho[pad16(j)] = rcur;
+      R kd = 0;
+      if (j < N - 1) {
+        const C e = X[pad16(j)];
+        const R I = pp.ereal ? e.x * e.x : e.x * e.x + e.y * e.y;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          R sl;
+          const R W = rate_eval<R>(pp, tabs, c, I, &sl);
+          const R K = pp.kdep ? sl : (R)pp.kfix[c];
+          kd += K * W * (pp.rho_nt[c] - rnext * pp.rho_nt[c] / rnt);
+        }
+      }
+      kdrho[pad16(j)] = kd;
+      out = max(out, rcur);
+    }
+    rcur = rnext;
+  }
+  __syncthreads();
+  return block_max<R>(out, rscratch);
+}
+
+// ---------------------------------------------------------------------------
 // Fused z-step of one row (blockIdx.x = row):
 //   E(t) = guard * fft(S_in)   (guard from the previous step, Models.jl:116-118)
 //   plasma solve on E(t)       (Models.jl:84-89)
@@ -451,11 +543,29 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   }
   load_time_row<R, N>(P, X, row, guard);
 
-  // ---- plasma
+  // ---- plasma: the ODE solve, or the surrogate's density for the rows the
+  // reduction flagged.  On a judge step every row is solved and the flagged
+  // rows also measure the surrogate against the solution.
   if constexpr (NC > 0) {
     if (P.plasma) {
-      R rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag,
+      const int slot = (P.nn_out && mode == 0) ? P.nn_slot[row] : -1;
+      const bool nn_row = slot >= 0 && slot < ctl->nn_rows;
+      const bool judge = P.nn_out && mode == 0 && ctl->nn_judge;
+      Aff<R, 1>* sc1 = reinterpret_cast<Aff<R, 1>*>(ascratch);
+      R rmax;
+      if (nn_row && !judge) {
+        rmax = nn_density<R, N, NC>(P, *tabs, X, P.nn_out + (size_t)slot * N, rho, kdrho, sc1, rscratch, false);
+      } else {
+        rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag,
                                     mode == 0 ? (R)ctl->rhomax : (R)0, dz, &ych);
+        if (judge) {
+          // rows not flagged carry rho0 in the surrogate form
+          const R diff = nn_row ? nn_density<R, N, NC>(P, *tabs, X, P.nn_out + (size_t)slot * N, rho, kdrho, sc1,
+                                                       rscratch, true)
+                                : max(rmax - (R)NC * P.pp.rho0, (R)0);
+          if (tid == 0) atomic_max_nonneg(&ctl->nn_diff_acc, (double)diff);
+        }
+      }
       if (tid == 0) {
         atomic_max_nonneg(&ctl->rhomax_acc, (double)rmax);
         P.rho_end[row] = (double)rho[pad16(N - 1)];
@@ -607,13 +717,13 @@ __global__ void __launch_bounds__(N / 16) k_rowreduce(RowParams<R> P, double* fl
   constexpr int T = N / 16, NP = N + N / 16, NW = T / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* X = reinterpret_cast<C*>(smem_raw);
-  R* rs = reinterpret_cast<R*>(X + NP);   // [2 * NW]
+  R* rs = reinterpret_cast<R*>(X + NP);   // [3 * NW]
   DevCtl* ctl = P.ctl;
   if (check_done && ctl->done) return;
   const int row = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   load_time_row<R, N>(P, X, row, ctl->guard_pending != 0);
   R s[4] = {0, 0, 0, 0};
-  R mx = 0;
+  R mx = 0, mr = 0;
 #pragma unroll
   for (int m = 0; m < 16; ++m) {
     int j = tid + m * T;
@@ -621,25 +731,58 @@ __global__ void __launch_bounds__(N / 16) k_rowreduce(RowParams<R> P, double* fl
     R I = e.x * e.x + e.y * e.y;
     s[m & 3] += I;
     mx = max(mx, I);
+    mr = max(mr, e.x * e.x);
     if (Iout) Iout[(size_t)row * N + j] = I;
   }
   R ts = warp_sum<R>((s[0] + s[1]) + (s[2] + s[3]));
   R tm = warp_max<R>(mx);
+  R tr = warp_max<R>(mr);
   if (lane == 0) {
     rs[w] = ts;
     rs[NW + w] = tm;
+    rs[2 * NW + w] = tr;
   }
   __syncthreads();
+  __shared__ int s_slot;
   if (tid == 0) {
-    double tot = 0, bm = 0;
+    double tot = 0, bm = 0, br = 0;
 #pragma unroll
     for (int i = 0; i < NW; ++i) {
       tot += (double)rs[i];
       bm = fmax(bm, (double)rs[NW + i]);
+      br = fmax(br, (double)rs[2 * NW + i]);
     }
     fluence[row] = tot * (double)P.dt;
     if (!isfinite(tot)) atomicOr(&ctl->flags, FIL_FLAG_NAN);
     else atomic_max_nonneg(&ctl->imax_acc, bm);
+    // learned surrogate: the coming step needs the network (it is in use,
+    // or the step is a judge step) and the plasma solve would not skip the
+    // row -> take a slot for its features
+    int slot = -1;
+    if (P.nn_feat && ctl->nn_on && (ctl->nn_use || ctl->nn_steps % ctl->nn_every == 0) && isfinite(tot)) {
+      const double rho_prev = __longlong_as_double((long long)ctl->rhomax_acc);
+      const double imax = P.pp.ereal ? br : bm;
+      if (!plasma_row_negligible<R>(P.pp, imax, br, (double)P.pp.dt * (N - 1), rho_prev))
+        slot = atomicAdd(&ctl->nn_count, 1);
+    }
+    if (P.nn_slot) P.nn_slot[row] = slot;
+    s_slot = slot;
+  }
+  if (P.nn_feat) {
+    __syncthreads();
+    const int slot = s_slot;
+    if (slot >= 0) {
+      // f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30)
+      __nv_bfloat16* f = P.nn_feat + (size_t)slot * 2 * N;
+#pragma unroll 4
+      for (int m = 0; m < 16; ++m) {
+        int j = tid + m * T;
+        C e = X[pad16(j)];
+        const float I = fmaxf((float)(e.x * e.x + e.y * e.y), 1e-30f);
+        f[j] = __float2bfloat16_rn(__logf(I) * 0.0625f);
+        f[N + j] = __float2bfloat16_rn((float)(e.x * e.x) / I);
+      }
+    }
   }
 }
 

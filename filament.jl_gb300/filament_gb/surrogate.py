@@ -1,0 +1,240 @@
+"""Host wrapper of the learned plasma surrogate (fil_nn_* of
+include/filament_gb.h): a 1-D convolutional network trained on the GPU by
+the library's own forward and backward kernels.
+
+The reference has no counterpart: it integrates the plasma rate equation
+for every transverse point (src/modules/plasma_equations.jl:46-72,
+src/modules/Models.jl:205-219).  The surrogate learns, per time row, the
+log of the effective ionisation rate w(t) from the intensity and the carrier
+phase; the density then follows in closed form,
+rho(t) = rho0 + (rho_nt - rho0) (1 - exp(-dt sum_{t'<t} w(t'))).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .backend import load_library
+
+_fp = C.POINTER(C.c_float)
+_bound = set()
+
+
+def _bind(b):
+    if id(b) in _bound:
+        return b.lib
+    L, vp = b.lib, C.c_void_p
+    for name, res, args in (
+            ("fil_nn_nparams", C.c_int, []),
+            ("fil_nn_last_error", C.c_char_p, [vp]),
+            ("fil_nn_create", C.c_int, [C.c_int, C.c_uint64, C.POINTER(vp)]),
+            ("fil_nn_destroy", C.c_int, [vp]),
+            ("fil_nn_get_params", C.c_int, [vp, _fp]),
+            ("fil_nn_set_params", C.c_int, [vp, _fp]),
+            ("fil_nn_forward", C.c_int, [vp, _fp, C.c_int, _fp]),
+            ("fil_nn_grad", C.c_int, [vp, _fp, _fp, _fp, C.c_int, _fp, _fp]),
+            ("fil_nn_train", C.c_int, [vp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_float,
+                                       C.c_uint64, _fp]),
+            ("fil_set_surrogate", C.c_int, [vp, vp, C.c_int, C.c_double]),
+            ("fil_get_surrogate_stats", C.c_int, [vp, C.POINTER(C.c_double), C.c_int])):
+        f = getattr(L, name)
+        f.restype, f.argtypes = res, args
+    _bound.add(id(b))
+    return L
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def _p(a):
+    return a.ctypes.data_as(_fp)
+
+
+def features(E, I=None):
+    """Network inputs of time rows E[..., nt] (complex field in units where
+    |E|^2 = I): f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30).
+    Returns float32 [rows][2][nt]."""
+    E = np.asarray(E)
+    E = E.reshape(-1, E.shape[-1])
+    I = np.abs(E) ** 2 if I is None else np.asarray(I).reshape(E.shape)
+    Ic = np.maximum(I, 1e-30)
+    return np.stack([np.log(Ic) / 16.0, E.real ** 2 / Ic], axis=1).astype(np.float32)
+
+
+def base_rate(pe, I):
+    """Wb(I) = sum_c W_c(I) rho_nt,c / rho_nt, the instantaneous rate the
+    network's output multiplies (log-log interpolation of the rate tables,
+    W(I <= 0) = 0), vectorised over I."""
+    I = np.asarray(I, dtype=np.float64)
+    pos = I > 0
+    lI = np.log(np.where(pos, I, 1.0))
+    out = np.zeros_like(I)
+    for tf, rn in zip(pe.tfs, pe.rho_nt):
+        i = np.clip(np.searchsorted(tf.lx, lI, side="right") - 1, 0, len(tf.lx) - 2)
+        sl = (tf.ly[i + 1] - tf.ly[i]) / (tf.lx[i + 1] - tf.lx[i])
+        out += np.where(pos, np.exp(tf.ly[i] + (lI - tf.lx[i]) * sl), 0.0) * rn
+    return out / float(np.sum(pe.rho_nt))
+
+
+def training_pairs(E, rho, pe, dt, row_frac=1e-9, min_frac=1e-6, tail_weight=1e-2):
+    """Network inputs, targets and loss weights from time rows of the field
+    E [rows][nt] (complex analytic signal) and the density rho [rows][nt]
+    that the plasma equation gives on them.
+
+    The effective rate of step j is w_j = -ln(1 - (rho_{j+1} - rho_j) / (rho_nt - rho_j)) / dt
+    (the closed form rho_{j+1} = rho_nt - (rho_nt - rho_j) e^{-w_j dt} then
+    reproduces the solve exactly), the target d_j = ln(w_j / Wb(I_j)).
+    Points whose density increment is at least `min_frac` of the row's
+    largest weigh 1; the other points with Wb > 0 weigh `tail_weight` with
+    target 0 (their rate does not move the density).  Rows whose density
+    rise is below `row_frac` of the largest rise are dropped."""
+    E = np.atleast_2d(np.asarray(E))
+    rho = np.atleast_2d(np.asarray(rho, dtype=np.float64))
+    rnt = float(np.sum(pe.rho_nt))
+    rise = rho[:, -1] - rho[:, 0]
+    keep = rise > row_frac * max(float(rise.max()), 0.0)
+    if not keep.any():
+        nt = E.shape[1]
+        return (np.zeros((0, 2, nt), np.float32), np.zeros((0, nt), np.float32), np.zeros((0, nt), np.float32))
+    E, rho = E[keep], rho[keep]
+    I = E.real ** 2 if pe.EREAL else np.abs(E) ** 2
+    drho = np.diff(rho, axis=1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        w = -np.log1p(-drho / (rnt - rho[:, :-1])) / dt
+        Wb = base_rate(pe, I[:, :-1])
+        good = (drho > min_frac * drho.max(axis=1, keepdims=True)) & (Wb > 0) & (w > 0)
+        d = np.where(good, np.log(np.where(good, w, 1.0) / np.where(good, Wb, 1.0)), 0.0)
+    tgt = np.zeros(rho.shape, np.float32)
+    mask = np.zeros(rho.shape, np.float32)
+    tgt[:, :-1] = d
+    mask[:, :-1] = np.where(good, 1.0, np.where(Wb > 0, tail_weight, 0.0))
+    return features(E), tgt, mask
+
+
+def solver_pairs(inp, snapshots, steps_between, precision="mixed", **kw):
+    """Training data from the plain solver: propagates `inp` with the device
+    loop (`precision` form) and at `snapshots` states, `steps_between`
+    steps apart (the first is the initial field), solves the plasma equation
+    of the current field in an FP64 handle.  Returns training_pairs(...)."""
+    from . import _abi
+    from .filament import Simulation
+    sim = Simulation(inp, precision=precision)
+    ref = Simulation(inp, precision="fp64")
+    ref.handle.set_option(_abi.OPT_STORE_PLASMA, 1)
+    pe, dt = sim.problem.pe, float(sim.grid.dt)
+    F, T, M = [], [], []
+    z = sim.z
+    try:
+        for k in range(snapshots):
+            if k:
+                _, st = sim.handle.run(z, sim.zmax, steps_between)
+                z = st["z"]
+                if z >= sim.zmax:
+                    break
+            E = sim.handle.get_field()
+            ref.handle.set_field(E, analytic=True)
+            f, t, m = training_pairs(E, ref.handle.get_plasma(0), pe, dt, **kw)
+            F.append(f)
+            T.append(t)
+            M.append(m)
+    finally:
+        sim.close()
+        ref.close()
+    return np.concatenate(F), np.concatenate(T), np.concatenate(M)
+
+
+class Surrogate:
+    """One network on the current device.  Parameters are FP32 masters;
+    the kernels compute with their BF16 copies."""
+
+    def __init__(self, nt, seed=1, binding=None):
+        self.b = binding if binding is not None else load_library()
+        self.L = _bind(self.b)
+        self.nt = int(nt)
+        self.h = C.c_void_p()
+        self._chk(self.L.fil_nn_create(self.nt, int(seed), C.byref(self.h)), "create", None)
+
+    @property
+    def nparams(self):
+        return self.L.fil_nn_nparams()
+
+    def _chk(self, code, what, h="self"):
+        if code < 0:
+            msg = self.L.fil_nn_last_error(self.h if h == "self" else None)
+            raise _abi.FilError(code, "fil_nn_%s failed: %s" % (what, msg.decode() if msg else "?"))
+        return code
+
+    def close(self):
+        if self.h:
+            self.L.fil_nn_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self):
+        out = np.empty(self.nparams, dtype=np.float32)
+        self._chk(self.L.fil_nn_get_params(self.h, _p(out)), "get_params")
+        return out
+
+    def set_params(self, p):
+        p = _f32(p, (self.nparams,))
+        self._chk(self.L.fil_nn_set_params(self.h, _p(p)), "set_params")
+
+    def forward(self, feat):
+        feat = _f32(feat, (-1, 2, self.nt))
+        out = np.empty((feat.shape[0], self.nt), dtype=np.float32)
+        self._chk(self.L.fil_nn_forward(self.h, _p(feat), feat.shape[0], _p(out)), "forward")
+        return out
+
+    def grad(self, feat, target, mask):
+        feat = _f32(feat, (-1, 2, self.nt))
+        rows = feat.shape[0]
+        target, mask = _f32(target, (rows, self.nt)), _f32(mask, (rows, self.nt))
+        g = np.empty(self.nparams, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        self._chk(self.L.fil_nn_grad(self.h, _p(feat), _p(target), _p(mask), rows, _p(g), _p(loss)), "grad")
+        return float(loss[0]), g
+
+    def train(self, feat, target, mask, iters, batch=64, lr=1e-3, seed=1):
+        """Adam on the device; returns the per-iteration batch losses."""
+        feat = _f32(feat, (-1, 2, self.nt))
+        rows = feat.shape[0]
+        target, mask = _f32(target, (rows, self.nt)), _f32(mask, (rows, self.nt))
+        hist = np.zeros(max(int(iters), 1), dtype=np.float32)
+        self._chk(self.L.fil_nn_train(self.h, _p(feat), _p(target), _p(mask), rows, int(batch), int(iters),
+                                      float(lr), int(seed), _p(hist)), "train")
+        return hist[:int(iters)]
+
+    def arm(self, handle, every=20, tol=1e-3):
+        """Use the network for the plasma density of `handle` (a backend
+        Handle) inside its device loop, judged every `every` steps."""
+        L = _bind(handle.b)
+        handle.b.check(handle.h, L.fil_set_surrogate(handle.h, self.h, int(every), float(tol)), "set_surrogate")
+        handle._surrogate = self
+
+
+def disarm(handle):
+    L = _bind(handle.b)
+    handle.b.check(handle.h, L.fil_set_surrogate(handle.h, None, 1, 1.0), "set_surrogate")
+    handle._surrogate = None
+
+
+STAT_KEYS = ("armed", "in_use", "steps", "steps_used", "checks", "checks_failed", "err_last", "err_max",
+             "rows_mean")
+
+
+def stats(handle):
+    """Surrogate counters of a handle (fil_get_surrogate_stats)."""
+    L = _bind(handle.b)
+    out = np.zeros(len(STAT_KEYS))
+    code = L.fil_get_surrogate_stats(handle.h, out.ctypes.data_as(C.POINTER(C.c_double)), len(out))
+    handle.b.check(handle.h, code, "get_surrogate_stats")
+    return dict(zip(STAT_KEYS, out.tolist()))

@@ -277,6 +277,45 @@ int fil_hankel_propagate_noalloc(const float* m1, const float* m2, const float* 
                                  const float* wg, int kparaxial, const float* in, float* out,
                                  int mpad, int nh, double dz, void* stream);
 
+/* ---- learned plasma surrogate (no counterpart in the reference, which
+ * always solves the plasma ODE, plasma_equations.jl:46-72).  A 1-D
+ * convolutional network (2 -> 64 -> 64 -> 64 -> 1 channels, kernel 9, tanh,
+ * BF16 weights and activations, FP32 accumulation) maps the features of one
+ * time row, f0 = ln(max(I, 1e-30)) / 16 and f1 = Re(E)^2 / max(I, 1e-30), to
+ * ln w(t), the log of the effective ionisation rate; the density is then
+ * rho(t) = rho0 + (rho_nt - rho0)(1 - exp(-dt sum_{t'<t} w(t'))).
+ * Feature arrays are [rows][2][nt], targets and masks [rows][nt] (FP32,
+ * host memory).                                                             */
+typedef struct fil_nn fil_nn;
+int fil_nn_nparams(void);
+const char* fil_nn_last_error(const fil_nn* n);
+int fil_nn_create(int nt, uint64_t seed, fil_nn** out);
+int fil_nn_destroy(fil_nn* n);
+int fil_nn_get_params(fil_nn* n, float* params);        /* fil_nn_nparams() FP32 */
+int fil_nn_set_params(fil_nn* n, const float* params);
+int fil_nn_forward(fil_nn* n, const float* feat, int rows, float* out);   /* out [rows][nt] */
+/* loss = sum mask (out - target)^2 / sum mask and its gradient */
+int fil_nn_grad(fil_nn* n, const float* feat, const float* target, const float* mask, int rows,
+                float* grad, float* loss);
+/* Adam training, `iters` batches of `batch` rows drawn with `seed`;
+ * loss_hist[iters] (may be NULL) receives the batch losses             */
+int fil_nn_train(fil_nn* n, const float* feat, const float* target, const float* mask, int rows,
+                 int batch, int iters, float lr, uint64_t seed, float* loss_hist);
+
+/* Arm the surrogate on a handle (T, RT or XYT geometry with a plasma
+ * equation; the network's nt must match): inside fil_run the density of
+ * every row whose plasma solve would not be skipped comes from the network.
+ * Every `every`-th step the ODE solves all rows and the largest
+ * |rho_net - rho_ode| / max rho_ode is measured; the network is used on the
+ * following steps only while that error is at most `tol` (the ODE takes
+ * over otherwise, until a later check passes).  fil_step always solves the
+ * ODE.  nn = NULL disarms.  The network must stay alive while armed.       */
+int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol);
+/* out[0..n): armed, in use, steps since armed, steps that used the network,
+ * checks, failed checks, last error, largest error, mean rows per step
+ * that used the network                                                    */
+int fil_get_surrogate_stats(fil_handle* h, double* out, int n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,93 @@
+"""Host side of the learned plasma surrogate (no GPU): the CPU reference of
+the network checked by finite differences, and the training targets, which
+must reproduce the plasma solve exactly through the closed form the row
+kernel uses."""
+import numpy as np
+import pytest
+
+
+def test_reference_gradient_matches_finite_differences(monkeypatch):
+    """The CPU reference's backward pass, with the BF16 rounding switched
+    off so that the loss is smooth, against central differences."""
+    import surrogate_ref as sr
+    monkeypatch.setattr(sr, "bf16", lambda x: np.asarray(x, dtype=np.float64))
+    rng = np.random.default_rng(3)
+    p = rng.uniform(-0.3, 0.3, sr.nparams())
+    f = rng.standard_normal((2, 2, 40))
+    t = rng.standard_normal((2, 40))
+    m = (rng.random((2, 40)) > 0.3).astype(float)
+    _, g = sr.grad(p, f, t, m)
+    offs = np.cumsum([0] + [co * ci * sr.K + co for ci, co in zip(sr.CI, sr.CO)])
+    # a weight and a bias of every layer
+    idx = [int(offs[l]) + 7 for l in range(4)] + [int(offs[l + 1]) - 1 for l in range(4)]
+    for i in idx:
+        eps = 1e-6
+        pp, pm = p.copy(), p.copy()
+        pp[i] += eps
+        pm[i] -= eps
+        fd = (sr.grad(pp, f, t, m)[0] - sr.grad(pm, f, t, m)[0]) / (2 * eps)
+        assert g[i] == pytest.approx(fd, rel=1e-6, abs=1e-9)
+
+
+def test_reference_bf16_rounding():
+    import surrogate_ref as sr
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, 1.0 + 2 ** -9, -2.5e-3], dtype=np.float32)
+    r = sr.bf16(x)
+    # ties to even: 1 + 2^-8 is a tie between 1 and 1 + 2^-7 -> 1
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0 + 2 ** -6 and r[3] == 1.0
+    assert abs(r[4] - (-2.5e-3)) <= 2.5e-3 * 2 ** -8
+
+
+class _PE:
+    """Plasma equation stand-in: one species, power law W = (I/I1)^8."""
+
+    def __init__(self):
+        from filament_gb.plasma import TFunction
+        I = np.logspace(-6, 2, 9)
+        self.tfs = [TFunction(I, (I / 0.5) ** 8)]
+        self.rho_nt = np.array([2.0])
+        self.EREAL = False
+
+
+def test_training_targets_reconstruct_the_density():
+    """rho from a sequential solve with a rate that is not the
+    instantaneous one (a midpoint rule plus a density feedback) gives
+    targets d; rho_nt - (rho_nt - rho0) exp(-dt sum Wb e^d) gives rho back."""
+    from filament_gb import surrogate as S
+    pe = _PE()
+    nt, dt = 256, 0.05
+    t = (np.arange(nt) - nt / 2) * dt
+    rows = []
+    rhos = []
+    for a in (0.6, 0.8, 1.0):
+        E = np.sqrt(a * np.exp(-(t / 2.0) ** 2)) * np.exp(1j * 3.0 * t)
+        I = np.abs(E) ** 2
+        W = S.base_rate(pe, I)
+        rho = np.zeros(nt)
+        for j in range(nt - 1):
+            w = 0.5 * (W[j] + W[j + 1]) * (1 + 0.3 * rho[j])
+            rho[j + 1] = 2.0 - (2.0 - rho[j]) * np.exp(-w * dt)
+        rows.append(E)
+        rhos.append(rho)
+    E, rho = np.array(rows), np.array(rhos)
+    f, d, m = S.training_pairs(E, rho, pe, dt, min_frac=0.0, tail_weight=0.0)
+    assert f.shape == (3, 2, nt) and d.shape == (3, nt)
+    assert np.allclose(f[:, 1], (E.real ** 2 / np.maximum(np.abs(E) ** 2, 1e-30)), atol=1e-6)
+    Wb = S.base_rate(pe, np.abs(E) ** 2)
+    w = np.where(m > 0, Wb * np.exp(d.astype(np.float64)), 0.0)
+    # float32 targets: the reconstruction holds to their rounding
+    S_ = np.concatenate([np.zeros((3, 1)), np.cumsum(w[:, :-1] * dt, axis=1)], axis=1)
+    rec = 2.0 - 2.0 * np.exp(-S_)
+    assert np.max(np.abs(rec - rho)) <= 1e-6 * np.max(rho)
+
+
+def test_training_rows_below_the_threshold_are_dropped():
+    from filament_gb import surrogate as S
+    pe = _PE()
+    nt = 64
+    E = np.ones((2, nt), complex)
+    rho = np.zeros((2, nt))
+    rho[0] = np.linspace(0, 1e-3, nt)
+    rho[1] = np.linspace(0, 1e-15, nt)
+    f, d, m = S.training_pairs(E, rho, pe, 0.1)
+    assert f.shape[0] == 1
