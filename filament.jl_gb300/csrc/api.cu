@@ -87,7 +87,7 @@ struct fil_handle {
   // learned plasma surrogate (fil_set_surrogate): the network (caller-owned)
   // and its per-step buffers
   const fil_nn* nn = nullptr;
-  void* nn_feat = nullptr;     // [nrows][2][nt] BF16
+  void* nn_feat = nullptr;     // [nrows][3][nt] BF16
   void* nn_a1 = nullptr;       // [nrows][64][nt] BF16
   void* nn_a2 = nullptr;
   float* nn_out = nullptr;     // [nrows][nt]
@@ -1216,7 +1216,7 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
     if (every < 1 || !(tol > 0)) return fail(h, FIL_ERR_ARG, "every >= 1 and tol > 0 required");
     if (!h->nn_feat) {
       const size_t rt = (size_t)h->nrows * h->nt;
-      CK(cudaMalloc(&h->nn_feat, rt * 2 * 2));
+      CK(cudaMalloc(&h->nn_feat, rt * 3 * 2));
       CK(cudaMalloc(&h->nn_a1, rt * 64 * 2));
       CK(cudaMalloc(&h->nn_a2, rt * 64 * 2));
       CK(cudaMalloc((void**)&h->nn_out, rt * sizeof(float)));

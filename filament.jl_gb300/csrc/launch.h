@@ -41,7 +41,7 @@ cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);
 
 // learned plasma surrogate (surrogate.cu): the network over the rows below
-// *count (device value) of x0 [rows][2][T] (BF16) into out [rows][T];
+// *count (device value) of x0 [rows][3][T] (BF16) into out [rows][T];
 // a1, a2: BF16 scratch [rows][64][T]; `stop` non-zero skips the launches
 struct fil_nn;
 int nn_time_points(const fil_nn* n);

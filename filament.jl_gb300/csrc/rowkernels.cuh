@@ -426,8 +426,11 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 
 // ---------------------------------------------------------------------------
 // Density of the row in X from the surrogate output d[j] (surrogate.cuh):
-// effective rate w_j = Wb(I_j) e^{d_j} with the base rate
-// Wb = sum_c W_c rho_nt,c / rho_nt (exact, pointwise), cumulative sum
+// effective rate w_j = Wb_j e^{d_j} over the step t_j -> t_{j+1}, with the
+// base rate Wb_j = sum_s b_s W(I at the stage point of s) -- the quadrature
+// of the time integrator of plasma_equations.jl:46-72 (stage points t_j,
+// the midpoint of the linearly interpolated field, t_{j+1}) applied to
+// W = sum_c W_c rho_nt,c / rho_nt, exact and pointwise; cumulative sum
 // S_j = dt sum_{i<j} w_i (block scan), rho_j = rho_a + (rho_nt - rho_a)(1 - e^{-S_j})
 // with rho_a = nc rho0 the initial density, and the loss term
 // Kdrho_j = sum_c K_c W_c(I_j) (rho_nt,c - rho_{j+1} rho_nt,c / rho_nt), 0 at the
@@ -442,21 +445,33 @@ FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
   const PlasmaParams<R>& pp = P.pp;
   const int j0 = threadIdx.x * 16;
   const R rnt = pp.rhont_sum, ra = (R)NC * pp.rho0, dt = pp.dt;
-  R wl[16];
-  R tsum = 0;
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const int j = j0 + q;
-    const C e = X[pad16(j)];
+  // quadrature weights of the stage points t_j, t_j + dt/2, t_{j+1}
+  R qw[3] = {0, 0, 0};
+  for (int st = 0; st < pp.ns; ++st) qw[pp.pidx[st]] += pp.b[st];
+  auto wsum = [&](C e) -> R {
     const R I = pp.ereal ? e.x * e.x : e.x * e.x + e.y * e.y;
-    R wb = 0;
+    R w = 0;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       R sl;
-      wb += rate_eval<R>(pp, tabs, c, I, &sl) * pp.rho_nt[c];
+      w += rate_eval<R>(pp, tabs, c, I, &sl) * pp.rho_nt[c];
     }
-    wb = wb / rnt;
-    const R w = (j < N - 1 && wb > (R)0) ? wb * exp((R)__ldg(&d[j])) * dt : (R)0;
+    return w;
+  };
+  R wl[16];
+  R tsum = 0;
+  R wcur = wsum(X[pad16(j0)]);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int j = j0 + q;
+    R w = 0;
+    if (j < N - 1) {
+      const C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
+      const R wnext = wsum(e1);
+      const R wb = (qw[0] * wcur + qw[1] * wsum((R)0.5 * (e0 + e1)) + qw[2] * wnext) / rnt;
+      if (wb > (R)0) w = wb * exp((R)__ldg(&d[j])) * dt;
+      wcur = wnext;
+    }
     wl[q] = w;
     tsum += w;
   }
@@ -704,6 +719,71 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
 }
 
 // ---------------------------------------------------------------------------
+// Inputs of the learned surrogate for the row in X (surrogate.cuh):
+// f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30) and
+// f2 = ln(max(S_j, 1e-30)) / 16 with S_j = dt sum_{i<j} Wb_i, Wb_i the base rate
+// of step i (the integrator's quadrature of W = sum_c W_c rho_nt,c / rho_nt
+// over t_i, the midpoint of the interpolated field and t_{i+1}, as in
+// nn_density).  Thread t owns j = 16t .. 16t+15; f is [3][N] (BF16).
+template <typename R, int N>
+FIL_DEV void nn_features(const RowParams<R>& P, const typename C2T<R>::type* X, __nv_bfloat16* f) {
+  typedef typename C2T<R>::type C;
+  __shared__ PlasmaSmem<R> tabs;
+  __shared__ Aff<R, 1> sc[32];
+  const PlasmaParams<R>& pp = P.pp;
+  for (int i = threadIdx.x; i < FIL_MAXCOMP * FIL_MAXRATE; i += blockDim.x) {
+    const int c = i / FIL_MAXRATE, q = i % FIL_MAXRATE;
+    tabs.lx[c][q] = (R)pp.lx[c][q];
+    tabs.ly[c][q] = (R)pp.ly[c][q];
+    tabs.sl[c][q] = (R)pp.sl[c][q];
+  }
+  __syncthreads();
+  R qw[3] = {0, 0, 0};
+  for (int st = 0; st < pp.ns; ++st) qw[pp.pidx[st]] += pp.b[st];
+  auto wsum = [&](C e) -> R {
+    const R I = pp.ereal ? e.x * e.x : e.x * e.x + e.y * e.y;
+    R w = 0;
+    for (int c = 0; c < pp.nc; ++c) {
+      R sl;
+      w += rate_eval<R>(pp, tabs, c, I, &sl) * pp.rho_nt[c];
+    }
+    return w;
+  };
+  const int j0 = threadIdx.x * 16;
+  const R scale = pp.dt / pp.rhont_sum;
+  R wl[16];
+  R tsum = 0;
+  R wcur = wsum(X[pad16(j0)]);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int j = j0 + q;
+    R w = 0;
+    if (j < N - 1) {
+      const C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
+      const R wnext = wsum(e1);
+      w = (qw[0] * wcur + qw[1] * wsum((R)0.5 * (e0 + e1)) + qw[2] * wnext) * scale;
+      wcur = wnext;
+    }
+    wl[q] = w;
+    tsum += w;
+  }
+  Aff<R, 1> G;
+  G.L[0][0] = 0;
+  G.B[0] = tsum;
+  R S = aff_block_exclusive_scan<R, 1>(G, sc).B[0];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int j = j0 + q;
+    const C e = X[pad16(j)];
+    const float I = fmaxf((float)(e.x * e.x + e.y * e.y), 1e-30f);
+    f[j] = __float2bfloat16_rn(__logf(I) * 0.0625f);
+    f[N + j] = __float2bfloat16_rn((float)(e.x * e.x) / I);
+    f[2 * N + j] = __float2bfloat16_rn(__logf(fmaxf((float)S, 1e-30f)) * 0.0625f);
+    S += wl[q];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Reductions over the current field (FieldAnalyzers.jl:166-215): Imax,
 // fluence per row F = sum_t |E|^2 dt, optionally |E|^2 itself into
 // Iout[row][t] (for the power P[t] = sum_row w_row |E|^2, k_colsum).  Flags
@@ -771,18 +851,7 @@ __global__ void __launch_bounds__(N / 16) k_rowreduce(RowParams<R> P, double* fl
   if (P.nn_feat) {
     __syncthreads();
     const int slot = s_slot;
-    if (slot >= 0) {
-      // f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30)
-      __nv_bfloat16* f = P.nn_feat + (size_t)slot * 2 * N;
-#pragma unroll 4
-      for (int m = 0; m < 16; ++m) {
-        int j = tid + m * T;
-        C e = X[pad16(j)];
-        const float I = fmaxf((float)(e.x * e.x + e.y * e.y), 1e-30f);
-        f[j] = __float2bfloat16_rn(__logf(I) * 0.0625f);
-        f[N + j] = __float2bfloat16_rn((float)(e.x * e.x) / I);
-      }
-    }
+    if (slot >= 0) nn_features<R, N>(P, X, P.nn_feat + (size_t)slot * 3 * N);
   }
 }
 

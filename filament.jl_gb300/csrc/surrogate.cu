@@ -69,10 +69,10 @@ static int nn_pack(fil_nn* n) {
 __global__ void k_nn_gather(const float* __restrict__ f, const int* __restrict__ idx, __nv_bfloat16* x0, int B,
                             int T) {
   const long i = blockIdx.x * 256L + threadIdx.x;
-  if (i >= (long)B * 2 * T) return;
-  const int b = (int)(i / (2L * T));
+  if (i >= (long)B * NN_IN * T) return;
+  const int b = (int)(i / ((long)NN_IN * T));
   const long r = idx ? idx[b] : b;
-  x0[i] = __float2bfloat16_rn(f[r * 2L * T + (i - (long)b * 2 * T)]);
+  x0[i] = __float2bfloat16_rn(f[r * NN_IN * (long)T + (i - (long)b * NN_IN * T)]);
 }
 __global__ void k_nn_gather_t(const float* __restrict__ t, const float* __restrict__ m, const int* __restrict__ idx,
                               float* to, float* mo, int B, int T) {
@@ -94,7 +94,7 @@ int nn_forward_dev(const fil_nn* n, const __nv_bfloat16* x0, __nv_bfloat16* a1, 
   const int gy64 = count ? std::max(1, std::min(B, (152 * 8 + gx64 - 1) / gx64)) : B;
   const int gy1 = count ? std::max(1, std::min(B, (152 * 16 + gx1 - 1) / gx1)) : B;
   dim3 g64(gx64, gy64), g1(gx1, gy1);
-  k_nn_conv<2, 64, 32, 8, 1><<<g64, 256, 0, st>>>(x0, n->wf[0], n->p + nn_poff(0) + nn_wsize(0), a1, T, B, count,
+  k_nn_conv<NN_IN, 64, 32, 8, 1><<<g64, 256, 0, st>>>(x0, n->wf[0], n->p + nn_poff(0) + nn_wsize(0), a1, T, B, count,
                                                   stop);
   k_nn_conv<64, 64, 32, 8, 1><<<g64, 256, 0, st>>>(a1, n->wf[1], n->p + nn_poff(1) + nn_wsize(1), a2, T, B, count,
                                                    stop);
@@ -146,7 +146,7 @@ static int nn_backward(fil_nn* n, int B, float inv_count) {
     d = dn;
   }
   // layer 0 (2 -> 64)
-  k_nn_wgrad<2, 64, 8><<<dim3(8, 2), 256, 0, n->st>>>(n->act[0], d, n->g + nn_poff(0), n->g + nn_poff(0) + nn_wsize(0),
+  k_nn_wgrad<NN_IN, 64, 8><<<dim3(8, NN_IN), 256, 0, n->st>>>(n->act[0], d, n->g + nn_poff(0), n->g + nn_poff(0) + nn_wsize(0),
                                                       B, T);
   NK(cudaGetLastError());
   return 0;
@@ -177,7 +177,7 @@ static int nn_reserve(fil_nn* n, int b) {
   if (n->tgt) cudaFree(n->tgt);
   if (n->mask) cudaFree(n->mask);
   const size_t bt = (size_t)b * n->T;
-  NK(cudaMalloc(&n->act[0], bt * 2 * sizeof(__nv_bfloat16)));
+  NK(cudaMalloc(&n->act[0], bt * NN_IN * sizeof(__nv_bfloat16)));
   for (int l = 1; l < NN_LAYERS; ++l) NK(cudaMalloc(&n->act[l], bt * NN_CH * sizeof(__nv_bfloat16)));
   NK(cudaMalloc(&n->out, bt * sizeof(float)));
   for (int i = 0; i < 2; ++i) NK(cudaMalloc(&n->gr[i], bt * NN_CH * sizeof(float)));
@@ -275,9 +275,9 @@ int fil_nn_forward(fil_nn* n, const float* feat, int b, float* out) {
   if (rc) return rc;
   const size_t bt = (size_t)b * n->T;
   float* df = nullptr;
-  NK(cudaMallocAsync((void**)&df, bt * 2 * sizeof(float), n->st));
-  NK(cudaMemcpyAsync(df, feat, bt * 2 * sizeof(float), cudaMemcpyHostToDevice, n->st));
-  k_nn_gather<<<(unsigned)((bt * 2 + 255) / 256), 256, 0, n->st>>>(df, nullptr, n->act[0], b, n->T);
+  NK(cudaMallocAsync((void**)&df, bt * NN_IN * sizeof(float), n->st));
+  NK(cudaMemcpyAsync(df, feat, bt * NN_IN * sizeof(float), cudaMemcpyHostToDevice, n->st));
+  k_nn_gather<<<(unsigned)((bt * NN_IN + 255) / 256), 256, 0, n->st>>>(df, nullptr, n->act[0], b, n->T);
   rc = nn_forward(n, b);
   if (rc) return rc;
   NK(cudaMemcpyAsync(out, n->out, bt * sizeof(float), cudaMemcpyDeviceToHost, n->st));
@@ -292,11 +292,11 @@ int fil_nn_grad(fil_nn* n, const float* feat, const float* tgt, const float* mas
   if (rc) return rc;
   const size_t bt = (size_t)b * n->T;
   float* df = nullptr;
-  NK(cudaMallocAsync((void**)&df, bt * 2 * sizeof(float), n->st));
-  NK(cudaMemcpyAsync(df, feat, bt * 2 * sizeof(float), cudaMemcpyHostToDevice, n->st));
+  NK(cudaMallocAsync((void**)&df, bt * NN_IN * sizeof(float), n->st));
+  NK(cudaMemcpyAsync(df, feat, bt * NN_IN * sizeof(float), cudaMemcpyHostToDevice, n->st));
   NK(cudaMemcpyAsync(n->tgt, tgt, bt * sizeof(float), cudaMemcpyHostToDevice, n->st));
   NK(cudaMemcpyAsync(n->mask, mask, bt * sizeof(float), cudaMemcpyHostToDevice, n->st));
-  k_nn_gather<<<(unsigned)((bt * 2 + 255) / 256), 256, 0, n->st>>>(df, nullptr, n->act[0], b, n->T);
+  k_nn_gather<<<(unsigned)((bt * NN_IN + 255) / 256), 256, 0, n->st>>>(df, nullptr, n->act[0], b, n->T);
   double cnt = 0;
   for (size_t i = 0; i < bt; ++i) cnt += mask[i];
   rc = nn_forward(n, b);
@@ -309,7 +309,7 @@ int fil_nn_grad(fil_nn* n, const float* feat, const float* tgt, const float* mas
   return FIL_OK;
 }
 
-// Adam training on a data set of `rows` rows (features [rows][2][T], targets
+// Adam training on a data set of `rows` rows (features [rows][3][T], targets
 // and masks [rows][T], host arrays), `iters` iterations of `batch` rows
 // drawn with a seeded generator; loss_hist[iters] receives the batch losses.
 int fil_nn_train(fil_nn* n, const float* feat, const float* tgt, const float* mask, int rows, int batch, int iters,
@@ -319,10 +319,10 @@ int fil_nn_train(fil_nn* n, const float* feat, const float* tgt, const float* ma
   if (rc) return rc;
   const size_t T = n->T;
   if (n->data_f) { cudaFree(n->data_f); cudaFree(n->data_t); cudaFree(n->data_m); }
-  NK(cudaMalloc(&n->data_f, rows * 2 * T * sizeof(float)));
+  NK(cudaMalloc(&n->data_f, rows * NN_IN * T * sizeof(float)));
   NK(cudaMalloc(&n->data_t, rows * T * sizeof(float)));
   NK(cudaMalloc(&n->data_m, rows * T * sizeof(float)));
-  NK(cudaMemcpyAsync(n->data_f, feat, rows * 2 * T * sizeof(float), cudaMemcpyHostToDevice, n->st));
+  NK(cudaMemcpyAsync(n->data_f, feat, rows * NN_IN * T * sizeof(float), cudaMemcpyHostToDevice, n->st));
   NK(cudaMemcpyAsync(n->data_t, tgt, rows * T * sizeof(float), cudaMemcpyHostToDevice, n->st));
   NK(cudaMemcpyAsync(n->data_m, mask, rows * T * sizeof(float), cudaMemcpyHostToDevice, n->st));
   std::vector<double> rowcnt(rows, 0.0);
@@ -350,7 +350,7 @@ int fil_nn_train(fil_nn* n, const float* feat, const float* tgt, const float* ma
   NK(cudaMalloc(&dloss, (size_t)iters * sizeof(float) + sizeof(float)));
   for (int it = 0; it < iters; ++it) {
     const int* bi = didx + (size_t)it * batch;
-    k_nn_gather<<<(unsigned)((bt * 2 + 255) / 256), 256, 0, n->st>>>(n->data_f, bi, n->act[0], batch, (int)T);
+    k_nn_gather<<<(unsigned)((bt * NN_IN + 255) / 256), 256, 0, n->st>>>(n->data_f, bi, n->act[0], batch, (int)T);
     k_nn_gather_t<<<(unsigned)((bt + 255) / 256), 256, 0, n->st>>>(n->data_t, n->data_m, bi, n->tgt, n->mask, batch,
                                                                    (int)T);
     rc = nn_forward(n, batch);

@@ -1,16 +1,21 @@
 // surrogate.cuh -- the learned plasma surrogate: a 4-layer 1-D convolutional
-// network (2 -> 64 -> 64 -> 64 -> 1 channels, kernel 9, "same" padding, tanh
+// network (3 -> 64 -> 64 -> 64 -> 1 channels, kernel 9, "same" padding, tanh
 // after the first three layers) evaluated on the time row of one transverse
-// point.  Its output is the log-ratio d(t) = ln w(t) - ln W(I(t)) of the
-// effective ionisation rate w to the instantaneous rate W of the medium
-// (evaluated exactly), and the density follows in closed form,
-//   rho(t) = rho0 + (rho_nt - rho0) (1 - exp(-dt sum_{t' < t} W(I(t')) e^{d(t')})),
+// point.  Its output is the log-ratio d_j = ln w_j - ln Wb_j of the
+// effective ionisation rate w of the step t_j -> t_{j+1} to the base rate Wb,
+// the medium's rate averaged with the time integrator's quadrature over the
+// stage points of the step (evaluated exactly), and the density follows in
+// closed form,
+//   rho_j = rho0 + (rho_nt - rho0) (1 - exp(-dt sum_{i < j} Wb_i e^{d_i})),
 // which replaces the ODE solve of plasma_equations.jl:46-72 (exact for
-// photoionisation with any time-dependent rate; d carries the discretisation
-// of the time integrator and the avalanche term).
+// photoionisation with any time-dependent rate; d carries the higher orders
+// of the integrator in W dt and the avalanche term).
 //
 // Inputs per time point: f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30)
-// (the carrier phase, which drives the avalanche term).  Weights and hidden
+// (the carrier phase, which drives the avalanche term) and
+// f2 = ln(max(S_j, 1e-30)) / 16 with S_j = dt sum_{i<j} Wb_i, the ionised fraction
+// of the base rate alone (the density history the avalanche term grows
+// from, beyond the network's 33-point receptive field).  Weights and hidden
 // activations are stored in BF16, every product is accumulated in FP32 and
 // the output layer is written in FP32; training keeps FP32 master weights
 // (Adam).
@@ -18,13 +23,14 @@
 #include <cuda_bf16.h>
 #include "common.cuh"
 
+#define NN_IN 3
 #define NN_CH 64
 #define NN_K 9
 #define NN_HALF 4
 #define NN_LAYERS 4
 
 // layer l: ci_l -> co_l
-__host__ __device__ constexpr int nn_ci(int l) { return l == 0 ? 2 : NN_CH; }
+__host__ __device__ constexpr int nn_ci(int l) { return l == 0 ? NN_IN : NN_CH; }
 __host__ __device__ constexpr int nn_co(int l) { return l == 3 ? 1 : NN_CH; }
 // FP32 parameter offsets: weights [co][ci][k] then bias [co], layer by layer
 __host__ __device__ constexpr int nn_wsize(int l) { return nn_co(l) * nn_ci(l) * NN_K; }
@@ -155,16 +161,16 @@ __global__ void k_nn_tanh_bwd(const float* __restrict__ d, const __nv_bfloat16* 
   }
 }
 
-// loss = sum mask (out - tgt)^2 / sum mask; g = d loss / d out
+// loss = sum m (out - tgt)^2 / sum m (m: the point weights); g = d loss / d out
 __global__ void k_nn_loss(const float* __restrict__ out, const float* __restrict__ tgt,
                           const float* __restrict__ mask, float* g, float* acc, long n, float inv_count) {
   __shared__ float sm[32];
   const long i = blockIdx.x * 256L + threadIdx.x;
   float l = 0.f;
   if (i < n) {
-    const float d = (out[i] - tgt[i]) * mask[i];
-    g[i] = 2.f * d * inv_count;
-    l = d * d * inv_count;
+    const float e = out[i] - tgt[i], me = mask[i] * e;
+    g[i] = 2.f * me * inv_count;
+    l = me * e * inv_count;
   }
   l = block_sum<float>(l, sm);
   if (threadIdx.x == 0) atomicAdd(acc, l);

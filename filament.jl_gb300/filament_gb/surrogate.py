@@ -54,15 +54,18 @@ def _p(a):
     return a.ctypes.data_as(_fp)
 
 
-def features(E, I=None):
-    """Network inputs of time rows E[..., nt] (complex field in units where
-    |E|^2 = I): f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30).
-    Returns float32 [rows][2][nt]."""
-    E = np.asarray(E)
-    E = E.reshape(-1, E.shape[-1])
-    I = np.abs(E) ** 2 if I is None else np.asarray(I).reshape(E.shape)
+def features(E, pe, dt):
+    """Network inputs of time rows E [rows][nt] (complex analytic field,
+    |E|^2 = I): f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30),
+    f2 = ln(max(S_j, 1e-30)) / 16 with S_j = dt sum_{i<j} Wb_i the ionised
+    fraction of the base rate (quad_rate).  Returns float32 [rows][3][nt]."""
+    E = np.atleast_2d(np.asarray(E))
+    I = np.abs(E) ** 2
     Ic = np.maximum(I, 1e-30)
-    return np.stack([np.log(Ic) / 16.0, E.real ** 2 / Ic], axis=1).astype(np.float32)
+    S = np.zeros(E.shape)
+    S[:, 1:] = np.cumsum(quad_rate(pe, E) * dt, axis=1)
+    return np.stack([np.log(Ic) / 16.0, E.real ** 2 / Ic, np.log(np.maximum(S, 1e-30)) / 16.0],
+                    axis=1).astype(np.float32)
 
 
 def base_rate(pe, I):
@@ -80,70 +83,118 @@ def base_rate(pe, I):
     return out / float(np.sum(pe.rho_nt))
 
 
-def training_pairs(E, rho, pe, dt, row_frac=1e-9, min_frac=1e-6, tail_weight=1e-2):
+# weights of the stage points (t_j, midpoint, t_{j+1}) in the RK tableaus of
+# the plasma equation's time integrator (plasma_equations.jl:46-72)
+QUADRATURE = {"RK2": (0.0, 1.0, 0.0), "RK3": (1 / 6, 4 / 6, 1 / 6), "RK4": (1 / 6, 4 / 6, 1 / 6)}
+
+
+def quad_rate(pe, E):
+    """Base rate of every step t_j -> t_{j+1} of the time rows E [rows][nt]:
+    Wb_j = sum_p q_p Wb(I_p) over the stage points of the integrator (the
+    field linearly interpolated at the midpoint, as the ODE solve does).
+    Returns [rows][nt - 1]."""
+    E = np.atleast_2d(np.asarray(E))
+    q0, qm, q1 = QUADRATURE[pe.alg]
+
+    def inten(e):
+        return e.real ** 2 if pe.EREAL else np.abs(e) ** 2
+
+    e0, e1 = E[:, :-1], E[:, 1:]
+    return (q0 * base_rate(pe, inten(e0)) + qm * base_rate(pe, inten(0.5 * (e0 + e1)))
+            + q1 * base_rate(pe, inten(e1)))
+
+
+def closed_form_density(E, d, pe, dt):
+    """The density the row kernel forms from the network output d [rows][nt]
+    (FP64): rho_j = rho_a + (rho_nt - rho_a)(1 - exp(-dt sum_{i<j} Wb_i e^{d_i}))."""
+    E = np.atleast_2d(np.asarray(E))
+    w = quad_rate(pe, E) * np.exp(np.asarray(d, dtype=np.float64)[:, :-1])
+    S = np.concatenate([np.zeros((E.shape[0], 1)), np.cumsum(w * dt, axis=1)], axis=1)
+    ra = len(pe.rho_nt) * float(pe.rho0)
+    rnt = float(np.sum(pe.rho_nt))
+    return ra + (rnt - ra) * -np.expm1(-S)
+
+
+def training_pairs(E, rho, pe, dt, row_frac=1e-9, resolve=1e-9, floor=1e-3):
     """Network inputs, targets and loss weights from time rows of the field
     E [rows][nt] (complex analytic signal) and the density rho [rows][nt]
     that the plasma equation gives on them.
 
     The effective rate of step j is w_j = -ln(1 - (rho_{j+1} - rho_j) / (rho_nt - rho_j)) / dt
     (the closed form rho_{j+1} = rho_nt - (rho_nt - rho_j) e^{-w_j dt} then
-    reproduces the solve exactly), the target d_j = ln(w_j / Wb(I_j)).
-    Points whose density increment is at least `min_frac` of the row's
-    largest weigh 1; the other points with Wb > 0 weigh `tail_weight` with
-    target 0 (their rate does not move the density).  Rows whose density
-    rise is below `row_frac` of the largest rise are dropped."""
+    reproduces the solve exactly), the target d_j = ln(w_j / Wb_j) with the
+    base rate of quad_rate.  An error e in d_j moves the final density by
+    about (rho_{j+1} - rho_j) e, so a point weighs its density increment
+    relative to the row's largest, at least `floor`; points whose increment
+    is below `resolve` times the density (not resolved by the solve) or
+    with Wb = 0 weigh 0.  Rows whose density rise is below `row_frac` of the
+    largest rise are dropped."""
     E = np.atleast_2d(np.asarray(E))
     rho = np.atleast_2d(np.asarray(rho, dtype=np.float64))
+    nt = E.shape[1]
     rnt = float(np.sum(pe.rho_nt))
     rise = rho[:, -1] - rho[:, 0]
     keep = rise > row_frac * max(float(rise.max()), 0.0)
     if not keep.any():
-        nt = E.shape[1]
-        return (np.zeros((0, 2, nt), np.float32), np.zeros((0, nt), np.float32), np.zeros((0, nt), np.float32))
+        return (np.zeros((0, 3, nt), np.float32), np.zeros((0, nt), np.float32), np.zeros((0, nt), np.float32))
     E, rho = E[keep], rho[keep]
-    I = E.real ** 2 if pe.EREAL else np.abs(E) ** 2
     drho = np.diff(rho, axis=1)
     with np.errstate(divide="ignore", invalid="ignore"):
         w = -np.log1p(-drho / (rnt - rho[:, :-1])) / dt
-        Wb = base_rate(pe, I[:, :-1])
-        good = (drho > min_frac * drho.max(axis=1, keepdims=True)) & (Wb > 0) & (w > 0)
+        Wb = quad_rate(pe, E)
+        good = (drho > resolve * np.abs(rho[:, 1:])) & (Wb > 0) & (w > 0)
         d = np.where(good, np.log(np.where(good, w, 1.0) / np.where(good, Wb, 1.0)), 0.0)
+    rel = drho / np.maximum(drho.max(axis=1, keepdims=True), 1e-300)
     tgt = np.zeros(rho.shape, np.float32)
     mask = np.zeros(rho.shape, np.float32)
     tgt[:, :-1] = d
-    mask[:, :-1] = np.where(good, 1.0, np.where(Wb > 0, tail_weight, 0.0))
-    return features(E), tgt, mask
+    mask[:, :-1] = np.where(good, np.maximum(rel, floor), 0.0)
+    return features(E, pe, dt), tgt, mask
 
 
-def solver_pairs(inp, snapshots, steps_between, precision="mixed", **kw):
-    """Training data from the plain solver: propagates `inp` with the device
-    loop (`precision` form) and at `snapshots` states, `steps_between`
-    steps apart (the first is the initial field), solves the plasma equation
-    of the current field in an FP64 handle.  Returns training_pairs(...)."""
+def solver_states(inp, snapshots, steps_between, precision="mixed", skip_steps=0):
+    """States of the plain solver with their plasma density: propagates
+    `inp` with the device loop (`precision` form), skips `skip_steps` steps,
+    then at `snapshots` states `steps_between` steps apart solves the plasma
+    equation of the current field in an FP64 handle.  Yields
+    (z, E [rows][nt], rho [rows][nt]); stops early at zmax."""
     from . import _abi
     from .filament import Simulation
     sim = Simulation(inp, precision=precision)
     ref = Simulation(inp, precision="fp64")
     ref.handle.set_option(_abi.OPT_STORE_PLASMA, 1)
-    pe, dt = sim.problem.pe, float(sim.grid.dt)
-    F, T, M = [], [], []
     z = sim.z
     try:
+        if skip_steps:
+            _, st = sim.handle.run(z, sim.zmax, skip_steps)
+            z = st["z"]
         for k in range(snapshots):
             if k:
                 _, st = sim.handle.run(z, sim.zmax, steps_between)
                 z = st["z"]
-                if z >= sim.zmax:
-                    break
+            if z >= sim.zmax:
+                break
             E = sim.handle.get_field()
             ref.handle.set_field(E, analytic=True)
-            f, t, m = training_pairs(E, ref.handle.get_plasma(0), pe, dt, **kw)
-            F.append(f)
-            T.append(t)
-            M.append(m)
+            yield z, E, ref.handle.get_plasma(0)
     finally:
         sim.close()
         ref.close()
+
+
+def solver_pairs(inp, snapshots, steps_between, precision="mixed", skip_steps=0, **kw):
+    """Training data from the plain solver: training_pairs of every state
+    of solver_states(...), concatenated."""
+    from .filament import Simulation
+    probe = Simulation(inp, precision=precision)
+    pe, dt = probe.problem.pe, float(probe.grid.dt)
+    probe.close()
+    F, T, M = [], [], []
+    for _, E, rho in solver_states(inp, snapshots, steps_between, precision, skip_steps):
+        f, t, m = training_pairs(E, rho, pe, dt, **kw)
+        F.append(f)
+        T.append(t)
+        M.append(m)
     return np.concatenate(F), np.concatenate(T), np.concatenate(M)
 
 
@@ -189,13 +240,13 @@ class Surrogate:
         self._chk(self.L.fil_nn_set_params(self.h, _p(p)), "set_params")
 
     def forward(self, feat):
-        feat = _f32(feat, (-1, 2, self.nt))
+        feat = _f32(feat, (-1, 3, self.nt))
         out = np.empty((feat.shape[0], self.nt), dtype=np.float32)
         self._chk(self.L.fil_nn_forward(self.h, _p(feat), feat.shape[0], _p(out)), "forward")
         return out
 
     def grad(self, feat, target, mask):
-        feat = _f32(feat, (-1, 2, self.nt))
+        feat = _f32(feat, (-1, 3, self.nt))
         rows = feat.shape[0]
         target, mask = _f32(target, (rows, self.nt)), _f32(mask, (rows, self.nt))
         g = np.empty(self.nparams, dtype=np.float32)
@@ -205,7 +256,7 @@ class Surrogate:
 
     def train(self, feat, target, mask, iters, batch=64, lr=1e-3, seed=1):
         """Adam on the device; returns the per-iteration batch losses."""
-        feat = _f32(feat, (-1, 2, self.nt))
+        feat = _f32(feat, (-1, 3, self.nt))
         rows = feat.shape[0]
         target, mask = _f32(target, (rows, self.nt)), _f32(mask, (rows, self.nt))
         hist = np.zeros(max(int(iters), 1), dtype=np.float32)

@@ -279,12 +279,16 @@ int fil_hankel_propagate_noalloc(const float* m1, const float* m2, const float* 
 
 /* ---- learned plasma surrogate (no counterpart in the reference, which
  * always solves the plasma ODE, plasma_equations.jl:46-72).  A 1-D
- * convolutional network (2 -> 64 -> 64 -> 64 -> 1 channels, kernel 9, tanh,
- * BF16 weights and activations, FP32 accumulation) maps the features of one
- * time row, f0 = ln(max(I, 1e-30)) / 16 and f1 = Re(E)^2 / max(I, 1e-30), to
- * ln w(t), the log of the effective ionisation rate; the density is then
- * rho(t) = rho0 + (rho_nt - rho0)(1 - exp(-dt sum_{t'<t} w(t'))).
- * Feature arrays are [rows][2][nt], targets and masks [rows][nt] (FP32,
+ * convolutional network (3 -> 64 -> 64 -> 64 -> 1 channels, kernel 9, tanh,
+ * BF16 weights and activations, FP32 accumulation and output) maps three
+ * inputs of every point of a time row,
+ *   f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30),
+ *   f2 = ln(max(S_j, 1e-30)) / 16, S_j = dt sum_{i<j} Wb_i,
+ * to d_j = ln(w_j / Wb_j), the log-ratio of the effective ionisation rate of
+ * the step t_j -> t_{j+1} to the base rate Wb_j (the medium's rate averaged
+ * with the time integrator's quadrature over the step); the density is then
+ * rho_j = rho0 + (rho_nt - rho0)(1 - exp(-dt sum_{i<j} Wb_i e^{d_i})).
+ * Feature arrays are [rows][3][nt], targets and masks [rows][nt] (FP32,
  * host memory).                                                             */
 typedef struct fil_nn fil_nn;
 int fil_nn_nparams(void);

@@ -5,13 +5,13 @@ hidden activations rounded to BF16 (round to nearest even), the output
 layer left unrounded, products accumulated in FP64 here (FP32 on the
 device), tanh after layers 0-2, "same" padding.
 
-Layer l maps ci_l -> co_l channels: 2 -> 64 -> 64 -> 64 -> 1, kernel 9.
+Layer l maps ci_l -> co_l channels: 3 -> 64 -> 64 -> 64 -> 1, kernel 9.
 Parameters (FP32, the layout of fil_nn_get_params): per layer the weights
 [co][ci][k] followed by the bias [co]."""
 import numpy as np
 
 CH, K, HALF = 64, 9, 4
-CI = [2, CH, CH, CH]
+CI = [3, CH, CH, CH]
 CO = [CH, CH, CH, 1]
 
 
@@ -71,14 +71,15 @@ def forward(p, feat):
 
 
 def grad(p, feat, tgt, mask):
-    """(loss, gradient of the FP32 parameters) of the masked squared error."""
+    """(loss, gradient of the FP32 parameters) of the weighted squared
+    error sum m (out - tgt)^2 / sum m."""
     layers = unpack(p)
     acts = forward(p, feat)
     out = acts[-1][:, 0, :]
     cnt = mask.sum()
-    d = (out - tgt) * mask
-    loss = float((d * d).sum() / cnt)
-    g = (2.0 * d / cnt)[:, None, :]
+    e = out - tgt
+    loss = float((mask * e * e).sum() / cnt)
+    g = (2.0 * mask * e / cnt)[:, None, :]
     grads = [None] * 4
     for l in range(3, -1, -1):
         w, _ = layers[l]

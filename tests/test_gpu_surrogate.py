@@ -1,7 +1,8 @@
 """The learned plasma surrogate on the GPU: forward and backward kernels
 against the CPU reference (oracle/surrogate_ref.py), training on data the
-plain solver generates, and the armed device loop -- its checks against
-the ODE, the fallback, and what it gains or loses against the plain form."""
+plain solver generates, what the trained network gains over the closed form
+without it, and the armed device loop -- its checks against the ODE, the
+fallback, and its cost against the plain form."""
 import time
 
 import numpy as np
@@ -13,9 +14,10 @@ pytestmark = pytest.mark.gpu
 
 
 def _random_rows(rng, b, T):
-    f = np.empty((b, 2, T), np.float32)
+    f = np.empty((b, 3, T), np.float32)
     f[:, 0] = rng.uniform(-3.0, 0.2, (b, T))
     f[:, 1] = rng.uniform(0.0, 1.0, (b, T))
+    f[:, 2] = rng.uniform(-4.3, -0.5, (b, T))
     return f
 
 
@@ -47,9 +49,9 @@ def test_gradient_matches_reference(gpu_lib):
     net.set_params(p)
     f = _random_rows(rng, 4, T)
     tgt = rng.standard_normal((4, T)).astype(np.float32) * 0.1
-    mask = (rng.random((4, T)) > 0.25).astype(np.float32)
-    loss, g = net.grad(f, tgt, mask)
-    lref, gref = sr.grad(p.astype(np.float64), f, tgt, mask)
+    w = (rng.random((4, T)) * (rng.random((4, T)) > 0.25)).astype(np.float32)
+    loss, g = net.grad(f, tgt, w)
+    lref, gref = sr.grad(p.astype(np.float64), f, tgt, w)
     assert loss == pytest.approx(lref, rel=1e-3)
     assert rel_l2(g, gref) < 5e-3
     # per layer, so that a small block is not hidden by a large one
@@ -68,34 +70,78 @@ def test_set_params_round_trip(gpu_lib):
     assert np.array_equal(net.get_params(), p)
 
 
-@pytest.fixture(scope="module")
-def solver_data(gpu_lib):
-    """(I, rho) pairs of the plain solver on the RT deck (64 x 512, RK3):
-    the initial field and 7 further states 4 steps apart."""
-    from filament_gb.surrogate import solver_pairs
-    return solver_pairs(rt_input(zmax=1.0), snapshots=8, steps_between=4)
+TRAIN_SCALES = (1.5, 2.0, 3.0, 3.5, 4.0)
+HELD_OUT_SCALE = 2.5
 
 
 @pytest.fixture(scope="module")
-def trained(solver_data):
+def data(gpu_lib):
+    """Training pairs of the plain solver on the RT deck (64 x 512, RK3,
+    3 Pcr): 8 states of the propagation 4 steps apart, and the initial
+    field scaled by TRAIN_SCALES (denser plasma), the plasma equation solved
+    in FP64.  Also the held-out scaled field with its density."""
+    import filament_gb as fg
+    from filament_gb import _abi
+    from filament_gb import surrogate as S
+    inp = rt_input(zmax=1.0)
+    f0, t0, m0 = S.solver_pairs(inp, snapshots=8, steps_between=4)
+    F, T, M = [f0], [t0], [m0]
+    ref = fg.Simulation(inp, precision="fp64")
+    ref.handle.set_option(_abi.OPT_STORE_PLASMA, 1)
+    pe, dt = ref.problem.pe, float(ref.grid.dt)
+    held = None
+    for sc in TRAIN_SCALES + (HELD_OUT_SCALE,):
+        ref.handle.set_field(ref.field.E0 * sc, analytic=False)
+        E, rho = ref.handle.get_field(), ref.handle.get_plasma(0)
+        if sc == HELD_OUT_SCALE:
+            held = (E, rho)
+            continue
+        f, t, m = S.training_pairs(E, rho, pe, dt)
+        F.append(f)
+        T.append(t)
+        M.append(m)
+    ref.close()
+    return np.concatenate(F), np.concatenate(T), np.concatenate(M), held, pe, dt
+
+
+@pytest.fixture(scope="module")
+def trained(data):
     from filament_gb.surrogate import Surrogate
-    f, t, m = solver_data
+    f, t, m = data[:3]
     net = Surrogate(f.shape[-1], seed=5)
-    hist = net.train(f, t, m, iters=600, batch=16, lr=2e-3, seed=9)
-    return net, hist
+    loss0, _ = net.grad(f, t, m)
+    hist = np.concatenate([net.train(f, t, m, iters=2000, batch=16, lr=1e-3, seed=9),
+                           net.train(f, t, m, iters=1000, batch=16, lr=3e-4, seed=10)])
+    return net, hist, loss0
 
 
-def test_training_on_solver_data_reduces_the_loss(solver_data, trained):
-    f, t, m = solver_data
-    assert f.shape[0] >= 16 and np.all(np.isfinite(t))
-    net, hist = trained
+def test_training_on_solver_data_reduces_the_loss(data, trained):
+    f, t, m = data[:3]
+    assert f.shape[0] >= 64 and np.all(np.isfinite(t))
+    net, hist, loss0 = trained
     assert np.all(np.isfinite(hist))
-    first, last = float(np.mean(hist[:20])), float(np.mean(hist[-50:]))
-    assert last < 0.1 * first, (first, last)
-    # held-in check of the loss through the forward pass
-    out = net.forward(f)
-    mse = float(np.sum(m * (out - t) ** 2) / np.sum(m))
-    assert mse < 0.2 * first
+    loss1, _ = net.grad(f, t, m)
+    print("weighted loss over the training set: %.3e -> %.3e" % (loss0, loss1))
+    assert loss1 < 0.05 * loss0
+
+
+def _density_error(rho_pred, rho):
+    """The check of the device loop: max |rho_net - rho_ode| / max rho_ode."""
+    return float(np.max(np.abs(rho_pred - rho)) / np.max(rho))
+
+
+def test_network_gain_on_a_held_out_field(data, trained):
+    """What the network adds: the density of a field it was not trained on
+    from the closed form with the network's d, against the closed form with
+    d = 0 (the base rate alone, no network), both against the FP64 ODE."""
+    from filament_gb import surrogate as S
+    (E, rho), pe, dt = data[3], data[4], data[5]
+    net = trained[0]
+    d = net.forward(S.features(E, pe, dt))
+    e_net = _density_error(S.closed_form_density(E, d, pe, dt), rho)
+    e_0 = _density_error(S.closed_form_density(E, np.zeros_like(d), pe, dt), rho)
+    print("held-out field (x%.1f): density error without network %.3e, with %.3e" % (HELD_OUT_SCALE, e_0, e_net))
+    assert e_net < 0.5 * e_0
 
 
 def _run(inp, net=None, steps=24, every=20, tol=1e-3):
@@ -113,41 +159,46 @@ def _run(inp, net=None, steps=24, every=20, tol=1e-3):
     return E, st, stats, dt
 
 
-def test_untrained_network_falls_back_to_the_ode(gpu_lib):
-    """An untrained network fails its first check; the ODE then solves every
-    step, so the run is the plain run to the last bit."""
+def test_failing_network_falls_back_to_the_ode(gpu_lib):
+    """A network whose rates are e^3 too large fails every check; the ODE
+    then solves every step, so the run is the plain run to the last bit."""
     from filament_gb.surrogate import Surrogate
     inp = rt_input(zmax=1.0)
     net = Surrogate(512, seed=1)
+    p = net.get_params()
+    p[-1] = 3.0   # output bias
+    net.set_params(p)
     E0, st0, _, _ = _run(inp)
     E1, st1, s, _ = _run(inp, net, steps=24, every=20)
     assert s["checks"] == 2 and s["checks_failed"] == 2 and s["steps_used"] == 0
-    assert s["err_last"] > 1e-3
+    assert s["err_last"] > 1.0
     assert st1["steps"] == st0["steps"]
     assert np.array_equal(E0, E1)
 
 
 def test_trained_network_in_the_loop(trained):
-    """The trained network supplies the density between checks; the field
-    stays within the density tolerance's reach of the plain run."""
-    net, _ = trained
+    """Two checks in 40 steps; where they pass the network supplies the
+    density of the 38 other steps, where they fail the ODE does.  Either
+    way the field stays close to the plain run."""
+    net = trained[0]
     inp = rt_input(zmax=1.0)
     E0, st0, _, _ = _run(inp, steps=40)
     E1, st1, s, _ = _run(inp, net, steps=40, every=20, tol=1e-3)
+    print("surrogate in the loop (tol 1e-3):", s)
     assert s["checks"] == 2
-    print("surrogate stats", s)
     if s["checks_failed"] == 0:
-        assert s["steps_used"] == 38 and s["err_max"] <= 1e-3
-        assert s["rows_mean"] > 0
+        assert s["steps_used"] == 38 and s["err_max"] <= 1e-3 and s["rows_mean"] > 0
+    else:
+        assert s["err_max"] > 1e-3
     assert rel_l2(E1, E0) < 1e-3
 
 
-def test_surrogate_gain_against_the_plain_form(trained):
-    """Ablation: the same steps with and without the network.  The plain
-    form's plasma solve is a parallel scan fused into the row kernel, so the
-    network (about 1.5e5 flop per point) costs more than it saves; this
-    test records the ratio and the field difference."""
-    net, _ = trained
+def test_surrogate_cost_against_the_plain_form(trained):
+    """Ablation of cost: the same steps with the network always used
+    (tol = 1) and without it.  The plain form's plasma solve is a parallel
+    scan fused into the row kernel, so the network (about 1.5e5 flop per
+    point) costs more than it saves; the ratio is printed."""
+    net = trained[0]
     inp = rt_input(zmax=1.0)
     _run(inp, steps=4)
     E0, _, _, t0 = _run(inp, steps=40)

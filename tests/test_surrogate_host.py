@@ -13,7 +13,7 @@ def test_reference_gradient_matches_finite_differences(monkeypatch):
     monkeypatch.setattr(sr, "bf16", lambda x: np.asarray(x, dtype=np.float64))
     rng = np.random.default_rng(3)
     p = rng.uniform(-0.3, 0.3, sr.nparams())
-    f = rng.standard_normal((2, 2, 40))
+    f = rng.standard_normal((2, 3, 40))
     t = rng.standard_normal((2, 40))
     m = (rng.random((2, 40)) > 0.3).astype(float)
     _, g = sr.grad(p, f, t, m)
@@ -46,13 +46,15 @@ class _PE:
         I = np.logspace(-6, 2, 9)
         self.tfs = [TFunction(I, (I / 0.5) ** 8)]
         self.rho_nt = np.array([2.0])
+        self.rho0 = 0.0
         self.EREAL = False
+        self.alg = "RK3"
 
 
 def test_training_targets_reconstruct_the_density():
-    """rho from a sequential solve with a rate that is not the
-    instantaneous one (a midpoint rule plus a density feedback) gives
-    targets d; rho_nt - (rho_nt - rho0) exp(-dt sum Wb e^d) gives rho back."""
+    """rho from a sequential solve with a rate that is not the base rate
+    (end-point average plus a density feedback) gives targets d; the closed
+    form of the row kernel with those d gives rho back."""
     from filament_gb import surrogate as S
     pe = _PE()
     nt, dt = 256, 0.05
@@ -70,15 +72,20 @@ def test_training_targets_reconstruct_the_density():
         rows.append(E)
         rhos.append(rho)
     E, rho = np.array(rows), np.array(rhos)
-    f, d, m = S.training_pairs(E, rho, pe, dt, min_frac=0.0, tail_weight=0.0)
-    assert f.shape == (3, 2, nt) and d.shape == (3, nt)
+    f, d, m = S.training_pairs(E, rho, pe, dt, resolve=0.0)
+    assert f.shape == (3, 3, nt) and d.shape == (3, nt)
     assert np.allclose(f[:, 1], (E.real ** 2 / np.maximum(np.abs(E) ** 2, 1e-30)), atol=1e-6)
-    Wb = S.base_rate(pe, np.abs(E) ** 2)
-    w = np.where(m > 0, Wb * np.exp(d.astype(np.float64)), 0.0)
+    # f2: log of the base rate's ionised fraction, 0 before the first step
+    Sb = np.cumsum(S.quad_rate(pe, E) * dt, axis=1)
+    assert np.allclose(f[:, 2, 1:], np.log(np.maximum(Sb, 1e-30)) / 16, atol=1e-6)
+    assert np.allclose(f[:, 2, 0], np.log(1e-30) / 16)
+    assert np.all(m[:, -1] == 0) and np.mean(m[:, :-1] > 0) > 0.3
     # float32 targets: the reconstruction holds to their rounding
-    S_ = np.concatenate([np.zeros((3, 1)), np.cumsum(w[:, :-1] * dt, axis=1)], axis=1)
-    rec = 2.0 - 2.0 * np.exp(-S_)
+    rec = S.closed_form_density(E, d, pe, dt)
     assert np.max(np.abs(rec - rho)) <= 1e-6 * np.max(rho)
+    # with d = 0 (no network) the base rate alone misses the feedback term
+    rec0 = S.closed_form_density(E, np.zeros_like(d), pe, dt)
+    assert np.max(np.abs(rec0 - rho)) > 1e-3 * np.max(rho)
 
 
 def test_training_rows_below_the_threshold_are_dropped():
