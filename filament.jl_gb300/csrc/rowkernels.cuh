@@ -76,7 +76,7 @@ template <typename R> struct RowParams {
   DevCtl* ctl;
   // learned plasma surrogate: network inputs of the flagged rows
   // [slot][2][N] (BF16), slot of each row (-1: not flagged), network output
-  // d(t) = ln w - ln W(I) [slot][N]
+  // g(t), the log-amplification of the avalanche term of nn_density [slot][N]
   __nv_bfloat16* nn_feat;
   int* nn_slot;
   const float* nn_out;
@@ -425,26 +425,34 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 }
 
 // ---------------------------------------------------------------------------
-// Density of the row in X from the surrogate output d[j] (surrogate.cuh):
-// effective rate w_j = Wb_j e^{d_j} over the step t_j -> t_{j+1}, with the
-// base rate Wb_j = sum_s b_s W(I at the stage point of s) -- the quadrature
-// of the time integrator of plasma_equations.jl:46-72 (stage points t_j,
-// the midpoint of the linearly interpolated field, t_{j+1}) applied to
-// W = sum_c W_c rho_nt,c / rho_nt, exact and pointwise; cumulative sum
-// S_j = dt sum_{i<j} w_i (block scan), rho_j = rho_a + (rho_nt - rho_a)(1 - e^{-S_j})
-// with rho_a = nc rho0 the initial density, and the loss term
-// Kdrho_j = sum_c K_c W_c(I_j) (rho_nt,c - rho_{j+1} rho_nt,c / rho_nt), 0 at the
-// last point (the photoionisation-only density of plasma_equations.jl:63-70
-// approximated by rho).  Thread t owns j = 16t .. 16t+15 as in plasma_row.
-// judge: compare with the density in rho[] instead of writing it; returns
-// max |difference|.  Otherwise writes rho[], kdrho[] and returns max rho.
+// Density of the row in X from the surrogate output g[j] (surrogate.cuh).
+// Effective rate of the step t_j -> t_{j+1}:
+//   w_j = Wb_j + kappa A_j (1 - e^{-S_j}) e^{g_j},
+// with Wb_j = sum_s b_s W(I at the stage point of s) the quadrature of the
+// time integrator of plasma_equations.jl:46-72 (stage points t_j, the
+// midpoint of the linearly interpolated field, t_{j+1}) applied to
+// W = sum_c W_c rho_nt,c / rho_nt; A_j the same quadrature of E^2 (the
+// avalanche drive); kappa = sum_c Rava_c; S_j = dt sum_{i<j} Wb_i the base
+// rate's ionised fraction exponent, so that the second term is the avalanche
+// rate of the photoionised density and e^{g} its learned correction (the
+// avalanche's own amplification).  Then S'_j = dt sum_{i<j} w_i (block scans),
+// rho_j = rho_a + (rho_nt - rho_a)(1 - e^{-S'_j}) with rho_a = nc rho0, and the
+// loss term Kdrho_j = sum_c K_c W_c(I_j) (rho_nt,c - rho_{j+1} rho_nt,c / rho_nt),
+// 0 at the last point (the photoionisation-only density of
+// plasma_equations.jl:63-70 approximated by rho).  Thread t owns
+// j = 16t .. 16t+15 as in plasma_row.  judge: compare with the density in
+// rho[] instead of writing it; returns max |difference|.  Otherwise writes
+// rho[], kdrho[] and returns max rho.
 template <typename R, int N, int NC>
 FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typename C2T<R>::type* X,
-                     const float* __restrict__ d, R* rho, R* kdrho, Aff<R, 1>* ascratch, R* rscratch, bool judge) {
+                     const float* __restrict__ g, R* rho, R* kdrho, Aff<R, 1>* ascratch, R* rscratch, bool judge) {
   typedef typename C2T<R>::type C;
   const PlasmaParams<R>& pp = P.pp;
   const int j0 = threadIdx.x * 16;
   const R rnt = pp.rhont_sum, ra = (R)NC * pp.rho0, dt = pp.dt;
+  R kappa = 0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) kappa += pp.rava_nt[c] * pp.rho_nt[c];
   // quadrature weights of the stage points t_j, t_j + dt/2, t_{j+1}
   R qw[3] = {0, 0, 0};
   for (int st = 0; st < pp.ns; ++st) qw[pp.pidx[st]] += pp.b[st];
@@ -458,28 +466,40 @@ FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
     }
     return w;
   };
-  R wl[16];
+  // base rate of step j times dt (0 for the last point)
+  auto base = [&](int j) -> R {
+    if (j >= N - 1) return (R)0;
+    const C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
+    return (qw[0] * wsum(e0) + qw[1] * wsum((R)0.5 * (e0 + e1)) + qw[2] * wsum(e1)) * (dt / rnt);
+  };
+  // pass 1: S_j
   R tsum = 0;
-  R wcur = wsum(X[pad16(j0)]);
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const int j = j0 + q;
-    R w = 0;
-    if (j < N - 1) {
-      const C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
-      const R wnext = wsum(e1);
-      const R wb = (qw[0] * wcur + qw[1] * wsum((R)0.5 * (e0 + e1)) + qw[2] * wnext) / rnt;
-      if (wb > (R)0) w = wb * exp((R)__ldg(&d[j])) * dt;
-      wcur = wnext;
-    }
-    wl[q] = w;
-    tsum += w;
-  }
+#pragma unroll 4
+  for (int q = 0; q < 16; ++q) tsum += base(j0 + q);
   Aff<R, 1> G;
   G.L[0][0] = 0;
   G.B[0] = tsum;
-  const Aff<R, 1> Pin = aff_block_exclusive_scan<R, 1>(G, ascratch);
-  R S = Pin.B[0];
+  R S = aff_block_exclusive_scan<R, 1>(G, ascratch).B[0];
+  // pass 2: effective rates
+  R wl[16];
+  tsum = 0;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int j = j0 + q;
+    const R wb = base(j);
+    R w = wb;
+    if (j < N - 1 && kappa != (R)0) {
+      const C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
+      const C em = (R)0.5 * (e0 + e1);
+      const R A = qw[0] * e0.x * e0.x + qw[1] * em.x * em.x + qw[2] * e1.x * e1.x;
+      w += kappa * A * dt * -expm1(-S) * exp((R)__ldg(&g[j]));
+    }
+    S += wb;
+    wl[q] = w;
+    tsum += w;
+  }
+  G.B[0] = tsum;
+  S = aff_block_exclusive_scan<R, 1>(G, ascratch).B[0];
   R out = 0;
   R rcur = ra + (rnt - ra) * -expm1(-S);
 #pragma unroll

@@ -1,24 +1,24 @@
 // surrogate.cuh -- the learned plasma surrogate: a 4-layer 1-D convolutional
 // network (3 -> 64 -> 64 -> 64 -> 1 channels, kernel 9, "same" padding, tanh
 // after the first three layers) evaluated on the time row of one transverse
-// point.  Its output is the log-ratio d_j = ln w_j - ln Wb_j of the
-// effective ionisation rate w of the step t_j -> t_{j+1} to the base rate Wb,
+// point, in place of the ODE solve of plasma_equations.jl:46-72.  The density
+// follows in closed form from the effective rate of every step t_j -> t_{j+1},
+//   w_j = Wb_j + kappa A_j (1 - e^{-S_j}) e^{g_j},
+//   rho_j = rho0 + (rho_nt - rho0) (1 - exp(-dt sum_{i<j} w_i)),
+// which is exact for photoionisation with any time-dependent rate: Wb_j is
 // the medium's rate averaged with the time integrator's quadrature over the
-// stage points of the step (evaluated exactly), and the density follows in
-// closed form,
-//   rho_j = rho0 + (rho_nt - rho0) (1 - exp(-dt sum_{i < j} Wb_i e^{d_i})),
-// which replaces the ODE solve of plasma_equations.jl:46-72 (exact for
-// photoionisation with any time-dependent rate; d carries the higher orders
-// of the integrator in W dt and the avalanche term).
+// stage points of the step, A_j the same quadrature of E^2, kappa the summed
+// avalanche coefficient and S_j = dt sum_{i<j} Wb_i, so that the second term is
+// the avalanche rate of the photoionised density.  The network's output g_j
+// is the log of that term's amplification by the avalanche itself (the
+// density history beyond photoionisation), learned from the ODE.
 //
 // Inputs per time point: f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30)
 // (the carrier phase, which drives the avalanche term) and
-// f2 = ln(max(S_j, 1e-30)) / 16 with S_j = dt sum_{i<j} Wb_i, the ionised fraction
-// of the base rate alone (the density history the avalanche term grows
-// from, beyond the network's 33-point receptive field).  Weights and hidden
-// activations are stored in BF16, every product is accumulated in FP32 and
-// the output layer is written in FP32; training keeps FP32 master weights
-// (Adam).
+// f2 = ln(max(S_j, 1e-30)) / 16 (the density history beyond the network's
+// 33-point receptive field).  Weights and hidden activations are stored in
+// BF16, every product is accumulated in FP32 and the output layer is written
+// in FP32; training keeps FP32 master weights (Adam).
 #pragma once
 #include <cuda_bf16.h>
 #include "common.cuh"

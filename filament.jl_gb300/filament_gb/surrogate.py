@@ -1,13 +1,17 @@
 """Host wrapper of the learned plasma surrogate (fil_nn_* of
 include/filament_gb.h): a 1-D convolutional network trained on the GPU by
-the library's own forward and backward kernels.
+the library's own forward and backward kernels, and its training data.
 
 The reference has no counterpart: it integrates the plasma rate equation
 for every transverse point (src/modules/plasma_equations.jl:46-72,
-src/modules/Models.jl:205-219).  The surrogate learns, per time row, the
-log of the effective ionisation rate w(t) from the intensity and the carrier
-phase; the density then follows in closed form,
-rho(t) = rho0 + (rho_nt - rho0) (1 - exp(-dt sum_{t'<t} w(t'))).
+src/modules/Models.jl:205-219).  The surrogate forms the density of a time
+row in closed form from the effective rate of every step,
+    w_j = Wb_j + kappa A_j (1 - e^{-S_j}) e^{g_j},
+    rho_j = rho_a + (rho_nt - rho_a) (1 - exp(-dt sum_{i<j} w_i)),
+where Wb_j and A_j are the medium's rate and E^2 averaged with the plasma
+integrator's quadrature over the step, kappa the summed avalanche
+coefficient, S_j = dt sum_{i<j} Wb_i, and g_j the network's output (the
+avalanche's amplification of itself, learned from the ODE).
 """
 import ctypes as C
 
@@ -58,7 +62,8 @@ def features(E, pe, dt):
     """Network inputs of time rows E [rows][nt] (complex analytic field,
     |E|^2 = I): f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30),
     f2 = ln(max(S_j, 1e-30)) / 16 with S_j = dt sum_{i<j} Wb_i the ionised
-    fraction of the base rate (quad_rate).  Returns float32 [rows][3][nt]."""
+    fraction exponent of the base rate (quad_rate).  Returns float32
+    [rows][3][nt]."""
     E = np.atleast_2d(np.asarray(E))
     I = np.abs(E) ** 2
     Ic = np.maximum(I, 1e-30)
@@ -104,31 +109,50 @@ def quad_rate(pe, E):
             + q1 * base_rate(pe, inten(e1)))
 
 
-def closed_form_density(E, d, pe, dt):
-    """The density the row kernel forms from the network output d [rows][nt]
-    (FP64): rho_j = rho_a + (rho_nt - rho_a)(1 - exp(-dt sum_{i<j} Wb_i e^{d_i}))."""
+def quad_ava(pe, E):
+    """kappa A_j: the avalanche drive of every step, kappa = sum_c Rava_c
+    times the integrator's quadrature of E^2 = Re(E)^2.  [rows][nt - 1]"""
     E = np.atleast_2d(np.asarray(E))
-    w = quad_rate(pe, E) * np.exp(np.asarray(d, dtype=np.float64)[:, :-1])
-    S = np.concatenate([np.zeros((E.shape[0], 1)), np.cumsum(w * dt, axis=1)], axis=1)
+    q0, qm, q1 = QUADRATURE[pe.alg]
+    e0, e1 = E[:, :-1], E[:, 1:]
+    em = 0.5 * (e0 + e1)
+    return float(np.sum(pe.rava)) * (q0 * e0.real ** 2 + qm * em.real ** 2 + q1 * e1.real ** 2)
+
+
+def _base_exponent(pe, E, dt):
+    """(Wb dt [rows][nt - 1], S_j = dt sum_{i<j} Wb_i for j < nt - 1)."""
+    wb = quad_rate(pe, E) * dt
+    S = np.concatenate([np.zeros((wb.shape[0], 1)), np.cumsum(wb, axis=1)[:, :-1]], axis=1)
+    return wb, S
+
+
+def closed_form_density(E, g, pe, dt):
+    """The density the row kernel forms from the network output g [rows][nt]
+    (FP64): w_j = Wb_j + kappa A_j (1 - e^{-S_j}) e^{g_j},
+    rho_j = rho_a + (rho_nt - rho_a)(1 - exp(-dt sum_{i<j} w_i))."""
+    E = np.atleast_2d(np.asarray(E))
+    wb, S = _base_exponent(pe, E, dt)
+    w = wb + quad_ava(pe, E) * dt * -np.expm1(-S) * np.exp(np.asarray(g, dtype=np.float64)[:, :-1])
+    St = np.concatenate([np.zeros((E.shape[0], 1)), np.cumsum(w, axis=1)], axis=1)
     ra = len(pe.rho_nt) * float(pe.rho0)
     rnt = float(np.sum(pe.rho_nt))
-    return ra + (rnt - ra) * -np.expm1(-S)
+    return ra + (rnt - ra) * -np.expm1(-St)
 
 
-def training_pairs(E, rho, pe, dt, row_frac=1e-9, resolve=1e-9, floor=1e-3):
+def training_pairs(E, rho, pe, dt, row_frac=1e-9, resolve=1e-6, floor=1e-3):
     """Network inputs, targets and loss weights from time rows of the field
     E [rows][nt] (complex analytic signal) and the density rho [rows][nt]
     that the plasma equation gives on them.
 
     The effective rate of step j is w_j = -ln(1 - (rho_{j+1} - rho_j) / (rho_nt - rho_j)) / dt
-    (the closed form rho_{j+1} = rho_nt - (rho_nt - rho_j) e^{-w_j dt} then
-    reproduces the solve exactly), the target d_j = ln(w_j / Wb_j) with the
-    base rate of quad_rate.  An error e in d_j moves the final density by
-    about (rho_{j+1} - rho_j) e, so a point weighs its density increment
-    relative to the row's largest, at least `floor`; points whose increment
-    is below `resolve` times the density (not resolved by the solve) or
-    with Wb = 0 weigh 0.  Rows whose density rise is below `row_frac` of the
-    largest rise are dropped."""
+    (the closed form then reproduces the solve exactly) and the target
+    g_j = ln((w_j - Wb_j) / (kappa A_j (1 - e^{-S_j}))).  An error e in g_j
+    moves the final density by about (rho_{j+1} - rho_j)(1 - Wb_j / w_j) e, so
+    a point weighs that increment relative to the row's largest, at least
+    `floor`; points where the avalanche part w_j - Wb_j is below `resolve`
+    times w_j (not resolved by the solve, or absent) or whose increment is
+    below 1e-10 of the density (not resolved in FP64) weigh 0.  Rows whose
+    density rise is below `row_frac` of the largest rise are dropped."""
     E = np.atleast_2d(np.asarray(E))
     rho = np.atleast_2d(np.asarray(rho, dtype=np.float64))
     nt = E.shape[1]
@@ -139,15 +163,20 @@ def training_pairs(E, rho, pe, dt, row_frac=1e-9, resolve=1e-9, floor=1e-3):
         return (np.zeros((0, 3, nt), np.float32), np.zeros((0, nt), np.float32), np.zeros((0, nt), np.float32))
     E, rho = E[keep], rho[keep]
     drho = np.diff(rho, axis=1)
+    wb, S = _base_exponent(pe, E, dt)
+    av = quad_ava(pe, E) * dt * -np.expm1(-S)
     with np.errstate(divide="ignore", invalid="ignore"):
-        w = -np.log1p(-drho / (rnt - rho[:, :-1])) / dt
-        Wb = quad_rate(pe, E)
-        good = (drho > resolve * np.abs(rho[:, 1:])) & (Wb > 0) & (w > 0)
-        d = np.where(good, np.log(np.where(good, w, 1.0) / np.where(good, Wb, 1.0)), 0.0)
-    rel = drho / np.maximum(drho.max(axis=1, keepdims=True), 1e-300)
+        w = -np.log1p(-drho / (rnt - rho[:, :-1]))
+        excess = w - wb
+        # the increment must be resolved in FP64 (rounding of rho below 1e-6
+        # of it) and carry an avalanche part
+        good = (excess > resolve * w) & (av > 0) & (drho > 1e-10 * np.abs(rho[:, 1:]))
+        g = np.where(good, np.log(np.where(good, excess, 1.0) / np.where(good, av, 1.0)), 0.0)
+        contrib = np.where(good, drho * excess / np.where(good, w, 1.0), 0.0)
+    rel = contrib / np.maximum(contrib.max(axis=1, keepdims=True), 1e-300)
     tgt = np.zeros(rho.shape, np.float32)
     mask = np.zeros(rho.shape, np.float32)
-    tgt[:, :-1] = d
+    tgt[:, :-1] = g
     mask[:, :-1] = np.where(good, np.maximum(rel, floor), 0.0)
     return features(E, pe, dt), tgt, mask
 

@@ -284,11 +284,12 @@ int fil_hankel_propagate_noalloc(const float* m1, const float* m2, const float* 
  * inputs of every point of a time row,
  *   f0 = ln(max(I, 1e-30)) / 16, f1 = Re(E)^2 / max(I, 1e-30),
  *   f2 = ln(max(S_j, 1e-30)) / 16, S_j = dt sum_{i<j} Wb_i,
- * to d_j = ln(w_j / Wb_j), the log-ratio of the effective ionisation rate of
- * the step t_j -> t_{j+1} to the base rate Wb_j (the medium's rate averaged
- * with the time integrator's quadrature over the step); the density is then
- * rho_j = rho0 + (rho_nt - rho0)(1 - exp(-dt sum_{i<j} Wb_i e^{d_i})).
- * Feature arrays are [rows][3][nt], targets and masks [rows][nt] (FP32,
+ * to g_j in the effective ionisation rate of the step t_j -> t_{j+1},
+ *   w_j = Wb_j + kappa A_j (1 - e^{-S_j}) e^{g_j},
+ * (Wb_j, A_j: the medium's rate and E^2 averaged with the time integrator's
+ * quadrature over the step; kappa: the summed avalanche coefficient); the
+ * density is rho_j = rho0 + (rho_nt - rho0)(1 - exp(-dt sum_{i<j} w_i)).
+ * Feature arrays are [rows][3][nt], targets and weights [rows][nt] (FP32,
  * host memory).                                                             */
 typedef struct fil_nn fil_nn;
 int fil_nn_nparams(void);
@@ -298,7 +299,8 @@ int fil_nn_destroy(fil_nn* n);
 int fil_nn_get_params(fil_nn* n, float* params);        /* fil_nn_nparams() FP32 */
 int fil_nn_set_params(fil_nn* n, const float* params);
 int fil_nn_forward(fil_nn* n, const float* feat, int rows, float* out);   /* out [rows][nt] */
-/* loss = sum mask (out - target)^2 / sum mask and its gradient */
+/* loss = sum m (out - target)^2 / sum m (m: the point weights) and its
+ * gradient                                                                 */
 int fil_nn_grad(fil_nn* n, const float* feat, const float* target, const float* mask, int rows,
                 float* grad, float* loss);
 /* Adam training, `iters` batches of `batch` rows drawn with `seed`;
