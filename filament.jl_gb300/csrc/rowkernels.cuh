@@ -12,6 +12,7 @@
 #include "common.cuh"
 #include "fft.cuh"
 #include "plasma.cuh"
+#include "surrogate.cuh"
 
 // Device control block: written by the controller kernel, read by the step
 // kernels (fil_run) or set by the host (fil_step).
@@ -435,7 +436,7 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 // avalanche drive); kappa = sum_c Rava_c; S_j = dt sum_{i<j} Wb_i the base
 // rate's ionised fraction exponent, so that the second term is the avalanche
 // rate of the photoionised density and e^{g} its learned correction (the
-// avalanche's own amplification).  Then S'_j = dt sum_{i<j} w_i (block scans),
+// avalanche's own amplification; g is held to [NN_G_LO, NN_G_HI]).  Then S'_j = dt sum_{i<j} w_i (block scans),
 // rho_j = rho_a + (rho_nt - rho_a)(1 - e^{-S'_j}) with rho_a = nc rho0, and the
 // loss term Kdrho_j = sum_c K_c W_c(I_j) (rho_nt,c - rho_{j+1} rho_nt,c / rho_nt),
 // 0 at the last point (the photoionisation-only density of
@@ -492,7 +493,8 @@ FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
       const C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
       const C em = (R)0.5 * (e0 + e1);
       const R A = qw[0] * e0.x * e0.x + qw[1] * em.x * em.x + qw[2] * e1.x * e1.x;
-      w += kappa * A * dt * -expm1(-S) * exp((R)__ldg(&g[j]));
+      const float gj = fminf(fmaxf(__ldg(&g[j]), NN_G_LO), NN_G_HI);
+      w += kappa * A * dt * -expm1(-S) * exp((R)gj);
     }
     S += wb;
     wl[q] = w;

@@ -232,7 +232,9 @@ int fil_nn_create(int nt, uint64_t seed, fil_nn** out) {
     return (double)(z >> 11) * (1.0 / 9007199254740992.0);
   };
   for (int l = 0; l < NN_LAYERS; ++l) {
-    const double a = std::sqrt(3.0 / (nn_ci(l) * NN_K));
+    // the output layer starts near zero: an untrained network gives g ~ 0,
+    // the closed form with first-order avalanche
+    const double a = std::sqrt(3.0 / (nn_ci(l) * NN_K)) * (l == NN_LAYERS - 1 ? 1e-2 : 1.0);
     for (int i = 0; i < nn_wsize(l); ++i) h[nn_poff(l) + i] = (float)((2.0 * rnd() - 1.0) * a);
   }
   if (cudaMemcpy(n->p, h.data(), np * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||

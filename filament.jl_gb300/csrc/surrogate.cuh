@@ -28,6 +28,11 @@
 #define NN_K 9
 #define NN_HALF 4
 #define NN_LAYERS 4
+// range of the network output g used by the density (the avalanche term's
+// amplification e^g stays within [e^-2, e^4]; the physical value,
+// ln(rho / rho_photoionised), is small and non-negative)
+#define NN_G_LO (-2.0f)
+#define NN_G_HI 4.0f
 
 // layer l: ci_l -> co_l
 __host__ __device__ constexpr int nn_ci(int l) { return l == 0 ? NN_IN : NN_CH; }

@@ -92,6 +92,9 @@ def base_rate(pe, I):
 # the plasma equation's time integrator (plasma_equations.jl:46-72)
 QUADRATURE = {"RK2": (0.0, 1.0, 0.0), "RK3": (1 / 6, 4 / 6, 1 / 6), "RK4": (1 / 6, 4 / 6, 1 / 6)}
 
+# range of the network output the density uses (NN_G_LO, NN_G_HI of the kernels)
+G_RANGE = (-2.0, 4.0)
+
 
 def quad_rate(pe, E):
     """Base rate of every step t_j -> t_{j+1} of the time rows E [rows][nt]:
@@ -132,14 +135,15 @@ def closed_form_density(E, g, pe, dt):
     rho_j = rho_a + (rho_nt - rho_a)(1 - exp(-dt sum_{i<j} w_i))."""
     E = np.atleast_2d(np.asarray(E))
     wb, S = _base_exponent(pe, E, dt)
-    w = wb + quad_ava(pe, E) * dt * -np.expm1(-S) * np.exp(np.asarray(g, dtype=np.float64)[:, :-1])
+    g = np.clip(np.asarray(g, dtype=np.float64)[:, :-1], *G_RANGE)
+    w = wb + quad_ava(pe, E) * dt * -np.expm1(-S) * np.exp(g)
     St = np.concatenate([np.zeros((E.shape[0], 1)), np.cumsum(w, axis=1)], axis=1)
     ra = len(pe.rho_nt) * float(pe.rho0)
     rnt = float(np.sum(pe.rho_nt))
     return ra + (rnt - ra) * -np.expm1(-St)
 
 
-def training_pairs(E, rho, pe, dt, row_frac=1e-9, resolve=1e-6, floor=1e-3):
+def training_pairs(E, rho, pe, dt, row_frac=1e-9, resolve=1e-6, floor=0.0):
     """Network inputs, targets and loss weights from time rows of the field
     E [rows][nt] (complex analytic signal) and the density rho [rows][nt]
     that the plasma equation gives on them.
@@ -149,7 +153,8 @@ def training_pairs(E, rho, pe, dt, row_frac=1e-9, resolve=1e-6, floor=1e-3):
     g_j = ln((w_j - Wb_j) / (kappa A_j (1 - e^{-S_j}))).  An error e in g_j
     moves the final density by about (rho_{j+1} - rho_j)(1 - Wb_j / w_j) e, so
     a point weighs that increment relative to the row's largest, at least
-    `floor`; points where the avalanche part w_j - Wb_j is below `resolve`
+    `floor`; targets are clipped to G_RANGE.  Points where the avalanche
+    part w_j - Wb_j is below `resolve`
     times w_j (not resolved by the solve, or absent) or whose increment is
     below 1e-10 of the density (not resolved in FP64) weigh 0.  Rows whose
     density rise is below `row_frac` of the largest rise are dropped."""
@@ -176,7 +181,7 @@ def training_pairs(E, rho, pe, dt, row_frac=1e-9, resolve=1e-6, floor=1e-3):
     rel = contrib / np.maximum(contrib.max(axis=1, keepdims=True), 1e-300)
     tgt = np.zeros(rho.shape, np.float32)
     mask = np.zeros(rho.shape, np.float32)
-    tgt[:, :-1] = g
+    tgt[:, :-1] = np.clip(g, *G_RANGE)
     mask[:, :-1] = np.where(good, np.maximum(rel, floor), 0.0)
     return features(E, pe, dt), tgt, mask
 

@@ -70,8 +70,8 @@ def test_set_params_round_trip(gpu_lib):
     assert np.array_equal(net.get_params(), p)
 
 
-TRAIN_SCALES = (1.5, 2.0, 3.0, 3.5, 4.0)
-HELD_OUT_SCALE = 2.5
+TRAIN_SCALES = (2.0, 3.0, 4.0, 4.5, 5.5, 6.0)
+HELD_OUT_SCALE = 5.0
 
 
 @pytest.fixture(scope="module")
