@@ -12,7 +12,7 @@
 #include "common.cuh"
 #include "fft.cuh"
 #include "plasma.cuh"
-#include "surrogate.cuh"
+#include "surrogate_consts.h"
 
 // Device control block: written by the controller kernel, read by the step
 // kernels (fil_run) or set by the host (fil_step).

@@ -22,17 +22,7 @@
 #pragma once
 #include <cuda_bf16.h>
 #include "common.cuh"
-
-#define NN_IN 3
-#define NN_CH 64
-#define NN_K 9
-#define NN_HALF 4
-#define NN_LAYERS 4
-// range of the network output g used by the density (the avalanche term's
-// amplification e^g stays within [e^-2, e^4]; the physical value,
-// ln(rho / rho_photoionised), is small and non-negative)
-#define NN_G_LO (-2.0f)
-#define NN_G_HI 4.0f
+#include "surrogate_consts.h"
 
 // layer l: ci_l -> co_l
 __host__ __device__ constexpr int nn_ci(int l) { return l == 0 ? NN_IN : NN_CH; }
