@@ -20,6 +20,7 @@
 
 #include "../../include/filament_gb.h"
 #include "launch.h"
+#include "nn_tc.h"
 #include "rowkernels.cuh"
 #include "dht_simt.cuh"
 #include "tc_params.h"
@@ -92,6 +93,9 @@ struct fil_handle {
   void* nn_a2 = nullptr;
   float* nn_out = nullptr;     // [nrows][nt]
   int* nn_slot = nullptr;      // [nrows]
+  int* nn_err = nullptr;       // tensor-core inference: a wait timed out
+  NnRowsPlan nn_plan;          // tensor-core inference over the buffers above
+  bool nn_tc = false;          // nt is a multiple of 128: tensor-core path
 };
 
 void fil_set_global_error(const std::string& m) { g_err = m; }
@@ -534,6 +538,7 @@ template <typename R> static cudaError_t enqueue_surrogate(fil_handle* h, RowPar
   if (!h->nn) return cudaSuccess;
   P.nn_slot = h->nn_slot;
   P.nn_out = h->nn_out;
+  if (h->nn_tc) return nn_infer(h->nn, h->nn_plan, h->st);
   return nn_forward_rows(h->nn, h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nt, h->nrows, &h->ctl->nn_rows,
                          &h->ctl->done, h->st);
 }
@@ -727,11 +732,13 @@ static int reduce(fil_handle* h, double* power, int check_done) {
 }
 
 static int check_tc(fil_handle* h) {
-  if (!h->tc_err) return 0;
-  int e = 0;
-  CK(cudaMemcpyAsync(&e, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  if (e) return fail(h, FIL_ERR_TIMEOUT, "a tensor-core pipeline wait timed out");
+  for (int* flag : {h->tc_err, h->nn_err}) {
+    if (!flag) continue;
+    int e = 0;
+    CK(cudaMemcpyAsync(&e, flag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (e) return fail(h, FIL_ERR_TIMEOUT, "a tensor-core pipeline wait timed out");
+  }
   return 0;
 }
 
@@ -748,7 +755,7 @@ static void free_all(fil_handle* h) {
                   h->qa1, h->qa2, h->BS[0], h->BS[1], h->BS[2], h->qb, h->kzt, h->gdt, h->tc_err,
                   h->kx2, h->ky2, h->sg1, h->sg2, h->twx, h->twy,
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
-                  h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot};
+                  h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -1222,6 +1229,20 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
       CK(cudaMalloc((void**)&h->nn_out, rt * sizeof(float)));
       CK(cudaMalloc((void**)&h->nn_slot, (size_t)h->nrows * sizeof(int)));
       CK(cudaMemset(h->nn_slot, 0xff, (size_t)h->nrows * sizeof(int)));
+      CK(cudaMalloc((void**)&h->nn_err, sizeof(int)));
+      CK(cudaMemset(h->nn_err, 0, sizeof(int)));
+      NnRowsPlan& pl = h->nn_plan;
+      std::memset(&pl, 0, sizeof pl);
+      pl.x0 = (const __nv_bfloat16*)h->nn_feat;
+      pl.a1 = (__nv_bfloat16*)h->nn_a1;
+      pl.a2 = (__nv_bfloat16*)h->nn_a2;
+      pl.out = h->nn_out;
+      pl.T = h->nt;
+      pl.maxrows = h->nrows;
+      pl.count = &h->ctl->nn_rows;
+      pl.stop = &h->ctl->done;
+      pl.err = h->nn_err;
+      h->nn_tc = nn_plan_init(&pl) == 0;
     }
   }
   int rc = read_ctl(h);

@@ -16,6 +16,7 @@
 
 #include "../../include/filament_gb.h"
 #include "launch.h"
+#include "nn_tc.h"
 #include "surrogate.cuh"
 
 struct fil_nn {
@@ -26,6 +27,8 @@ struct fil_nn {
   float* g = nullptr;   // gradients
   __nv_bfloat16* wf[NN_LAYERS] = {};   // [ci][k][co]
   __nv_bfloat16* wb[NN_LAYERS] = {};   // [co][k][ci], k flipped
+  __nv_bfloat16* wt[NN_LAYERS] = {};   // [k][co][ci], layers 1 and 2 (tensor cores)
+  CUtensorMap wmap[NN_LAYERS];         // TMA maps over wt
   __nv_bfloat16* act[NN_LAYERS] = {};   // x0, y0, y1, y2: [B][C][T]
   float* out = nullptr;                 // [B][T]
   float* gr[2] = {};    // FP32 gradients of the activations [B][64][T]
@@ -58,7 +61,7 @@ static int nn_fail(fil_nn* n, int code, const std::string& m) {
 static int nn_pack(fil_nn* n) {
   for (int l = 0; l < NN_LAYERS; ++l) {
     const int w = nn_wsize(l);
-    k_nn_pack<<<(w + 255) / 256, 256, 0, n->st>>>(n->p, n->wf[l], n->wb[l], l);
+    k_nn_pack<<<(w + 255) / 256, 256, 0, n->st>>>(n->p, n->wf[l], n->wb[l], n->wt[l], l);
     NK(cudaGetLastError());
   }
   return 0;
@@ -106,6 +109,19 @@ int nn_forward_dev(const fil_nn* n, const __nv_bfloat16* x0, __nv_bfloat16* a1, 
 }
 
 int nn_time_points(const fil_nn* n) { return n->T; }
+
+cudaError_t nn_infer(const fil_nn* n, const NnRowsPlan& p, cudaStream_t st) {
+  cudaError_t e = nn_launch_l0_cl(p.x0, n->wf[0], n->p + nn_poff(0) + nn_wsize(0), p.a1, p.T, p.maxrows, p.count,
+                                  p.stop, st);
+  if (e == cudaSuccess)
+    e = nn_launch_conv_tc(p.map_a1, n->wmap[1], n->p + nn_poff(1) + nn_wsize(1), p.a2, p, st);
+  if (e == cudaSuccess)
+    e = nn_launch_conv_tc(p.map_a2, n->wmap[2], n->p + nn_poff(2) + nn_wsize(2), p.a1, p, st);
+  if (e == cudaSuccess)
+    e = nn_launch_l3_cl(p.a1, n->wf[3], n->p + nn_poff(3) + nn_wsize(3), p.out, p.T, p.maxrows, p.count, p.stop,
+                        st);
+  return e;
+}
 
 cudaError_t nn_forward_rows(const fil_nn* n, const void* x0, void* a1, void* a2, float* out, int T, int maxrows,
                             const int* count, const int* stop, cudaStream_t st) {
@@ -160,6 +176,7 @@ static void nn_free(fil_nn* n) {
   for (int l = 0; l < NN_LAYERS; ++l) {
     if (n->wf[l]) cudaFree(n->wf[l]);
     if (n->wb[l]) cudaFree(n->wb[l]);
+    if (n->wt[l]) cudaFree(n->wt[l]);
   }
   for (int l = 0; l < NN_LAYERS; ++l)
     if (n->act[l]) cudaFree(n->act[l]);
@@ -213,6 +230,10 @@ int fil_nn_create(int nt, uint64_t seed, fil_nn** out) {
   for (int l = 0; l < NN_LAYERS && !rc; ++l) {
     rc = mk((void**)&n->wf[l], nn_wsize(l) * sizeof(__nv_bfloat16));
     if (!rc) rc = mk((void**)&n->wb[l], nn_wsize(l) * sizeof(__nv_bfloat16));
+    if (!rc && (l == 1 || l == 2)) {
+      rc = mk((void**)&n->wt[l], nn_wsize(l) * sizeof(__nv_bfloat16));
+      if (!rc && nn_weight_map(&n->wmap[l], n->wt[l])) rc = nn_fail(n, FIL_ERR_CUDA, "weight tensor map");
+    }
   }
   if (rc) {
     nn_free(n);
@@ -285,6 +306,47 @@ int fil_nn_forward(fil_nn* n, const float* feat, int b, float* out) {
   NK(cudaMemcpyAsync(out, n->out, bt * sizeof(float), cudaMemcpyDeviceToHost, n->st));
   NK(cudaFreeAsync(df, n->st));
   NK(cudaStreamSynchronize(n->st));
+  return FIL_OK;
+}
+
+// The inference path the simulation runs (tensor-core layers 1 and 2,
+// channel-last activations) on host features; nt a multiple of 128.
+int fil_nn_infer(fil_nn* n, const float* feat, int b, float* out) {
+  if (!n || !feat || !out || b < 1) return nn_fail(n, FIL_ERR_ARG, "bad argument");
+  if (n->T % 128) return nn_fail(n, FIL_ERR_UNSUPPORTED, "tensor-core inference needs nt a multiple of 128");
+  const size_t bt = (size_t)b * n->T;
+  float* df = nullptr;
+  NnRowsPlan pl;
+  std::memset(&pl, 0, sizeof pl);
+  void* buf = nullptr;
+  const size_t bytes = bt * NN_IN * 2 + 2 * bt * 64 * 2 + bt * sizeof(float) + 256;
+  NK(cudaMallocAsync(&buf, bytes, n->st));
+  NK(cudaMallocAsync((void**)&df, bt * NN_IN * sizeof(float), n->st));
+  uint8_t* q = (uint8_t*)buf;
+  pl.a1 = (__nv_bfloat16*)q;
+  pl.a2 = pl.a1 + bt * 64;
+  pl.out = (float*)(pl.a2 + bt * 64);
+  __nv_bfloat16* x0 = (__nv_bfloat16*)(pl.out + bt);
+  pl.x0 = x0;
+  pl.err = (int*)(x0 + bt * NN_IN + 64);
+  pl.T = n->T;
+  pl.maxrows = b;
+  if (nn_plan_init(&pl)) {
+    cudaFreeAsync(df, n->st);
+    cudaFreeAsync(buf, n->st);
+    return nn_fail(n, FIL_ERR_CUDA, "tensor map of the activations");
+  }
+  NK(cudaMemsetAsync(pl.err, 0, sizeof(int), n->st));
+  NK(cudaMemcpyAsync(df, feat, bt * NN_IN * sizeof(float), cudaMemcpyHostToDevice, n->st));
+  k_nn_gather<<<(unsigned)((bt * NN_IN + 255) / 256), 256, 0, n->st>>>(df, nullptr, x0, b, n->T);
+  NK(nn_infer(n, pl, n->st));
+  int e = 0;
+  NK(cudaMemcpyAsync(out, pl.out, bt * sizeof(float), cudaMemcpyDeviceToHost, n->st));
+  NK(cudaMemcpyAsync(&e, pl.err, sizeof(int), cudaMemcpyDeviceToHost, n->st));
+  NK(cudaFreeAsync(df, n->st));
+  NK(cudaFreeAsync(buf, n->st));
+  NK(cudaStreamSynchronize(n->st));
+  if (e) return nn_fail(n, FIL_ERR_TIMEOUT, "a tensor-core pipeline wait timed out");
   return FIL_OK;
 }
 

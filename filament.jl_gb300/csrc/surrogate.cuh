@@ -186,7 +186,9 @@ __global__ void k_nn_adam(float* p, float* m, float* v, const float* g, int n, N
   v[i] = vi;
   p[i] -= a.lr * (mi / a.c1) / (sqrtf(vi / a.c2) + a.eps);
 }
-__global__ void k_nn_pack(const float* __restrict__ p, __nv_bfloat16* wf, __nv_bfloat16* wb, int l) {
+// wt (optional): the tensor-core layout [k][co][ci] of the 64 -> 64 layers
+__global__ void k_nn_pack(const float* __restrict__ p, __nv_bfloat16* wf, __nv_bfloat16* wb, __nv_bfloat16* wt,
+                          int l) {
   const int ci_n = nn_ci(l), co_n = nn_co(l), n = co_n * ci_n * NN_K;
   const int i = blockIdx.x * 256 + threadIdx.x;
   if (i >= n) return;
@@ -194,4 +196,5 @@ __global__ void k_nn_pack(const float* __restrict__ p, __nv_bfloat16* wf, __nv_b
   const __nv_bfloat16 v = __float2bfloat16_rn(p[nn_poff(l) + i]);
   wf[((size_t)ci * NN_K + k) * co_n + co] = v;
   wb[((size_t)co * NN_K + (NN_K - 1 - k)) * ci_n + ci] = v;
+  if (wt) wt[((size_t)k * co_n + co) * ci_n + ci] = v;
 }

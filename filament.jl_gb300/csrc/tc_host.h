@@ -39,3 +39,25 @@ static inline int tc_make_map(CUtensorMap* m, const void* base, int elem, unsign
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : (int)r;
 }
+
+// BF16 tensor of rank 2 or 3 (dims[0] contiguous, dims[i] elements, packed
+// rows), box `box`; 128-byte swizzle (the box row must be 128 B); elements
+// outside the tensor read as zero.  Returns 0 on success.
+static inline int tc_make_map_bf16(CUtensorMap* m, const void* base, int rank, const unsigned long long* dims,
+                                   const unsigned* box) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = tc_encode_fn();
+  if (!fn) return -1;
+  if (rank < 2 || rank > 3 || box[0] * 2 != 128) return -2;
+  cuuint64_t d[3], s[2];
+  cuuint32_t b[3], es[3] = {1, 1, 1};
+  for (int i = 0; i < rank; ++i) {
+    d[i] = dims[i];
+    b[i] = box[i];
+  }
+  s[0] = dims[0] * 2ull;
+  if (rank == 3) s[1] = dims[0] * dims[1] * 2ull;
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void*>(base), d, s, b, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : (int)r;
+}

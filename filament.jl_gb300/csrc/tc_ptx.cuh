@@ -57,6 +57,14 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
 // ---- tensor memory ------------------------------------------------------------
 // executed by all 32 threads of one warp
 __device__ __forceinline__ void tmem_alloc(uint32_t slot_smem, uint32_t ncols) {
@@ -179,6 +187,11 @@ __device__ __forceinline__ uint64_t desc_k64(uint32_t saddr) {
 // Instruction descriptor, kind::f16: D f32, A/B f16, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
   return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// Instruction descriptor, kind::f16 with BF16 operands: D f32, A/B bf16,
+// both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 // Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {

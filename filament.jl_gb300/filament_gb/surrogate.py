@@ -36,6 +36,7 @@ def _bind(b):
             ("fil_nn_get_params", C.c_int, [vp, _fp]),
             ("fil_nn_set_params", C.c_int, [vp, _fp]),
             ("fil_nn_forward", C.c_int, [vp, _fp, C.c_int, _fp]),
+            ("fil_nn_infer", C.c_int, [vp, _fp, C.c_int, _fp]),
             ("fil_nn_grad", C.c_int, [vp, _fp, _fp, _fp, C.c_int, _fp, _fp]),
             ("fil_nn_train", C.c_int, [vp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_float,
                                        C.c_uint64, _fp]),
@@ -277,6 +278,14 @@ class Surrogate:
         feat = _f32(feat, (-1, 3, self.nt))
         out = np.empty((feat.shape[0], self.nt), dtype=np.float32)
         self._chk(self.L.fil_nn_forward(self.h, _p(feat), feat.shape[0], _p(out)), "forward")
+        return out
+
+    def infer(self, feat):
+        """The simulation's inference path (tensor-core layers); nt a
+        multiple of 128."""
+        feat = _f32(feat, (-1, 3, self.nt))
+        out = np.empty((feat.shape[0], self.nt), dtype=np.float32)
+        self._chk(self.L.fil_nn_infer(self.h, _p(feat), feat.shape[0], _p(out)), "infer")
         return out
 
     def grad(self, feat, target, mask):

@@ -299,6 +299,9 @@ int fil_nn_destroy(fil_nn* n);
 int fil_nn_get_params(fil_nn* n, float* params);        /* fil_nn_nparams() FP32 */
 int fil_nn_set_params(fil_nn* n, const float* params);
 int fil_nn_forward(fil_nn* n, const float* feat, int rows, float* out);   /* out [rows][nt] */
+/* the same network through the inference kernels the simulation runs (the
+ * 64 -> 64 layers as tcgen05 implicit GEMMs); nt a multiple of 128          */
+int fil_nn_infer(fil_nn* n, const float* feat, int rows, float* out);
 /* loss = sum m (out - target)^2 / sum m (m: the point weights) and its
  * gradient                                                                 */
 int fil_nn_grad(fil_nn* n, const float* feat, const float* target, const float* mask, int rows,

@@ -62,6 +62,30 @@ def test_gradient_matches_reference(gpu_lib):
         o += n
 
 
+def test_tensor_core_inference_matches_reference(gpu_lib):
+    """The simulation's inference path (channel-last activations, the
+    64 -> 64 layers as tcgen05 implicit GEMMs with TMA-loaded taps) against
+    the CPU reference and the CUDA-core forward pass, including the
+    zero padding at both ends of a row and several 128-point tiles."""
+    import surrogate_ref as sr
+    from filament_gb.surrogate import Surrogate
+    T = 512
+    rng = np.random.default_rng(4)
+    net = Surrogate(T, seed=13)
+    p = net.get_params()
+    o3 = sum(co * ci * sr.K + co for ci, co in zip(sr.CI[:3], sr.CO[:3]))
+    p[o3:] *= 30.0   # output layer at the scale of a trained one
+    p[:o3] += rng.uniform(-0.05, 0.05, o3).astype(np.float32)
+    net.set_params(p)
+    f = _random_rows(rng, 5, T)
+    out = net.infer(f)
+    ref = sr.forward(p, f)[-1][:, 0, :]
+    simt = net.forward(f)
+    assert rel_l2(out, ref) < 2e-3
+    assert rel_l2(out, simt) < 2e-3
+    assert np.max(np.abs(out - ref)) < 2e-2 * np.max(np.abs(ref))
+
+
 def test_set_params_round_trip(gpu_lib):
     from filament_gb.surrogate import Surrogate
     net = Surrogate(64, seed=3)
