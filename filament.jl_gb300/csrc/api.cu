@@ -68,7 +68,8 @@ struct fil_handle {
   int bugcompat = 0, clamp_last = 0, timing = 0;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev[8];
-  double tsum[5] = {0, 0, 0, 0, 0};   // row, dht fwd, dht inv, reduce+control, whole step
+  double tsum[6] = {0, 0, 0, 0, 0, 0};   // row (with the surrogate), dht fwd, dht inv, reduce+control,
+                                         // whole step, surrogate network
   long tcount = 0;
   void* flushbuf = nullptr;            // > L2, benchmark timing only
   size_t flushbytes = 0;
@@ -96,6 +97,8 @@ struct fil_handle {
   int* nn_err = nullptr;       // tensor-core inference: a wait timed out
   NnRowsPlan nn_plan;          // tensor-core inference over the buffers above
   bool nn_tc = false;          // nt is a multiple of 128: tensor-core path
+  int nn_every = 1;
+  double nn_tol = 0;
 };
 
 void fil_set_global_error(const std::string& m) { g_err = m; }
@@ -554,6 +557,7 @@ template <typename R> static int enqueue_zstep_xyt(fil_handle* h, bool timed) {
   P.S_out = (C*)h->W1;
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
   CK(enqueue_surrogate<R>(h, P));
+  if (timed) CK(cudaEventRecord(h->ev[5], h->st));
   CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
   if (timed) CK(cudaEventRecord(h->ev[2], h->st));
   const int nx = h->n1, ny = h->n2, nh = h->nh;
@@ -670,6 +674,7 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   }
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
   CK(enqueue_surrogate<R>(h, P));
+  if (timed) CK(cudaEventRecord(h->ev[5], h->st));
   CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
   if (timed) CK(cudaEventRecord(h->ev[2], h->st));
   if (tcp) {
@@ -729,6 +734,20 @@ static int zstep(fil_handle* h, bool timed) {
 }
 static int reduce(fil_handle* h, double* power, int check_done) {
   return h->fp64 ? enqueue_reduce<double>(h, power, check_done) : enqueue_reduce<float>(h, power, check_done);
+}
+
+// surrogate fields of a control block: armed (with fresh counters) when the
+// handle holds a network
+static void arm_surrogate(const fil_handle* h, DevCtl& c) {
+  c.nn_on = h->nn ? 1 : 0;
+  c.nn_use = 1;
+  c.nn_judge = 0;
+  c.nn_every = h->nn ? h->nn_every : 1;
+  c.nn_tol = h->nn ? h->nn_tol : 0;
+  c.nn_count = c.nn_rows = 0;
+  c.nn_steps = c.nn_used = c.nn_judged = c.nn_rejected = 0;
+  c.nn_diff_acc = 0;
+  c.nn_err = c.nn_err_max = c.nn_rows_sum = 0;
 }
 
 static int check_tc(fil_handle* h) {
@@ -816,10 +835,12 @@ template <typename R> static int set_field_t(fil_handle* h, const void* E, int d
   }
   CK(cudaMemcpyAsync(h->stage, rows.data(), rows.size() * sizeof(R), cudaMemcpyHostToDevice, h->st));
   CK(launch_field_in<R>((const C*)h->stage, (C*)h->S, h->nh, (const C*)h->tw, analytic, h->nrows, h->nt, h->st));
-  // control block: fresh simulation, no pending guard
+  // control block: fresh simulation, no pending guard; an armed surrogate
+  // stays armed with fresh counters
   DevCtl c;
   std::memset(&c, 0, sizeof c);
   c.first = 1;
+  arm_surrogate(h, c);
   CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
   CK(cudaMemsetAsync(h->rho_end, 0, h->nrows * sizeof(double), h->st));
   if (h->cfg.plasma) {   // Models.jl:66: plasma solved on the initial field
@@ -980,7 +1001,7 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
     h->clamp_last = value != 0;
   } else if (option == FIL_OPT_TIMING) {
     h->timing = value != 0;
-    for (int i = 0; i < 5; ++i) h->tsum[i] = 0;
+    for (int i = 0; i < 6; ++i) h->tsum[i] = 0;
     h->tcount = 0;
   } else if (option == FIL_OPT_DHT_SIMT) {
     if (!h->fp64) h->use_tc = (value == 0) && h->MA1[0] != nullptr;
@@ -1116,6 +1137,11 @@ int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stat
       h->tsum[2] += t[3];
       h->tsum[3] += t[0];
       h->tsum[4] += tot;
+      if (h->geom == FIL_GEOM_RT || h->geom == FIL_GEOM_T || h->geom == FIL_GEOM_XYT) {
+        float tn;
+        CK(cudaEventElapsedTime(&tn, h->ev[1], h->ev[5]));
+        h->tsum[5] += tn;
+      }
       h->tcount += 1;
     }
   } else {
@@ -1247,19 +1273,13 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
   }
   int rc = read_ctl(h);
   if (rc) return rc;
+  h->nn = nn;
+  h->nn_every = every;
+  h->nn_tol = tol;
   DevCtl c = *h->ctl_host;
-  c.nn_on = nn ? 1 : 0;
-  c.nn_use = 1;
-  c.nn_judge = 0;
-  c.nn_every = nn ? every : 1;
-  c.nn_tol = nn ? tol : 0;
-  c.nn_count = c.nn_rows = 0;
-  c.nn_steps = c.nn_used = c.nn_judged = c.nn_rejected = 0;
-  c.nn_diff_acc = 0;
-  c.nn_err = c.nn_err_max = c.nn_rows_sum = 0;
+  arm_surrogate(h, c);
   CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
   CK(cudaStreamSynchronize(h->st));
-  h->nn = nn;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -1282,6 +1302,7 @@ int fil_get_surrogate_stats(fil_handle* h, double* out, int n) {
 int fil_kernel_times(fil_handle* h, double* ms, int n) {
   if (!h || !ms) return fail(h, FIL_ERR_ARG, "null argument");
   for (int i = 0; i < n; ++i) ms[i] = (i < 5 && h->tcount) ? h->tsum[i] / h->tcount : 0.0;
+  if (n > 6) ms[6] = h->tcount ? h->tsum[5] / h->tcount : 0.0;
   if (n > 5) ms[5] = (double)h->tcount;
   return FIL_OK;
 }

@@ -250,8 +250,10 @@ int fil_get_stats(fil_handle* h, fil_stats* st);
 
 /* Average device time per step of each kernel family over the timed steps
  * since FIL_OPT_TIMING was set, in ms: 0 row kernel (plasma + nonlinear
- * step), 1 forward transverse transform + propagator, 2 inverse transform,
- * 3 reductions + controller, 4 whole step; ms[5] = number of timed steps. */
+ * step, with the surrogate network when armed), 1 forward transverse
+ * transform + propagator, 2 inverse transform, 3 reductions + controller,
+ * 4 whole step; ms[5] = number of timed steps; ms[6] = the surrogate
+ * network's part of ms[0].                                                  */
 int fil_kernel_times(fil_handle* h, double* ms, int n);
 
 /* ---- linear propagator without device allocation ----------------------------
@@ -318,7 +320,8 @@ int fil_nn_train(fil_nn* n, const float* feat, const float* target, const float*
  * |rho_net - rho_ode| / max rho_ode is measured; the network is used on the
  * following steps only while that error is at most `tol` (the ODE takes
  * over otherwise, until a later check passes).  fil_step always solves the
- * ODE.  nn = NULL disarms.  The network must stay alive while armed.       */
+ * ODE; fil_set_field keeps the handle armed with fresh counters.  nn = NULL
+ * disarms.  The network must stay alive while armed.                      */
 int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol);
 /* out[0..n): armed, in use, steps since armed, steps that used the network,
  * checks, failed checks, last error, largest error, mean rows per step
