@@ -119,7 +119,16 @@ def _prepare(**over):
     return fg.prepare(DECK, **kw)
 
 
-def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, simt_dht=False, net=None):
+def _profiler(on):
+    """cuProfilerStart / cuProfilerStop (driver API): with
+    `ncu --profile-from-start off` only the launches in between are
+    captured."""
+    import ctypes
+    lib = ctypes.CDLL("libcuda.so.1")
+    (lib.cuProfilerStart if on else lib.cuProfilerStop)()
+
+
+def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, simt_dht=False, net=None, profile=False):
     """Warm-up steps in graph mode, then the timed steps from z = 0 (the
     field re-uploaded) up to `steps` steps or z = zend, one at a time with L2
     flushed, then the same range in graph mode (warm L2, for information);
@@ -137,9 +146,13 @@ def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, simt_dht=
     h.run(0.0, zend, warmup)
     h.set_field(sim.field.E0, analytic=False)
     h.set_option(_abi.OPT_TIMING, 1)
+    if profile:
+        _profiler(True)
     t0 = time.perf_counter()
     code, st2 = h.run(0.0, zend, steps)
     wall = time.perf_counter() - t0
+    if profile:
+        _profiler(False)
     kt = h.kernel_times(7)
     sstats = None
     if net is not None:
@@ -393,6 +406,8 @@ def main():
     ap.add_argument("--no-xyt", action="store_true", help="skip the 512^3 XYT measurement")
     ap.add_argument("--xyt-steps", type=int, default=10)
     ap.add_argument("--train-iters", type=int, default=3000, help="Adam iterations of the surrogate")
+    ap.add_argument("--profile", action="store_true",
+                    help="only the headline form's timed steps, between cuProfilerStart/Stop (for ncu)")
     args = ap.parse_args()
     rank, local_rank, world = _env_rank()
     if world > 1:
@@ -426,6 +441,12 @@ def main():
     _b.build()
     # the surrogate is trained before any timed region
     net, train_info = surrogate_train(iters=args.train_iters)
+    if args.profile:
+        r = time_device_loop("mixed", args.warmup, args.steps, args.accuracy_zend, net=net, profile=True)
+        print(json.dumps({"profile": "mixed_surrogate", "timed_steps": r["timed_steps"],
+                          "ms_per_step": r["ms_per_step"], "surrogate_ms": r["surrogate_ms"],
+                          "surrogate_stats": r["surrogate_stats"], "training": train_info}))
+        return
     sampler = ClockSampler(0)
     if dist is not None:
         dist.barrier()
