@@ -92,7 +92,7 @@ struct fil_handle {
   void* nn_feat = nullptr;     // [nrows][3][nt] BF16
   void* nn_a1 = nullptr;       // [nrows][64][nt] BF16
   void* nn_a2 = nullptr;
-  float* nn_out = nullptr;     // [nrows][nt]
+  float* nn_out = nullptr;     // [nrows][nt] network output, or [nrows][9][nt] layer-3 partial sums
   int* nn_slot = nullptr;      // [nrows]
   int* nn_err = nullptr;       // tensor-core inference: a wait timed out
   NnRowsPlan nn_plan;          // tensor-core inference over the buffers above
@@ -541,7 +541,11 @@ template <typename R> static cudaError_t enqueue_surrogate(fil_handle* h, RowPar
   if (!h->nn) return cudaSuccess;
   P.nn_slot = h->nn_slot;
   P.nn_out = h->nn_out;
-  if (h->nn_tc) return nn_infer(h->nn, h->nn_plan, h->st);
+  if (h->nn_tc) {
+    P.nn_part = 1;
+    P.nn_b3 = nn_out_bias(h->nn);
+    return nn_infer(h->nn, h->nn_plan, h->st);
+  }
   return nn_forward_rows(h->nn, h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nt, h->nrows, &h->ctl->nn_rows,
                          &h->ctl->done, h->st);
 }
@@ -1252,7 +1256,7 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
       CK(cudaMalloc(&h->nn_feat, rt * 3 * 2));
       CK(cudaMalloc(&h->nn_a1, rt * 64 * 2));
       CK(cudaMalloc(&h->nn_a2, rt * 64 * 2));
-      CK(cudaMalloc((void**)&h->nn_out, rt * sizeof(float)));
+      CK(cudaMalloc((void**)&h->nn_out, rt * NN_K * sizeof(float)));
       CK(cudaMalloc((void**)&h->nn_slot, (size_t)h->nrows * sizeof(int)));
       CK(cudaMemset(h->nn_slot, 0xff, (size_t)h->nrows * sizeof(int)));
       CK(cudaMalloc((void**)&h->nn_err, sizeof(int)));
@@ -1262,7 +1266,7 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
       pl.x0 = (const __nv_bfloat16*)h->nn_feat;
       pl.a1 = (__nv_bfloat16*)h->nn_a1;
       pl.a2 = (__nv_bfloat16*)h->nn_a2;
-      pl.out = h->nn_out;
+      pl.part = h->nn_out;
       pl.T = h->nt;
       pl.maxrows = h->nrows;
       pl.count = &h->ctl->nn_rows;

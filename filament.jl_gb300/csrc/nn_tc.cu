@@ -33,7 +33,7 @@
 #include "tc_ptx.cuh"
 
 #define NT_BM 128                      // time points per tile
-#define NT_STAGES 4
+#define NT_STAGES 8
 #define NT_A_BYTES (NT_BM * 128)       // one tap's activation tile
 #define NT_W_BYTES (64 * 128)          // one tap's weights
 #define NT_W_OFF 0
@@ -54,20 +54,36 @@ static __device__ __forceinline__ bool nt_wait(uint32_t bar, uint32_t parity, vo
 static __device__ __forceinline__ void nt_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
+// hardware tanh (tanh.approx.f32, relative error about 2^-11, below the
+// BF16 rounding of the activations it feeds)
+static __device__ __forceinline__ float nt_tanh(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 
 struct NtParams {
   const float* bias;       // [64]
-  __nv_bfloat16* out;      // [rows][T][64]
+  __nv_bfloat16* out;      // [rows][T][64] (layer 1)
+  const __nv_bfloat16* w3; // layer 3 weights [ci][k] (FINAL)
+  float* part;             // [rows][9][T] layer-3 partial sums (FINAL)
   int T, tiles_per_row, maxrows;
   const int* count;
   const int* stop;
   int* err;
 };
 
+// FINAL (layer 2): the epilogue applies layer 3 to its own point instead of
+// storing the activations: P_k[t] = sum_ci w3[ci][k] y[t][ci] for the nine
+// taps k (the BF16-rounded activations, as stored between layers), so that
+// out[t] = b3 + sum_k P_k[t + k - 4] (nn_out_at).
+template <bool FINAL>
 __global__ void __launch_bounds__(NT_THREADS, 1)
     k_nn_conv_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap tw, NtParams p) {
   extern __shared__ __align__(1024) uint8_t nt_smem[];
   __shared__ volatile int s_fail;
+  __shared__ __align__(16) float s_bias[64];
+  __shared__ __align__(16) float s_w3[FINAL ? NN_K * 64 : 4];   // [k][ci]
   if (p.stop && *p.stop) return;
   const int nrows = p.count ? min(*p.count, p.maxrows) : p.maxrows;
   const int ntiles = nrows * p.tiles_per_row;
@@ -86,6 +102,9 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
   volatile uint32_t* tmem_slot_g = reinterpret_cast<volatile uint32_t*>(gbase + NT_BAR_OFF + 112);
 
   if (tid == 0) s_fail = 0;
+  if (tid < 64) s_bias[tid] = p.bias[tid];
+  if (FINAL)
+    for (int i = tid; i < NN_K * 64; i += NT_THREADS) s_w3[(i % NN_K) * 64 + i / NN_K] = __bfloat162float(p.w3[i]);
   if (warp == 0) tc::tmem_alloc(tmem_slot, 128);
   if (tid == 0) {
     for (int s = 0; s < NT_STAGES; ++s) {
@@ -175,17 +194,53 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
       __syncwarp();
       if (lane == 0) nt_arrive(acce_bar(buf));
       const int b = tile / tpr, t = (tile - b * tpr) * NT_BM + 32 * warp + lane;
-      if (t < p.T) {
+      if (FINAL && t < p.T) {
+        float y[64];
+        const float4* bv = reinterpret_cast<const float4*>(s_bias);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const float4 bq = bv[q];
+          const float bb[4] = {bq.x, bq.y, bq.z, bq.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int c = 4 * q + e;
+            const float v = __uint_as_float(c < 32 ? r0[c] : r1[c - 32]) + bb[e];
+            y[c] = __bfloat162float(__float2bfloat16_rn(nt_tanh(v)));
+          }
+        }
+        float* dst = p.part + (size_t)b * NN_K * p.T + t;
+#pragma unroll
+        for (int k = 0; k < NN_K; ++k) {
+          const float4* wk = reinterpret_cast<const float4*>(s_w3 + 64 * k);
+          float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+          for (int q = 0; q < 16; q += 2) {
+            const float4 u = wk[q], v = wk[q + 1];
+            a0 = fmaf(u.x, y[4 * q], a0);
+            a0 = fmaf(u.y, y[4 * q + 1], a0);
+            a0 = fmaf(u.z, y[4 * q + 2], a0);
+            a0 = fmaf(u.w, y[4 * q + 3], a0);
+            a1 = fmaf(v.x, y[4 * q + 4], a1);
+            a1 = fmaf(v.y, y[4 * q + 5], a1);
+            a1 = fmaf(v.z, y[4 * q + 6], a1);
+            a1 = fmaf(v.w, y[4 * q + 7], a1);
+          }
+          dst[(size_t)k * p.T] = a0 + a1;
+        }
+      } else if (t < p.T) {
         uint4* dst = reinterpret_cast<uint4*>(p.out + ((size_t)b * p.T + t) * 64);
+        const float4* bv = reinterpret_cast<const float4*>(s_bias);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
+          const float4 b0 = bv[2 * q], b1 = bv[2 * q + 1];
+          const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
           uint32_t pk[4];
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             const int c = 8 * q + 2 * e;
-            const float v0 = __uint_as_float(c < 32 ? r0[c] : r1[c - 32]) + __ldg(&p.bias[c]);
-            const float v1 = __uint_as_float(c + 1 < 32 ? r0[c + 1] : r1[c + 1 - 32]) + __ldg(&p.bias[c + 1]);
-            const __nv_bfloat162 h = __floats2bfloat162_rn(tanhf(v0), tanhf(v1));
+            const float v0 = __uint_as_float(c < 32 ? r0[c] : r1[c - 32]) + bb[2 * e];
+            const float v1 = __uint_as_float(c + 1 < 32 ? r0[c + 1] : r1[c + 1 - 32]) + bb[2 * e + 1];
+            const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(v0), nt_tanh(v1));
             pk[e] = *reinterpret_cast<const uint32_t*>(&h);
           }
           dst[q] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
@@ -203,95 +258,75 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
-// Layer 0 (3 -> 64, tanh): x [rows][3][T] -> y [rows][T][64].  Block: 32 time
-// points x 8 channel groups of 8; rows b = blockIdx.y, + gridDim.y, ...
-__global__ void __launch_bounds__(256) k_nn_l0_cl(const __nv_bfloat16* __restrict__ x,
+// Layer 0 (3 -> 64, tanh): x [rows][3][T] -> y [rows][T][64].  One thread
+// per time point (128 per block) computes all 64 channels: its 27 inputs in
+// registers, the weights broadcast from shared memory as float4 (four FMA
+// per shared load); rows b = blockIdx.y, + gridDim.y, ...
+__global__ void __launch_bounds__(128) k_nn_l0_cl(const __nv_bfloat16* __restrict__ x,
                                                   const __nv_bfloat16* __restrict__ w,   // [ci][k][co]
                                                   const float* __restrict__ bias, __nv_bfloat16* y, int T,
                                                   int maxrows, const int* count, const int* stop) {
-  constexpr int TT = 32, W2 = TT + NN_K - 1;
+  constexpr int TT = 128, W2 = TT + NN_K - 1, NI = NN_IN * NN_K;
   __shared__ float xs[NN_IN][W2];
-  __shared__ float ws[NN_IN * NN_K][64];
+  __shared__ __align__(16) float ws[NI][64];
+  __shared__ __align__(16) float bs[64];
   if (stop && *stop) return;
   const int nb = count ? min(*count, maxrows) : maxrows;
-  const int tid = threadIdx.x, tl = tid & 31, cg = tid >> 5;
-  for (int i = tid; i < NN_IN * NN_K * 64; i += 256) ws[i / 64][i % 64] = __bfloat162float(w[i]);
-  const int t0 = blockIdx.x * TT;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < NI * 64; i += TT) ws[i / 64][i % 64] = __bfloat162float(w[i]);
+  if (tid < 64) bs[tid] = bias[tid];
+  const int t0 = blockIdx.x * TT, t = t0 + tid;
   for (int b = blockIdx.y; b < nb; b += gridDim.y) {
     __syncthreads();
-    for (int i = tid; i < NN_IN * W2; i += 256) {
-      const int ci = i / W2, j = i - ci * W2, t = t0 + j - NN_HALF;
-      xs[ci][j] = (t >= 0 && t < T) ? __bfloat162float(x[((size_t)b * NN_IN + ci) * T + t]) : 0.f;
+    for (int i = tid; i < NN_IN * W2; i += TT) {
+      const int ci = i / W2, j = i - ci * W2, tt = t0 + j - NN_HALF;
+      xs[ci][j] = (tt >= 0 && tt < T) ? __bfloat162float(x[((size_t)b * NN_IN + ci) * T + tt]) : 0.f;
     }
     __syncthreads();
-    float acc[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) acc[c] = bias[8 * cg + c];
+    float xv[NI];
 #pragma unroll
     for (int ci = 0; ci < NN_IN; ++ci)
 #pragma unroll
-      for (int k = 0; k < NN_K; ++k) {
-        const float xv = xs[ci][tl + k];
+      for (int k = 0; k < NN_K; ++k) xv[ci * NN_K + k] = xs[ci][tid + k];
+    uint4* dst = reinterpret_cast<uint4*>(y + ((size_t)b * T + t) * 64);
+#pragma unroll 1
+    for (int g = 0; g < 8; ++g) {
+      const float4 c0 = reinterpret_cast<const float4*>(bs)[2 * g], c1 = reinterpret_cast<const float4*>(bs)[2 * g + 1];
+      float acc[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
 #pragma unroll
-        for (int c = 0; c < 8; ++c) acc[c] = fmaf(ws[ci * NN_K + k][8 * cg + c], xv, acc[c]);
+      for (int i = 0; i < NI; ++i) {
+        const float4 w0 = reinterpret_cast<const float4*>(ws[i])[2 * g];
+        const float4 w1 = reinterpret_cast<const float4*>(ws[i])[2 * g + 1];
+        acc[0] = fmaf(w0.x, xv[i], acc[0]);
+        acc[1] = fmaf(w0.y, xv[i], acc[1]);
+        acc[2] = fmaf(w0.z, xv[i], acc[2]);
+        acc[3] = fmaf(w0.w, xv[i], acc[3]);
+        acc[4] = fmaf(w1.x, xv[i], acc[4]);
+        acc[5] = fmaf(w1.y, xv[i], acc[5]);
+        acc[6] = fmaf(w1.z, xv[i], acc[6]);
+        acc[7] = fmaf(w1.w, xv[i], acc[7]);
       }
-    const int t = t0 + tl;
-    if (t < T) {
-      uint32_t pk[4];
+      if (t < T) {
+        uint32_t pk[4];
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const __nv_bfloat162 h = __floats2bfloat162_rn(tanhf(acc[2 * e]), tanhf(acc[2 * e + 1]));
-        pk[e] = *reinterpret_cast<const uint32_t*>(&h);
+        for (int e = 0; e < 4; ++e) {
+          const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(acc[2 * e]), nt_tanh(acc[2 * e + 1]));
+          pk[e] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        dst[g] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
-      *reinterpret_cast<uint4*>(y + ((size_t)b * T + t) * 64 + 8 * cg) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
     }
   }
 }
 
-// Layer 3 (64 -> 1, no activation): y [rows][T][64] -> out [rows][T] (FP32).
-// Block: 128 time points; the tile with its halo is staged in shared memory
-// with a row pitch of 33 words (conflict-free column reads).
-__global__ void __launch_bounds__(128) k_nn_l3_cl(const __nv_bfloat16* __restrict__ y,
-                                                  const __nv_bfloat16* __restrict__ w,   // [ci][k]
-                                                  const float* __restrict__ bias, float* out, int T, int maxrows,
-                                                  const int* count, const int* stop) {
-  constexpr int TT = 128, W2 = TT + NN_K - 1, PITCH = 33;
-  __shared__ uint32_t ys[W2 * PITCH];   // bf16 pairs
-  __shared__ float ws[NN_K][64];
-  if (stop && *stop) return;
-  const int nb = count ? min(*count, maxrows) : maxrows;
-  const int tid = threadIdx.x;
-  for (int i = tid; i < 64 * NN_K; i += TT) ws[i % NN_K][i / NN_K] = __bfloat162float(w[i]);
-  const int t0 = blockIdx.x * TT;
-  for (int b = blockIdx.y; b < nb; b += gridDim.y) {
-    __syncthreads();
-    // W2 rows x 32 words, 4 words per 16-byte load
-    for (int i = tid; i < W2 * 8; i += TT) {
-      const int r = i >> 3, q = i & 7, t = t0 + r - NN_HALF;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (t >= 0 && t < T) v = *reinterpret_cast<const uint4*>(y + ((size_t)b * T + t) * 64 + 8 * q);
-      uint32_t* d = ys + r * PITCH + 4 * q;
-      d[0] = v.x;
-      d[1] = v.y;
-      d[2] = v.z;
-      d[3] = v.w;
-    }
-    __syncthreads();
-    float acc = bias[0];
-#pragma unroll
-    for (int k = 0; k < NN_K; ++k) {
-      const uint32_t* row = ys + (tid + k) * PITCH;
-#pragma unroll 8
-      for (int c2 = 0; c2 < 32; ++c2) {
-        const uint32_t u = row[c2];
-        const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&u);
-        acc = fmaf(ws[k][2 * c2], __low2float(h), acc);
-        acc = fmaf(ws[k][2 * c2 + 1], __high2float(h), acc);
-      }
-    }
-    const int t = t0 + tid;
-    if (t < T) out[(size_t)b * T + t] = acc;
-  }
+// Network output from the layer-3 partial sums (the inference path outside
+// the row kernel): out[b][t] = b3 + sum_k P_k[t + k - 4].
+__global__ void __launch_bounds__(256) k_nn_out(const float* __restrict__ part, const float* __restrict__ b3,
+                                                float* out, int T, int rows) {
+  const long i = blockIdx.x * 256L + threadIdx.x;
+  if (i >= (long)rows * T) return;
+  const int b = (int)(i / T), t = (int)(i - (long)b * T);
+  out[i] = nn_out_at(part + (size_t)b * NN_K * T, b3[0], t, T);
 }
 
 // ---------------------------------------------------------------------------
@@ -318,29 +353,32 @@ int nn_weight_map(CUtensorMap* m, const __nv_bfloat16* wt) {
 
 cudaError_t nn_launch_l0_cl(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* y,
                             int T, int maxrows, const int* count, const int* stop, cudaStream_t st) {
-  const int gx = (T + 31) / 32, gy = std::max(1, std::min(maxrows, (152 * 8 + gx - 1) / gx));
-  k_nn_l0_cl<<<dim3(gx, gy), 256, 0, st>>>(x, w, bias, y, T, maxrows, count, stop);
+  const int gx = (T + 127) / 128, gy = std::max(1, std::min(maxrows, (152 * 16 + gx - 1) / gx));
+  k_nn_l0_cl<<<dim3(gx, gy), 128, 0, st>>>(x, w, bias, y, T, maxrows, count, stop);
   return cudaGetLastError();
 }
 
-cudaError_t nn_launch_l3_cl(const __nv_bfloat16* y, const __nv_bfloat16* w, const float* bias, float* out, int T,
-                            int maxrows, const int* count, const int* stop, cudaStream_t st) {
-  const int gx = (T + 127) / 128, gy = std::max(1, std::min(maxrows, (152 * 16 + gx - 1) / gx));
-  k_nn_l3_cl<<<dim3(gx, gy), 128, 0, st>>>(y, w, bias, out, T, maxrows, count, stop);
+cudaError_t nn_launch_out(const float* part, const float* b3, float* out, int T, int rows, cudaStream_t st) {
+  const long n = (long)rows * T;
+  k_nn_out<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, b3, out, T, rows);
   return cudaGetLastError();
 }
 
 cudaError_t nn_launch_conv_tc(const CUtensorMap& tx, const CUtensorMap& tw, const float* bias, __nv_bfloat16* out,
-                              const NnRowsPlan& p, cudaStream_t st) {
+                              const __nv_bfloat16* w3, float* part, const NnRowsPlan& p, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_nn_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_nn_conv_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_nn_conv_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   NtParams q;
   q.bias = bias;
   q.out = out;
+  q.w3 = w3;
+  q.part = part;
   q.T = p.T;
   q.tiles_per_row = p.T / NT_BM;
   q.maxrows = p.maxrows;
@@ -349,6 +387,9 @@ cudaError_t nn_launch_conv_tc(const CUtensorMap& tx, const CUtensorMap& tw, cons
   q.err = p.err;
   const int tiles = p.maxrows * q.tiles_per_row;
   const int grid = std::max(1, std::min(p.sms, tiles));
-  k_nn_conv_tc<<<grid, NT_THREADS, NT_SMEM, st>>>(tx, tw, q);
+  if (part)
+    k_nn_conv_tc<true><<<grid, NT_THREADS, NT_SMEM, st>>>(tx, tw, q);
+  else
+    k_nn_conv_tc<false><<<grid, NT_THREADS, NT_SMEM, st>>>(tx, tw, q);
   return cudaGetLastError();
 }

@@ -11,7 +11,7 @@ struct NnRowsPlan {
   const __nv_bfloat16* x0;   // [rows][3][T] network inputs
   __nv_bfloat16* a1;         // [rows][T][64] hidden activations (channel-last)
   __nv_bfloat16* a2;
-  float* out;                // [rows][T]
+  float* part;               // [rows][9][T] layer-3 partial sums (nn_out_at)
   int T, maxrows;
   const int* count;          // device row count (NULL: maxrows)
   const int* stop;           // device flag: non-zero skips the launches (or NULL)
@@ -29,12 +29,29 @@ int nn_weight_map(CUtensorMap* m, const __nv_bfloat16* wt);
 
 cudaError_t nn_launch_l0_cl(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* y,
                             int T, int maxrows, const int* count, const int* stop, cudaStream_t st);
-cudaError_t nn_launch_l3_cl(const __nv_bfloat16* y, const __nv_bfloat16* w, const float* bias, float* out, int T,
-                            int maxrows, const int* count, const int* stop, cudaStream_t st);
+// layer 1 (part == NULL: activations into out) or layer 2 with layer 3
+// applied in the epilogue (partial sums into part)
 cudaError_t nn_launch_conv_tc(const CUtensorMap& tx, const CUtensorMap& tw, const float* bias, __nv_bfloat16* out,
-                              const NnRowsPlan& p, cudaStream_t st);
+                              const __nv_bfloat16* w3, float* part, const NnRowsPlan& p, cudaStream_t st);
+// out [rows][T] from the partial sums [rows][9][T]
+cudaError_t nn_launch_out(const float* part, const float* b3, float* out, int T, int rows, cudaStream_t st);
+
+// network output at t of one row from its layer-3 partial sums P [9][T]:
+// b3 + sum_k P_k[t + k - 4] (terms outside [0, T) are zero padding)
+__device__ __forceinline__ float nn_out_at(const float* __restrict__ P, float b3, int t, int T) {
+  float s = b3;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int u = t + k - 4;
+    if (u >= 0 && u < T) s += __ldg(&P[(size_t)k * T + u]);
+  }
+  return s;
+}
 
 struct fil_nn;
-// the four layers over the rows of the plan (layer 0 and 3 on CUDA cores,
-// 1 and 2 on the tensor cores); surrogate.cu
+// the network over the rows of the plan: layer 0 on CUDA cores, layers 1
+// and 2 on the tensor cores with layer 3 in layer 2's epilogue, leaving the
+// partial sums in p.part; surrogate.cu
 cudaError_t nn_infer(const fil_nn* n, const NnRowsPlan& p, cudaStream_t st);
+// device pointer to the output layer's bias (the b3 of nn_out_at)
+const float* nn_out_bias(const fil_nn* n);

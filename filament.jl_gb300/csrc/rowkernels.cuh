@@ -13,6 +13,7 @@
 #include "fft.cuh"
 #include "plasma.cuh"
 #include "surrogate_consts.h"
+#include "nn_tc.h"
 
 // Device control block: written by the controller kernel, read by the step
 // kernels (fil_run) or set by the host (fil_step).
@@ -77,10 +78,14 @@ template <typename R> struct RowParams {
   DevCtl* ctl;
   // learned plasma surrogate: network inputs of the flagged rows
   // [slot][2][N] (BF16), slot of each row (-1: not flagged), network output
-  // g(t), the log-amplification of the avalanche term of nn_density [slot][N]
+  // g(t), the log-amplification of the avalanche term of nn_density: [slot][N],
+  // or with nn_part its layer-3 partial sums [slot][9][N] (nn_out_at) and the
+  // output bias at nn_b3
   __nv_bfloat16* nn_feat;
   int* nn_slot;
   const float* nn_out;
+  int nn_part;
+  const float* nn_b3;
 };
 
 template <typename R> FIL_DEV R row_guard(const RowParams<R>& P, int row, int* iy) {
@@ -454,6 +459,7 @@ FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
   R kappa = 0;
 #pragma unroll
   for (int c = 0; c < NC; ++c) kappa += pp.rava_nt[c] * pp.rho_nt[c];
+  const float b3 = P.nn_part ? __ldg(P.nn_b3) : 0.f;
   // quadrature weights of the stage points t_j, t_j + dt/2, t_{j+1}
   R qw[3] = {0, 0, 0};
   for (int st = 0; st < pp.ns; ++st) qw[pp.pidx[st]] += pp.b[st];
@@ -493,7 +499,8 @@ FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
       const C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
       const C em = (R)0.5 * (e0 + e1);
       const R A = qw[0] * e0.x * e0.x + qw[1] * em.x * em.x + qw[2] * e1.x * e1.x;
-      const float gj = fminf(fmaxf(__ldg(&g[j]), NN_G_LO), NN_G_HI);
+      const float gr = P.nn_part ? nn_out_at(g, b3, j, N) : __ldg(&g[j]);
+      const float gj = fminf(fmaxf(gr, NN_G_LO), NN_G_HI);
       w += kappa * A * dt * -expm1(-S) * exp((R)gj);
     }
     S += wb;
@@ -590,15 +597,15 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
       const bool judge = P.nn_out && mode == 0 && ctl->nn_judge;
       Aff<R, 1>* sc1 = reinterpret_cast<Aff<R, 1>*>(ascratch);
       R rmax;
+      const float* gslot = P.nn_out + (size_t)slot * N * (P.nn_part ? NN_K : 1);
       if (nn_row && !judge) {
-        rmax = nn_density<R, N, NC>(P, *tabs, X, P.nn_out + (size_t)slot * N, rho, kdrho, sc1, rscratch, false);
+        rmax = nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, false);
       } else {
         rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag,
                                     mode == 0 ? (R)ctl->rhomax : (R)0, dz, &ych);
         if (judge) {
           // rows not flagged carry rho0 in the surrogate form
-          const R diff = nn_row ? nn_density<R, N, NC>(P, *tabs, X, P.nn_out + (size_t)slot * N, rho, kdrho, sc1,
-                                                       rscratch, true)
+          const R diff = nn_row ? nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, true)
                                 : max(rmax - (R)NC * P.pp.rho0, (R)0);
           if (tid == 0) atomic_max_nonneg(&ctl->nn_diff_acc, (double)diff);
         }

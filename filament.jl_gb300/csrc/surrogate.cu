@@ -114,14 +114,13 @@ cudaError_t nn_infer(const fil_nn* n, const NnRowsPlan& p, cudaStream_t st) {
   cudaError_t e = nn_launch_l0_cl(p.x0, n->wf[0], n->p + nn_poff(0) + nn_wsize(0), p.a1, p.T, p.maxrows, p.count,
                                   p.stop, st);
   if (e == cudaSuccess)
-    e = nn_launch_conv_tc(p.map_a1, n->wmap[1], n->p + nn_poff(1) + nn_wsize(1), p.a2, p, st);
+    e = nn_launch_conv_tc(p.map_a1, n->wmap[1], n->p + nn_poff(1) + nn_wsize(1), p.a2, nullptr, nullptr, p, st);
   if (e == cudaSuccess)
-    e = nn_launch_conv_tc(p.map_a2, n->wmap[2], n->p + nn_poff(2) + nn_wsize(2), p.a1, p, st);
-  if (e == cudaSuccess)
-    e = nn_launch_l3_cl(p.a1, n->wf[3], n->p + nn_poff(3) + nn_wsize(3), p.out, p.T, p.maxrows, p.count, p.stop,
-                        st);
+    e = nn_launch_conv_tc(p.map_a2, n->wmap[2], n->p + nn_poff(2) + nn_wsize(2), nullptr, n->wf[3], p.part, p, st);
   return e;
 }
+
+const float* nn_out_bias(const fil_nn* n) { return n->p + nn_poff(3) + nn_wsize(3); }
 
 cudaError_t nn_forward_rows(const fil_nn* n, const void* x0, void* a1, void* a2, float* out, int T, int maxrows,
                             const int* count, const int* stop, cudaStream_t st) {
@@ -319,14 +318,15 @@ int fil_nn_infer(fil_nn* n, const float* feat, int b, float* out) {
   NnRowsPlan pl;
   std::memset(&pl, 0, sizeof pl);
   void* buf = nullptr;
-  const size_t bytes = bt * NN_IN * 2 + 2 * bt * 64 * 2 + bt * sizeof(float) + 256;
+  const size_t bytes = bt * NN_IN * 2 + 2 * bt * 64 * 2 + 10 * bt * sizeof(float) + 256;
   NK(cudaMallocAsync(&buf, bytes, n->st));
   NK(cudaMallocAsync((void**)&df, bt * NN_IN * sizeof(float), n->st));
   uint8_t* q = (uint8_t*)buf;
   pl.a1 = (__nv_bfloat16*)q;
   pl.a2 = pl.a1 + bt * 64;
-  pl.out = (float*)(pl.a2 + bt * 64);
-  __nv_bfloat16* x0 = (__nv_bfloat16*)(pl.out + bt);
+  pl.part = (float*)(pl.a2 + bt * 64);
+  float* dout = pl.part + 9 * bt;
+  __nv_bfloat16* x0 = (__nv_bfloat16*)(dout + bt);
   pl.x0 = x0;
   pl.err = (int*)(x0 + bt * NN_IN + 64);
   pl.T = n->T;
@@ -340,8 +340,9 @@ int fil_nn_infer(fil_nn* n, const float* feat, int b, float* out) {
   NK(cudaMemcpyAsync(df, feat, bt * NN_IN * sizeof(float), cudaMemcpyHostToDevice, n->st));
   k_nn_gather<<<(unsigned)((bt * NN_IN + 255) / 256), 256, 0, n->st>>>(df, nullptr, x0, b, n->T);
   NK(nn_infer(n, pl, n->st));
+  NK(nn_launch_out(pl.part, nn_out_bias(n), dout, n->T, b, n->st));
   int e = 0;
-  NK(cudaMemcpyAsync(out, pl.out, bt * sizeof(float), cudaMemcpyDeviceToHost, n->st));
+  NK(cudaMemcpyAsync(out, dout, bt * sizeof(float), cudaMemcpyDeviceToHost, n->st));
   NK(cudaMemcpyAsync(&e, pl.err, sizeof(int), cudaMemcpyDeviceToHost, n->st));
   NK(cudaFreeAsync(df, n->st));
   NK(cudaFreeAsync(buf, n->st));
