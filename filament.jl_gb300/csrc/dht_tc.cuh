@@ -56,6 +56,9 @@
 #define TC_SMEM_BYTES (TC_STAGES * TC_STAGE_BYTES + 1024 + 256)
 #define TC_WAIT_LIMIT (1u << 26)
 #define TC_OFF_A(s) ((s) * TC_SLICE_BYTES)
+// the barrier block of k_dht_tc (full[4] at 0, empty[4] at 32, accumulator
+// barriers from 64) is laid out for four stages
+static_assert(TC_STAGES == 4, "k_dht_tc barrier offsets assume four stages");
 #define TC_OFF_B(s) ((3 + (s)) * TC_SLICE_BYTES)
 
 // bounded wait that also stops when *fail is set by another role

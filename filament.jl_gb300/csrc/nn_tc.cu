@@ -39,7 +39,18 @@
 #define NT_W_OFF 0
 #define NT_A_OFF (NN_K * NT_W_BYTES)
 #define NT_BAR_OFF (NT_A_OFF + NT_STAGES * NT_A_BYTES)
-#define NT_SMEM (NT_BAR_OFF + 256 + 1024)
+#define NT_BAR_BYTES 256               // barrier block (layout below) + tensor-memory slot
+#define NT_SMEM (NT_BAR_OFF + NT_BAR_BYTES + 1024)
+// barrier block, 8 bytes each: full[S] empty[S] accf[2] acce[2] wbar done, then the
+// tensor-memory address slot
+#define NT_FULL(s) (8u * (s))
+#define NT_EMPTY(s) (8u * (NT_STAGES + (s)))
+#define NT_ACCF(b) (8u * (2 * NT_STAGES + (b)))
+#define NT_ACCE(b) (8u * (2 * NT_STAGES + 2 + (b)))
+#define NT_WBAR (8u * (2 * NT_STAGES + 4))
+#define NT_DONE (8u * (2 * NT_STAGES + 5))
+#define NT_SLOT (8u * (2 * NT_STAGES + 6))
+static_assert(NT_SLOT + 4 <= NT_BAR_BYTES, "barrier block overflows its reserved bytes");
 #define NT_THREADS 192
 #define NT_WAIT_LIMIT (1u << 26)
 
@@ -93,13 +104,12 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
   const uint32_t sbase = (raw + 1023u) & ~1023u;
   uint8_t* gbase = nt_smem + (sbase - raw);
   const uint32_t bars = sbase + NT_BAR_OFF;
-  // barrier block: full[4] empty[4] accf[2] acce[2] wbar done tmem_slot
-  auto full_bar = [&](int s) { return bars + 8u * s; };
-  auto empty_bar = [&](int s) { return bars + 32u + 8u * s; };
-  auto accf_bar = [&](int b) { return bars + 64u + 8u * b; };
-  auto acce_bar = [&](int b) { return bars + 80u + 8u * b; };
-  const uint32_t wbar = bars + 96u, done_bar = bars + 104u, tmem_slot = bars + 112u;
-  volatile uint32_t* tmem_slot_g = reinterpret_cast<volatile uint32_t*>(gbase + NT_BAR_OFF + 112);
+  auto full_bar = [&](int s) { return bars + NT_FULL(s); };
+  auto empty_bar = [&](int s) { return bars + NT_EMPTY(s); };
+  auto accf_bar = [&](int b) { return bars + NT_ACCF(b); };
+  auto acce_bar = [&](int b) { return bars + NT_ACCE(b); };
+  const uint32_t wbar = bars + NT_WBAR, done_bar = bars + NT_DONE, tmem_slot = bars + NT_SLOT;
+  volatile uint32_t* tmem_slot_g = reinterpret_cast<volatile uint32_t*>(gbase + NT_BAR_OFF + NT_SLOT);
 
   if (tid == 0) s_fail = 0;
   if (tid < 64) s_bias[tid] = p.bias[tid];
