@@ -9,10 +9,11 @@
 // The 64 -> 64 convolution is an implicit GEMM per tile of 128 time points:
 //   Y[t][co] = sum_k sum_ci X[t + k - 4][ci] W_k[co][ci],
 // M = 128 (time points, one tensor-memory lane each), N = 64 (channels),
-// K = 9 taps x 64 channels.  For every tap one TMA load brings the shifted
-// tile X[t0 + k - 4 .. t0 + k + 123][0..63] (128 B rows, 128-byte swizzle,
-// K-major A); rows outside [0, T) are zero-filled by the copy, which is the
-// convolution's "same" padding.  The nine weight matrices W_k[co][ci]
+// K = 9 taps x 64 channels.  One TMA load per tile brings the halo tile
+// X[t0 - 4 .. t0 + 131][0..63] (136 rows of 128 B, 128-byte swizzle, K-major
+// A); the A operand of tap k starts k rows into it (its descriptor carries the
+// swizzle phase of that row).  Rows outside [0, T) are zero-filled by the
+// copy, which is the convolution's "same" padding.  The nine weight matrices W_k[co][ci]
 // (K-major B, 72 KB) stay in shared memory for the whole launch.  Four MMAs
 // of K = 16 per tap accumulate in FP32 in tensor memory; two 64-column
 // accumulators alternate between tiles so that the epilogue of one tile
@@ -33,12 +34,14 @@
 #include "tc_ptx.cuh"
 
 #define NT_BM 128                      // time points per tile
-#define NT_STAGES 8
-#define NT_A_BYTES (NT_BM * 128)       // one tap's activation tile
+#define NT_STAGES 6
+#define NT_HALO (NT_BM + NN_K - 1)     // rows of one tile with its halo
+#define NT_A_BYTES (NT_HALO * 128)     // the halo tile as loaded
+#define NT_A_STRIDE 18432              // stage pitch: NT_A_BYTES rounded up to 1024
 #define NT_W_BYTES (64 * 128)          // one tap's weights
 #define NT_W_OFF 0
 #define NT_A_OFF (NN_K * NT_W_BYTES)
-#define NT_BAR_OFF (NT_A_OFF + NT_STAGES * NT_A_BYTES)
+#define NT_BAR_OFF (NT_A_OFF + NT_STAGES * NT_A_STRIDE)
 #define NT_BAR_BYTES 256               // barrier block (layout below) + tensor-memory slot
 #define NT_SMEM (NT_BAR_OFF + NT_BAR_BYTES + 1024)
 // barrier block, 8 bytes each: full[S] empty[S] accf[2] acce[2] wbar done, then the
@@ -51,6 +54,7 @@
 #define NT_DONE (8u * (2 * NT_STAGES + 5))
 #define NT_SLOT (8u * (2 * NT_STAGES + 6))
 static_assert(NT_SLOT + 4 <= NT_BAR_BYTES, "barrier block overflows its reserved bytes");
+static_assert(NT_A_STRIDE % 1024 == 0 && NT_A_STRIDE >= NT_A_BYTES, "stage pitch");
 #define NT_THREADS 192
 #define NT_WAIT_LIMIT (1u << 26)
 
@@ -141,14 +145,12 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
       tc::mbar_expect_tx(wbar, NN_K * NT_W_BYTES);
       for (int k = 0; k < NN_K; ++k) tc::tma_load_2d(sbase + NT_W_OFF + k * NT_W_BYTES, &tw, 0, 64 * k, wbar);
       int it = 0;
-      for (int tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x) {
+      for (int tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x, ++it) {
         const int b = tile / tpr, t0 = (tile - b * tpr) * NT_BM;
-        for (int k = 0; k < NN_K; ++k, ++it) {
-          const int s = it % NT_STAGES, use = it / NT_STAGES;
-          if (use > 0 && !nt_wait(empty_bar(s), (use - 1) & 1, &s_fail)) break;
-          tc::mbar_expect_tx(full_bar(s), NT_A_BYTES);
-          tc::tma_load_3d(sbase + NT_A_OFF + s * NT_A_BYTES, &tx, 0, t0 + k - NN_HALF, b, full_bar(s));
-        }
+        const int s = it % NT_STAGES, use = it / NT_STAGES;
+        if (use > 0 && !nt_wait(empty_bar(s), (use - 1) & 1, &s_fail)) break;
+        tc::mbar_expect_tx(full_bar(s), NT_A_BYTES);
+        tc::tma_load_3d(sbase + NT_A_OFF + s * NT_A_STRIDE, &tx, 0, t0 - NN_HALF, b, full_bar(s));
       }
       // wait for the last loads so that no copy lands after the block exits
       nt_wait(wbar, 0, &s_fail);
@@ -160,26 +162,25 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
     if (lane == 0) {
       const uint32_t idesc = tc::idesc_bf16(NT_BM, 64);
       if (nt_wait(wbar, 0, &s_fail)) {
-        int it = 0, lt = 0;
+        int lt = 0;
         for (int tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x, ++lt) {
           const int buf = lt & 1, ub = lt >> 1;
           if (ub > 0 && !nt_wait(acce_bar(buf), (ub - 1) & 1, &s_fail)) break;
+          const int s = lt % NT_STAGES;
+          if (!nt_wait(full_bar(s), (lt / NT_STAGES) & 1, &s_fail)) break;
           tc::tc_fence_after();
           const uint32_t acc = tmem + (uint32_t)(buf * 64);
-          bool ok = true;
-          for (int k = 0; k < NN_K; ++k, ++it) {
-            const int s = it % NT_STAGES;
-            if (!nt_wait(full_bar(s), (it / NT_STAGES) & 1, &s_fail)) { ok = false; break; }
-            tc::tc_fence_after();
-            const uint32_t a = sbase + NT_A_OFF + s * NT_A_BYTES, w = sbase + NT_W_OFF + k * NT_W_BYTES;
+          const uint32_t a = sbase + NT_A_OFF + s * NT_A_STRIDE;
+#pragma unroll 1
+          for (int k = 0; k < NN_K; ++k) {
+            const uint32_t ak = a + 128u * k, w = sbase + NT_W_OFF + k * NT_W_BYTES;
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {   // 16 channels = 32 bytes per MMA
-              tc::mma_f16(acc, tc::desc_k128(a + 32u * kk), tc::desc_k128(w + 32u * kk), idesc,
+              tc::mma_f16(acc, tc::desc_k128_at(ak + 32u * kk), tc::desc_k128(w + 32u * kk), idesc,
                           (k | kk) ? 1u : 0u);
             }
-            tc::mma_commit(empty_bar(s));
           }
-          if (!ok) break;
+          tc::mma_commit(empty_bar(s));
           tc::mma_commit(accf_bar(buf));
         }
       }
@@ -343,7 +344,7 @@ __global__ void __launch_bounds__(256) k_nn_out(const float* __restrict__ part, 
 int nn_plan_init(NnRowsPlan* p) {
   if (p->T % NT_BM) return -3;
   const unsigned long long d1[3] = {64ull, (unsigned long long)p->T, (unsigned long long)p->maxrows};
-  const unsigned box[3] = {64u, (unsigned)NT_BM, 1u};
+  const unsigned box[3] = {64u, (unsigned)NT_HALO, 1u};
   int rc = tc_make_map_bf16(&p->map_a1, p->a1, 3, d1, box);
   if (!rc) rc = tc_make_map_bf16(&p->map_a2, p->a2, 3, d1, box);
   if (rc) return rc;

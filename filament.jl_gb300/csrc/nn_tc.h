@@ -16,7 +16,7 @@ struct NnRowsPlan {
   const int* count;          // device row count (NULL: maxrows)
   const int* stop;           // device flag: non-zero skips the launches (or NULL)
   int* err;                  // set to 1 when a bounded wait gave up
-  CUtensorMap map_a1, map_a2;   // 3-D maps {64, T, rows}, box {64, 128, 1}
+  CUtensorMap map_a1, map_a2;   // 3-D maps {64, T, rows}, box {64, 136, 1} (a tile with its halo)
   int sms;                   // persistent grid size of the tensor-core layers
 };
 

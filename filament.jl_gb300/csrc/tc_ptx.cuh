@@ -174,6 +174,12 @@ __device__ __forceinline__ uint64_t desc_k128(uint32_t saddr) {
   d |= (uint64_t)2 << 61;                              // 128-byte swizzle
   return d;
 }
+// Same, for a start address that is not on a 1024-byte boundary of the
+// swizzle pattern (a matrix whose first row is row r of a swizzled tile): the
+// matrix base offset field holds the pattern phase (start >> 7) & 7.
+__device__ __forceinline__ uint64_t desc_k128_at(uint32_t saddr) {
+  return desc_k128(saddr) | ((uint64_t)((saddr >> 7) & 7u) << 49);
+}
 // Same for 64-byte swizzle: rows of 64 B, 8-row core groups 512 B apart.
 __device__ __forceinline__ uint64_t desc_k64(uint32_t saddr) {
   uint64_t d = 0;
