@@ -11,8 +11,9 @@
 // M = 128 (time points, one tensor-memory lane each), N = 64 (channels),
 // K = 9 taps x 64 channels.  One TMA load per tile brings the halo tile
 // X[t0 - 4 .. t0 + 131][0..63] (136 rows of 128 B, 128-byte swizzle, K-major
-// A); the A operand of tap k starts k rows into it (its descriptor carries the
-// swizzle phase of that row).  Rows outside [0, T) are zero-filled by the
+// A); the A operand of tap k starts k rows (k * 128 B) into it -- the swizzle
+// is a function of the shared-memory address, so the shifted operand reads
+// the rows as the copy wrote them.  Rows outside [0, T) are zero-filled by the
 // copy, which is the convolution's "same" padding.  The nine weight matrices W_k[co][ci]
 // (K-major B, 72 KB) stay in shared memory for the whole launch.  Four MMAs
 // of K = 16 per tap accumulate in FP32 in tensor memory; two 64-column
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
             const uint32_t ak = a + 128u * k, w = sbase + NT_W_OFF + k * NT_W_BYTES;
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {   // 16 channels = 32 bytes per MMA
-              tc::mma_f16(acc, tc::desc_k128_at(ak + 32u * kk), tc::desc_k128(w + 32u * kk), idesc,
+              tc::mma_f16(acc, tc::desc_k128(ak + 32u * kk), tc::desc_k128(w + 32u * kk), idesc,
                           (k | kk) ? 1u : 0u);
             }
           }

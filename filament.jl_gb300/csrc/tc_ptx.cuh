@@ -164,7 +164,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 
 // ---- descriptors ----------------------------------------------------------------
 // Shared-memory matrix descriptor, K-major operand, 128-byte swizzle: rows of
-// 128 B, 8-row core groups 1024 B apart (stride byte offset), version 1.
+// 128 B, 8-row core groups 1024 B apart (stride byte offset), version 1.  The
+// swizzle follows the shared-memory address bits, so a matrix may start at
+// any 128-byte row of a swizzled tile (base offset field 0; checked by the
+// tensor-core convolution's parity test).
 __device__ __forceinline__ uint64_t desc_k128(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);          // start address
@@ -173,12 +176,6 @@ __device__ __forceinline__ uint64_t desc_k128(uint32_t saddr) {
   d |= (uint64_t)1 << 46;                              // descriptor version
   d |= (uint64_t)2 << 61;                              // 128-byte swizzle
   return d;
-}
-// Same, for a start address that is not on a 1024-byte boundary of the
-// swizzle pattern (a matrix whose first row is row r of a swizzled tile): the
-// matrix base offset field holds the pattern phase (start >> 7) & 7.
-__device__ __forceinline__ uint64_t desc_k128_at(uint32_t saddr) {
-  return desc_k128(saddr) | ((uint64_t)((saddr >> 7) & 7u) << 49);
 }
 // Same for 64-byte swizzle: rows of 64 B, 8-row core groups 512 B apart.
 __device__ __forceinline__ uint64_t desc_k64(uint32_t saddr) {
