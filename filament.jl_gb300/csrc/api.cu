@@ -92,7 +92,7 @@ struct fil_handle {
   void* nn_feat = nullptr;     // [nrows][3][nt] BF16
   void* nn_a1 = nullptr;       // [nrows][64][nt] BF16
   void* nn_a2 = nullptr;
-  float* nn_out = nullptr;     // [nrows][nt] network output, or [nrows][2][9][nt] layer-3 partial sums
+  float* nn_out = nullptr;     // [nrows][nt] network output, or [nrows][9][nt] layer-3 partial sums
   int* nn_slot = nullptr;      // [nrows]
   int* nn_err = nullptr;       // tensor-core inference: a wait timed out
   NnRowsPlan nn_plan;          // tensor-core inference over the buffers above
@@ -1256,7 +1256,7 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
       CK(cudaMalloc(&h->nn_feat, rt * 3 * 2));
       CK(cudaMalloc(&h->nn_a1, rt * 64 * 2));
       CK(cudaMalloc(&h->nn_a2, rt * 64 * 2));
-      CK(cudaMalloc((void**)&h->nn_out, rt * 2 * NN_K * sizeof(float)));
+      CK(cudaMalloc((void**)&h->nn_out, rt * NN_K * sizeof(float)));
       CK(cudaMalloc((void**)&h->nn_slot, (size_t)h->nrows * sizeof(int)));
       CK(cudaMemset(h->nn_slot, 0xff, (size_t)h->nrows * sizeof(int)));
       CK(cudaMalloc((void**)&h->nn_err, sizeof(int)));

@@ -21,11 +21,8 @@
 // (bias, tanh, BF16, 128 B store per time point) overlaps the MMAs of the
 // next.  Persistent grid: one block per SM walks the tiles of all rows.
 //
-// Roles (320 threads): warps 0-7 epilogue (warp w owns tensor-memory lanes
-// 32(w & 3) .. +31, i.e. those time points, and channels 32(w >> 2) .. +31),
-// warp 8 TMA producer, warp 9 MMA issuer.  An epilogue warp stages its 32 x
-// 64 B of output in shared memory and stores it as 64 B row segments, eight
-// rows per instruction.  Every mbarrier
+// Roles (192 threads): warps 0-3 epilogue (warp w owns tensor-memory lanes
+// 32w .. 32w+31), warp 4 TMA producer, warp 5 MMA issuer.  Every mbarrier
 // wait is bounded and gives up once another role failed; a failure sets
 // *err and the block releases its tensor memory after its MMAs completed.
 #include <algorithm>
@@ -47,10 +44,7 @@
 #define NT_A_OFF (NN_K * NT_W_BYTES)
 #define NT_BAR_OFF (NT_A_OFF + NT_STAGES * NT_A_STRIDE)
 #define NT_BAR_BYTES 256               // barrier block (layout below) + tensor-memory slot
-#define NT_EPI_WARPS 8                 // epilogue warps: lane quadrant (w & 3) x channel half (w >> 2)
-#define NT_STG_BYTES 2048              // per epilogue warp: 32 points x 64 B output staging
-#define NT_STG_OFF (NT_BAR_OFF + NT_BAR_BYTES)
-#define NT_SMEM (NT_STG_OFF + NT_EPI_WARPS * NT_STG_BYTES + 1024)
+#define NT_SMEM (NT_BAR_OFF + NT_BAR_BYTES + 1024)
 // barrier block, 8 bytes each: full[S] empty[S] accf[2] acce[2] wbar done, then the
 // tensor-memory address slot
 #define NT_FULL(s) (8u * (s))
@@ -62,7 +56,7 @@
 #define NT_SLOT (8u * (2 * NT_STAGES + 6))
 static_assert(NT_SLOT + 4 <= NT_BAR_BYTES, "barrier block overflows its reserved bytes");
 static_assert(NT_A_STRIDE % 1024 == 0 && NT_A_STRIDE >= NT_A_BYTES, "stage pitch");
-#define NT_THREADS (32 * NT_EPI_WARPS + 64)
+#define NT_THREADS 192
 #define NT_WAIT_LIMIT (1u << 26)
 
 static __device__ __forceinline__ bool nt_wait(uint32_t bar, uint32_t parity, volatile int* fail) {
@@ -88,7 +82,7 @@ struct NtParams {
   const float* bias;       // [64]
   __nv_bfloat16* out;      // [rows][T][64] (layer 1)
   const __nv_bfloat16* w3; // layer 3 weights [ci][k] (FINAL)
-  float* part;             // [rows][2][9][T] layer-3 partial sums (FINAL), per channel half
+  float* part;             // [rows][9][T] layer-3 partial sums (FINAL)
   int T, tiles_per_row, maxrows;
   const int* count;
   const int* stop;
@@ -96,10 +90,9 @@ struct NtParams {
 };
 
 // FINAL (layer 2): the epilogue applies layer 3 to its own point instead of
-// storing the activations: P_hk[t] = sum_{ci in half h} w3[ci][k] y[t][ci] for
-// the nine taps k and the two channel halves h (the BF16-rounded activations,
-// as stored between layers), so that out[t] = b3 + sum_hk P_hk[t + k - 4]
-// (nn_out_at).
+// storing the activations: P_k[t] = sum_ci w3[ci][k] y[t][ci] for the nine
+// taps k (the BF16-rounded activations, as stored between layers), so that
+// out[t] = b3 + sum_k P_k[t + k - 4] (nn_out_at).
 template <bool FINAL>
 __global__ void __launch_bounds__(NT_THREADS, 1)
     k_nn_conv_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap tw, NtParams p) {
@@ -135,7 +128,7 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(accf_bar(b), 1);
-      tc::mbar_init(acce_bar(b), NT_EPI_WARPS);
+      tc::mbar_init(acce_bar(b), 4);
     }
     tc::mbar_init(wbar, 1);
     tc::mbar_init(done_bar, 1);
@@ -147,7 +140,7 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
   const uint32_t tmem = *tmem_slot_g;
   const int tpr = p.tiles_per_row;
 
-  if (warp == NT_EPI_WARPS) {
+  if (warp == 4) {
     // ---------------- producer: weights once, then one activation tile per tap
     if (lane == 0) {
       tc::mbar_expect_tx(wbar, NN_K * NT_W_BYTES);
@@ -165,7 +158,7 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
       for (int i = (it > NT_STAGES ? it - NT_STAGES : 0); i < it; ++i)
         nt_wait(full_bar(i % NT_STAGES), (i / NT_STAGES) & 1, &s_fail);
     }
-  } else if (warp == NT_EPI_WARPS + 1) {
+  } else if (warp == 5) {
     // ---------------- MMA issuer
     if (lane == 0) {
       const uint32_t idesc = tc::idesc_bf16(NT_BM, 64);
@@ -197,40 +190,43 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
       tc::mbar_wait(done_bar, 0, NT_WAIT_LIMIT);
     }
   } else {
-    // ---------------- epilogue: time points 32 qd .. +31 of the tile, channels 32 h .. +31
-    const int qd = warp & 3, h = warp >> 2;
-    uint8_t* stg = gbase + NT_STG_OFF + warp * NT_STG_BYTES;
+    // ---------------- epilogue: warp w owns time points 32w .. 32w+31 of the tile
     int lt = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
       const int buf = lt & 1;
       if (!nt_wait(accf_bar(buf), (lt >> 1) & 1, &s_fail)) break;
       tc::tc_fence_after();
-      const uint32_t taddr = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(buf * 64 + 32 * h);
-      uint32_t r[32];
-      tc::tmem_ld32_async(taddr, r);
-      tc::tmem_wait_ld(r);
+      const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(buf * 64);
+      uint32_t r0[32], r1[32];
+      tc::tmem_ld32_async(taddr, r0);
+      tc::tmem_ld32_async(taddr + 32u, r1);
+      tc::tmem_wait_ld(r0);
+      tc::tmem_wait_ld(r1);
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) nt_arrive(acce_bar(buf));
-      const int b = tile / tpr, t0 = (tile - b * tpr) * NT_BM + 32 * qd, t = t0 + lane;
-      const float4* bv = reinterpret_cast<const float4*>(s_bias + 32 * h);
-      if (FINAL) {
-        float y[32];
+      const int b = tile / tpr, t = (tile - b * tpr) * NT_BM + 32 * warp + lane;
+      if (FINAL && t < p.T) {
+        float y[64];
+        const float4* bv = reinterpret_cast<const float4*>(s_bias);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
+        for (int q = 0; q < 16; ++q) {
           const float4 bq = bv[q];
           const float bb[4] = {bq.x, bq.y, bq.z, bq.w};
 #pragma unroll
-          for (int e = 0; e < 4; ++e)
-            y[4 * q + e] = __bfloat162float(__float2bfloat16_rn(nt_tanh(__uint_as_float(r[4 * q + e]) + bb[e])));
+          for (int e = 0; e < 4; ++e) {
+            const int c = 4 * q + e;
+            const float v = __uint_as_float(c < 32 ? r0[c] : r1[c - 32]) + bb[e];
+            y[c] = __bfloat162float(__float2bfloat16_rn(nt_tanh(v)));
+          }
         }
-        float* dst = p.part + ((size_t)b * 2 + h) * NN_K * p.T + t;
+        float* dst = p.part + (size_t)b * NN_K * p.T + t;
 #pragma unroll
         for (int k = 0; k < NN_K; ++k) {
-          const float4* wk = reinterpret_cast<const float4*>(s_w3 + 64 * k + 32 * h);
+          const float4* wk = reinterpret_cast<const float4*>(s_w3 + 64 * k);
           float a0 = 0.f, a1 = 0.f;
 #pragma unroll
-          for (int q = 0; q < 8; q += 2) {
+          for (int q = 0; q < 16; q += 2) {
             const float4 u = wk[q], v = wk[q + 1];
             a0 = fmaf(u.x, y[4 * q], a0);
             a0 = fmaf(u.y, y[4 * q + 1], a0);
@@ -241,34 +237,26 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
             a1 = fmaf(v.z, y[4 * q + 6], a1);
             a1 = fmaf(v.w, y[4 * q + 7], a1);
           }
-          if (t < p.T) dst[(size_t)k * p.T] = a0 + a1;
+          dst[(size_t)k * p.T] = a0 + a1;
         }
-      } else {
-        // row `lane` of the staging buffer: chunk c (8 channels, 16 B) at
-        // 16 (c ^ ((row >> 1) & 3)), conflict-free for both access patterns
+      } else if (t < p.T) {
+        uint4* dst = reinterpret_cast<uint4*>(p.out + ((size_t)b * p.T + t) * 64);
+        const float4* bv = reinterpret_cast<const float4*>(s_bias);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const float4 b0 = bv[2 * c], b1 = bv[2 * c + 1];
+        for (int q = 0; q < 8; ++q) {
+          const float4 b0 = bv[2 * q], b1 = bv[2 * q + 1];
           const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
           uint32_t pk[4];
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            const __nv_bfloat162 hv = __floats2bfloat162_rn(nt_tanh(__uint_as_float(r[8 * c + 2 * e]) + bb[2 * e]),
-                                                            nt_tanh(__uint_as_float(r[8 * c + 2 * e + 1]) + bb[2 * e + 1]));
-            pk[e] = *reinterpret_cast<const uint32_t*>(&hv);
+            const int c = 8 * q + 2 * e;
+            const float v0 = __uint_as_float(c < 32 ? r0[c] : r1[c - 32]) + bb[2 * e];
+            const float v1 = __uint_as_float(c + 1 < 32 ? r0[c + 1] : r1[c + 1 - 32]) + bb[2 * e + 1];
+            const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(v0), nt_tanh(v1));
+            pk[e] = *reinterpret_cast<const uint32_t*>(&h);
           }
-          *reinterpret_cast<uint4*>(stg + lane * 64 + 16 * (c ^ ((lane >> 1) & 3))) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+          dst[q] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
         }
-        __syncwarp();
-        // 32 rows x 4 chunks: instruction i stores rows 8i .. 8i+7
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int g = 32 * i + lane, row = g >> 2, c = g & 3;
-          const uint4 v = *reinterpret_cast<const uint4*>(stg + row * 64 + 16 * (c ^ ((row >> 1) & 3)));
-          if (t0 + row < p.T)
-            *reinterpret_cast<uint4*>(p.out + ((size_t)b * p.T + t0 + row) * 64 + 32 * h + 8 * c) = v;
-        }
-        __syncwarp();
       }
     }
   }
@@ -350,7 +338,7 @@ __global__ void __launch_bounds__(256) k_nn_out(const float* __restrict__ part, 
   const long i = blockIdx.x * 256L + threadIdx.x;
   if (i >= (long)rows * T) return;
   const int b = (int)(i / T), t = (int)(i - (long)b * T);
-  out[i] = nn_out_at(part + (size_t)b * 2 * NN_K * T, b3[0], t, T);
+  out[i] = nn_out_at(part + (size_t)b * NN_K * T, b3[0], t, T);
 }
 
 // ---------------------------------------------------------------------------

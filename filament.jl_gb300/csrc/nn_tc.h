@@ -11,7 +11,7 @@ struct NnRowsPlan {
   const __nv_bfloat16* x0;   // [rows][3][T] network inputs
   __nv_bfloat16* a1;         // [rows][T][64] hidden activations (channel-last)
   __nv_bfloat16* a2;
-  float* part;               // [rows][2][9][T] layer-3 partial sums (nn_out_at)
+  float* part;               // [rows][9][T] layer-3 partial sums (nn_out_at)
   int T, maxrows;
   const int* count;          // device row count (NULL: maxrows)
   const int* stop;           // device flag: non-zero skips the launches (or NULL)
@@ -33,23 +33,19 @@ cudaError_t nn_launch_l0_cl(const __nv_bfloat16* x, const __nv_bfloat16* w, cons
 // applied in the epilogue (partial sums into part)
 cudaError_t nn_launch_conv_tc(const CUtensorMap& tx, const CUtensorMap& tw, const float* bias, __nv_bfloat16* out,
                               const __nv_bfloat16* w3, float* part, const NnRowsPlan& p, cudaStream_t st);
-// out [rows][T] from the partial sums [rows][2][9][T]
+// out [rows][T] from the partial sums [rows][9][T]
 cudaError_t nn_launch_out(const float* part, const float* b3, float* out, int T, int rows, cudaStream_t st);
 
-// network output at t of one row from its layer-3 partial sums P [2][9][T]
-// (two channel halves): b3 + sum_hk P_hk[t + k - 4] (terms outside [0, T) are
-// zero padding)
+// network output at t of one row from its layer-3 partial sums P [9][T]:
+// b3 + sum_k P_k[t + k - 4] (terms outside [0, T) are zero padding)
 __device__ __forceinline__ float nn_out_at(const float* __restrict__ P, float b3, int t, int T) {
-  float s0 = 0.f, s1 = 0.f;
+  float s = b3;
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     const int u = t + k - 4;
-    if (u >= 0 && u < T) {
-      s0 += __ldg(&P[(size_t)k * T + u]);
-      s1 += __ldg(&P[(size_t)(9 + k) * T + u]);
-    }
+    if (u >= 0 && u < T) s += __ldg(&P[(size_t)k * T + u]);
   }
-  return b3 + (s0 + s1);
+  return s;
 }
 
 struct fil_nn;

@@ -79,7 +79,7 @@ template <typename R> struct RowParams {
   // learned plasma surrogate: network inputs of the flagged rows
   // [slot][2][N] (BF16), slot of each row (-1: not flagged), network output
   // g(t), the log-amplification of the avalanche term of nn_density: [slot][N],
-  // or with nn_part its layer-3 partial sums [slot][2][9][N] (nn_out_at) and the
+  // or with nn_part its layer-3 partial sums [slot][9][N] (nn_out_at) and the
   // output bias at nn_b3
   __nv_bfloat16* nn_feat;
   int* nn_slot;
@@ -597,7 +597,7 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
       const bool judge = P.nn_out && mode == 0 && ctl->nn_judge;
       Aff<R, 1>* sc1 = reinterpret_cast<Aff<R, 1>*>(ascratch);
       R rmax;
-      const float* gslot = P.nn_out + (size_t)slot * N * (P.nn_part ? 2 * NN_K : 1);
+      const float* gslot = P.nn_out + (size_t)slot * N * (P.nn_part ? NN_K : 1);
       if (nn_row && !judge) {
         rmax = nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, false);
       } else {

@@ -318,14 +318,14 @@ int fil_nn_infer(fil_nn* n, const float* feat, int b, float* out) {
   NnRowsPlan pl;
   std::memset(&pl, 0, sizeof pl);
   void* buf = nullptr;
-  const size_t bytes = bt * NN_IN * 2 + 2 * bt * 64 * 2 + 19 * bt * sizeof(float) + 256;
+  const size_t bytes = bt * NN_IN * 2 + 2 * bt * 64 * 2 + 10 * bt * sizeof(float) + 256;
   NK(cudaMallocAsync(&buf, bytes, n->st));
   NK(cudaMallocAsync((void**)&df, bt * NN_IN * sizeof(float), n->st));
   uint8_t* q = (uint8_t*)buf;
   pl.a1 = (__nv_bfloat16*)q;
   pl.a2 = pl.a1 + bt * 64;
   pl.part = (float*)(pl.a2 + bt * 64);
-  float* dout = pl.part + 18 * bt;
+  float* dout = pl.part + 9 * bt;
   __nv_bfloat16* x0 = (__nv_bfloat16*)(dout + bt);
   pl.x0 = x0;
   pl.err = (int*)(x0 + bt * NN_IN + 64);
