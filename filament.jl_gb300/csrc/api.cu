@@ -66,6 +66,7 @@ struct fil_handle {
   std::complex<double> c0 = 0.0;           // XY: i QZ(w0) Rnl_cubic(w0)
   bool field_set = false, store_plasma = false;
   int bugcompat = 0, clamp_last = 0, timing = 0;
+  int gen = 0;                         // bumped by every option change (batch graphs rebuild)
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev[8];
   double tsum[6] = {0, 0, 0, 0, 0, 0};   // row (with the surrogate), dht fwd, dht inv, reduce+control,
@@ -765,6 +766,16 @@ static int check_tc(fil_handle* h) {
   return 0;
 }
 
+// zeroes the Hankel-step work buffers W1, W2 (their padding rows and
+// columns are read by the next step but written by neither path)
+static int clear_work(fil_handle* h) {
+  const size_t sz = (size_t)h->mpad * h->nh * (h->fp64 ? sizeof(double2) : sizeof(float2));
+  CK(cudaMemsetAsync(h->W1, 0, sz, h->st));
+  CK(cudaMemsetAsync(h->W2, 0, sz, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
 static int read_ctl(fil_handle* h) {
   CK(cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -1008,13 +1019,21 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
     for (int i = 0; i < 6; ++i) h->tsum[i] = 0;
     h->tcount = 0;
   } else if (option == FIL_OPT_DHT_SIMT) {
-    if (!h->fp64) h->use_tc = (value == 0) && h->MA1[0] != nullptr;
+    const bool tc = !h->fp64 && (value == 0) && h->MA1[0] != nullptr;
+    if (!h->fp64 && tc != h->use_tc) {
+      // the two paths lay out W1 and W2 differently ([2 nh][mpad] vs
+      // [mpad][2 nh]); padding the new path never writes must read zero
+      h->use_tc = tc;
+      int rc = clear_work(h);
+      if (rc) return rc;
+    }
   } else if (option == FIL_OPT_ANALYTIC_PROJECTION) {
     // the field state is the analytic half spectrum: always projected
   }
   else {
     return fail(h, FIL_ERR_ARG, "unknown option");
   }
+  h->gen += 1;
   if (h->graph) {           // parameters baked into the graph changed
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -1091,10 +1110,8 @@ static int build_graph(fil_handle* h) {
   return 0;
 }
 
-int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stats) {
-  if (!h) return fail(h, FIL_ERR_ARG, "null handle");
-  if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
-  // arm the controller
+// arms the device controller of a run from z0 to zmax (at most nmax steps)
+static int arm_run(fil_handle* h, double z0, double zmax, int64_t nmax) {
   CK(cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   DevCtl c = *h->ctl_host;
@@ -1115,6 +1132,17 @@ int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stat
   c.imax_acc = 0;
   c.nn_count = 0;
   CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stats) {
+  if (!h) return fail(h, FIL_ERR_ARG, "null handle");
+  if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
+  {
+    int rc = arm_run(h, z0, zmax, nmax);
+    if (rc) return rc;
+  }
   if (h->timing) {
     // benchmark path: one step at a time, L2 flushed before each step
     // (outside the timed events), device time of each kernel accumulated
@@ -1309,6 +1337,439 @@ int fil_kernel_times(fil_handle* h, double* ms, int n) {
   if (n > 6) ms[6] = h->tcount ? h->tsum[5] / h->tcount : 0.0;
   if (n > 5) ms[5] = (double)h->tcount;
   return FIL_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched parameter sweep: many RT problems of uneven (Nr, Nt) stepped
+// together.  One CUDA graph holds one z-step of every member: a fork to
+// `nbranch` streams, each running the reduce + controller + row kernel +
+// Hankel step of its members in sequence (every member keeps its own
+// device controller and adaptive dz, and a member whose controller is done
+// turns its kernels into no-ops), then a join and one block counting the
+// members still live.  The host replays the graph and reads that count
+// every kBatchCheck steps.  fil_batch_tune measures each member's step with
+// each Hankel transform kernel it can run (tcgen05 128 x 128 FP16-slice
+// tiles or the CUDA-core 128 x 128 FP32 tiles), keeps the faster, then
+// spreads the members over 1, 2, 4, ... branches by longest-step-first
+// assignment on the measured times and keeps the branch count whose graph
+// replays fastest.  Member states are saved before and restored after
+// every trial.
+namespace {
+const int kBatchCheck = 32;
+const int kBatchMaxBranches = 32;
+}
+
+struct fil_batch {
+  std::vector<fil_handle*> m;
+  std::vector<int> branch;     // branch of each member
+  std::vector<double> cost;    // ms per step of each member (measured by the tuner, else a size model)
+  std::vector<double> tune_ms; // ms per batch step for 1, 2, 4, ... branches (tuner)
+  int nbranch = 0;
+  bool tuned = false;
+  int gen = -1;                // sum of the members' option generations baked into the graph
+  cudaStream_t st = nullptr;   // the graph's launch stream
+  std::vector<cudaStream_t> bst;
+  std::vector<cudaEvent_t> ev; // fork, joins, timing
+  cudaGraphExec_t graph = nullptr;
+  DevCtl** ctls = nullptr;     // device array of the members' control blocks
+  int* live = nullptr;         // device
+  int* live_host = nullptr;    // pinned
+  std::string err;
+};
+
+static int bfail(fil_batch* b, int code, const std::string& m) {
+  if (b) b->err = m;
+  g_err = m;
+  return code;
+}
+#define CKB(call)                                                                        \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return bfail(b, FIL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+static int batch_gen(const fil_batch* b) {
+  int g = 0;
+  for (fil_handle* h : b->m) g += h->gen;
+  return g;
+}
+
+// size model used before tuning: Hankel GEMMs (Mpad^2 Nt) + row work (Mpad Nt log Nt)
+static double batch_model_cost(const fil_handle* h) {
+  const double lg = std::log2((double)h->nt);
+  return 1e-9 * ((double)h->mpad * h->mpad * h->nt * (h->use_tc ? 0.1 : 1.0) + 40.0 * h->mpad * h->nt * lg);
+}
+
+// longest-step-first assignment of the members to k branches
+static void batch_assign(fil_batch* b, int k) {
+  const int n = (int)b->m.size();
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->cost[x] > b->cost[y]; });
+  std::vector<double> load(k, 0.0);
+  b->branch.assign(n, 0);
+  for (int i : order) {
+    int best = 0;
+    for (int j = 1; j < k; ++j)
+      if (load[j] < load[best]) best = j;
+    b->branch[i] = best;
+    load[best] += b->cost[i];
+  }
+  b->nbranch = k;
+}
+
+static int batch_build_graph(fil_batch* b) {
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  const int n = (int)b->m.size();
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->cost[x] > b->cost[y]; });
+  cudaGraph_t g;
+  CKB(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  int rc = 0;
+  cudaError_t e = cudaEventRecord(b->ev[0], b->st);
+  for (int k = 0; k < b->nbranch && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->bst[k], b->ev[0], 0);
+  if (e != cudaSuccess) rc = bfail(b, FIL_ERR_CUDA, std::string("batch fork: ") + cudaGetErrorString(e));
+  for (int k = 0; k < b->nbranch && !rc; ++k) {
+    for (int i : order) {
+      if (b->branch[i] != k) continue;
+      fil_handle* h = b->m[i];
+      cudaStream_t own = h->st;
+      h->st = b->bst[k];
+      rc = reduce(h, nullptr, 1);
+      if (!rc) {
+        cudaError_t e2 = launch_control(h->ctl, h->fluence, h->pw, h->nrows, h->st);
+        if (e2 != cudaSuccess) rc = fail(h, FIL_ERR_CUDA, cudaGetErrorString(e2));
+      }
+      if (!rc) rc = zstep(h, false);
+      h->st = own;
+      if (rc) {
+        rc = bfail(b, rc, "member " + std::to_string(i) + ": " + h->err);
+        break;
+      }
+    }
+  }
+  for (int k = 0; k < b->nbranch && !rc; ++k) {
+    e = cudaEventRecord(b->ev[1 + k], b->bst[k]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->ev[1 + k], 0);
+    if (e != cudaSuccess) rc = bfail(b, FIL_ERR_CUDA, std::string("batch join: ") + cudaGetErrorString(e));
+  }
+  if (!rc) {
+    e = launch_batch_live(b->ctls, n, b->live, b->st);
+    if (e != cudaSuccess) rc = bfail(b, FIL_ERR_CUDA, cudaGetErrorString(e));
+  }
+  e = cudaStreamEndCapture(b->st, &g);
+  if (rc) {
+    if (e == cudaSuccess) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return bfail(b, FIL_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return bfail(b, FIL_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(e));
+  b->gen = batch_gen(b);
+  return 0;
+}
+
+static int batch_check_members(fil_batch* b) {
+  for (size_t i = 0; i < b->m.size(); ++i) {
+    fil_handle* h = b->m[i];
+    if (!h->field_set) return bfail(b, FIL_ERR_STATE, "member " + std::to_string(i) + ": field not set");
+    if (h->nn) return bfail(b, FIL_ERR_UNSUPPORTED, "member " + std::to_string(i) + ": surrogate armed (not batched)");
+  }
+  return 0;
+}
+
+// saved field state and controller of every member (tuner trials)
+struct BatchSaved {
+  std::vector<void*> S;
+  std::vector<DevCtl> ctl;
+};
+static size_t state_bytes(const fil_handle* h) {
+  return (size_t)h->mpad * h->nh * (h->fp64 ? sizeof(double2) : sizeof(float2));
+}
+static int batch_save(fil_batch* b, BatchSaved& sv) {
+  const size_t n = b->m.size();
+  sv.S.assign(n, nullptr);
+  sv.ctl.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    fil_handle* h = b->m[i];
+    CKB(cudaMalloc(&sv.S[i], state_bytes(h)));
+    CKB(cudaMemcpyAsync(sv.S[i], h->S, state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
+    CKB(cudaMemcpyAsync(&sv.ctl[i], h->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, h->st));
+    CKB(cudaStreamSynchronize(h->st));
+  }
+  return 0;
+}
+static int member_restore(fil_batch* b, const BatchSaved& sv, int i) {
+  fil_handle* h = b->m[i];
+  CKB(cudaMemcpyAsync(h->S, sv.S[i], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
+  CKB(cudaMemcpyAsync(h->ctl, &sv.ctl[i], sizeof(DevCtl), cudaMemcpyHostToDevice, h->st));
+  CKB(cudaStreamSynchronize(h->st));
+  // a trial with the other Hankel kernel left its layout in W1, W2
+  if (clear_work(h)) return bfail(b, FIL_ERR_CUDA, h->err);
+  return 0;
+}
+static int batch_restore(fil_batch* b, const BatchSaved& sv) {
+  CKB(cudaStreamSynchronize(b->st));
+  for (size_t i = 0; i < b->m.size(); ++i) {
+    int rc = member_restore(b, sv, (int)i);
+    if (rc) return rc;
+  }
+  return 0;
+}
+static void batch_free_saved(BatchSaved& sv) {
+  for (void* p : sv.S)
+    if (p) cudaFree(p);
+  sv.S.clear();
+}
+
+// controller armed for trial steps that never stop on z or the step count
+static int batch_arm_trial(fil_batch* b, const BatchSaved& sv) {
+  for (size_t i = 0; i < b->m.size(); ++i) {
+    int rc = arm_run(b->m[i], sv.ctl[i].z, 1e300, (int64_t)1 << 60);
+    if (rc) return bfail(b, rc, "member " + std::to_string(i) + ": " + b->m[i]->err);
+  }
+  return 0;
+}
+
+// ms per step of member h alone on its own stream: one warm-up step, then
+// `reps` timed steps
+static int batch_time_member(fil_batch* b, fil_handle* h, int reps, double* ms) {
+  for (int s = 0; s < 1 + reps; ++s) {
+    if (s == 1) CKB(cudaEventRecord(b->ev[kBatchMaxBranches + 1], h->st));
+    int rc = reduce(h, nullptr, 1);
+    if (!rc) {
+      cudaError_t e = launch_control(h->ctl, h->fluence, h->pw, h->nrows, h->st);
+      if (e != cudaSuccess) rc = fail(h, FIL_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (!rc) rc = zstep(h, false);
+    if (rc) return bfail(b, rc, h->err);
+  }
+  CKB(cudaEventRecord(b->ev[kBatchMaxBranches + 2], h->st));
+  CKB(cudaEventSynchronize(b->ev[kBatchMaxBranches + 2]));
+  float t = 0;
+  CKB(cudaEventElapsedTime(&t, b->ev[kBatchMaxBranches + 1], b->ev[kBatchMaxBranches + 2]));
+  *ms = t / reps;
+  return 0;
+}
+
+static void batch_free(fil_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (cudaStream_t s : b->bst)
+    if (s) cudaStreamDestroy(s);
+  for (cudaEvent_t e : b->ev)
+    if (e) cudaEventDestroy(e);
+  if (b->st) cudaStreamDestroy(b->st);
+  if (b->ctls) cudaFree(b->ctls);
+  if (b->live) cudaFree(b->live);
+  if (b->live_host) cudaFreeHost(b->live_host);
+  for (fil_handle* h : b->m) fil_destroy(h);
+  b->m.clear();
+}
+
+extern "C" {
+
+const char* fil_batch_last_error(const fil_batch* b) { return b ? b->err.c_str() : g_err.c_str(); }
+
+int fil_create_batch(int n, const fil_config* cfg, const fil_tables* tab, fil_batch** out) {
+  fil_batch* b = nullptr;
+  if (!cfg || !tab || !out || n < 1) return bfail(b, FIL_ERR_ARG, "fil_create_batch: bad argument");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i)
+    if (cfg[i].geometry != FIL_GEOM_RT)
+      return bfail(b, FIL_ERR_UNSUPPORTED, "fil_create_batch: members must use the RT geometry");
+  b = new fil_batch();
+  for (int i = 0; i < n; ++i) {
+    fil_handle* h = nullptr;
+    int rc = fil_create(&cfg[i], &tab[i], &h);
+    if (rc) {
+      std::string m = "member " + std::to_string(i) + ": " + g_err;
+      batch_free(b);
+      delete b;
+      return bfail(nullptr, rc, m);
+    }
+    b->m.push_back(h);
+  }
+  b->cost.resize(n);
+  for (int i = 0; i < n; ++i) b->cost[i] = batch_model_cost(b->m[i]);
+#define CKBC(call)                                                              \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) {                                                    \
+      std::string m_ = std::string(#call) + ": " + cudaGetErrorString(e_);      \
+      batch_free(b);                                                            \
+      delete b;                                                                 \
+      return bfail(nullptr, FIL_ERR_CUDA, m_);                                  \
+    }                                                                           \
+  } while (0)
+  CKBC(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+  b->bst.assign(kBatchMaxBranches, nullptr);
+  for (int k = 0; k < kBatchMaxBranches; ++k) CKBC(cudaStreamCreateWithFlags(&b->bst[k], cudaStreamNonBlocking));
+  b->ev.assign(kBatchMaxBranches + 3, nullptr);
+  for (int k = 0; k < kBatchMaxBranches + 1; ++k) CKBC(cudaEventCreateWithFlags(&b->ev[k], cudaEventDisableTiming));
+  CKBC(cudaEventCreate(&b->ev[kBatchMaxBranches + 1]));
+  CKBC(cudaEventCreate(&b->ev[kBatchMaxBranches + 2]));
+  std::vector<DevCtl*> c(n);
+  for (int i = 0; i < n; ++i) c[i] = b->m[i]->ctl;
+  CKBC(cudaMalloc((void**)&b->ctls, n * sizeof(DevCtl*)));
+  CKBC(cudaMemcpy(b->ctls, c.data(), n * sizeof(DevCtl*), cudaMemcpyHostToDevice));
+  CKBC(cudaMalloc((void**)&b->live, sizeof(int)));
+  CKBC(cudaMallocHost((void**)&b->live_host, sizeof(int)));
+#undef CKBC
+  batch_assign(b, std::min(n, 8));
+  *out = b;
+  return FIL_OK;
+}
+
+int fil_batch_destroy(fil_batch* b) {
+  if (!b) return FIL_OK;
+  batch_free(b);
+  delete b;
+  return FIL_OK;
+}
+
+int fil_batch_size(const fil_batch* b) { return b ? (int)b->m.size() : 0; }
+
+fil_handle* fil_batch_member(fil_batch* b, int i) {
+  if (!b || i < 0 || i >= (int)b->m.size()) return nullptr;
+  return b->m[i];
+}
+
+int fil_batch_tune(fil_batch* b, int max_branches, double* ms_per_branches, int n_out) {
+  if (!b) return bfail(b, FIL_ERR_ARG, "null batch");
+  int rc = batch_check_members(b);
+  if (rc) return rc;
+  const int n = (int)b->m.size();
+  max_branches = std::max(1, std::min(std::min(max_branches, kBatchMaxBranches), n));
+  BatchSaved sv;
+  rc = batch_save(b, sv);
+  if (!rc) rc = batch_arm_trial(b, sv);
+  // 1. the Hankel transform kernel of each member
+  for (int i = 0; i < n && !rc; ++i) {
+    fil_handle* h = b->m[i];
+    const bool can_tc = !h->fp64 && h->MA1[0] != nullptr;
+    double best = 0;
+    bool best_tc = h->use_tc;
+    for (int path = 0; path < (can_tc ? 2 : 1) && !rc; ++path) {
+      if (can_tc) h->use_tc = (path == 0);
+      double ms = 0;
+      rc = batch_time_member(b, h, 3, &ms);
+      if (!rc) rc = member_restore(b, sv, i);
+      if (!rc) rc = arm_run(h, sv.ctl[i].z, 1e300, (int64_t)1 << 60);
+      if (!rc && (path == 0 || ms < best)) {
+        best = ms;
+        best_tc = h->use_tc;
+      }
+    }
+    h->use_tc = best_tc;
+    b->cost[i] = best;
+    if (h->graph) {   // the member's own fil_run graph may hold the other kernel
+      cudaGraphExecDestroy(h->graph);
+      h->graph = nullptr;
+    }
+  }
+  // 2. the branch count
+  b->tune_ms.clear();
+  int best_k = 1;
+  double best_ms = 0;
+  for (int k = 1; k <= max_branches && !rc; k *= 2) {
+    batch_assign(b, k);
+    rc = batch_build_graph(b);
+    if (rc) break;
+    const int reps = 5;
+    for (int s = 0; s < 1 + reps && !rc; ++s) {
+      if (s == 1) CKB(cudaEventRecord(b->ev[kBatchMaxBranches + 1], b->st));
+      cudaError_t e = cudaGraphLaunch(b->graph, b->st);
+      if (e != cudaSuccess) rc = bfail(b, FIL_ERR_CUDA, std::string("batch replay: ") + cudaGetErrorString(e));
+    }
+    if (rc) break;
+    CKB(cudaEventRecord(b->ev[kBatchMaxBranches + 2], b->st));
+    CKB(cudaEventSynchronize(b->ev[kBatchMaxBranches + 2]));
+    float t = 0;
+    CKB(cudaEventElapsedTime(&t, b->ev[kBatchMaxBranches + 1], b->ev[kBatchMaxBranches + 2]));
+    const double ms = t / reps;
+    b->tune_ms.push_back(ms);
+    if (k == 1 || ms < best_ms) {
+      best_ms = ms;
+      best_k = k;
+    }
+    rc = batch_restore(b, sv);
+    if (!rc) rc = batch_arm_trial(b, sv);
+  }
+  // the members' states as they were before tuning
+  if (!rc) rc = batch_restore(b, sv);
+  batch_free_saved(sv);
+  for (int i = 0; i < n && !rc; ++i) rc = check_tc(b->m[i]) ? bfail(b, FIL_ERR_TIMEOUT, b->m[i]->err) : 0;
+  if (rc) return rc;
+  batch_assign(b, best_k);
+  rc = batch_build_graph(b);
+  if (rc) return rc;
+  b->tuned = true;
+  if (ms_per_branches)
+    for (int j = 0; j < n_out; ++j) ms_per_branches[j] = j < (int)b->tune_ms.size() ? b->tune_ms[j] : 0.0;
+  return FIL_OK;
+}
+
+int fil_batch_plan(const fil_batch* b, int* branch, int* dht_simt, double* cost_ms) {
+  if (!b) return bfail(nullptr, FIL_ERR_ARG, "null batch");
+  for (size_t i = 0; i < b->m.size(); ++i) {
+    if (branch) branch[i] = b->branch[i];
+    if (dht_simt) dht_simt[i] = b->m[i]->use_tc ? 0 : 1;
+    if (cost_ms) cost_ms[i] = b->cost[i];
+  }
+  return b->nbranch;
+}
+
+int fil_batch_run(fil_batch* b, const double* z0, const double* zmax, int64_t nmax, fil_stats* stats) {
+  if (!b || !z0 || !zmax) return bfail(b, FIL_ERR_ARG, "null argument");
+  int rc = batch_check_members(b);
+  if (rc) return rc;
+  const int n = (int)b->m.size();
+  for (int i = 0; i < n; ++i) {
+    rc = arm_run(b->m[i], z0[i], zmax[i], nmax);
+    if (rc) return bfail(b, rc, "member " + std::to_string(i) + ": " + b->m[i]->err);
+  }
+  if (!b->graph || b->gen != batch_gen(b)) {
+    rc = batch_build_graph(b);
+    if (rc) return rc;
+  }
+  for (;;) {
+    for (int i = 0; i < kBatchCheck; ++i) CKB(cudaGraphLaunch(b->graph, b->st));
+    CKB(cudaMemcpyAsync(b->live_host, b->live, sizeof(int), cudaMemcpyDeviceToHost, b->st));
+    CKB(cudaStreamSynchronize(b->st));
+    if (*b->live_host == 0) break;
+  }
+  int worst = FIL_OK;
+  for (int i = 0; i < n; ++i) {
+    fil_handle* h = b->m[i];
+    rc = read_ctl(h);
+    if (!rc) rc = check_tc(h);
+    if (rc) return bfail(b, rc, "member " + std::to_string(i) + ": " + h->err);
+    const DevCtl& r = *h->ctl_host;
+    if (stats) {
+      fil_stats& s = stats[i];
+      s.z = r.z;
+      s.dz = r.dz;
+      s.imax = r.imax;
+      s.rhomax = r.rhomax;
+      s.energy = r.energy;
+      s.steps = r.steps;
+      s.status = r.status;
+      s.flags = r.flags | (std::min(r.newton_max, 255) << 8);
+    }
+    if (r.status < 0 && worst >= 0) {
+      worst = r.status;
+      b->err = "member " + std::to_string(i) + ": non-finite field during fil_batch_run";
+    }
+  }
+  return worst;
 }
 
 }  // extern "C"

@@ -39,6 +39,7 @@ cudaError_t launch_slice_prop(const float* W, const float2* kz, const float* gd,
 cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
 cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);
+cudaError_t launch_batch_live(DevCtl* const* c, int n, int* live, cudaStream_t st);
 
 // learned plasma surrogate (surrogate.cu): the network over the rows below
 // *count (device value) of x0 [rows][3][T] (BF16) into out [rows][T];

@@ -194,6 +194,23 @@ cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Batched sweep: number of members whose controller has not raised done
+// (one block; read by the host after a run of batch steps).
+__global__ void k_batch_live(DevCtl* const* c, int n, int* live) {
+  __shared__ int s_live;
+  if (threadIdx.x == 0) s_live = 0;
+  __syncthreads();
+  int k = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) k += c[i]->done ? 0 : 1;
+  if (k) atomicAdd(&s_live, k);
+  __syncthreads();
+  if (threadIdx.x == 0) *live = s_live;
+}
+cudaError_t launch_batch_live(DevCtl* const* c, int n, int* live, cudaStream_t st) {
+  k_batch_live<<<1, 256, 0, st>>>(c, n, live);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st) {
   k_setdz<<<1, 1, 0, st>>>(c, z, dz);
   return cudaGetLastError();

@@ -18,3 +18,5 @@ dzphimax = math.inf
 Istop = 1e3
 ALG = RK2
 PPcr = 3.0          # peak power in units of the critical power
+beam_a0 = 1e-3      # 1/e intensity radius of the beam (m)
+chirp_fs2 = 0.0     # spectral phase phi2 (w - w0)^2 / 2 of the pulse (fs^2)

@@ -6,8 +6,10 @@ sm_103a) through the C ABI of include/filament_gb.h.
 """
 from .input import prepare
 from .filament import run, Simulation, main_loop
-from .backend import load_library, library_path, Handle
+from .backend import load_library, library_path, Handle, Batch
 from . import _abi
 
+from . import sweep
+
 __all__ = ["prepare", "run", "Simulation", "main_loop", "load_library",
-           "library_path", "Handle"]
+           "library_path", "Handle", "Batch", "sweep"]

@@ -44,10 +44,22 @@ class Handle:
             raise _abi.FilError(code, "%screate failed: %s" % (self.b.prefix, msg.decode() if msg else "?"))
         self.shape = problem.field_shape
 
+    @classmethod
+    def borrow(cls, binding, problem, hptr):
+        """A Handle object for a handle that something else owns (a batch
+        member): closing it does not destroy the handle."""
+        self = cls.__new__(cls)
+        self.b = binding
+        self.problem = problem
+        self.h = C.c_void_p(hptr)
+        self.shape = problem.field_shape
+        self._owned = False
+        return self
+
     def close(self):
-        if self.h:
+        if self.h and getattr(self, "_owned", True):
             self.b.destroy(self.h)
-            self.h = C.c_void_p()
+        self.h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -113,3 +125,101 @@ class Handle:
         self._chk(self.b.kernel_times(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), n),
                   "kernel_times")
         return out
+
+
+def _batch_fns(lib):
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int)
+    sigs = {
+        "fil_create_batch": (C.c_int, [C.c_int, C.POINTER(_abi.fil_config), C.POINTER(_abi.fil_tables),
+                                       C.POINTER(vp)]),
+        "fil_batch_destroy": (C.c_int, [vp]),
+        "fil_batch_last_error": (C.c_char_p, [vp]),
+        "fil_batch_size": (C.c_int, [vp]),
+        "fil_batch_member": (vp, [vp, C.c_int]),
+        "fil_batch_tune": (C.c_int, [vp, C.c_int, dp, C.c_int]),
+        "fil_batch_plan": (C.c_int, [vp, ip, ip, dp]),
+        "fil_batch_run": (C.c_int, [vp, dp, dp, C.c_int64, C.POINTER(_abi.fil_stats)]),
+    }
+    out = {}
+    for name, (res, args) in sigs.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+        out[name[4:]] = f
+    return out
+
+
+class Batch:
+    """Many RT problems stepped together on one device (fil_create_batch):
+    one CUDA graph per z-step runs every member's step, each member with
+    its own adaptive-dz controller.  `members[i]` is a Handle for member i
+    (set_field, get_field, analyze, set_option)."""
+
+    def __init__(self, problems, binding=None):
+        self.b = binding if binding is not None else load_library()
+        self.f = _batch_fns(self.b.lib)
+        self.problems = list(problems)
+        n = len(self.problems)
+        cfgs = (_abi.fil_config * n)(*[p.config for p in self.problems])
+        tabs = (_abi.fil_tables * n)(*[p.tables for p in self.problems])
+        self.ptr = C.c_void_p()
+        code = self.f["create_batch"](n, cfgs, tabs, C.byref(self.ptr))
+        if code < 0:
+            msg = self.f["batch_last_error"](None)
+            raise _abi.FilError(code, "fil_create_batch failed: %s" % (msg.decode() if msg else "?"))
+        self.members = [Handle.borrow(self.b, p, self.f["batch_member"](self.ptr, i))
+                        for i, p in enumerate(self.problems)]
+
+    def __len__(self):
+        return len(self.members)
+
+    def _chk(self, code, what):
+        if code < 0:
+            msg = self.f["batch_last_error"](self.ptr)
+            raise _abi.FilError(code, "fil_batch_%s failed: %s" % (what, msg.decode() if msg else "?"))
+        return code
+
+    def tune(self, max_branches=16):
+        """Runs the autotuner; returns the batch step time (ms) per branch
+        count tried (1, 2, 4, ...)."""
+        ms = np.zeros(8)
+        self._chk(self.f["batch_tune"](self.ptr, int(max_branches), ms.ctypes.data_as(C.POINTER(C.c_double)),
+                                       len(ms)), "tune")
+        return {1 << j: float(v) for j, v in enumerate(ms) if v > 0}
+
+    def plan(self):
+        n = len(self.members)
+        br = np.zeros(n, dtype=np.int32)
+        simt = np.zeros(n, dtype=np.int32)
+        cost = np.zeros(n)
+        ip = C.POINTER(C.c_int)
+        k = self._chk(self.f["batch_plan"](self.ptr, br.ctypes.data_as(ip), simt.ctypes.data_as(ip),
+                                           cost.ctypes.data_as(C.POINTER(C.c_double))), "plan")
+        return {"branches": k, "branch": br.tolist(), "dht_simt": simt.tolist(), "cost_ms": cost.tolist()}
+
+    def run(self, z0, zmax, nmax):
+        """Every member i from z0[i] to zmax[i] (scalars broadcast), at most
+        nmax steps; returns (code, [stats of each member])."""
+        n = len(self.members)
+        z0 = np.ascontiguousarray(np.broadcast_to(np.asarray(z0, dtype=np.float64), (n,)))
+        zm = np.ascontiguousarray(np.broadcast_to(np.asarray(zmax, dtype=np.float64), (n,)))
+        st = (_abi.fil_stats * n)()
+        dp = C.POINTER(C.c_double)
+        code = self._chk(self.f["batch_run"](self.ptr, z0.ctypes.data_as(dp), zm.ctypes.data_as(dp), int(nmax), st),
+                         "run")
+        return code, [st[i].as_dict() for i in range(n)]
+
+    def close(self):
+        if self.ptr:
+            for m in self.members:
+                m.h = C.c_void_p()
+            self.f["batch_destroy"](self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -62,7 +62,7 @@ class AStep:
 class Simulation:
     """Everything Filament.run builds (Filament.jl:72-79)."""
 
-    def __init__(self, input, binding=None, precision="mixed"):
+    def __init__(self, input, binding=None, precision="mixed", make_handle=True):
         g = input["geometry"]
         self.geometry = g
         self.unit = Units.Unit(g, input["p_unit"])
@@ -82,17 +82,25 @@ class Simulation:
             pe = plasma_dict["init"](self.grid.t, None, w0, units, plasma_dict)
         self.problem = Problem(g, self.unit, self.grid, self.field.w0, self.medium, self.guard,
                                resps, pe, keys, input["p_dzadaptive"], precision)
-        self.handle = Handle(self.problem, binding)
-        self.handle.set_field(self.field.E0, analytic=False)
         self.z = input["z"]
         self.zmax = input["zmax"]
         self.Istop = input["Istop"]
         self.dzadaptive = AStep(self.problem.config)
-        self.analyzer = FieldAnalyzer(g, self.grid, self.handle, self.z)
+        self.handle = None
+        if make_handle:
+            self.attach(Handle(self.problem, binding))
+
+    def attach(self, handle):
+        """Uses `handle` (made from self.problem, e.g. a batch member) and
+        uploads the initial field."""
+        self.handle = handle
+        self.handle.set_field(self.field.E0, analytic=False)
+        self.analyzer = FieldAnalyzer(self.geometry, self.grid, self.handle, self.z)
         self.analyzer.analyze(self.z)
 
     def close(self):
-        self.handle.close()
+        if self.handle is not None:
+            self.handle.close()
 
 
 def run(input, binding=None, precision="mixed", device_loop=False, write_files=True,

@@ -328,6 +328,44 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol);
  * that used the network                                                    */
 int fil_get_surrogate_stats(fil_handle* h, double* out, int n);
 
+/* ---- batched parameter sweep ------------------------------------------------
+ * Many RT problems with uneven (Nr, Nt) grids stepped together.  The
+ * reference runs one problem per Filament.run call (src/Filament.jl:
+ * 100-172); a sweep there is a host loop over decks.  Here the members'
+ * z-steps (src/Filament.jl:123-172 with Models.zstep, Models.jl:75-121, and
+ * the adaptive step, AdaptiveSteps.jl:96-107, each member with its own
+ * controller) are one CUDA graph per z-step whose branches run the members
+ * concurrently.
+ * fil_create_batch: n members from cfg[n] and tab[n] (RT only); the members
+ *   are handles owned by the batch (fil_batch_member), used with
+ *   fil_set_field, fil_get_field, fil_analyze and fil_set_option as usual;
+ *   do not destroy them.  A member may not have the surrogate armed.
+ * fil_batch_tune: the autotuner.  For every member it times one z-step with
+ *   each Hankel transform kernel the member can run (tensor-core 128 x 128
+ *   FP16-slice tiles, or CUDA-core 128 x 128 FP32 tiles) and keeps the
+ *   faster; then it assigns the members to 1, 2, 4, ... max_branches
+ *   concurrent branches (longest measured step first, to the least loaded
+ *   branch) and keeps the branch count whose graph runs fastest.
+ *   ms_per_branches[j] (j < n_out, may be NULL) receives the batch step
+ *   time with 2^j branches (0 where not tried).  Field states and
+ *   controllers are restored after the trials.
+ * fil_batch_run: every member i from z0[i] to zmax[i] (or nmax steps, or
+ *   Istop), stats[i] as fil_run's.  Returns FIL_OK, or the negative status
+ *   of the first member that failed.
+ * fil_batch_plan: branch, Hankel kernel (1 = CUDA core) and step cost (ms,
+ *   measured by the tuner, else a size model) of each member; returns the
+ *   branch count.                                                          */
+typedef struct fil_batch fil_batch;
+int fil_create_batch(int n, const fil_config* cfg, const fil_tables* tab, fil_batch** out);
+int fil_batch_destroy(fil_batch* b);
+const char* fil_batch_last_error(const fil_batch* b);
+int fil_batch_size(const fil_batch* b);
+fil_handle* fil_batch_member(fil_batch* b, int i);
+int fil_batch_tune(fil_batch* b, int max_branches, double* ms_per_branches, int n_out);
+int fil_batch_plan(const fil_batch* b, int* branch, int* dht_simt, double* cost_ms);
+int fil_batch_run(fil_batch* b, const double* z0, const double* zmax, int64_t nmax,
+                  fil_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif
