@@ -2,11 +2,10 @@
 // buffers, without any device allocation.
 //
 // Some callers cannot allocate device memory at the point where they need
-// the propagator: code that runs inside a region where cudaMalloc is not
-// allowed (for example while the caller itself is capturing a CUDA graph, or
-// in a host that pre-reserves all device memory and hands out fixed pools),
-// or a caller that must not grow the process's memory footprint after start-
-// up.  fil_hankel_propagate_noalloc serves them: the caller passes every
+// the propagator: a host that pre-reserves all device memory and hands out
+// fixed pools, a loop that must not pay for the device-wide synchronisation
+// of cudaMalloc/cudaFree, or a caller that must not grow the process's
+// memory footprint after start-up.  fil_hankel_propagate_noalloc serves them: the caller passes every
 // input and the output; the one intermediate (the Hankel-transformed,
 // propagated spectrum) lives in a file-scope __device__ array of fixed size
 // that every GPU loading this library holds until the process exits.

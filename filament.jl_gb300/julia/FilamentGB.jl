@@ -43,4 +43,26 @@ analyze(h, F, P, rho_end) = ccall((:fil_analyze, LIB), Cint,
     (Ptr{Cvoid}, Ptr{FilStats}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), h, C_NULL, F, P, rho_end)
 get_field!(h, E::Array{ComplexF64}) =
     ccall((:fil_get_field, LIB), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}, Cint, Cint), h, E, 1, 0)
+
+# batched sweep: members on uneven grids, one CUDA graph per z-step
+function create_batch(cfgs::Vector{FilConfig}, tabs::Vector{FilTables})
+    b = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:fil_create_batch, LIB), Cint, (Cint, Ptr{FilConfig}, Ptr{FilTables}, Ref{Ptr{Cvoid}}),
+               length(cfgs), cfgs, tabs, b)
+    rc < 0 && error(unsafe_string(ccall((:fil_batch_last_error, LIB), Cstring, (Ptr{Cvoid},), C_NULL)))
+    return b[]
+end
+batch_member(b, i) = ccall((:fil_batch_member, LIB), Ptr{Cvoid}, (Ptr{Cvoid}, Cint), b, i - 1)
+function batch_tune!(b, max_branches=16)
+    ms = zeros(8)
+    ccall((:fil_batch_tune, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint), b, max_branches, ms, 8)
+    return ms
+end
+function batch_run!(b, z0::Vector{Float64}, zmax::Vector{Float64}, nmax)
+    st = Vector{FilStats}(undef, length(z0))
+    rc = ccall((:fil_batch_run, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Int64, Ptr{FilStats}),
+               b, z0, zmax, nmax, st)
+    return rc, st
+end
+batch_destroy(b) = ccall((:fil_batch_destroy, LIB), Cint, (Ptr{Cvoid},), b)
 end
