@@ -270,63 +270,71 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
-// Layer 0 (3 -> 64, tanh): x [rows][3][T] -> y [rows][T][64].  One thread
-// per time point (128 per block) computes all 64 channels: its 27 inputs in
-// registers, the weights broadcast from shared memory as float4 (four FMA
-// per shared load); rows b = blockIdx.y, + gridDim.y, ...
+// Layer 0 (3 -> 64, tanh): x [rows][3][T] -> y [rows][T][64].  A block of
+// 128 threads takes one (row, 256-point tile) work item at a time (flat
+// index over rows x tiles, stride gridDim.x); each thread computes all 64
+// channels of two time points (tile + tid, tile + tid + 128): their 2 x 27
+// inputs in registers, the weights broadcast from shared memory as float4
+// (eight FMA per shared load).
 __global__ void __launch_bounds__(128) k_nn_l0_cl(const __nv_bfloat16* __restrict__ x,
                                                   const __nv_bfloat16* __restrict__ w,   // [ci][k][co]
                                                   const float* __restrict__ bias, __nv_bfloat16* y, int T,
                                                   int maxrows, const int* count, const int* stop) {
-  constexpr int TT = 128, W2 = TT + NN_K - 1, NI = NN_IN * NN_K;
+  constexpr int NTH = 128, TT = 2 * NTH, W2 = TT + NN_K - 1, NI = NN_IN * NN_K;
   __shared__ float xs[NN_IN][W2];
   __shared__ __align__(16) float ws[NI][64];
   __shared__ __align__(16) float bs[64];
   if (stop && *stop) return;
   const int nb = count ? min(*count, maxrows) : maxrows;
   const int tid = threadIdx.x;
-  for (int i = tid; i < NI * 64; i += TT) ws[i / 64][i % 64] = __bfloat162float(w[i]);
+  for (int i = tid; i < NI * 64; i += NTH) ws[i / 64][i % 64] = __bfloat162float(w[i]);
   if (tid < 64) bs[tid] = bias[tid];
-  const int t0 = blockIdx.x * TT, t = t0 + tid;
-  for (int b = blockIdx.y; b < nb; b += gridDim.y) {
+  const int tiles = (T + TT - 1) / TT;
+  for (int item = blockIdx.x; item < nb * tiles; item += gridDim.x) {
+    const int b = item / tiles, t0 = (item - b * tiles) * TT;
     __syncthreads();
-    for (int i = tid; i < NN_IN * W2; i += TT) {
+    for (int i = tid; i < NN_IN * W2; i += NTH) {
       const int ci = i / W2, j = i - ci * W2, tt = t0 + j - NN_HALF;
       xs[ci][j] = (tt >= 0 && tt < T) ? __bfloat162float(x[((size_t)b * NN_IN + ci) * T + tt]) : 0.f;
     }
     __syncthreads();
-    float xv[NI];
+    float xa[NI], xb[NI];
 #pragma unroll
     for (int ci = 0; ci < NN_IN; ++ci)
 #pragma unroll
-      for (int k = 0; k < NN_K; ++k) xv[ci * NN_K + k] = xs[ci][tid + k];
-    uint4* dst = reinterpret_cast<uint4*>(y + ((size_t)b * T + t) * 64);
+      for (int k = 0; k < NN_K; ++k) {
+        xa[ci * NN_K + k] = xs[ci][tid + k];
+        xb[ci * NN_K + k] = xs[ci][tid + NTH + k];
+      }
+    const int ta = t0 + tid, tb = ta + NTH;
+    uint4* da = reinterpret_cast<uint4*>(y + ((size_t)b * T + ta) * 64);
+    uint4* db = reinterpret_cast<uint4*>(y + ((size_t)b * T + tb) * 64);
 #pragma unroll 1
     for (int g = 0; g < 8; ++g) {
       const float4 c0 = reinterpret_cast<const float4*>(bs)[2 * g], c1 = reinterpret_cast<const float4*>(bs)[2 * g + 1];
-      float acc[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+      float aa[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+      float ab[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
 #pragma unroll
       for (int i = 0; i < NI; ++i) {
         const float4 w0 = reinterpret_cast<const float4*>(ws[i])[2 * g];
         const float4 w1 = reinterpret_cast<const float4*>(ws[i])[2 * g + 1];
-        acc[0] = fmaf(w0.x, xv[i], acc[0]);
-        acc[1] = fmaf(w0.y, xv[i], acc[1]);
-        acc[2] = fmaf(w0.z, xv[i], acc[2]);
-        acc[3] = fmaf(w0.w, xv[i], acc[3]);
-        acc[4] = fmaf(w1.x, xv[i], acc[4]);
-        acc[5] = fmaf(w1.y, xv[i], acc[5]);
-        acc[6] = fmaf(w1.z, xv[i], acc[6]);
-        acc[7] = fmaf(w1.w, xv[i], acc[7]);
-      }
-      if (t < T) {
-        uint32_t pk[4];
+        const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(acc[2 * e]), nt_tanh(acc[2 * e + 1]));
-          pk[e] = *reinterpret_cast<const uint32_t*>(&h);
+        for (int e = 0; e < 8; ++e) {
+          aa[e] = fmaf(wv[e], xa[i], aa[e]);
+          ab[e] = fmaf(wv[e], xb[i], ab[e]);
         }
-        dst[g] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
+      uint32_t pa[4], pb[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const __nv_bfloat162 ha = __floats2bfloat162_rn(nt_tanh(aa[2 * e]), nt_tanh(aa[2 * e + 1]));
+        const __nv_bfloat162 hb = __floats2bfloat162_rn(nt_tanh(ab[2 * e]), nt_tanh(ab[2 * e + 1]));
+        pa[e] = *reinterpret_cast<const uint32_t*>(&ha);
+        pb[e] = *reinterpret_cast<const uint32_t*>(&hb);
+      }
+      if (ta < T) da[g] = make_uint4(pa[0], pa[1], pa[2], pa[3]);
+      if (tb < T) db[g] = make_uint4(pb[0], pb[1], pb[2], pb[3]);
     }
   }
 }
@@ -365,8 +373,19 @@ int nn_weight_map(CUtensorMap* m, const __nv_bfloat16* wt) {
 
 cudaError_t nn_launch_l0_cl(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* y,
                             int T, int maxrows, const int* count, const int* stop, cudaStream_t st) {
-  const int gx = (T + 127) / 128, gy = std::max(1, std::min(maxrows, (152 * 16 + gx - 1) / gx));
-  k_nn_l0_cl<<<dim3(gx, gy), 128, 0, st>>>(x, w, bias, y, T, maxrows, count, stop);
+  static int resident = 0;   // blocks per SM at this kernel's register and shared-memory use
+  if (!resident) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_nn_l0_cl, 128, 0);
+    if (e != cudaSuccess) return e;
+    resident = std::max(1, resident);
+  }
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                cudaSuccess || sms < 1)
+    sms = 152;
+  const int tiles = (T + 255) / 256;
+  const int grid = std::max(1, std::min(maxrows * tiles, sms * resident));
+  k_nn_l0_cl<<<grid, 128, 0, st>>>(x, w, bias, y, T, maxrows, count, stop);
   return cudaGetLastError();
 }
 
