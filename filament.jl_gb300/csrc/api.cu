@@ -63,6 +63,7 @@ struct fil_handle {
   int ns;
   double A0[4], A1[4], B[4];
   double sc = 1, sf = 1, sl = 1, sr = 1;   // response channel pre-scales
+  double cc_max = -1;                      // linear-only row test (FP32 form), < 0: off
   std::complex<double> c0 = 0.0;           // XY: i QZ(w0) Rnl_cubic(w0)
   bool field_set = false, store_plasma = false;
   int bugcompat = 0, clamp_last = 0, timing = 0;
@@ -229,6 +230,14 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
       return a[a.size() / 2];
     };
     h->sc = scale(t->rnl_cubic);
+    if (!h->fp64) {
+      // the FP32 form skips the stages of rows whose nonlinear step is below
+      // its resolution (k_rowstep); the FP64 form computes every row
+      h->cc_max = 0;
+      if (t->rnl_cubic && t->qz && (c.resp_mask & FIL_RESP_CUBIC))
+        for (int k = 0; k < nh; ++k) h->cc_max = std::max(h->cc_max, std::abs(coef(t->rnl_cubic, k)));
+      if (!std::isfinite(h->cc_max)) h->cc_max = -1;
+    }
     h->sf = scale(t->rnl_free);
     h->sl = scale(t->rnl_losses);
     h->sr = scale(t->rnl_raman);
@@ -503,6 +512,7 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
   P.raman_thg = c.raman_thg;
   P.ramh = (const C*)h->ramh;
   P.sc = (R)h->sc;
+  P.cc_max = (R)h->cc_max;
   P.sf = (R)h->sf;
   P.sl = (R)h->sl;
   P.ns = h->ns;
