@@ -832,15 +832,33 @@ FIL_DEV void nn_features(const RowParams<R>& P, const typename C2T<R>::type* X, 
   G.L[0][0] = 0;
   G.B[0] = tsum;
   R S = aff_block_exclusive_scan<R, 1>(G, sc).B[0];
+  // the thread's 16 consecutive points of each channel, packed and written
+  // as two 16-byte stores per channel (one channel at a time, the scanned
+  // channel first so that its per-step rates are released early)
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const int j = j0 + q;
-    const C e = X[pad16(j)];
-    const float I = fmaxf((float)(e.x * e.x + e.y * e.y), 1e-30f);
-    f[j] = __float2bfloat16_rn(__logf(I) * 0.0625f);
-    f[N + j] = __float2bfloat16_rn((float)(e.x * e.x) / I);
-    f[2 * N + j] = __float2bfloat16_rn(__logf(fmaxf((float)S, 1e-30f)) * 0.0625f);
-    S += wl[q];
+  for (int cc = 0; cc < 3; ++cc) {
+    const int ch = (cc + 2) % 3;
+    uint32_t pk[8];
+#pragma unroll
+    for (int q = 0; q < 16; q += 2) {
+      float v[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const C e = X[pad16(j0 + q + u)];
+        const float I = fmaxf((float)(e.x * e.x + e.y * e.y), 1e-30f);
+        if (ch == 0) v[u] = __logf(I) * 0.0625f;
+        else if (ch == 1) v[u] = (float)(e.x * e.x) / I;
+        else {
+          v[u] = __logf(fmaxf((float)S, 1e-30f)) * 0.0625f;
+          S += wl[q + u];
+        }
+      }
+      const __nv_bfloat162 h = __floats2bfloat162_rn(v[0], v[1]);
+      pk[q / 2] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    uint4* d = reinterpret_cast<uint4*>(f + ch * N + j0);
+    d[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    d[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
   }
 }
 
