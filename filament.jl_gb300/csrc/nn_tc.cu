@@ -78,6 +78,17 @@ static __device__ __forceinline__ float nt_tanh(float x) {
   return y;
 }
 
+// two FP32 FMAs in one instruction (fma.rn.f32x2): lane-wise
+// round-to-nearest, the same results as fmaf on each lane
+static __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n .reg .b64 a, b, c, d;\n mov.b64 a, {%2, %3};\n mov.b64 b, {%4, %5};\n mov.b64 c, {%6, %7};\n"
+      " fma.rn.f32x2 d, a, b, c;\n mov.b64 {%0, %1}, d;\n}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
 struct NtParams {
   const float* bias;       // [64]
   __nv_bfloat16* out;      // [rows][T][64] (layer 1)
@@ -99,7 +110,9 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
   extern __shared__ __align__(1024) uint8_t nt_smem[];
   __shared__ volatile int s_fail;
   __shared__ __align__(16) float s_bias[64];
-  __shared__ __align__(16) float s_w3[FINAL ? NN_K * 64 : 4];   // [k][ci]
+  // layer-3 weights as tap pairs: s_w3[(kp * 64 + ci) * 2 + u] = w3[ci][2 kp + u]
+  // (kp < 5; the tenth tap is zero)
+  __shared__ __align__(16) float s_w3[FINAL ? 5 * 64 * 2 : 4];
   if (p.stop && *p.stop) return;
   const int nrows = p.count ? min(*p.count, p.maxrows) : p.maxrows;
   const int ntiles = nrows * p.tiles_per_row;
@@ -119,7 +132,10 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
   if (tid == 0) s_fail = 0;
   if (tid < 64) s_bias[tid] = p.bias[tid];
   if (FINAL)
-    for (int i = tid; i < NN_K * 64; i += NT_THREADS) s_w3[(i % NN_K) * 64 + i / NN_K] = __bfloat162float(p.w3[i]);
+    for (int i = tid; i < 5 * 64 * 2; i += NT_THREADS) {
+      const int u = i & 1, ci = (i >> 1) & 63, k = 2 * (i >> 7) + u;
+      s_w3[i] = k < NN_K ? __bfloat162float(p.w3[ci * NN_K + k]) : 0.f;
+    }
   if (warp == 0) tc::tmem_alloc(tmem_slot, 128);
   if (tid == 0) {
     for (int s = 0; s < NT_STAGES; ++s) {
@@ -221,23 +237,20 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
           }
         }
         float* dst = p.part + (size_t)b * NN_K * p.T + t;
+        // P_k = sum_ci w3[ci][k] y[ci], taps k and k+1 in one fma.rn.f32x2;
+        // two chains per tap pair (even and odd ci), joined at the end
 #pragma unroll
-        for (int k = 0; k < NN_K; ++k) {
-          const float4* wk = reinterpret_cast<const float4*>(s_w3 + 64 * k);
-          float a0 = 0.f, a1 = 0.f;
+        for (int kp = 0; kp < 5; ++kp) {
+          const float4* wk = reinterpret_cast<const float4*>(s_w3 + kp * 128);
+          float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
 #pragma unroll
-          for (int q = 0; q < 16; q += 2) {
-            const float4 u = wk[q], v = wk[q + 1];
-            a0 = fmaf(u.x, y[4 * q], a0);
-            a0 = fmaf(u.y, y[4 * q + 1], a0);
-            a0 = fmaf(u.z, y[4 * q + 2], a0);
-            a0 = fmaf(u.w, y[4 * q + 3], a0);
-            a1 = fmaf(v.x, y[4 * q + 4], a1);
-            a1 = fmaf(v.y, y[4 * q + 5], a1);
-            a1 = fmaf(v.z, y[4 * q + 6], a1);
-            a1 = fmaf(v.w, y[4 * q + 7], a1);
+          for (int ci = 0; ci < 64; ci += 2) {
+            const float4 w = wk[ci / 2];   // (w3[ci][2kp], w3[ci][2kp+1], w3[ci+1][2kp], w3[ci+1][2kp+1])
+            a0 = fma2(make_float2(w.x, w.y), make_float2(y[ci], y[ci]), a0);
+            a1 = fma2(make_float2(w.z, w.w), make_float2(y[ci + 1], y[ci + 1]), a1);
           }
-          dst[(size_t)k * p.T] = a0 + a1;
+          dst[(size_t)(2 * kp) * p.T] = a0.x + a1.x;
+          if (2 * kp + 1 < NN_K) dst[(size_t)(2 * kp + 1) * p.T] = a0.y + a1.y;
         }
       } else if (t < p.T) {
         uint4* dst = reinterpret_cast<uint4*>(p.out + ((size_t)b * p.T + t) * 64);
@@ -314,16 +327,32 @@ __global__ void __launch_bounds__(128) k_nn_l0_cl(const __nv_bfloat16* __restric
       const float4 c0 = reinterpret_cast<const float4*>(bs)[2 * g], c1 = reinterpret_cast<const float4*>(bs)[2 * g + 1];
       float aa[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
       float ab[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+      // channel pairs in fma.rn.f32x2 (the same per-lane FMA sequence)
+      float2 a2[4], b2[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        a2[e] = make_float2(aa[2 * e], aa[2 * e + 1]);
+        b2[e] = make_float2(ab[2 * e], ab[2 * e + 1]);
+      }
 #pragma unroll
       for (int i = 0; i < NI; ++i) {
         const float4 w0 = reinterpret_cast<const float4*>(ws[i])[2 * g];
         const float4 w1 = reinterpret_cast<const float4*>(ws[i])[2 * g + 1];
-        const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+        const float2 wv[4] = {make_float2(w0.x, w0.y), make_float2(w0.z, w0.w), make_float2(w1.x, w1.y),
+                              make_float2(w1.z, w1.w)};
+        const float2 xa2 = make_float2(xa[i], xa[i]), xb2 = make_float2(xb[i], xb[i]);
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          aa[e] = fmaf(wv[e], xa[i], aa[e]);
-          ab[e] = fmaf(wv[e], xb[i], ab[e]);
+        for (int e = 0; e < 4; ++e) {
+          a2[e] = fma2(wv[e], xa2, a2[e]);
+          b2[e] = fma2(wv[e], xb2, b2[e]);
         }
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        aa[2 * e] = a2[e].x;
+        aa[2 * e + 1] = a2[e].y;
+        ab[2 * e] = b2[e].x;
+        ab[2 * e + 1] = b2[e].y;
       }
       uint32_t pa[4], pb[4];
 #pragma unroll
