@@ -301,7 +301,7 @@ def time_xyt(steps, warmup=3):
     return out
 
 
-def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True):
+def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1, dist=None):
     """The 64-pulse parameter sweep: members drawn from `seed` (Nr from
     {256, 512, 1000}, Nt from {1024, 2048, 4096}, 2-10 Pcr, +-500 fs^2 chirp,
     w0 0.5-2 mm; RK4, adaptive dz, the workload's air model) in one batch,
@@ -309,55 +309,91 @@ def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True):
     batch steps, then `steps` batch steps timed on the host clock around
     fil_batch_run (the batch's ~3 GB state is far larger than L2).
     Accuracy: every member's field and fluence against the plain FP64 form
-    run alone from the same initial field to the same z (last dz clamped)."""
+    run alone from the same initial field to the same z (last dz clamped).
+    With world > 1 each rank runs its shard of the members on its own GPU
+    (no exchange); the wall time and the error maxima are reduced by MAX
+    over the ranks, the z-steps by SUM (strong scaling: the member set is
+    fixed).  Every rank makes the same collective calls, also after an
+    error."""
     import numpy as np
     import filament_gb as fg
     from filament_gb import _abi, sweep
-    params = sweep.draw(n, seed)
-    t0 = time.perf_counter()
-    sw = sweep.Sweep(params)
-    setup_s = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    tune = sw.tune(16)
-    tune_s = time.perf_counter() - t0
-    plan = sw.plan()
-    sw.run(zmax=3.0, nmax=warmup, z0=0.0)
-    steps0 = [m.stats()["steps"] for m in sw.batch.members]
-    t0 = time.perf_counter()
-    code, st = sw.run(zmax=3.0, nmax=steps)
-    wall = time.perf_counter() - t0
-    taken = [s["steps"] - a for s, a in zip(st, steps0)]
-    pts = [p["Nr"] * p["Nt"] for p in params]
+    params_all = sweep.draw(n, seed)
+    mine = sweep.shard(params_all, rank, world) if world > 1 else list(range(n))
+    params = [params_all[i] for i in mine]
     out = {"workload": "%d RT pulses (seed %d): Nr in {256,512,1000}, Nt in {1024,2048,4096}, 2-10 Pcr, "
                        "+-500 fs^2 chirp, w0 0.5-2 mm; RK4, adaptive dz" % (n, seed),
-           "members": n, "grid_points": int(sum(pts)), "timed_batch_steps": steps,
-           "z_steps_total": int(sum(taken)), "wall_s": wall,
-           "z_steps_per_s": sum(taken) / wall, "batch_steps_per_s": steps / wall,
-           "ms_per_batch_step": 1000.0 * wall / steps,
-           "tuner": {"ms_per_batch_step_by_branches": tune, "branches": plan["branches"],
-                     "cuda_core_dht_members": int(sum(plan["dht_simt"])), "tune_s": tune_s},
-           "setup_s": setup_s, "status": [s["status"] for s in st],
+           "members": n, "grid_points": int(sum(p["Nr"] * p["Nt"] for p in params_all)),
+           "timed_batch_steps": steps, "ranks": world, "scaling": "strong" if world > 1 else None,
            "l2": "batch state ~3 GB, larger than L2"}
+    err = None
+    sw = None
+    wall, taken, errs, ferrs, zs = 0.0, [], [], [], []
+    try:
+        if params:
+            t0 = time.perf_counter()
+            sw = sweep.Sweep(params)
+            out["setup_s"] = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            tune = sw.tune(16)
+            plan = sw.plan()
+            out["tuner"] = {"ms_per_batch_step_by_branches": tune, "branches": plan["branches"],
+                            "cuda_core_dht_members": int(sum(plan["dht_simt"])),
+                            "tune_s": time.perf_counter() - t0}
+            sw.run(zmax=3.0, nmax=warmup, z0=0.0)
+    except Exception as e:   # reported in the line; the headline stands
+        err = str(e)
+    if dist is not None:
+        dist.barrier()
+    try:
+        if sw is not None and err is None:
+            steps0 = [m.stats()["steps"] for m in sw.batch.members]
+            t0 = time.perf_counter()
+            code, st = sw.run(zmax=3.0, nmax=steps)
+            wall = time.perf_counter() - t0
+            taken = [s["steps"] - a for s, a in zip(st, steps0)]
+            out["status"] = [s["status"] for s in st]
+            zs = [s["z"] for s in st]
+            if accuracy:
+                F = [m.analyze()["fluence"] for m in sw.batch.members]
+                E = sw.fields()
+                sw.close()
+                sw = None
+                for i, p in enumerate(params):
+                    ref = fg.Simulation(sweep.member_input(p), precision="fp64")
+                    ref.handle.set_option(_abi.OPT_CLAMP_LAST_DZ, 1)
+                    ref.handle.run(0.0, zs[i], 10 ** 6)
+                    Ed = ref.handle.get_field()
+                    Fd = ref.handle.analyze()["fluence"]
+                    ref.close()
+                    errs.append(float(np.linalg.norm(E[i] - Ed) / np.linalg.norm(Ed)))
+                    ferrs.append(float(np.linalg.norm(F[i] - Fd) / np.linalg.norm(Fd)))
+    except Exception as e:
+        err = str(e)
+    if sw is not None:
+        sw.close()
+    emax = max(errs) if errs else 0.0
+    fmax = max(ferrs) if ferrs else 0.0
+    total = float(sum(taken))
+    failed = 1.0 if err else 0.0
+    if dist is not None:
+        import torch
+        t = torch.tensor([wall, emax, fmax, failed], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall, emax, fmax, failed = (float(v) for v in t)
+        c = torch.tensor([total], dtype=torch.float64)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        total = float(c[0])
+    if failed:
+        out["error"] = err or "failed on another rank"
+        return out
+    out.update({"z_steps_total": int(total), "wall_s": wall, "z_steps_per_s": total / wall,
+                "batch_steps_per_s": steps / wall, "ms_per_batch_step": 1000.0 * wall / steps})
     if accuracy:
-        zs = [s["z"] for s in st]
-        F = [m.analyze()["fluence"] for m in sw.batch.members]
-        E = sw.fields()
-        sw.close()
-        errs, ferrs = [], []
-        for i, p in enumerate(params):
-            ref = fg.Simulation(sweep.member_input(p), precision="fp64")
-            ref.handle.set_option(_abi.OPT_CLAMP_LAST_DZ, 1)
-            ref.handle.run(0.0, zs[i], 10 ** 6)
-            Ed = ref.handle.get_field()
-            Fd = ref.handle.analyze()["fluence"]
-            ref.close()
-            errs.append(float(np.linalg.norm(E[i] - Ed) / np.linalg.norm(Ed)))
-            ferrs.append(float(np.linalg.norm(F[i] - Fd) / np.linalg.norm(Fd)))
-        out["accuracy_vs_fp64"] = {"field_rel_l2_max": max(errs), "field_rel_l2_median": float(np.median(errs)),
-                                   "fluence_rel_l2_max": max(ferrs), "z_end_min": min(zs), "z_end_max": max(zs),
-                                   "field_rel_l2": errs}
-    else:
-        sw.close()
+        out["accuracy_vs_fp64"] = {"field_rel_l2_max": emax, "fluence_rel_l2_max": fmax}
+        if world == 1:
+            out["accuracy_vs_fp64"].update({"field_rel_l2_median": float(np.median(errs)),
+                                            "z_end_min": min(zs), "z_end_max": max(zs), "field_rel_l2": errs})
     return out
 
 
@@ -503,7 +539,9 @@ def main():
     import build as _b
     _b.build()
     if args.sweep_only:
-        print(json.dumps({"sweep": time_sweep(steps=args.sweep_steps)}))
+        r = time_sweep(steps=args.sweep_steps, rank=rank, world=world, dist=dist)
+        if rank == 0:
+            print(json.dumps({"sweep": r}))
         return
     # the surrogate is trained before any timed region
     net, train_info = surrogate_train(iters=args.train_iters)
@@ -529,17 +567,13 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_local = float(t[0])
     value = world * 1000.0 / t_local
+    # the sweep shards its members over the ranks (every rank takes part)
+    sweep64 = None if args.no_sweep else time_sweep(steps=args.sweep_steps, rank=rank, world=world, dist=dist)
     if rank != 0:
         return
     e2e = e2e_device_loop(net, args.accuracy_zend, surr["timed_steps"])
     e2e_plain = e2e_host_loop(max(10, min(300, mixed["timed_steps"])))
     xyt = None if args.no_xyt else time_xyt(args.xyt_steps)
-    sweep64 = None
-    if not args.no_sweep:
-        try:
-            sweep64 = time_sweep(steps=args.sweep_steps)
-        except Exception as e:   # reported in the line; the headline stands
-            sweep64 = {"error": str(e)}
     acc = None if args.no_accuracy else accuracy_run(args.accuracy_zend, 200000, net=net)
     sps_cpu, cpu_wall = cpu_oracle(args.cpu_steps)
     hbm, bf16, src = _peaks()

@@ -8,7 +8,9 @@ its own grid, tables, field state and adaptive-dz controller, and the
 autotuner (fil_batch_tune) picks each member's Hankel transform kernel and
 the number of concurrent branches from measured step times.
 
-`draw` makes the 64-pulse sweep's parameters from a seed: Nr from
+`shard` splits the members over the ranks of a multi-GPU run (one process
+per GPU, no data exchange; only the timing and the error maxima are
+reduced).  `draw` makes the 64-pulse sweep's parameters from a seed: Nr from
 {256, 512, 1000}, Nt from {1024, 2048, 4096}, peak power uniform in
 2-10 Pcr, linear chirp (spectral phase phi2 (w - w0)^2 / 2) uniform in
 +-500 fs^2, and beam radius w0 uniform in 0.5-2 mm, all with numpy's PCG64.
@@ -43,6 +45,31 @@ def draw(n=64, seed=0):
     w0 = rng.uniform(0.5, 2.0, n)
     return [dict(Nr=int(nr[i]), Nt=int(nt[i]), PPcr=float(p[i]), chirp_fs2=float(chirp[i]),
                  beam_a0=float(w0[i]) * 1e-3) for i in range(n)]
+
+
+def step_cost(params):
+    """Relative cost of one z-step of a member: the two Hankel GEMMs
+    (Mpad^2 Nt, tensor cores) and the row work (Mpad Nt log Nt)."""
+    mpad = (params["Nr"] + 127) // 128 * 128
+    nt = params["Nt"]
+    return 0.1 * mpad * mpad * nt + 40.0 * mpad * nt * np.log2(nt)
+
+
+def shard(params, rank, world):
+    """Indices of the members that rank `rank` of `world` runs: members are
+    independent, so the sweep splits across GPUs without any exchange.
+    Longest step first, each to the rank with the least total cost (ties
+    to the lower rank); the same on every rank."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad rank %r of world %r" % (rank, world))
+    order = sorted(range(len(params)), key=lambda i: (-step_cost(params[i]), i))
+    load = [0.0] * world
+    owner = [0] * len(params)
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        owner[i] = r
+        load[r] += step_cost(params[i])
+    return [i for i in range(len(params)) if owner[i] == rank]
 
 
 def member_input(params, deck=RT_DECK, **over):
