@@ -476,6 +476,47 @@ def e2e_host_loop(steps):
             "d2h_bytes_per_step": int((3 * nr + nt) * 8 + 64 + field_bytes / steps)}
 
 
+def time_c1(cpu_steps=300):
+    """The plain method at the reference's CPU-runnable size: RT 256 x 1024,
+    3 Pcr, RK2, fixed dz = 1 mm over 1 m (the RT deck's defaults).  GPU: the
+    whole run through fil_run (device loop, CUDA graphs) on the host clock,
+    mixed and FP64 forms, each after a 3-step warm-up of the same handle and
+    a fresh upload of the initial field; the mixed field and fluence against
+    the FP64 ones at z = 1 m (the same fixed steps).  CPU: the FP64 oracle on
+    all host cores, `cpu_steps` steps from z = 0 (a bounded sample)."""
+    import numpy as np
+    import filament_gb as fg
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    inp = fg.prepare(DECK)
+    out = {"workload": "RT 256x1024, 3 Pcr, RK2, dz = 1 mm fixed, z = 0..1 m"}
+    fields = {}
+    for prec in ("mixed", "fp64"):
+        sim = fg.Simulation(inp, precision=prec)
+        sim.handle.run(0.0, inp["zmax"], 3)
+        sim.handle.set_field(sim.field.E0, analytic=False)
+        s0 = sim.handle.stats()["steps"]
+        t0 = time.perf_counter()
+        code, st = sim.handle.run(0.0, inp["zmax"], 10 ** 6)
+        wall = time.perf_counter() - t0
+        n = st["steps"] - s0
+        out[prec] = {"z_steps_per_s": n / wall, "steps": int(n), "wall_s": wall, "status": code, "z_end": st["z"]}
+        fields[prec] = (sim.handle.get_field(), sim.handle.analyze()["fluence"])
+        sim.close()
+    (Em, Fm), (Ed, Fd) = fields["mixed"], fields["fp64"]
+    out["mixed"]["rel_l2_field_vs_fp64"] = float(np.linalg.norm(Em - Ed) / np.linalg.norm(Ed))
+    out["mixed"]["rel_l2_fluence_vs_fp64"] = float(np.linalg.norm(Fm - Fd) / np.linalg.norm(Fd))
+    out["speedup_mixed_over_fp64"] = out["mixed"]["z_steps_per_s"] / out["fp64"]["z_steps_per_s"]
+    ref = fg.Simulation(inp, binding=oracle.binding())
+    t0 = time.perf_counter()
+    code, st = ref.handle.run(0.0, inp["zmax"], cpu_steps)
+    wall = time.perf_counter() - t0
+    ref.close()
+    out["cpu_oracle"] = {"z_steps_per_s": st["steps"] / wall, "steps": int(st["steps"]), "wall_s": wall,
+                         "cores": os.cpu_count(), "kind": "port"}
+    return out
+
+
 def cpu_oracle(steps):
     import filament_gb as fg
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -503,6 +544,7 @@ def main():
     ap.add_argument("--xyt-steps", type=int, default=10)
     ap.add_argument("--train-iters", type=int, default=3000, help="Adam iterations of the surrogate")
     ap.add_argument("--no-sweep", action="store_true", help="skip the 64-pulse batched sweep")
+    ap.add_argument("--no-c1", action="store_true", help="skip the 256 x 1024 plain-method run")
     ap.add_argument("--sweep-steps", type=int, default=40)
     ap.add_argument("--sweep-only", action="store_true", help="only the batched sweep (one JSON line)")
     ap.add_argument("--profile", action="store_true",
@@ -574,6 +616,12 @@ def main():
     e2e = e2e_device_loop(net, args.accuracy_zend, surr["timed_steps"])
     e2e_plain = e2e_host_loop(max(10, min(300, mixed["timed_steps"])))
     xyt = None if args.no_xyt else time_xyt(args.xyt_steps)
+    c1 = None
+    if not args.no_c1:
+        try:
+            c1 = time_c1()
+        except Exception as e:   # reported in the line; the headline stands
+            c1 = {"error": str(e)}
     acc = None if args.no_accuracy else accuracy_run(args.accuracy_zend, 200000, net=net)
     sps_cpu, cpu_wall = cpu_oracle(args.cpu_steps)
     hbm, bf16, src = _peaks()
@@ -620,6 +668,7 @@ def main():
         "accuracy": acc,
         "xyt_512": xyt,
         "sweep_64": sweep64,
+        "c1_256x1024": c1,
         "roofline": {"kernel": "k_rowstep (plasma + RK4 nonlinear step, fused)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": src, "traffic": row_traffic,
