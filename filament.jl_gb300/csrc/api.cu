@@ -1660,6 +1660,7 @@ int fil_batch_tune(fil_batch* b, int max_branches, double* ms_per_branches, int 
   max_branches = std::max(1, std::min(std::min(max_branches, kBatchMaxBranches), n));
   BatchSaved sv;
   rc = batch_save(b, sv);
+  const bool saved = rc == 0;   // every member's state copied
   if (!rc) rc = batch_arm_trial(b, sv);
   // 1. the Hankel transform kernel of each member
   for (int i = 0; i < n && !rc; ++i) {
@@ -1689,21 +1690,25 @@ int fil_batch_tune(fil_batch* b, int max_branches, double* ms_per_branches, int 
   b->tune_ms.clear();
   int best_k = 1;
   double best_ms = 0;
+  // errors end the trials through rc, so that the states are still restored
+  // and the saved copies freed below
+  auto ck = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && !rc) rc = bfail(b, FIL_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  };
   for (int k = 1; k <= max_branches && !rc; k *= 2) {
     batch_assign(b, k);
     rc = batch_build_graph(b);
     if (rc) break;
     const int reps = 5;
     for (int s = 0; s < 1 + reps && !rc; ++s) {
-      if (s == 1) CKB(cudaEventRecord(b->ev[kBatchMaxBranches + 1], b->st));
-      cudaError_t e = cudaGraphLaunch(b->graph, b->st);
-      if (e != cudaSuccess) rc = bfail(b, FIL_ERR_CUDA, std::string("batch replay: ") + cudaGetErrorString(e));
+      if (s == 1) ck(cudaEventRecord(b->ev[kBatchMaxBranches + 1], b->st), "batch timing");
+      if (!rc) ck(cudaGraphLaunch(b->graph, b->st), "batch replay");
     }
-    if (rc) break;
-    CKB(cudaEventRecord(b->ev[kBatchMaxBranches + 2], b->st));
-    CKB(cudaEventSynchronize(b->ev[kBatchMaxBranches + 2]));
     float t = 0;
-    CKB(cudaEventElapsedTime(&t, b->ev[kBatchMaxBranches + 1], b->ev[kBatchMaxBranches + 2]));
+    if (!rc) ck(cudaEventRecord(b->ev[kBatchMaxBranches + 2], b->st), "batch timing");
+    if (!rc) ck(cudaEventSynchronize(b->ev[kBatchMaxBranches + 2]), "batch timing");
+    if (!rc) ck(cudaEventElapsedTime(&t, b->ev[kBatchMaxBranches + 1], b->ev[kBatchMaxBranches + 2]), "batch timing");
+    if (rc) break;
     const double ms = t / reps;
     b->tune_ms.push_back(ms);
     if (k == 1 || ms < best_ms) {
@@ -1713,8 +1718,11 @@ int fil_batch_tune(fil_batch* b, int max_branches, double* ms_per_branches, int 
     rc = batch_restore(b, sv);
     if (!rc) rc = batch_arm_trial(b, sv);
   }
-  // the members' states as they were before tuning
-  if (!rc) rc = batch_restore(b, sv);
+  // the members' states as they were before tuning (also after a failed trial)
+  if (saved) {
+    const int rr = batch_restore(b, sv);
+    if (!rc) rc = rr;
+  }
   batch_free_saved(sv);
   for (int i = 0; i < n && !rc; ++i) rc = check_tc(b->m[i]) ? bfail(b, FIL_ERR_TIMEOUT, b->m[i]->err) : 0;
   if (rc) return rc;
