@@ -107,7 +107,10 @@ class Sweep:
         the deck's), at most nmax steps."""
         n = len(self.sims)
         if z0 is None:
-            z0 = [m.stats()["z"] if m.stats()["steps"] else s.z for s, m in zip(self.sims, self.batch.members)]
+            z0 = []
+            for s, m in zip(self.sims, self.batch.members):
+                st = m.stats()
+                z0.append(st["z"] if st["steps"] else s.z)
         if zmax is None:
             zmax = [s.zmax for s in self.sims]
         return self.batch.run(np.broadcast_to(np.asarray(z0, float), (n,)),
