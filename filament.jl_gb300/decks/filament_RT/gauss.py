@@ -13,13 +13,16 @@ def initial_condition(r, t, ru, tu, Iu):
     n0 = math.sqrt(permittivity(w0))
     Pcr = 3.79 * lam0 ** 2 / (8 * pi * n0 * n2)      # Media.critical_power
     I0 = PPcr * Pcr / (pi * a0 ** 2)
-    R, T = np.meshgrid(r, t, indexing="ij")
+    # separable: beam factor of r times pulse factor of t, each evaluated on
+    # its axis (element by element the same products as on the full grid)
+    r = np.asarray(r, dtype=float)
+    t = np.asarray(t, dtype=float)
+    beam = np.sqrt(I0 / Iu) * np.exp(-0.5 * (r * ru) ** 2 / a0 ** 2)
     if chirp_fs2 != 0.0:
         # the transform-limited spectrum times exp(i phi2 (w - w0)^2 / 2):
         # complex envelope (t0 / tau) exp(-t^2 / (2 tau^2)), tau^2 = t0^2 - i phi2
         tau2 = t0 ** 2 - 1j * chirp_fs2 * 1e-30
-        env = np.sqrt(t0 ** 2 / tau2) * np.exp(-0.5 * (T * tu) ** 2 / tau2)
-        return (np.sqrt(I0 / Iu) * np.exp(-0.5 * (R * ru) ** 2 / a0 ** 2)
-                * np.real(env * np.exp(1j * w0 * T * tu))) + 0j
-    return (np.sqrt(I0 / Iu) * np.exp(-0.5 * (R * ru) ** 2 / a0 ** 2)
-            * np.exp(-0.5 * (T * tu) ** 2 / t0 ** 2) * np.cos(w0 * T * tu)) + 0j
+        env = np.sqrt(t0 ** 2 / tau2) * np.exp(-0.5 * (t * tu) ** 2 / tau2)
+        return (beam[:, None] * np.real(env * np.exp(1j * w0 * t * tu))[None, :]) + 0j
+    return (beam[:, None] * np.exp(-0.5 * (t * tu) ** 2 / t0 ** 2)[None, :]
+            * np.cos(w0 * t * tu)[None, :]) + 0j
