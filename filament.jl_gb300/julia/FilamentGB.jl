@@ -1,5 +1,5 @@
 # FilamentGB.jl -- ccall binding of libfilament_gb.so for Filament.jl.
-# Mirrors include/filament_gb.h; see INTEGRATION.md for the replacement of
+# Mirrors include/filament_gb.h; `run!` replaces the step loop of
 # Filament.main_loop (src/Filament.jl:111-184).  Not executed in this
 # environment (no Julia); the Python binding filament_gb/_abi.py is the
 # tested twin.

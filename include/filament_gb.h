@@ -270,7 +270,9 @@ int fil_kernel_times(fil_handle* h, double* ms, int n);
  * The one intermediate lives in a fixed 16 MiB __device__ array that every
  * GPU loading this library holds until exit; the call allocates and frees
  * nothing.  The first call on a device looks up that array's device address
- * (do it before any stream capture).  All calls share the array: calls that
+ * (do it before any stream capture); the lookup is redone when the device's
+ * current context has changed since (a cudaDeviceReset in between, for
+ * example).  All calls share the array: calls that
  * overlap on the GPU (different streams or threads) race.  Runs on `stream`
  * (NULL = default stream) and returns without synchronising; errors go to
  * fil_last_error(NULL).                                                     */

@@ -76,19 +76,26 @@ def _bench_rank(rank, world, port, out):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     import bench
+    from filament_gb import sweep
+
+    class FailingSweep:
+        # the failure is made on the host: creating the batch raises on
+        # every rank, with or without a GPU
+        def __init__(self, *a, **k):
+            raise RuntimeError("injected batch creation failure")
+
+    sweep.Sweep = FailingSweep
     r = bench.time_sweep(n=4, steps=2, warmup=1, rank=rank, world=world, dist=dist)
     out.put((rank, r))
     dist.destroy_process_group()
 
 
 def test_sharded_sweep_makes_the_same_collectives_after_an_error():
-    """Without a GPU every rank fails to create its batch; all ranks still
-    reach the barrier and the reductions, and report the error instead of
-    waiting on each other."""
+    """Every rank fails to create its batch (a failure injected on the
+    host); all ranks still reach the barrier and the reductions, and report
+    the error instead of waiting on each other."""
     import multiprocessing as mp
     import socket
-    import build as b
-    b.build()
     s = socket.socket()
     s.bind(("127.0.0.1", 0))
     port = s.getsockname()[1]
@@ -103,4 +110,4 @@ def test_sharded_sweep_makes_the_same_collectives_after_an_error():
         p.join(timeout=60)
         assert p.exitcode == 0
     for rank, r in res:
-        assert r["ranks"] == 2 and "error" in r
+        assert r["ranks"] == 2 and "injected" in r["error"]

@@ -103,3 +103,7 @@ def test_noalloc_rejects_sizes_beyond_the_fixed_array(gpu_lib):
     rc = prop(one, one, one, one, one, None, None, 0, one, one, 4096, 1024, 1e-3, None)
     assert rc == -1
     assert b"exceeds" in last_error(None)
+    # an nh whose 2 * nh would overflow an int is rejected as too large too
+    rc = prop(one, one, one, one, one, None, None, 0, one, one, 128, 2 ** 30 + 64, 1e-3, None)
+    assert rc == -1
+    assert b"exceeds" in last_error(None)
