@@ -129,11 +129,14 @@ def _profiler(on):
 
 
 def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, simt_dht=False, net=None, profile=False):
-    """Warm-up steps in graph mode, then the timed steps from z = 0 (the
-    field re-uploaded) up to `steps` steps or z = zend, one at a time with L2
-    flushed, then the same range in graph mode (warm L2, for information);
-    with load_seconds > 0 graph-mode runs continue that long so the clock
-    sampler sees the kernels under sustained load."""
+    """Warm-up steps in graph mode; the whole run from z = 0 to zend in graph
+    mode (warm L2, for the step count n_run and for information); then the
+    timed run: from z = 0 again (the field re-uploaded), steps one at a time,
+    one step in every m = n_run // steps timed with L2 flushed before it, so
+    that exactly min(steps, n_run) timed steps are spread evenly over the
+    run (the collapse and the filament included).  With load_seconds > 0
+    graph-mode runs continue that long so the clock sampler sees the kernels
+    under sustained load."""
     import filament_gb as fg
     from filament_gb import _abi
     inp = _prepare()
@@ -145,11 +148,17 @@ def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, simt_dht=
         net.arm(h, every=SURR_EVERY, tol=SURR_TOL)
     h.run(0.0, zend, warmup)
     h.set_field(sim.field.E0, analytic=False)
-    h.set_option(_abi.OPT_TIMING, 1)
+    t1 = time.perf_counter()
+    code3, st3 = h.run(0.0, zend, 10 ** 9)
+    graph_wall = time.perf_counter() - t1
+    n_run = int(st3["steps"])
+    stride = max(1, n_run // max(1, steps))
+    h.set_field(sim.field.E0, analytic=False)
+    h.set_option(_abi.OPT_TIMING, stride)
     if profile:
         _profiler(True)
     t0 = time.perf_counter()
-    code, st2 = h.run(0.0, zend, steps)
+    code, st2 = h.run(0.0, zend, min(steps, n_run) * stride)
     wall = time.perf_counter() - t0
     if profile:
         _profiler(False)
@@ -159,17 +168,14 @@ def time_device_loop(precision, warmup, steps, zend, load_seconds=0.0, simt_dht=
         from filament_gb import surrogate as S
         sstats = S.stats(h)
     h.set_option(_abi.OPT_TIMING, 0)
-    h.set_field(sim.field.E0, analytic=False)
-    t1 = time.perf_counter()
-    code3, st3 = h.run(0.0, zend, steps)
-    graph_wall = time.perf_counter() - t1
     t2 = time.perf_counter()
     while time.perf_counter() - t2 < load_seconds:
         h.set_field(sim.field.E0, analytic=False)
         h.run(0.0, STABLE_Z, 10 ** 9)
     res = {"ms_per_step": kt[4], "row_ms": kt[0], "dht_fwd_ms": kt[1], "dht_inv_ms": kt[2],
-           "reduce_ms": kt[3], "timed_steps": int(kt[5]), "z_end": st2["z"], "wall_s": wall,
-           "graph_steps_per_s": st3["steps"] / graph_wall if graph_wall > 0 else None}
+           "reduce_ms": kt[3], "timed_steps": int(kt[5]), "run_steps": n_run, "stride": stride,
+           "z_last_timed": st2["z"], "wall_s": wall,
+           "graph_steps_per_s": n_run / graph_wall if graph_wall > 0 else None}
     if net is not None:
         res["surrogate_ms"] = kt[6]
         res["surrogate_stats"] = sstats
@@ -248,11 +254,12 @@ def surrogate_train(seed=1, iters=3000):
     return net, info
 
 
-def e2e_device_loop(net, zend, steps):
+def e2e_device_loop(net, zend):
     """The same metric end to end through the public API with the
-    surrogate armed: upload of the host field, the device loop (fil_run),
-    the reductions (fil_analyze: fluence, power, rho_end to the host) and
-    the download of the final field."""
+    surrogate armed, over the whole run: upload of the host field, the
+    device loop (fil_run) from z = 0 to zend, the reductions (fil_analyze:
+    fluence, power, rho_end to the host) and the download of the final
+    field."""
     import numpy as np
     import filament_gb as fg
     inp = _prepare()
@@ -262,7 +269,7 @@ def e2e_device_loop(net, zend, steps):
     sim.handle.run(0.0, zend, 8)                          # warm the kernels and the graph
     t0 = time.perf_counter()
     sim.handle.set_field(E0)                              # H2D of the field
-    code, st = sim.handle.run(0.0, zend, steps)
+    code, st = sim.handle.run(0.0, zend, 10 ** 9)
     a = sim.handle.analyze()                              # D2H of the reductions
     E = sim.handle.get_field()                            # D2H of the field
     wall = time.perf_counter() - t0
@@ -393,23 +400,33 @@ def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1,
         out["accuracy_vs_fp64"] = {"field_rel_l2_max": emax, "fluence_rel_l2_max": fmax}
         if world == 1:
             out["accuracy_vs_fp64"].update({"field_rel_l2_median": float(np.median(errs)),
-                                            "z_end_min": min(zs), "z_end_max": max(zs), "field_rel_l2": errs})
+                                            "z_end_min": min(zs), "z_end_max": max(zs)})
     return out
 
 
-def accuracy_run(zend, nmax, net=None):
-    """Mixed form (tensor-core and CUDA-core Hankel transforms) vs the plain
-    FP64 form from the same field to the same z (dz clamped on the last
-    step), relative L2 of the field and fluence."""
+def accuracy_run(zend, nmax, net=None, oracle_check=True):
+    """The GPU forms (mixed with tensor-core and with CUDA-core Hankel
+    transforms, mixed + surrogate, plain FP64) and the FP64 CPU oracle of
+    the reference's method (full spectrum kept, OpenMP on all host cores),
+    each from the same field to the same z (dz clamped on the last step);
+    relative L2 of the field and of the fluence against the oracle, and
+    against the GPU's own FP64 form."""
     import numpy as np
     import filament_gb as fg
     from filament_gb import _abi
     inp = _prepare(zmax=zend)
-    out = {}
+    out = {"z_end": zend}
     fields = {}
     forms = ("mixed", "mixed_simt", "fp64") + (("mixed_surrogate",) if net is not None else ())
+    if oracle_check:
+        forms = forms + ("oracle",)
     for prec in forms:
-        sim = fg.Simulation(inp, precision="fp64" if prec == "fp64" else "mixed")
+        if prec == "oracle":
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            sim = fg.Simulation(inp, binding=oracle.binding())
+        else:
+            sim = fg.Simulation(inp, precision="fp64" if prec == "fp64" else "mixed")
         if prec == "mixed_simt":
             sim.handle.set_option(_abi.OPT_DHT_SIMT, 1)
         if prec == "mixed_surrogate":
@@ -417,28 +434,28 @@ def accuracy_run(zend, nmax, net=None):
         sim.handle.set_option(_abi.OPT_CLAMP_LAST_DZ, 1)
         t0 = time.perf_counter()
         code, st = sim.handle.run(0.0, zend, nmax)
-        out[prec + "_wall_s"] = time.perf_counter() - t0
-        out[prec + "_steps"] = st["steps"]
-        out[prec + "_z"] = st["z"]
+        wall = time.perf_counter() - t0
         a = sim.handle.analyze()
-        fields[prec] = (sim.handle.get_field(), a["fluence"], a["imax"])
+        fields[prec] = (sim.handle.get_field(), a["fluence"])
+        out[prec] = {"steps": int(st["steps"]), "z": st["z"], "wall_s": wall, "imax_end": a["imax"]}
         if prec == "mixed_surrogate":
             from filament_gb import surrogate as S
             out["surrogate_stats"] = S.stats(sim.handle)
         sim.close()
-    Em, Fm, Im = fields["mixed"]
-    Ed, Fd, Id = fields["fp64"]
-    Es, Fs, Is = fields["mixed_simt"]
-    out["rel_l2_field"] = float(np.linalg.norm(Em - Ed) / np.linalg.norm(Ed))
-    out["rel_l2_fluence"] = float(np.linalg.norm(Fm - Fd) / np.linalg.norm(Fd))
-    out["cuda_core_dht_rel_l2_field"] = float(np.linalg.norm(Es - Ed) / np.linalg.norm(Ed))
-    out["cuda_core_dht_rel_l2_fluence"] = float(np.linalg.norm(Fs - Fd) / np.linalg.norm(Fd))
-    if net is not None:
-        Eu, Fu, Iu = fields["mixed_surrogate"]
-        out["surrogate_rel_l2_field"] = float(np.linalg.norm(Eu - Ed) / np.linalg.norm(Ed))
-        out["surrogate_rel_l2_fluence"] = float(np.linalg.norm(Fu - Fd) / np.linalg.norm(Fd))
-    out["imax_end"] = Id
-    out["z_end"] = zend
+
+    def err(a, b):
+        (Ea, Fa), (Eb, Fb) = fields[a], fields[b]
+        return {"field_rel_l2": float(np.linalg.norm(Ea - Eb) / np.linalg.norm(Eb)),
+                "fluence_rel_l2": float(np.linalg.norm(Fa - Fb) / np.linalg.norm(Fb))}
+    for prec in forms:
+        if prec in ("fp64", "oracle"):
+            continue
+        out[prec]["vs_fp64_gpu"] = err(prec, "fp64")
+        if oracle_check:
+            out[prec]["vs_oracle"] = err(prec, "oracle")
+    if oracle_check:
+        out["fp64"]["vs_oracle"] = err("fp64", "oracle")
+        out["oracle"]["cores"] = os.cpu_count()
     return out
 
 
@@ -539,6 +556,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=30)
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-oracle-accuracy", action="store_true",
+                    help="accuracy against the GPU FP64 form only (skips the ~100 s oracle run)")
     ap.add_argument("--accuracy-zend", type=float, default=ACCURACY_ZEND)
     ap.add_argument("--no-xyt", action="store_true", help="skip the 512^3 XYT measurement")
     ap.add_argument("--xyt-steps", type=int, default=10)
@@ -613,8 +632,8 @@ def main():
     sweep64 = None if args.no_sweep else time_sweep(steps=args.sweep_steps, rank=rank, world=world, dist=dist)
     if rank != 0:
         return
-    e2e = e2e_device_loop(net, args.accuracy_zend, surr["timed_steps"])
-    e2e_plain = e2e_host_loop(max(10, min(300, mixed["timed_steps"])))
+    e2e = e2e_device_loop(net, args.accuracy_zend)
+    e2e_plain = e2e_host_loop(max(10, min(300, mixed["run_steps"])))
     xyt = None if args.no_xyt else time_xyt(args.xyt_steps)
     c1 = None
     if not args.no_c1:
@@ -622,14 +641,17 @@ def main():
             c1 = time_c1()
         except Exception as e:   # reported in the line; the headline stands
             c1 = {"error": str(e)}
-    acc = None if args.no_accuracy else accuracy_run(args.accuracy_zend, 200000, net=net)
+    acc = None if args.no_accuracy else accuracy_run(args.accuracy_zend, 200000, net=net,
+                                                     oracle_check=not args.no_oracle_accuracy)
     sps_cpu, cpu_wall = cpu_oracle(args.cpu_steps)
     hbm, bf16, src = _peaks()
     nr, nt, s = WORKLOAD["Nr"], WORKLOAD["Nt"], 4
-    # algorithmic bytes of the row kernel per launch (complex 8 B, real 4 B):
-    # plasma (read E, write rho, Kdrho) + t->w (r+w) + s stages (read base and
-    # previous k, read rho and Kdrho, write k) + RK combine (read E, k1..ks,
-    # write E) = c(4s+5) + q(2s+2) per grid point
+    # algorithmic bytes of the row kernel per launch (complex 8 B, real 4 B),
+    # counted as the reference's separate passes move them: plasma (read E,
+    # write rho, Kdrho) + t->w (r+w) + s stages (read base and previous k,
+    # read rho and Kdrho, write k) + RK combine (read E, k1..ks, write E) =
+    # c(4s+5) + q(2s+2) per grid point.  The fused kernel itself moves
+    # 16 B in + 16 B out per (r, w) point; its DRAM traffic is row_traffic.
     b_row = nr * nt * (8 * (4 * s + 5) + 4 * (2 * s + 2))
     # DRAM bytes (read + write) of one k_rowstep launch of this workload,
     # from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); the
@@ -638,6 +660,15 @@ def main():
     # the row kernel of the headline form (its time without the network's)
     row_ms = surr["row_ms"] - surr["surrogate_ms"]
     achieved = b_row / (row_ms * 1e-3) / 1e9
+    # compute side of the row kernel: FP32 flops of its complex FFTs (5 N
+    # log2 N per N-point transform: field to time, t -> w, and per RK stage
+    # one inverse and two forward transforms) on every row; the responses,
+    # the plasma scan and the skipped rows' savings are not counted
+    lg = math.log2(nt)
+    row_flops = nr * (2 + 3 * s) * 5.0 * nt * lg
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12      # TFLOP/s at the sampled clock
+    row_tflops = row_flops / (row_ms * 1e-3) / 1e12
     # tensor-core Hankel transform: 2 Mpad^2 Nt FLOP per transform (FP32
     # product), executed as six FP16 slice products
     mpad = (nr + 127) // 128 * 128
@@ -648,6 +679,23 @@ def main():
     ss = surr["surrogate_stats"]
     f_nn = 2.0 * (3 * 64 * 9 + 2 * 64 * 64 * 9 + 64 * 9) * ss["rows_mean"] * nt
     nn_tf = f_nn / (surr["surrogate_ms"] * 1e-3) / 1e12 if surr["surrogate_ms"] > 0 else None
+    speed_surr = fp64["ms_per_step"] / surr["ms_per_step"]
+    headline = {"form": "mixed + learned surrogate", "z_steps_per_s": value,
+                "speedup_over_plain_fp64": speed_surr,
+                "speedup_mixed_over_plain_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
+                "surrogate_over_mixed_time": surr["ms_per_step"] / mixed["ms_per_step"],
+                "timed": "%d steps sampled evenly over z = 0..%.2f m (%d steps)" % (surr["timed_steps"],
+                                                                                   args.accuracy_zend,
+                                                                                   surr["run_steps"])}
+    if acc is not None:
+        key = "vs_oracle" if "oracle" in acc else "vs_fp64_gpu"
+        a = acc["mixed_surrogate"][key]
+        headline.update({"z_end": acc["z_end"], "accuracy_vs": key[3:],
+                         "field_rel_l2": a["field_rel_l2"], "fluence_rel_l2": a["fluence_rel_l2"],
+                         "target_met": bool(speed_surr >= 5.0 and a["field_rel_l2"] <= 1e-4
+                                            and a["fluence_rel_l2"] <= 1e-3)})
+        if "oracle" in acc:
+            headline["fp64_gpu_vs_oracle_field_rel_l2"] = acc["fp64"]["vs_oracle"]["field_rel_l2"]
     line = {
         "metric": "RT z-steps/s", "value": value, "unit": "z-steps/s", "n_gpus": args.gpus,
         "steps": surr["timed_steps"], "warmup": args.warmup, "ms_per_step": t_local,
@@ -655,9 +703,11 @@ def main():
         "data": "synthetic",
         "config": _config(args, {"form": "mixed precision (complex FP32, tcgen05 Hankel transforms) with the "
                                          "learned plasma surrogate (checked against the ODE every %d steps, "
-                                         "tol %g)" % (SURR_EVERY, SURR_TOL)}),
+                                         "tol %g)" % (SURR_EVERY, SURR_TOL),
+                                 "timed_steps": "one step in every %d of the %d-step run, L2 flushed before "
+                                                "each" % (surr["stride"], surr["run_steps"])}),
         "forms": {"mixed_surrogate": surr, "mixed": mixed, "mixed_cuda_core_dht": mixed_simt, "fp64": fp64,
-                  "speedup_surrogate_over_fp64": fp64["ms_per_step"] / surr["ms_per_step"],
+                  "speedup_surrogate_over_fp64": speed_surr,
                   "speedup_mixed_over_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
                   "surrogate_over_mixed_time": surr["ms_per_step"] / mixed["ms_per_step"]},
         "surrogate": {"training": train_info, "check_every": SURR_EVERY, "tol": SURR_TOL,
@@ -674,6 +724,12 @@ def main():
                      "peak_source": src, "traffic": row_traffic,
                      "traffic_source": "ncu, one k_rowstep launch of this workload",
                      "algorithmic_bytes_per_launch": b_row,
+                     "algorithmic_bytes_note": "notional: the bytes the reference's unfused passes move; the fused "
+                                               "kernel's own DRAM traffic is `traffic`",
+                     "compute": {"fp32_flops_per_launch": row_flops, "achieved_tflops": row_tflops,
+                                 "peak_tflops_fp32": fp32_peak, "frac": row_tflops / fp32_peak,
+                                 "peak_source": "152 SMs x 128 FP32 lanes x 2 x sampled SM clock",
+                                 "flops_note": "complex FFTs only, 5 N log2 N each, (2 + 3 s) per row"},
                      "dht_tensor": {"kernel": "k_dht_tc (tcgen05 kind::f16, 6 slice products), inverse transform",
                                     "achieved_tflops_f16": dht_tf,
                                     "ms_per_launch": surr["dht_inv_ms"]},
@@ -687,9 +743,10 @@ def main():
         "e2e": e2e,
         "e2e_host_loop_plain": e2e_plain,
         "clocks": clocks,
-        # per timed step: L2 flush, row reduction, controller, 4 network
-        # layers, row kernel, 2 x (slice + tensor-core transform)
-        "gpu_launches": 12 * surr["timed_steps"],
+        # per timed step: row reduction, controller, 4 network layers, row
+        # kernel, 2 x (slice + tensor-core transform)
+        "gpu_launches": 11 * surr["timed_steps"],
+        "headline": headline,
     }
     print(json.dumps(line))
 

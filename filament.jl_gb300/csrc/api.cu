@@ -66,7 +66,8 @@ struct fil_handle {
   double cc_max = -1;                      // linear-only row test (FP32 form), < 0: off
   std::complex<double> c0 = 0.0;           // XY: i QZ(w0) Rnl_cubic(w0)
   bool field_set = false, store_plasma = false;
-  int bugcompat = 0, clamp_last = 0, timing = 0;
+  int bugcompat = 0, clamp_last = 0;
+  int timing = 0;                      // FIL_OPT_TIMING: time one step in every `timing` (0: off)
   int gen = 0;                         // bumped by every option change (batch graphs rebuild)
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev[8];
@@ -1025,7 +1026,8 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
   } else if (option == FIL_OPT_CLAMP_LAST_DZ) {
     h->clamp_last = value != 0;
   } else if (option == FIL_OPT_TIMING) {
-    h->timing = value != 0;
+    if (value < 0 || value > (1 << 30)) return fail(h, FIL_ERR_ARG, "timing stride out of range");
+    h->timing = (int)value;
     for (int i = 0; i < 6; ++i) h->tsum[i] = 0;
     h->tcount = 0;
   } else if (option == FIL_OPT_DHT_SIMT) {
@@ -1154,23 +1156,28 @@ int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax, fil_stats* stat
     if (rc) return rc;
   }
   if (h->timing) {
-    // benchmark path: one step at a time, L2 flushed before each step
-    // (outside the timed events), device time of each kernel accumulated
+    // benchmark path: one step at a time; every `timing`-th step (the first
+    // included) is timed: L2 flushed before it (outside the timed events),
+    // device time of each kernel accumulated
     if (!h->flushbuf) {
       h->flushbytes = (size_t)512 << 20;
       CK(cudaMalloc(&h->flushbuf, h->flushbytes));
     }
-    for (;;) {
-      CK(launch_flush(h->flushbuf, h->flushbytes, h->st));
-      CK(cudaEventRecord(h->ev[0], h->st));
+    for (long n = 0;; ++n) {
+      const bool timed = (n % h->timing) == 0;
+      if (timed) {
+        CK(launch_flush(h->flushbuf, h->flushbytes, h->st));
+        CK(cudaEventRecord(h->ev[0], h->st));
+      }
       int rc = reduce(h, nullptr, 1);
       if (rc) return rc;
       CK(launch_control(h->ctl, h->fluence, h->pw, h->nrows, h->st));
-      rc = zstep(h, true);
+      rc = zstep(h, timed);
       if (rc) return rc;
       rc = read_ctl(h);
       if (rc) return rc;
       if (h->ctl_host->done) break;
+      if (!timed) continue;
       float t[4], tot;
       for (int i = 0; i < 4; ++i) CK(cudaEventElapsedTime(&t[i], h->ev[i], h->ev[i + 1]));
       CK(cudaEventElapsedTime(&tot, h->ev[0], h->ev[4]));

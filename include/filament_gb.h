@@ -92,10 +92,12 @@ extern "C" {
                                   indexed by the y index) in XYT           */
 #define FIL_OPT_CLAMP_LAST_DZ 3 /* fil_run shortens the last step so that z
                                   lands on zmax exactly (off = reference)  */
-#define FIL_OPT_TIMING 4       /* benchmark mode: fil_run runs steps one at
-                                  a time, writes a buffer larger than L2
-                                  before each step and records per-kernel
-                                  device times (fil_kernel_times)          */
+#define FIL_OPT_TIMING 4       /* benchmark mode (value m >= 1, 0 = off):
+                                  fil_run runs steps one at a time and times
+                                  every m-th (the first included): a buffer
+                                  larger than L2 is written before it and
+                                  its per-kernel device times are recorded
+                                  (fil_kernel_times)                       */
 #define FIL_OPT_DHT_SIMT 6      /* mixed form: run the Hankel transforms as
                                   FP32 CUDA-core GEMMs instead of the
                                   tcgen05 tensor-core GEMMs on exact FP16

@@ -36,6 +36,31 @@ def two_species_rates():
     return [n2, o2]
 
 
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def reference_air_components():
+    """The reference's two-species air (examples/RT/air.jl:96-108): N2 and
+    O2 with the multiphoton rates of its examples/RT/multiphoton_N2.tf and
+    multiphoton_O2.tf (copied to tests/golden), loaded by file name through
+    TFunction.from_file as init_photoionization_avalanche does."""
+    n2 = {"fraction": 0.79, "ionization_energy": 15.576,
+          "ionization_rate": os.path.join(GOLDEN, "multiphoton_N2.tf")}
+    o2 = {"fraction": 0.21, "ionization_energy": 12.063,
+          "ionization_rate": os.path.join(GOLDEN, "multiphoton_O2.tf")}
+    return [n2, o2]
+
+
+def saturating_rate(n=14):
+    """A tabulated rate that is not a power law: W = W8(I) / (1 + (I/Is)^5),
+    W8 the sigma_8 I^8 multiphoton rate of the decks, Is = 5e17 W/m^2, so
+    the local order d ln W / d ln I falls from 8 to 3 across the table (the
+    general interpolation branch and tfpower on distinct segments)."""
+    I = np.logspace(9.0, 20.0, n)
+    W = 8.85e12 * (I / 1e18) ** 8 / (1.0 + (I / 5e17) ** 5)
+    return I, W
+
+
 def pair(inp, precision="mixed", store_plasma=False, project=True):
     """(CUDA simulation, oracle simulation) on the same input.  With
     project=True the oracle drops negative frequencies after each t->w

@@ -68,7 +68,7 @@ def test_sweep_leg_reports_every_member(monkeypatch):
     assert r["z_steps_total"] == 24 and r["status"] == [3] * 6
     assert r["tuner"]["branches"] == 2
     acc = r["accuracy_vs_fp64"]
-    assert abs(acc["field_rel_l2_max"] - 1e-5) < 1e-9 and len(acc["field_rel_l2"]) == 6
+    assert abs(acc["field_rel_l2_max"] - 1e-5) < 1e-9 and abs(acc["field_rel_l2_median"] - 1e-5) < 1e-9
 
 
 def test_c1_leg_with_the_oracle_standing_in(monkeypatch, oracle_binding):
@@ -85,3 +85,24 @@ def test_c1_leg_with_the_oracle_standing_in(monkeypatch, oracle_binding):
         assert abs(r[form]["z_end"] - 0.02) < 1e-12
     assert r["mixed"]["rel_l2_field_vs_fp64"] < 1e-12   # the oracle computes both forms in FP64
     assert r["cpu_oracle"]["steps"] == 3 and r["cpu_oracle"]["z_steps_per_s"] > 0
+
+
+def test_accuracy_leg_with_the_oracle_standing_in(monkeypatch, oracle_binding):
+    """accuracy_run's bookkeeping (every form against the oracle and
+    against the GPU FP64 form) with the oracle standing in for the device
+    library on a 2 cm run of a 64 x 512 grid."""
+    import bench
+    import filament_gb as fg
+    prepare, Simulation = fg.prepare, fg.Simulation
+    monkeypatch.setattr(bench, "WORKLOAD", dict(bench.WORKLOAD, Nr=64, Nt=512, rmax=2.0, tmin=-100.0, tmax=100.0))
+    monkeypatch.setattr(fg, "Simulation",
+                        lambda inp, binding=None, precision="mixed": Simulation(inp, binding=oracle_binding,
+                                                                               precision=precision))
+    r = bench.accuracy_run(0.02, 1000)
+    assert r["z_end"] == 0.02
+    for form in ("mixed", "mixed_simt", "fp64", "oracle"):
+        assert abs(r[form]["z"] - 0.02) < 1e-12 and r[form]["steps"] >= 2
+    for form in ("mixed", "mixed_simt"):
+        assert r[form]["vs_oracle"]["field_rel_l2"] < 1e-12      # all FP64 here
+        assert r[form]["vs_fp64_gpu"]["fluence_rel_l2"] < 1e-12
+    assert r["fp64"]["vs_oracle"]["field_rel_l2"] < 1e-12

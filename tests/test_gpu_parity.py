@@ -8,7 +8,8 @@ bound for whole runs is 1e-4 relative L2 field error and 1e-3 fluence error.
 import numpy as np
 import pytest
 
-from gpu_helpers import pair, rel_l2, rt_input, step_both, two_species_rates
+from gpu_helpers import (pair, reference_air_components, rel_l2, rt_input, saturating_rate, step_both,
+                         two_species_rates)
 
 pytestmark = pytest.mark.gpu
 
@@ -186,3 +187,81 @@ def test_linear_only_rows_keep_parity(gpu_lib):
     code_r, st_r = r.handle.run(0.0, inp["zmax"], 10 ** 6)
     assert code_g == code_r == 1 and st_g["steps"] == st_r["steps"]
     assert rel_l2(g.handle.get_field(), r.handle.get_field()) < 10 * TOL["mixed"]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_reference_air_rate_tables(gpu_lib, precision):
+    """The reference's own air plasma (examples/RT/air.jl:96-121): N2 and O2
+    with the rate tables of multiphoton_N2.tf / multiphoton_O2.tf read from
+    file, KDEP = true (K from the tables' local order), rho_nt = 2.5e25,
+    RK3 plasma integrator.  Density, loss term and a full RK4 step against
+    the oracle."""
+    inp = rt_input(PPcr=150.0, ALG="RK4")
+    pe = inp["p_model"][1]
+    pe["components"] = reference_air_components()
+    pe["KDEP"] = True
+    pe["rho_nt"] = 2.5e25
+    g, r = pair(inp, precision, store_plasma=True)
+    assert g.problem.pe.rate_n == 10 and len(g.problem.pe.rho_nt) == 2
+    rho_g, rho_r = g.handle.get_plasma(0), r.handle.get_plasma(0)
+    kd_g, kd_r = g.handle.get_plasma(1), r.handle.get_plasma(1)
+    assert np.max(rho_r) > 1e-6
+    tol = TOL[precision]
+    assert rel_l2(rho_g, rho_r) < tol
+    assert rel_l2(kd_g, kd_r) < tol
+    step_both(g, r, 3, 1e-3)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < tol
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("kdep", [True, False])
+def test_tabulated_rate_general_branch(gpu_lib, precision, kdep):
+    """A rate table that is not a power law (local order 8 falling to 3):
+    the device interpolates it by segment search, and with KDEP the loss
+    term's K is the slope of the segment the intensity falls in."""
+    inp = rt_input(PPcr=150.0, ALG="RK4")
+    pe = inp["p_model"][1]
+    pe["components"] = [{"fraction": 1.0, "ionization_energy": 12.06, "ionization_rate": saturating_rate()}]
+    pe["KDEP"] = kdep
+    g, r = pair(inp, precision, store_plasma=True)
+    slopes = np.diff(g.problem.pe.rate_ly) / np.diff(g.problem.pe.rate_lx)
+    assert slopes.max() - slopes.min() > 3.0       # not a power law
+    rho_g, rho_r = g.handle.get_plasma(0), r.handle.get_plasma(0)
+    kd_g, kd_r = g.handle.get_plasma(1), r.handle.get_plasma(1)
+    assert np.max(rho_r) > 1e-6
+    tol = TOL[precision]
+    assert rel_l2(rho_g, rho_r) < tol
+    assert rel_l2(kd_g, kd_r) < tol
+    step_both(g, r, 3, 1e-3)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < tol
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_cubic_without_thg(gpu_lib, precision):
+    """cubic.jl:41-46 (THG = false): F = 3/4 |E|^2 Re(E), with plasma."""
+    inp = rt_input(PPcr=150.0, ALG="RK4")
+    inp["p_model"][0][0]["THG"] = False
+    g, r = pair(inp, precision)
+    assert g.problem.config.cubic_thg == 0
+    step_both(g, r, 3, 1e-3)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_ereal_losses_and_plasma(gpu_lib, precision):
+    """EREAL = true in current_losses (current_losses.jl:36-44: the loss
+    term divides by Re(E)^2) and in the plasma equation
+    (photoionization_avalanche.jl:1-17: the rate's argument is Re(E)^2)."""
+    inp = rt_input(PPcr=150.0, ALG="RK4")
+    responses = inp["p_model"][0]
+    for resp in responses:
+        if "EREAL" in resp:
+            resp["EREAL"] = True
+    inp["p_model"][1]["EREAL"] = True
+    g, r = pair(inp, precision, store_plasma=True)
+    assert g.problem.config.losses_ereal == 1 and g.problem.config.plasma_ereal == 1
+    tol = TOL[precision]
+    assert rel_l2(g.handle.get_plasma(0), r.handle.get_plasma(0)) < tol
+    assert rel_l2(g.handle.get_plasma(1), r.handle.get_plasma(1)) < tol
+    step_both(g, r, 3, 1e-3)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < tol
