@@ -41,7 +41,7 @@ def build(force=False, verbose=False, ptxas_v=False):
             sys.stderr.write(r.stderr)
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 4))) as ex:
         objs = list(ex.map(compile_one, sources()))
     tmp = LIB + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]

@@ -52,6 +52,18 @@ struct fil_handle {
   void* kt2 = nullptr; void* beta = nullptr; void* dfr = nullptr; void* kmax2 = nullptr; void* wg = nullptr;
   void* rho_g = nullptr; void* kdrho_g = nullptr;
   void* stage = nullptr;  // field staging [nrows][nt] complex
+  // upper half of the spectrum (RT; the reference keeps it, rowkernels.cuh):
+  // state [nrows][nh] complex, Re KZ [nrows][nh] FP64, (Im KZ, guard) [nrows][nh]
+  void* SU = nullptr;
+  double* u_kzr = nullptr;
+  void* u_kg = nullptr;
+  bool full_spec = false;   // SU carried (FIL_OPT_ANALYTIC_PROJECTION off)
+  // non-paraxial prefactor (QPARAXIAL = false, RT): per-stage buffers
+  // [mpad][nh] complex (S0, k1, k of the last stage, running sum) and the
+  // tensor-core path's factor QZ(kt, w) / QZ(w) * Kguard Wguard, [nh][mpad]
+  bool np = false;
+  void* np_S0 = nullptr; void* np_K1 = nullptr; void* np_KS = nullptr; void* np_ACC = nullptr;
+  void* qrt = nullptr;
   double* fluence = nullptr;   // [nrows]
   double* power = nullptr;     // [nt]
   double* pw = nullptr;        // [nrows] transverse weights
@@ -277,6 +289,40 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
       if (upload<R>(h, &h->wg, w)) return FIL_ERR_CUDA;
     }
   }
+  if (h->geom == FIL_GEOM_RT) {
+    // upper half of the spectrum, columns j = nh + k (FFTW order, w < 0 and
+    // the Nyquist bin): KZ(k_i, w_j) + frame (spectral.jl:78-101,160-184)
+    // and Kguard(k_i, w_j) Wguard(w_j) (Guards.jl:95-126), applied in
+    // r-space as the reference's broadcast does
+    std::vector<double> kr((size_t)nr * nh);
+    std::vector<double> kg((size_t)nr * nh * 2);
+    for (int i = 0; i < nr; ++i) {
+      const double kt2 = t->kt1[i] * t->kt1[i];
+      for (int k = 0; k < nh; ++k) {
+        const int j = nh + k;
+        const cd b(t->beta[2 * j], t->beta[2 * j + 1]), d(t->dfr[2 * j], t->dfr[2 * j + 1]);
+        cd K;
+        if (c.kparaxial) K = (b != cd(0, 0)) ? b - kt2 / (2.0 * b) : cd(0, 0);
+        else K = std::sqrt(b * b - kt2 + cd(0.0, 0.0));
+        K += d - b;
+        double g = 1.0;
+        if (t->kmax) {
+          const double km = t->kmax[j];
+          g = (km == 0.0) ? 0.0 : std::exp(-std::pow(kt2 / (km * km), 20));
+        }
+        if (t->wguard) g *= t->wguard[j];
+        kr[(size_t)i * nh + k] = K.real();
+        kg[2 * ((size_t)i * nh + k)] = K.imag();
+        kg[2 * ((size_t)i * nh + k) + 1] = g;
+      }
+    }
+    CK(cudaMalloc((void**)&h->u_kzr, kr.size() * sizeof(double)));
+    CK(cudaMemcpy(h->u_kzr, kr.data(), kr.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (upload<R>(h, &h->u_kg, kg)) return FIL_ERR_CUDA;
+    CK(cudaMalloc(&h->SU, (size_t)nr * nh * 2 * sizeof(R)));
+    CK(cudaMemset(h->SU, 0, (size_t)nr * nh * 2 * sizeof(R)));
+    h->full_spec = true;
+  }
   if (h->geom == FIL_GEOM_XYT || h->geom == FIL_GEOM_XY) {
     // transverse 2-D transform tables (xyfft.cu)
     const int nx = h->n1, ny = h->n2;
@@ -483,6 +529,53 @@ static int create_tc(fil_handle* h, const fil_tables* t) {
   return 0;
 }
 
+// Buffers of the non-paraxial prefactor (QPARAXIAL = false, RT): the
+// per-stage state, the density rows of the step's plasma solve, and for the
+// tensor-core path the factor QZ(kt_i, w_j) / QZ(w_j) * Kguard Wguard =
+// beta / sqrt(beta^2 - kt^2) * guard (Qfunc_nonparaxial,
+// nonlinear_propagators.jl:232-241; 0 where the root is 0), [nh][mpad].
+static int create_np(fil_handle* h, const fil_tables* t) {
+  typedef std::complex<double> cd;
+  const int n1 = h->n1, nh = h->nh, mp = h->mpad;
+  const size_t es = h->fp64 ? sizeof(double2) : sizeof(float2);
+  const size_t sz = (size_t)mp * nh * es;
+  for (void** b : {&h->np_S0, &h->np_K1, &h->np_KS, &h->np_ACC}) {
+    CK(cudaMalloc(b, sz));
+    CK(cudaMemset(*b, 0, sz));
+  }
+  if (h->cfg.plasma && !h->rho_g) {
+    const size_t rs = (size_t)h->nrows * h->nt * (h->fp64 ? sizeof(double) : sizeof(float));
+    CK(cudaMalloc(&h->rho_g, rs));
+    CK(cudaMalloc(&h->kdrho_g, rs));
+    CK(cudaMemset(h->rho_g, 0, rs));
+    CK(cudaMemset(h->kdrho_g, 0, rs));
+  }
+  if (h->use_tc) {
+    std::vector<float> q((size_t)nh * mp * 2, 0.f);
+    for (int i = 0; i < n1; ++i) {
+      const double kt2 = t->kt1[i] * t->kt1[i];
+      for (int j = 0; j < nh; ++j) {
+        const cd b(t->beta[2 * j], t->beta[2 * j + 1]);
+        const cd kz = std::sqrt(b * b - kt2 + cd(0.0, 0.0));
+        cd r = (kz == cd(0, 0)) ? cd(0, 0) : b / kz;
+        double g = 1.0;
+        if (t->kmax) {
+          const double km = t->kmax[j];
+          g = (km == 0.0) ? 0.0 : std::exp(-std::pow(kt2 / (km * km), 20));
+        }
+        if (t->wguard) g *= t->wguard[j];
+        r *= g;
+        q[((size_t)j * mp + i) * 2] = (float)r.real();
+        q[((size_t)j * mp + i) * 2 + 1] = (float)r.imag();
+      }
+    }
+    CK(cudaMalloc(&h->qrt, q.size() * sizeof(float)));
+    CK(cudaMemcpy(h->qrt, q.data(), q.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  h->np = true;
+  return 0;
+}
+
 template <typename R> static RowParams<R> row_params(fil_handle* h) {
   typedef typename C2T<R>::type C;
   RowParams<R> P;
@@ -531,6 +624,16 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
   P.ctl = h->ctl;
   P.out_T = 0;
   P.ldT = h->mpad;
+  if (h->full_spec) {
+    P.U_in = (const C*)h->SU;
+    P.U_out = (C*)h->SU;
+    P.u_kzr = h->u_kzr;
+    P.u_kg = (const C*)h->u_kg;
+  }
+  P.np_S0 = (C*)h->np_S0;
+  P.np_K1 = (const C*)h->np_K1;
+  P.np_KS = (const C*)h->np_KS;
+  P.np_ACC = (C*)h->np_ACC;
   return P;
 }
 
@@ -675,6 +778,59 @@ template <typename R> static int enqueue_zstep_xy(fil_handle* h, bool timed) {
   return 0;
 }
 
+// Hankel pair of a non-paraxial stage: k = M2 (QZ(kt, w)/QZ(w) Kguard Wguard)
+// (M1 W1), out = the stage's transformed right-hand side (row layout)
+template <typename R> static int enqueue_np_transverse(fil_handle* h, void* out) {
+  const int Nc = 2 * h->nh;
+  if (h->use_tc && sizeof(R) == 4) {
+    TcGemmParams p1;
+    std::memset(&p1, 0, sizeof p1);
+    p1.out = (float*)h->W2;
+    p1.ldo = h->mpad;
+    p1.K = h->mpad;
+    p1.mode = 1;
+    p1.qa = (const float*)h->qa1;
+    p1.qb = (const float*)h->qb;
+    p1.ldqb = Nc;
+    p1.ctl = h->ctl;
+    p1.err = h->tc_err;
+    CK(launch_slice((const float*)h->W1, h->BS, (float*)h->qb, Nc, h->mpad, h->ctl, h->st));
+    CK(launch_dht_tc(h->tm_a1, h->tm_b, p1, h->mpad, Nc, h->st));
+    TcGemmParams p2 = p1;
+    p2.out = (float*)out;
+    p2.ldo = Nc;
+    p2.mode = 3;
+    p2.qa = (const float*)h->qa2;
+    CK(launch_slice_mul((const float*)h->W2, (const float2*)h->qrt, h->BS, (float*)h->qb, h->nh, h->mpad, h->ctl,
+                        h->st));
+    CK(launch_dht_tc(h->tm_a2, h->tm_b, p2, h->mpad, Nc, h->st));
+  } else {
+    PropParams<R> pp = prop_params<R>(h);
+    CK(launch_dht_simt<R>((const R*)h->M1, (const R*)h->W1, (R*)h->W2, h->mpad, Nc, h->mpad, pp, h->ctl, 3, h->st));
+    CK(launch_dht_simt<R>((const R*)h->M2, (const R*)h->W2, (R*)out, h->mpad, Nc, h->mpad, pp, h->ctl, 4, h->st));
+  }
+  return 0;
+}
+
+// The nonlinear part of a z-step with the non-paraxial prefactor
+// (QPARAXIAL = false, nonlinear_propagators.jl:56-63): the plasma solve,
+// then per RK stage the row kernel's paraxial right-hand side, the Hankel
+// pair with QZ(kt, w) in between, and finally the RK combination into W1,
+// the linear step's operand.
+template <typename R> static int enqueue_nonlinear_np(fil_handle* h, RowParams<R>& P) {
+  typedef typename C2T<R>::type C;
+  if (h->cfg.plasma) CK(launch_rowstep<R>(P, h->nt, h->nc, 4, h->st));
+  P.S_out = (C*)h->W1;
+  for (int s = 0; s < h->ns; ++s) {
+    P.np_stage = s;
+    CK(launch_rowstage<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, h->st));
+    int rc = enqueue_np_transverse<R>(h, s == 0 ? h->np_K1 : h->np_KS);
+    if (rc) return rc;
+  }
+  CK(launch_np_combine<R>(P, h->nh, h->st));
+  return 0;
+}
+
 template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   if (h->geom == FIL_GEOM_XYT) return enqueue_zstep_xyt<R>(h, timed);
   if (h->geom == FIL_GEOM_XY) return enqueue_zstep_xy<R>(h, timed);
@@ -691,7 +847,12 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   if (timed) CK(cudaEventRecord(h->ev[1], h->st));
   CK(enqueue_surrogate<R>(h, P));
   if (timed) CK(cudaEventRecord(h->ev[5], h->st));
-  CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
+  if (h->np) {
+    int rc = enqueue_nonlinear_np<R>(h, P);
+    if (rc) return rc;
+  } else {
+    CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
+  }
   if (timed) CK(cudaEventRecord(h->ev[2], h->st));
   if (tcp) {
     TcGemmParams p1;
@@ -800,7 +961,8 @@ static void free_all(fil_handle* h) {
                   h->qa1, h->qa2, h->BS[0], h->BS[1], h->BS[2], h->qb, h->kzt, h->gdt, h->tc_err,
                   h->kx2, h->ky2, h->sg1, h->sg2, h->twx, h->twy,
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
-                  h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err};
+                  h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err,
+                  h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -860,7 +1022,8 @@ template <typename R> static int set_field_t(fil_handle* h, const void* E, int d
     return 0;
   }
   CK(cudaMemcpyAsync(h->stage, rows.data(), rows.size() * sizeof(R), cudaMemcpyHostToDevice, h->st));
-  CK(launch_field_in<R>((const C*)h->stage, (C*)h->S, h->nh, (const C*)h->tw, analytic, h->nrows, h->nt, h->st));
+  CK(launch_field_in<R>((const C*)h->stage, (C*)h->S, h->full_spec ? (C*)h->SU : nullptr, h->nh, (const C*)h->tw,
+                        analytic, h->nrows, h->nt, h->st));
   // control block: fresh simulation, no pending guard; an armed surrogate
   // stays armed with fresh counters
   DevCtl c;
@@ -927,8 +1090,8 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (cfg->geometry != FIL_GEOM_XY && (!is_pow2(cfg->nt) || cfg->nt < 512 || cfg->nt > 4096))
     return fail(h, FIL_ERR_UNSUPPORTED, "nt must be a power of two in [512, 4096]");
   if (cfg->n1 < 1 || cfg->n1 > 65536) return fail(h, FIL_ERR_ARG, "bad n1");
-  if (cfg->nonlinearity && !cfg->qparaxial)
-    return fail(h, FIL_ERR_UNSUPPORTED, "QPARAXIAL=false is not built");
+  if (cfg->nonlinearity && !cfg->qparaxial && cfg->geometry != FIL_GEOM_RT)
+    return fail(h, FIL_ERR_UNSUPPORTED, "QPARAXIAL=false is built for the RT geometry");
   if (cfg->nonlinearity && (cfg->resp_mask & FIL_RESP_RAMAN) && !t->raman_h)
     return fail(h, FIL_ERR_ARG, "missing Raman response table");
   if (cfg->plasma && (cfg->plasma_ncomp < 1 || cfg->plasma_ncomp > FIL_MAXCOMP))
@@ -999,6 +1162,7 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
     rc = create_tc(h, t);
     h->use_tc = (rc == 0);
   }
+  if (!rc && h->geom == FIL_GEOM_RT && cfg->nonlinearity && !cfg->qparaxial) rc = create_np(h, t);
   if (rc) {
     g_err = h->err;
     free_all(h);
@@ -1040,7 +1204,17 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
       if (rc) return rc;
     }
   } else if (option == FIL_OPT_ANALYTIC_PROJECTION) {
-    // the field state is the analytic half spectrum: always projected
+    // on: the state is the analytic half spectrum (the upper half dropped
+    // after every t->w transform); off (RT default): the upper half is kept
+    // as the reference keeps it.  XYT always projects.
+    const bool full = (value == 0) && h->SU != nullptr;
+    if (full != h->full_spec) {
+      if (full) {   // the upper half restarts from zero
+        CK(cudaMemsetAsync(h->SU, 0, (size_t)h->nrows * h->nh * (h->fp64 ? sizeof(double2) : sizeof(float2)), h->st));
+        CK(cudaStreamSynchronize(h->st));
+      }
+      h->full_spec = full;
+    }
   }
   else {
     return fail(h, FIL_ERR_ARG, "unknown option");

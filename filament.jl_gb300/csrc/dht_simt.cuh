@@ -71,6 +71,32 @@ FIL_DEV typename C2T<R>::type propagator(const PropParams<R>& P, R kt2, int j, R
   return mk<R>(amp * cs, amp * sn);
 }
 
+// Factor of the non-paraxial prefactor for transverse index i (kt2) and
+// frequency column j: QZ(kt, w) / QZ(w) = beta / kz, kz = sqrt(beta^2 - kt^2)
+// (0 where kz = 0, as Qfunc_nonparaxial, nonlinear_propagators.jl:232-241),
+// times the spectral guard Kguard Wguard.
+template <typename R>
+FIL_DEV typename C2T<R>::type qz_ratio(const PropParams<R>& P, R kt2, int j) {
+  typedef typename C2T<R>::type C;
+  const C b = P.beta[j];
+  const C b2 = cmul(b, b);
+  const C kz = csqrt_p<R>(mk<R>(b2.x - kt2, b2.y));
+  if (kz.x == (R)0 && kz.y == (R)0) return mk<R>(0, 0);
+  C q = cdiv<R>(b, kz);
+  R g = (R)1;
+  if (P.kmax2) {
+    R km2 = P.kmax2[j];
+    if (km2 == (R)0) {
+      g = 0;
+    } else {
+      R x = kt2 / km2, x2 = x * x, x4 = x2 * x2, x5 = x4 * x, x10 = x5 * x5;
+      g = exp(-(x10 * x10));
+    }
+  }
+  if (P.wg) g *= P.wg[j];
+  return mk<R>(g * q.x, g * q.y);
+}
+
 template <typename R> struct GemmVec;
 template <> struct GemmVec<float> {
   static FIL_DEV void ld4(const float* p, float (&v)[4]) {
@@ -95,7 +121,9 @@ template <> struct GemmVec<double> {
 // C[M x N] = A[M x K] B[K x N], row-major, M,K multiples of 128 / 8,
 // N multiple of 128.  256 threads, 128x128 tile, 8x8 outputs per thread.
 // EPI = 1: multiply complex pairs of C by the propagator (row i, column
-// j = col/2); EPI = 2: plain store and mark the field guard pending.
+// j = col/2); EPI = 2: plain store and mark the field guard pending;
+// EPI = 3: multiply by the non-paraxial prefactor's factor (qz_ratio);
+// EPI = 4: plain store.
 template <typename R, int EPI>
 __global__ void __launch_bounds__(256) k_dht_simt(const R* __restrict__ A, const R* __restrict__ B,
                                                   R* __restrict__ C, int M, int N, int K,
@@ -161,15 +189,16 @@ __global__ void __launch_bounds__(256) k_dht_simt(const R* __restrict__ A, const
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int row = bm + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
-    R kt2 = (EPI == 1) ? pp.kt2[row] : (R)0;
+    R kt2 = (EPI == 1 || EPI == 3) ? pp.kt2[row] : (R)0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int col = bn + h * 64 + tx * 4;
       R v[4] = {acc[i][h * 4 + 0], acc[i][h * 4 + 1], acc[i][h * 4 + 2], acc[i][h * 4 + 3]};
-      if (EPI == 1) {
+      if (EPI == 1 || EPI == 3) {
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
-          typename C2T<R>::type pr = propagator<R>(pp, kt2, (col >> 1) + p, dz);
+          typename C2T<R>::type pr = EPI == 1 ? propagator<R>(pp, kt2, (col >> 1) + p, dz)
+                                              : qz_ratio<R>(pp, kt2, (col >> 1) + p);
           R re = v[2 * p], im = v[2 * p + 1];
           v[2 * p] = re * pr.x - im * pr.y;
           v[2 * p + 1] = re * pr.y + im * pr.x;

@@ -34,8 +34,20 @@ cudaError_t launch_slice_prop(const float* W, const float2* kz, const float* gd,
   const int nch = K / TC_CHUNK;
   __half2 *s0 = (__half2*)s[0], *s1 = (__half2*)s[1], *s2 = (__half2*)s[2];
   if (nch % 2 == 0)
-    k_slice_prop<2><<<(nh * (nch / 2) + 7) / 8, 256, 0, st>>>(W, kz, gd, s0, s1, s2, qb, nh, K, ctl, 0.f);
+    k_slice_prop<2, false><<<(nh * (nch / 2) + 7) / 8, 256, 0, st>>>(W, kz, gd, s0, s1, s2, qb, nh, K, ctl, 0.f);
   else
-    k_slice_prop<1><<<(nh * nch + 7) / 8, 256, 0, st>>>(W, kz, gd, s0, s1, s2, qb, nh, K, ctl, 0.f);
+    k_slice_prop<1, false><<<(nh * nch + 7) / 8, 256, 0, st>>>(W, kz, gd, s0, s1, s2, qb, nh, K, ctl, 0.f);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_slice_mul(const float* W, const float2* f, void* const (&s)[3], float* qb, int nh, int K,
+                             const DevCtl* ctl, cudaStream_t st) {
+  if (K % TC_CHUNK) return cudaErrorInvalidValue;
+  const int nch = K / TC_CHUNK;
+  __half2 *s0 = (__half2*)s[0], *s1 = (__half2*)s[1], *s2 = (__half2*)s[2];
+  if (nch % 2 == 0)
+    k_slice_prop<2, true><<<(nh * (nch / 2) + 7) / 8, 256, 0, st>>>(W, f, nullptr, s0, s1, s2, qb, nh, K, ctl, 0.f);
+  else
+    k_slice_prop<1, true><<<(nh * nch + 7) / 8, 256, 0, st>>>(W, f, nullptr, s0, s1, s2, qb, nh, K, ctl, 0.f);
   return cudaGetLastError();
 }

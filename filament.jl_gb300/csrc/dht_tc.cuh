@@ -129,7 +129,10 @@ __global__ void __launch_bounds__(256) k_slice(const float* __restrict__ B, __ha
 // are [nh][K] (radial index contiguous).  One warp per (frequency w,
 // CH consecutive chunks); both rows of w are sliced with their own chunk
 // scales.
-template <int CH>
+// MUL = false: the linear propagator exp(i KZ dz) gd from kz = KZ (zu
+// units) and the guard gd; MUL = true: a plain complex factor kz (the
+// non-paraxial QZ(kt, w) / QZ(w) times the spectral guard), gd unused.
+template <int CH, bool MUL>
 __global__ void __launch_bounds__(256) k_slice_prop(const float* __restrict__ W, const float2* __restrict__ kz,
                                                     const float* __restrict__ gd, __half2* b0, __half2* b1,
                                                     __half2* b2, float* qb, int nh, int K, const DevCtl* ctl,
@@ -145,7 +148,7 @@ __global__ void __launch_bounds__(256) k_slice_prop(const float* __restrict__ W,
   const float2* re = reinterpret_cast<const float2*>(W + (size_t)(2 * w) * K) + kb;
   const float2* im = reinterpret_cast<const float2*>(W + (size_t)(2 * w + 1) * K) + kb;
   const float4* kq = reinterpret_cast<const float4*>(kz + (size_t)w * K) + kb;
-  const float2* gq = reinterpret_cast<const float2*>(gd + (size_t)w * K) + kb;
+  const float2* gq = MUL ? nullptr : reinterpret_cast<const float2*>(gd + (size_t)w * K) + kb;
   float2 vr[CH], vi[CH], gg[CH];
   float4 kk[CH];
 #pragma unroll
@@ -153,7 +156,7 @@ __global__ void __launch_bounds__(256) k_slice_prop(const float* __restrict__ W,
     vr[u] = __ldg(re + u * (TC_CHUNK / 2));
     vi[u] = __ldg(im + u * (TC_CHUNK / 2));
     kk[u] = __ldg(kq + u * (TC_CHUNK / 2));
-    gg[u] = __ldg(gq + u * (TC_CHUNK / 2));
+    gg[u] = MUL ? make_float2(1.f, 1.f) : __ldg(gq + u * (TC_CHUNK / 2));
   }
 #pragma unroll
   for (int u = 0; u < CH; ++u) {
@@ -163,9 +166,15 @@ __global__ void __launch_bounds__(256) k_slice_prop(const float* __restrict__ W,
     const float ar[2] = {vr[u].x, vr[u].y}, ai[2] = {vi[u].x, vi[u].y};
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
-      const float amp = gv[i] * expf(-ky[i] * dz);
-      float sn, cs;
-      sincosf(kx[i] * dz, &sn, &cs);
+      float amp, sn, cs;
+      if (MUL) {
+        amp = 1.f;
+        cs = kx[i];
+        sn = ky[i];
+      } else {
+        amp = gv[i] * expf(-ky[i] * dz);
+        sincosf(kx[i] * dz, &sn, &cs);
+      }
       xr[i] = amp * (ar[i] * cs - ai[i] * sn);
       xi[i] = amp * (ar[i] * sn + ai[i] * cs);
     }
@@ -369,5 +378,5 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
   if (s_fail && tid == 0) atomicExch(p.err, 1);
   if (p.mode == 2 && p.ctl && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0 && !s_fail)
-    p.ctl->guard_pending = 1;
+    p.ctl->guard_pending = 1;   // mode 3: the same store without the flag
 }

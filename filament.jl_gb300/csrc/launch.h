@@ -17,13 +17,18 @@ template <typename R> struct PropParams;
 template <typename R>
 cudaError_t launch_rowstep(const RowParams<R>& P, int n, int nc, int mode, cudaStream_t st);
 template <typename R>
+cudaError_t launch_rowstage(const RowParams<R>& P, int n, int nc, cudaStream_t st);
+template <typename R>
+cudaError_t launch_np_combine(const RowParams<R>& P, int nh, cudaStream_t st);
+template <typename R>
 cudaError_t launch_rowreduce(const RowParams<R>& P, int n, double* fluence, R* Iout, int check_done,
                              cudaStream_t st);
 template <typename R>
 cudaError_t launch_colsum(const R* I, const double* w, double* power, int nrows, int nt, cudaStream_t st);
 template <typename R>
-cudaError_t launch_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S, int ld,
-                            const typename C2T<R>::type* tw, int analytic, int nrows, int n, cudaStream_t st);
+cudaError_t launch_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S, typename C2T<R>::type* U,
+                            int ld, const typename C2T<R>::type* tw, int analytic, int nrows, int n,
+                            cudaStream_t st);
 template <typename R>
 cudaError_t launch_field_out(const RowParams<R>& P, int n, typename C2T<R>::type* E, cudaStream_t st);
 template <typename R>
@@ -36,6 +41,10 @@ cudaError_t launch_slice(const float* B, void* const (&s)[3], float* qb, int N, 
                          cudaStream_t st);
 cudaError_t launch_slice_prop(const float* W, const float2* kz, const float* gd, void* const (&s)[3], float* qb, int nh,
                               int K, const DevCtl* ctl, cudaStream_t st);
+// slices of the forward transform's output W [2 nh][K] times the complex
+// factor f [nh][K] (non-paraxial prefactor)
+cudaError_t launch_slice_mul(const float* W, const float2* f, void* const (&s)[3], float* qb, int nh, int K,
+                             const DevCtl* ctl, cudaStream_t st);
 cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
 cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);

@@ -106,6 +106,31 @@ cudaError_t launch_rowstep(const RowParams<R>& P, int n, int nc, int mode, cudaS
 }
 
 template <typename R, int N>
+static cudaError_t launch_rowstage_n(const RowParams<R>& P, int nc, cudaStream_t st) {
+  const bool ram = P.has_raman != 0;
+  if (nc == 0) return ram ? launch_rowstage_t<R, N, 0, true>(P, st) : launch_rowstage_t<R, N, 0, false>(P, st);
+  if (nc == 1) return ram ? launch_rowstage_t<R, N, 1, true>(P, st) : launch_rowstage_t<R, N, 1, false>(P, st);
+  return ram ? launch_rowstage_t<R, N, 2, true>(P, st) : launch_rowstage_t<R, N, 2, false>(P, st);
+}
+
+template <typename R>
+cudaError_t launch_rowstage(const RowParams<R>& P, int n, int nc, cudaStream_t st) {
+  switch (n) {
+    case 512: return launch_rowstage_n<R, 512>(P, nc, st);
+    case 1024: return launch_rowstage_n<R, 1024>(P, nc, st);
+    case 2048: return launch_rowstage_n<R, 2048>(P, nc, st);
+    case 4096: return launch_rowstage_n<R, 4096>(P, nc, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename R>
+cudaError_t launch_np_combine(const RowParams<R>& P, int nh, cudaStream_t st) {
+  k_np_combine<R><<<P.nrows, 256, 0, st>>>(P, nh);
+  return cudaGetLastError();
+}
+
+template <typename R, int N>
 static cudaError_t launch_rowreduce_n(const RowParams<R>& P, double* fl, R* Iout, int check_done, cudaStream_t st) {
   size_t sm = x_smem<R, N>();
   cudaError_t e = cudaFuncSetAttribute(k_rowreduce<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -131,22 +156,24 @@ cudaError_t launch_colsum(const R* I, const double* w, double* power, int nrows,
 }
 
 template <typename R, int N>
-static cudaError_t launch_field_in_n(const typename C2T<R>::type* E, typename C2T<R>::type* S, int ld,
-                                     const typename C2T<R>::type* tw, int analytic, int nrows, cudaStream_t st) {
+static cudaError_t launch_field_in_n(const typename C2T<R>::type* E, typename C2T<R>::type* S,
+                                     typename C2T<R>::type* U, int ld, const typename C2T<R>::type* tw,
+                                     int analytic, int nrows, cudaStream_t st) {
   size_t sm = x_smem<R, N>();
   cudaError_t e = cudaFuncSetAttribute(k_field_in<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k_field_in<R, N><<<nrows, N / 16, sm, st>>>(E, S, ld, tw, analytic);
+  k_field_in<R, N><<<nrows, N / 16, sm, st>>>(E, S, U, ld, tw, analytic);
   return cudaGetLastError();
 }
 template <typename R>
-cudaError_t launch_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S, int ld,
-                            const typename C2T<R>::type* tw, int analytic, int nrows, int n, cudaStream_t st) {
+cudaError_t launch_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S, typename C2T<R>::type* U,
+                            int ld, const typename C2T<R>::type* tw, int analytic, int nrows, int n,
+                            cudaStream_t st) {
   switch (n) {
-    case 512: return launch_field_in_n<R, 512>(E, S, ld, tw, analytic, nrows, st);
-    case 1024: return launch_field_in_n<R, 1024>(E, S, ld, tw, analytic, nrows, st);
-    case 2048: return launch_field_in_n<R, 2048>(E, S, ld, tw, analytic, nrows, st);
-    case 4096: return launch_field_in_n<R, 4096>(E, S, ld, tw, analytic, nrows, st);
+    case 512: return launch_field_in_n<R, 512>(E, S, U, ld, tw, analytic, nrows, st);
+    case 1024: return launch_field_in_n<R, 1024>(E, S, U, ld, tw, analytic, nrows, st);
+    case 2048: return launch_field_in_n<R, 2048>(E, S, U, ld, tw, analytic, nrows, st);
+    case 4096: return launch_field_in_n<R, 4096>(E, S, U, ld, tw, analytic, nrows, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -175,7 +202,9 @@ cudaError_t launch_dht_simt(const R* A, const R* B, R* C, int M, int N, int K, c
                             DevCtl* ctl, int epi, cudaStream_t st) {
   dim3 grid(N / 128, M / 128);
   if (epi == 1) k_dht_simt<R, 1><<<grid, 256, 0, st>>>(A, B, C, M, N, K, pp, ctl);
-  else k_dht_simt<R, 2><<<grid, 256, 0, st>>>(A, B, C, M, N, K, pp, ctl);
+  else if (epi == 2) k_dht_simt<R, 2><<<grid, 256, 0, st>>>(A, B, C, M, N, K, pp, ctl);
+  else if (epi == 3) k_dht_simt<R, 3><<<grid, 256, 0, st>>>(A, B, C, M, N, K, pp, ctl);
+  else k_dht_simt<R, 4><<<grid, 256, 0, st>>>(A, B, C, M, N, K, pp, ctl);
   return cudaGetLastError();
 }
 
@@ -218,10 +247,12 @@ cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st) {
 
 #define INST(R)                                                                                          \
   template cudaError_t launch_rowstep<R>(const RowParams<R>&, int, int, int, cudaStream_t);            \
+  template cudaError_t launch_rowstage<R>(const RowParams<R>&, int, int, cudaStream_t);                \
+  template cudaError_t launch_np_combine<R>(const RowParams<R>&, int, cudaStream_t);                   \
   template cudaError_t launch_rowreduce<R>(const RowParams<R>&, int, double*, R*, int, cudaStream_t);   \
   template cudaError_t launch_colsum<R>(const R*, const double*, double*, int, int, cudaStream_t);       \
-  template cudaError_t launch_field_in<R>(const C2T<R>::type*, C2T<R>::type*, int, const C2T<R>::type*, \
-                                          int, int, int, cudaStream_t);                                  \
+  template cudaError_t launch_field_in<R>(const C2T<R>::type*, C2T<R>::type*, C2T<R>::type*, int,         \
+                                          const C2T<R>::type*, int, int, int, cudaStream_t);             \
   template cudaError_t launch_field_out<R>(const RowParams<R>&, int, C2T<R>::type*, cudaStream_t);      \
   template cudaError_t launch_dht_simt<R>(const R*, const R*, R*, int, int, int, const PropParams<R>&,  \
                                           DevCtl*, int, cudaStream_t);

@@ -89,6 +89,29 @@ template <typename R> struct RowParams {
   // linear-only rows (FP32 form): max_k |i QZ Rnl_cubic (k ? 2 : 1)| (the
   // Kerr coefficient before the channel pre-scale); < 0 disables the test
   R cc_max;
+  // Upper half of the spectrum: bins N/2 .. N-1 (the Nyquist bin and the
+  // negative frequencies) that the time-domain field guard creates.  The
+  // reference keeps them in its full-length spectrum: every analytic
+  // response leaves them unchanged (rsig2aspec! zeroes them), the linear
+  // step multiplies them by exp(i KZ dz) Kguard Wguard in r-space (its
+  // Hankel transform covers the first N/2 columns only,
+  // linear_propagators/spectral.jl:16-26, Fields.jl:108-110), and they
+  // enter the time-domain field of every plasma solve and RK stage.
+  // [row][N/2] complex (row stride ld); NULL = dropped (the analytic
+  // projection).  U_in is read at load; U_out receives the t->w transform
+  // of the guarded field (re-read by the stages) and then its propagated
+  // value; the two may alias (each block touches its own row only).
+  const C* U_in;
+  C* U_out;
+  const double* u_kzr;          // [row][N/2] Re KZ (zu units) in FP64: the phase KZ dz is reduced exactly
+  const C* u_kg;                // [row][N/2] (Im KZ, Kguard Wguard)
+  // non-paraxial prefactor (k_rowstep modes 2, 3; k_np_combine): [row][N/2]
+  // complex, row stride ld; rho_g, kdrho_g hold the step's density rows
+  C* np_S0;                     // t -> w transform of the guarded field
+  const C* np_K1;               // stage 0's transformed right-hand side
+  const C* np_KS;               // the last stage's transformed right-hand side
+  C* np_ACC;                    // sum of B[l] k_l over the stages before
+  int np_stage;                 // k_rowstage: the stage
 };
 
 template <typename R> FIL_DEV R row_guard(const RowParams<R>& P, int row, int* iy) {
@@ -110,11 +133,12 @@ FIL_DEV void load_time_row(const RowParams<R>& P, typename C2T<R>::type* X, int 
   constexpr int T = N / 16, NH = N / 2, EW = NH / T;
   const int tid = threadIdx.x;
   const C* src = P.S_in + (size_t)row * P.ld;
+  const C* up = P.U_in ? P.U_in + (size_t)row * P.ld : nullptr;
 #pragma unroll
   for (int m = 0; m < EW; ++m) {
     int k = tid + m * T;
     X[pad16(k)] = src[k];
-    X[pad16(k + NH)] = mk<R>(0, 0);
+    X[pad16(k + NH)] = up ? up[k] : mk<R>(0, 0);
   }
   filfft::block_fft<C, N, -1>(X, P.tw);
   if (guard) {
@@ -545,16 +569,145 @@ FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 }
 
 // ---------------------------------------------------------------------------
+// One evaluation of func! (nonlinear_propagators.jl:38-67) on the row's stage
+// input u(m) (analytic half, k = tid + m N/16 < N/2, EW = 8 per thread; d(m,
+// value) receives the result at the same k) with the upper half of the
+// spectrum from uo (NULL = zero): w -> t, the responses in the time domain
+// (medium_responses/*.jl) times the field filter, their analytic spectra
+// (rsig2aspec!) times Rnl and the paraxial i QZ (the C_ch tables), summed
+// into d.  Channels are packed two per complex FFT by scale: X holds the
+// Kerr response (real part) and the Raman response (imaginary part), Y the
+// two plasma responses (free current in the real part, losses in the
+// imaginary part); each channel is pre-scaled by |C_ch| at the carrier so
+// packed partners have comparable size.  ych = false leaves the plasma
+// channels out (their response is below the row's resolution).
+template <typename R, int N, int NC, bool RAM, typename In, typename Out>
+FIL_DEV void stage_rhs(const RowParams<R>& P, typename C2T<R>::type* X, typename C2T<R>::type* Y,
+                       const R* rho, const R* kdrho, R gs, int iy, bool ych,
+                       const typename C2T<R>::type* uo, In u, Out d) {
+  typedef typename C2T<R>::type C;
+  constexpr int T = N / 16, NH = N / 2, EW = NH / T;
+  static_assert(EW == 8, "eight half-spectrum points per thread");
+  const int tid = threadIdx.x;
+  const R invN = (R)1 / (R)N;
+  __syncthreads();   // X and Y free
+#pragma unroll
+  for (int m = 0; m < EW; ++m) {
+    int k = tid + m * T;
+    X[pad16(k)] = u(m);
+    X[pad16(k + NH)] = uo ? uo[k] : mk<R>(0, 0);
+  }
+  filfft::block_fft<C, N, -1>(X, P.tw);            // inverse_transform_time!
+  if (RAM) {
+    // raman.jl:80-98: conv = fft(H * ifft(x)), x = Re(E)^2 or 3/4 |E|^2,
+    // in Y (free until the responses below are written)
+#pragma unroll 4
+    for (int m = 0; m < 16; ++m) {
+      int j = tid + m * T;
+      C e = X[pad16(j)];
+      R x = P.raman_thg ? e.x * e.x : (R)0.75 * (e.x * e.x + e.y * e.y);
+      Y[pad16(j)] = mk<R>(x, 0);
+    }
+    filfft::block_fft<C, N, +1>(Y, P.tw);
+#pragma unroll 4
+    for (int m = 0; m < 16; ++m) {
+      int j = tid + m * T;
+      Y[pad16(j)] = invN * cmul(Y[pad16(j)], __ldg(&P.ramh[j]));
+    }
+    filfft::block_fft<C, N, -1>(Y, P.tw);
+  }
+#pragma unroll 4
+  for (int m = 0; m < 16; ++m) {
+    int j = tid + m * T;
+    C e = X[pad16(j)];
+    R re = e.x;
+    R I = e.x * e.x + e.y * e.y;
+    R g = gs * P.gt[P.gt_bug ? iy : j];
+    R fc = 0, ff = 0, fl = 0, fr = 0;
+    if (P.has_cubic) fc = P.cubic_thg ? re * re * re : (R)0.75 * I * re;
+    if (RAM) fr = Y[pad16(j)].x * re;
+    if (NC > 0 && P.has_free) ff = rho[pad16(j)] * re;
+    if (NC > 0 && P.has_losses) {
+      R Il = P.losses_ereal ? re * re : I;
+      R inv = (Il >= (R)1e-30) ? (R)1 / Il : (R)0;
+      fl = kdrho[pad16(j)] * inv * re;
+    }
+    X[pad16(j)] = mk<R>(g * (R)P.sc * fc, RAM ? g * P.sr * fr : (R)0);
+    Y[pad16(j)] = mk<R>(g * (R)P.sf * ff, g * (R)P.sl * fl);
+  }
+  const bool plas = NC > 0 && (P.has_free || P.has_losses) && ych;
+  if (P.has_cubic || RAM) filfft::block_fft<C, N, +1>(X, P.tw);   // rsig2aspec!
+  if (plas) filfft::block_fft<C, N, +1>(Y, P.tw);
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < EW; ++m) {
+    int k = tid + m * T;
+    const int km = (N - k) & (N - 1);
+    C dd = mk<R>(0, 0);
+    if (P.has_cubic || RAM) {
+      C z = X[pad16(k)], zm = cconj(X[pad16(km)]);
+      if (P.has_cubic) dd = cmul(__ldg(&P.Cc[k]), ((R)0.5 * invN) * (z + zm));
+      if (RAM) {
+        C dl = z - zm;
+        dd = dd + cmul(__ldg(&P.Cr[k]), mk<R>(dl.y * (R)0.5 * invN, -dl.x * (R)0.5 * invN));
+      }
+    }
+    if (plas) {
+      C z = Y[pad16(k)], zm = cconj(Y[pad16(km)]);
+      C ffr = ((R)0.5 * invN) * (z + zm);                 // (z + conj z_-k)/2
+      C dl = z - zm;
+      C flr = mk<R>(dl.y * (R)0.5 * invN, -dl.x * (R)0.5 * invN);  // (z - conj z_-k)/(2i)
+      if (P.has_free) dd = dd + cmul(__ldg(&P.Cf[k]), ffr);
+      if (P.has_losses) dd = dd + cmul(__ldg(&P.Cl[k]), flr);
+    }
+    d(m, dd);
+  }
+}
+
+// One value of a row's output (of a step, or of a non-paraxial stage): the
+// half-spectrum point k in the Hankel GEMM's operand layout (real column
+// 2k + c, transverse index contiguous, scaled by s_row) or in the row layout.
+template <typename R>
+FIL_DEV void write_out(const RowParams<R>& P, int row, int k, typename C2T<R>::type v) {
+  if (P.out_T) {
+    R* base = reinterpret_cast<R*>(P.S_out);
+    const R sc = P.out_scale ? P.out_scale[row] : (R)1;
+    base[(size_t)(2 * k) * P.ldT + row] = sc * v.x;
+    base[(size_t)(2 * k + 1) * P.ldT + row] = sc * v.y;
+  } else {
+    P.S_out[(size_t)row * P.ld + k] = v;
+  }
+}
+
+// Linear step of the upper half of the spectrum at (row, k): u exp(i KZ dz)
+// Kguard Wguard in r-space.  |Re KZ dz| reaches ~1e5 rad at the negative
+// frequencies (moving frame), so the phase is formed in FP64 in units of pi
+// and reduced there to [-1, 1] (exact: 2 rint(t/2) is representable), and
+// sin/cos of pi x need no further argument reduction.
+template <typename R>
+FIL_DEV typename C2T<R>::type upper_prop(const RowParams<R>& P, size_t idx, typename C2T<R>::type u, double dzd) {
+  const double t = __ldg(&P.u_kzr[idx]) * dzd * 0.3183098861837907;   // phase / pi
+  const R x = (R)(t - 2.0 * rint(0.5 * t));
+  const typename C2T<R>::type kg = P.u_kg[idx];
+  const R amp = kg.y * exp(-kg.x * (R)dzd);
+  R sn, cs;
+  sincospi(x, &sn, &cs);
+  return cmul(u, mk<R>(amp * cs, amp * sn));
+}
+
+// ---------------------------------------------------------------------------
 // Fused z-step of one row (blockIdx.x = row):
 //   E(t) = guard * fft(S_in)   (guard from the previous step, Models.jl:116-118)
 //   plasma solve on E(t)       (Models.jl:84-89)
 //   S0 = ifft(E)[0:N/2]        (Models.jl:91-96)
 //   RK step of func!            (Models.jl:98-103, nonlinear_propagators.jl:38-74)
 //   S_out = S0 + dz sum b_s k_s
-// mode 1: plasma only (initialisation), no S_out.  RAM: the Raman channel
-// (compiled only where used, it costs registers).  Blocks are held to 128
-// registers so that two (4096-point rows) to sixteen (512-point rows, the
-// XYT geometry) share an SM.
+// mode 1: plasma only (initialisation), no S_out.  mode 4: the plasma solve
+// of a step only (with the surrogate when armed), rho and Kdrho rows to
+// rho_g, kdrho_g: the first launch of a non-paraxial step (k_rowstage).
+// RAM: the Raman channel (compiled only where used, it costs registers).
+// Blocks are held to 128 registers so that two (4096-point rows) to sixteen
+// (512-point rows, the XYT geometry) share an SM.
 template <typename R, int N, int NC, bool RAM>
 __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(RowParams<R> P, int mode) {
   typedef typename C2T<R>::type C;
@@ -577,6 +730,7 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   const R dz = (R)ctl->dz;
   const bool guard = ctl->guard_pending != 0;
   if (tid == 0) s_flag = 0;
+  C* uo = P.U_out ? P.U_out + (size_t)row * P.ld : nullptr;
 
   if constexpr (NC > 0) {
     if (P.plasma) {
@@ -591,7 +745,7 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   load_time_row<R, N>(P, X, row, guard);
   // largest |E|^2 of the row (the linear-only test below)
   R e2row = 0;
-  if (!RAM && P.nonlin && P.cc_max >= (R)0) {
+  if (!RAM && mode == 0 && P.nonlin && P.cc_max >= (R)0) {
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
       const C e = X[pad16(tid + m * T)];
@@ -605,9 +759,10 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   // rows also measure the surrogate against the solution.
   if constexpr (NC > 0) {
     if (P.plasma) {
-      const int slot = (P.nn_out && mode == 0) ? P.nn_slot[row] : -1;
+      const bool stepping = mode == 0 || mode == 4;
+      const int slot = (P.nn_out && stepping) ? P.nn_slot[row] : -1;
       const bool nn_row = slot >= 0 && slot < ctl->nn_rows;
-      const bool judge = P.nn_out && mode == 0 && ctl->nn_judge;
+      const bool judge = P.nn_out && stepping && ctl->nn_judge;
       Aff<R, 1>* sc1 = reinterpret_cast<Aff<R, 1>*>(ascratch);
       R rmax;
       const float* gslot = P.nn_out + (size_t)slot * N * (P.nn_part ? NN_K : 1);
@@ -615,7 +770,7 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
         rmax = nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, false);
       } else {
         rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag,
-                                    mode == 0 ? (R)ctl->rhomax : (R)0, dz, &ych);
+                                    stepping ? (R)ctl->rhomax : (R)0, dz, &ych);
         if (judge) {
           // rows not flagged carry rho0 in the surrogate form
           const R diff = nn_row ? nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, true)
@@ -628,7 +783,7 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
         P.rho_end[row] = (double)rho[pad16(N - 1)];
         if (s_flag) atomicOr(&ctl->flags, FIL_FLAG_NEWTON);
       }
-      if (P.store_plasma) {
+      if (P.store_plasma || mode == 4) {
         for (int m = 0; m < 16; ++m) {
           int j = tid + m * T;
           P.rho_g[(size_t)row * N + j] = rho[pad16(j)];
@@ -637,9 +792,10 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
       }
     }
   }
-  if (mode == 1) return;
+  if (mode == 1 || mode == 4) return;
 
-  // ---- t -> w, keep the analytic half
+  // ---- t -> w: the analytic half in registers, the upper half (when kept)
+  // to the row's slice of U_out, where the stages read it back
   filfft::block_fft<C, N, +1>(X, P.tw);
   const R invN = (R)1 / (R)N;
   C S0[EW], k1[EW], kp[EW], acc[EW];
@@ -647,6 +803,7 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   for (int m = 0; m < EW; ++m) {
     int k = tid + m * T;
     S0[m] = invN * X[pad16(k)];
+    if (uo) uo[k] = invN * X[pad16(k + NH)];
     acc[m] = mk<R>(0, 0);
   }
   // Linear-only row: with the plasma channels off for this row (no plasma,
@@ -672,110 +829,123 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
     int iy;
     const R gs = row_guard(P, row, &iy);
     for (int s = 0; s < P.ns; ++s) {
-      const R a0 = (R)P.A0[s], a1 = (R)P.A1[s];
-      __syncthreads();   // X and Y free
+      const R a0 = (R)P.A0[s], a1 = (R)P.A1[s], bs = (R)P.B[s];
+      auto u = [&](int m) -> C { return s > 0 ? S0[m] + (dz * a0) * k1[m] + (dz * a1) * kp[m] : S0[m]; };
+      auto d = [&](int m, C v) {
+        if (s == 0) k1[m] = v;
+        kp[m] = v;
+        acc[m] = acc[m] + bs * v;
+      };
+      stage_rhs<R, N, NC, RAM>(P, X, Y, rho, kdrho, gs, iy, ych, uo, u, d);
+    }
+  }
 #pragma unroll
-      for (int m = 0; m < EW; ++m) {
-        int k = tid + m * T;
-        C u = S0[m];
-        if (s > 0) u = u + (dz * a0) * k1[m] + (dz * a1) * kp[m];
-        X[pad16(k)] = u;
-        X[pad16(k + NH)] = mk<R>(0, 0);
-      }
-      filfft::block_fft<C, N, -1>(X, P.tw);            // inverse_transform_time!
-      if (RAM) {
-        // raman.jl:80-98: conv = fft(H * ifft(x)), x = Re(E)^2 or 3/4 |E|^2,
-        // in Y (free until the responses below are written)
-#pragma unroll 4
-        for (int m = 0; m < 16; ++m) {
-          int j = tid + m * T;
-          C e = X[pad16(j)];
-          R x = P.raman_thg ? e.x * e.x : (R)0.75 * (e.x * e.x + e.y * e.y);
-          Y[pad16(j)] = mk<R>(x, 0);
-        }
-        filfft::block_fft<C, N, +1>(Y, P.tw);
-#pragma unroll 4
-        for (int m = 0; m < 16; ++m) {
-          int j = tid + m * T;
-          Y[pad16(j)] = invN * cmul(Y[pad16(j)], __ldg(&P.ramh[j]));
-        }
-        filfft::block_fft<C, N, -1>(Y, P.tw);
-      }
-      // responses in the time domain (medium_responses/*.jl) times the field
-      // filter.  Channels are packed two per complex FFT by scale: X holds
-      // the Kerr response (real part) and the Raman response (imaginary
-      // part), Y the two plasma responses (free current in the real part,
-      // losses in the imaginary part); each channel is pre-scaled by |C_ch|
-      // at the carrier so packed partners have comparable size.
+  for (int m = 0; m < EW; ++m) write_out<R>(P, row, tid + m * T, S0[m] + dz * acc[m]);
+  if (uo) {
+    // linear step of the upper half (the lower half's follows in the
+    // Hankel transforms)
+    const double dzd = ctl->dz;
+    const size_t base = (size_t)row * P.ld;
+#pragma unroll 2
+    for (int m = 0; m < EW; ++m) {
+      const int k = tid + m * T;
+      uo[k] = upper_prop<R>(P, base + k, uo[k], dzd);
+    }
+  }
+}
+
+// One RK stage of a non-paraxial step (QPARAXIAL = false).  func! then
+// transforms its sum along r before the prefactor
+// (nonlinear_propagators.jl:58-63), so every stage is one launch with the
+// Hankel pair and i QZ(kt, w) in between (api.cu); the density rows come
+// from the step's plasma launch (k_rowstep mode 4) in rho_g, kdrho_g.
+// Stage 0 (np_stage = 0): E(t) = guard * fft(S_in), t -> w; S0 to np_S0,
+//   the upper half to U_out; stage 0's paraxial right-hand side to S_out.
+// Stage s >= 1: the stage input S0 + dz (A0 k1 + A1 k_prev) from np_S0,
+//   np_K1 and np_KS (the transformed right-hand sides of stages 0 and
+//   s - 1), the running sum np_ACC += B[s-1] k_{s-1}; this stage's paraxial
+//   right-hand side to S_out.
+template <typename R, int N, int NC, bool RAM>
+__global__ void __launch_bounds__(N / 16) k_rowstage(RowParams<R> P) {
+  typedef typename C2T<R>::type C;
+  constexpr int T = N / 16, NH = N / 2, EW = NH / T, NP = N + N / 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* X = reinterpret_cast<C*>(smem_raw);
+  C* Y = X + NP;
+  R* rho = reinterpret_cast<R*>(Y + NP);                 // [NP], pad16 index
+  R* kdrho = rho + NP;
+  const DevCtl* ctl = P.ctl;
+  if (ctl->done) return;
+  const int row = blockIdx.x;
+  const int tid = threadIdx.x;
+  const R dz = (R)ctl->dz;
+  const int s = P.np_stage;
+  const size_t rb = (size_t)row * P.ld;
+  C* uo = P.U_out ? P.U_out + rb : nullptr;
+  if constexpr (NC > 0) {
+    if (P.plasma) {
 #pragma unroll 4
       for (int m = 0; m < 16; ++m) {
         int j = tid + m * T;
-        C e = X[pad16(j)];
-        R re = e.x;
-        R I = e.x * e.x + e.y * e.y;
-        R g = gs * P.gt[P.gt_bug ? iy : j];
-        R fc = 0, ff = 0, fl = 0, fr = 0;
-        if (P.has_cubic) fc = P.cubic_thg ? re * re * re : (R)0.75 * I * re;
-        if (RAM) fr = Y[pad16(j)].x * re;
-        if (NC > 0 && P.has_free) ff = rho[pad16(j)] * re;
-        if (NC > 0 && P.has_losses) {
-          R Il = P.losses_ereal ? re * re : I;
-          R inv = (Il >= (R)1e-30) ? (R)1 / Il : (R)0;
-          fl = kdrho[pad16(j)] * inv * re;
-        }
-        X[pad16(j)] = mk<R>(g * (R)P.sc * fc, RAM ? g * P.sr * fr : (R)0);
-        Y[pad16(j)] = mk<R>(g * (R)P.sf * ff, g * (R)P.sl * fl);
-      }
-      const bool plas = NC > 0 && (P.has_free || P.has_losses) && ych;
-      if (P.has_cubic || RAM) filfft::block_fft<C, N, +1>(X, P.tw);   // rsig2aspec!
-      if (plas) filfft::block_fft<C, N, +1>(Y, P.tw);
-      __syncthreads();
-#pragma unroll
-      for (int m = 0; m < EW; ++m) {
-        int k = tid + m * T;
-        const int km = (N - k) & (N - 1);
-        C d = mk<R>(0, 0);
-        if (P.has_cubic || RAM) {
-          C z = X[pad16(k)], zm = cconj(X[pad16(km)]);
-          if (P.has_cubic) d = cmul(__ldg(&P.Cc[k]), ((R)0.5 * invN) * (z + zm));
-          if (RAM) {
-            C dl = z - zm;
-            d = d + cmul(__ldg(&P.Cr[k]), mk<R>(dl.y * (R)0.5 * invN, -dl.x * (R)0.5 * invN));
-          }
-        }
-        if (plas) {
-          C z = Y[pad16(k)], zm = cconj(Y[pad16(km)]);
-          C ffr = ((R)0.5 * invN) * (z + zm);                 // (z + conj z_-k)/2
-          C dl = z - zm;
-          C flr = mk<R>(dl.y * (R)0.5 * invN, -dl.x * (R)0.5 * invN);  // (z - conj z_-k)/(2i)
-          if (P.has_free) d = d + cmul(__ldg(&P.Cf[k]), ffr);
-          if (P.has_losses) d = d + cmul(__ldg(&P.Cl[k]), flr);
-        }
-        if (s == 0) k1[m] = d;
-        kp[m] = d;
-        acc[m] = acc[m] + (R)P.B[s] * d;
+        rho[pad16(j)] = P.rho_g[(size_t)row * N + j];
+        kdrho[pad16(j)] = P.kdrho_g[(size_t)row * N + j];
       }
     }
   }
-  if (P.out_T) {
-    // operand layout of the tensor-core Hankel GEMM: real column 2k + c,
-    // transverse index contiguous, scaled by s_row
-    R* base = reinterpret_cast<R*>(P.S_out);
-    const R sc = P.out_scale ? P.out_scale[row] : (R)1;
+  int iy;
+  const R gs = row_guard(P, row, &iy);
+  auto d = [&](int m, C v) { write_out<R>(P, row, tid + m * T, v); };
+  if (s == 0) {
+    load_time_row<R, N>(P, X, row, ctl->guard_pending != 0);
+    filfft::block_fft<C, N, +1>(X, P.tw);
+    const R invN = (R)1 / (R)N;
+    C S0[EW];
 #pragma unroll
     for (int m = 0; m < EW; ++m) {
-      int k = tid + m * T;
-      C v = S0[m] + dz * acc[m];
+      const int k = tid + m * T;
+      S0[m] = invN * X[pad16(k)];
+      P.np_S0[rb + k] = S0[m];
+      if (uo) uo[k] = invN * X[pad16(k + NH)];
+    }
+    auto u = [&](int m) -> C { return S0[m]; };
+    stage_rhs<R, N, NC, RAM>(P, X, Y, rho, kdrho, gs, iy, true, uo, u, d);
+  } else {
+    const R a0 = (R)P.A0[s], a1 = (R)P.A1[s], bp = (R)P.B[s - 1];
+    auto u = [&](int m) -> C {
+      const int k = tid + m * T;
+      const C k1 = P.np_K1[rb + k];
+      const C kp = (s == 1) ? k1 : P.np_KS[rb + k];
+      P.np_ACC[rb + k] = (s == 1) ? bp * k1 : P.np_ACC[rb + k] + bp * kp;
+      return P.np_S0[rb + k] + (dz * a0) * k1 + (dz * a1) * kp;
+    };
+    stage_rhs<R, N, NC, RAM>(P, X, Y, rho, kdrho, gs, iy, true, uo, u, d);
+  }
+}
+
+// Non-paraxial step, after the last stage's Hankel pair: S_out (operand or
+// row layout) = S0 + dz (ACC + B_last k_last), and the upper half's linear
+// step.  One block per row.
+template <typename R>
+__global__ void __launch_bounds__(256) k_np_combine(RowParams<R> P, int nh) {
+  typedef typename C2T<R>::type C;
+  const DevCtl* ctl = P.ctl;
+  if (ctl->done) return;
+  const int row = blockIdx.x;
+  const R dz = (R)ctl->dz;
+  const double dzd = ctl->dz;
+  const R bl = (R)P.B[P.ns - 1];
+  const size_t rb = (size_t)row * P.ld;
+  const R sc = (P.out_T && P.out_scale) ? P.out_scale[row] : (R)1;
+  for (int k = threadIdx.x; k < nh; k += blockDim.x) {
+    const C v = P.np_S0[rb + k] + dz * (P.np_ACC[rb + k] + bl * P.np_KS[rb + k]);
+    if (P.out_T) {
+      R* base = reinterpret_cast<R*>(P.S_out);
       base[(size_t)(2 * k) * P.ldT + row] = sc * v.x;
       base[(size_t)(2 * k + 1) * P.ldT + row] = sc * v.y;
+    } else {
+      P.S_out[rb + k] = v;
     }
-  } else {
-    C* dst = P.S_out + (size_t)row * P.ld;
-#pragma unroll
-    for (int m = 0; m < EW; ++m) {
-      int k = tid + m * T;
-      dst[k] = S0[m] + dz * acc[m];
-    }
+    if (P.U_out) P.U_out[rb + k] = upper_prop<R>(P, rb + k, P.U_out[rb + k], dzd);
   }
 }
 
@@ -958,7 +1128,8 @@ __global__ void __launch_bounds__(256) k_colsum(const R* __restrict__ I, const d
 // with c_0 = 1, c_k = 2 (rsig2asig!, Fields.jl:115) or c_k = 1 (analytic).
 template <typename R, int N>
 __global__ void __launch_bounds__(N / 16) k_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S,
-                                                     int ld, const typename C2T<R>::type* tw, int analytic) {
+                                                     typename C2T<R>::type* U, int ld,
+                                                     const typename C2T<R>::type* tw, int analytic) {
   typedef typename C2T<R>::type C;
   constexpr int T = N / 16, NH = N / 2, EW = NH / T, NP = N + N / 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -978,6 +1149,8 @@ __global__ void __launch_bounds__(N / 16) k_field_in(const typename C2T<R>::type
     int k = tid + m * T;
     R c = (analytic || k == 0) ? invN : (R)2 * invN;
     S[(size_t)row * ld + k] = c * X[pad16(k)];
+    // upper half: kept as given for an analytic field, zero after rsig2asig!
+    if (U) U[(size_t)row * ld + k] = analytic ? invN * X[pad16(k + N / 2)] : mk<R>(0, 0);
   }
 }
 

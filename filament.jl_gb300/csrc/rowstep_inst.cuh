@@ -34,3 +34,33 @@ cudaError_t launch_rowstep_t(const RowParams<R>& P, int mode, cudaStream_t st) {
   template cudaError_t launch_rowstep_t<R, 4096, 0, RAM>(const RowParams<R>&, int, cudaStream_t); \
   template cudaError_t launch_rowstep_t<R, 4096, 1, RAM>(const RowParams<R>&, int, cudaStream_t); \
   template cudaError_t launch_rowstep_t<R, 4096, 2, RAM>(const RowParams<R>&, int, cudaStream_t);
+
+template <typename R, int N>
+static size_t rowstage_smem() {
+  typedef typename C2T<R>::type C;
+  constexpr int NP = N + N / 16;
+  return 2 * NP * sizeof(C) + 2 * NP * sizeof(R);
+}
+
+template <typename R, int N, int NC, bool RAM>
+cudaError_t launch_rowstage_t(const RowParams<R>& P, cudaStream_t st) {
+  size_t sm = rowstage_smem<R, N>();
+  cudaError_t e =
+      cudaFuncSetAttribute(k_rowstage<R, N, NC, RAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_rowstage<R, N, NC, RAM><<<P.nrows, N / 16, sm, st>>>(P);
+  return cudaGetLastError();
+}
+
+#define FIL_ROWSTAGE_INST_N(R, N)                                                                 \
+  template cudaError_t launch_rowstage_t<R, N, 0, false>(const RowParams<R>&, cudaStream_t);    \
+  template cudaError_t launch_rowstage_t<R, N, 1, false>(const RowParams<R>&, cudaStream_t);    \
+  template cudaError_t launch_rowstage_t<R, N, 2, false>(const RowParams<R>&, cudaStream_t);    \
+  template cudaError_t launch_rowstage_t<R, N, 0, true>(const RowParams<R>&, cudaStream_t);     \
+  template cudaError_t launch_rowstage_t<R, N, 1, true>(const RowParams<R>&, cudaStream_t);     \
+  template cudaError_t launch_rowstage_t<R, N, 2, true>(const RowParams<R>&, cudaStream_t);
+#define FIL_ROWSTAGE_INST(R)        \
+  FIL_ROWSTAGE_INST_N(R, 512)       \
+  FIL_ROWSTAGE_INST_N(R, 1024)      \
+  FIL_ROWSTAGE_INST_N(R, 2048)      \
+  FIL_ROWSTAGE_INST_N(R, 4096)

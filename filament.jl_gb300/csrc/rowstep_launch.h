@@ -6,3 +6,7 @@
 
 template <typename R, int N, int NC, bool RAM>
 cudaError_t launch_rowstep_t(const RowParams<R>& P, int mode, cudaStream_t st);
+
+// non-paraxial stage kernel (k_rowstage) of the same shapes
+template <typename R, int N, int NC, bool RAM>
+cudaError_t launch_rowstage_t(const RowParams<R>& P, cudaStream_t st);

@@ -9,7 +9,8 @@ struct TcGemmParams {
   float* out;
   int ldo;                // leading dimension of out (floats)
   int K;                  // contraction length, multiple of 64
-  int mode;               // 1 transposed store; 2 row-major store (+ guard pending)
+  int mode;               // 1 transposed store; 2 row-major store (+ guard pending);
+                          // 3 row-major store
   const float* qa;        // [M] row scales of A (powers of two)
   const float* qb;        // [K/64][ldqb] chunk scales of B (powers of two)
   int ldqb;

@@ -154,8 +154,9 @@ class Problem:
 
         # nonlinear prefactor and responses
         if cfg.nonlinearity:
-            if not cfg.qparaxial:
-                qz = None  # the library reports FIL_ERR_UNSUPPORTED
+            # the paraxial QZ(w); with QPARAXIAL = false the library forms
+            # QZ(kt, w) = QZ(w) beta(w) / sqrt(beta^2 - kt^2)
+            # (Qfunc_nonparaxial, nonlinear_propagators.jl:232-241)
             qz = np.array([qfunc_paraxial(medium, wj) for wj in w]) * zu / Eu
             tab.qz = _abi.dptr(self._keep("qz", _c(qz)))
             chan = {"cubic": np.zeros(nt, complex), "free": np.zeros(nt, complex),

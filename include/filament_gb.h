@@ -102,12 +102,17 @@ extern "C" {
                                   FP32 CUDA-core GEMMs instead of the
                                   tcgen05 tensor-core GEMMs on exact FP16
                                   slices (the default)                    */
-#define FIL_OPT_ANALYTIC_PROJECTION 5 /* drop negative frequencies after
-                                  every t->w transform.  The library's field
-                                  state is the analytic half spectrum, so
-                                  this is always on there; an implementation
-                                  that keeps the full spectrum (as the
-                                  reference does) can switch it on to match */
+#define FIL_OPT_ANALYTIC_PROJECTION 5 /* 1: drop the upper half of the
+                                  spectrum (bins Nt/2..Nt-1, the negative
+                                  frequencies the time guard creates) after
+                                  every t->w transform, i.e. keep only the
+                                  analytic half.  0 (default): keep it as the
+                                  reference does -- it enters the time-domain
+                                  field and receives the linear step's
+                                  exp(i KZ dz) Kguard Wguard in r-space
+                                  (spectral.jl:16-26; its Hankel transform
+                                  covers the first Nt/2 columns).  RT only;
+                                  XYT always projects.                     */
 
 typedef struct fil_config {
   int32_t abi_version;   /* FIL_ABI_VERSION                                  */

@@ -10,6 +10,7 @@
 //   linear propagator             src/modules/linear_propagators/spectral.jl:16-26
 //   KZ                            src/modules/linear_propagators/spectral.jl:78-184
 //   nonlinear RHS func!           src/modules/nonlinear_propagators.jl:38-67
+//   QZ (paraxial, non-paraxial)   src/modules/nonlinear_propagators.jl:139-229
 //   update_dE!                    src/modules/nonlinear_propagators.jl:246-283
 //   responses                     src/modules/medium_responses/cubic.jl:33-54,
 //                                 current_free.jl:31-37, current_losses.jl:36-83,
@@ -437,6 +438,57 @@ void plasma_solve(fil_handle* h) {
   h->rhomax = m;
 }
 
+// QZ of the non-paraxial prefactor (nonlinear_propagators.jl:232-241):
+// mu0 mu w^2 / (2 kz) with kz = sqrt(beta^2 - kt^2 + 0im), 0 where kz = 0.
+// The tables carry the paraxial QZ(w) = mu0 mu w^2 / (2 beta) zu / Eu
+// (0 where beta = 0, i.e. w = 0, where the non-paraxial value is 0 too),
+// so QZ_np = QZ(w) beta / kz.
+cd qz_nonparaxial(const fil_handle* h, double kt2, int j) {
+  const cd b = h->beta[j];
+  const cd kz = std::sqrt(b * b - kt2 + cd(0.0, 0.0));
+  if (kz == cd(0, 0) || h->qz[j] == cd(0, 0)) return cd(0, 0);
+  return h->qz[j] * b / kz;
+}
+
+// func!'s non-paraxial branch (nonlinear_propagators.jl:58-63): dE is the
+// sum of Rnl aspec(F) in the w-domain; forward transverse transform,
+// dE *= i QZ(kt, w), spectral filter, inverse transform.
+void nl_transverse(fil_handle* h, std::vector<cd>& dE) {
+  const int nt = h->nt;
+  if (h->geom == FIL_GEOM_R || h->geom == FIL_GEOM_RT) {
+    const int ncol = h->geom == FIL_GEOM_RT ? h->nh : 1;
+    if (h->n1 > 1) dht_apply(h, dE, ncol, true, false);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < h->n1; ++i) {
+      const double k2 = h->kt1[i] * h->kt1[i];
+      for (int j = 0; j < nt; ++j) {
+        const double g = kguard_value(h, k2, j) * (h->wg.empty() ? 1.0 : h->wg[j]);
+        dE[(size_t)i * nt + j] *= cd(0, 1) * qz_nonparaxial(h, k2, j) * g;
+      }
+    }
+    if (h->n1 > 1) dht_apply(h, dE, ncol, false, true);
+  } else if (h->geom == FIL_GEOM_T) {
+    for (int j = 0; j < nt; ++j)
+      dE[j] *= cd(0, 1) * qz_nonparaxial(h, 0.0, j) * (h->wg.empty() ? 1.0 : h->wg[j]);
+  } else {  // XY, XYT
+    xy_fft(h, dE, -1);
+    const int nx = h->n1, ny = h->n2;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int ix = 0; ix < nx; ++ix)
+      for (int iy = 0; iy < ny; ++iy) {
+        const double k2 = h->kt1[ix] * h->kt1[ix] + h->kt2[iy] * h->kt2[iy];
+        const double sg = h->sg1[ix] * h->sg2[iy];
+        const size_t base = ((size_t)ix * ny + iy) * nt;
+        for (int j = 0; j < nt; ++j) {
+          const int jw = (h->bugcompat && h->geom == FIL_GEOM_XYT) ? iy : j;  // Guards.jl:314
+          const double g = sg * (h->wg.empty() ? 1.0 : h->wg[jw]);
+          dE[base + j] *= cd(0, 1) * qz_nonparaxial(h, k2, j) * g;
+        }
+      }
+    xy_fft(h, dE, +1);
+  }
+}
+
 // ---------------------------------------------------------- func! -------
 // dE = i QZ sum_resp Rnl(w) aspec(guard * calc(E)).  U is in the w-domain
 // (t geometries) or space domain (R, XY).
@@ -510,9 +562,11 @@ void nl_rhs(fil_handle* h, const std::vector<cd>& U, std::vector<cd>& dE) {
         else R = &h->rnl_r;
         for (int j = 0; j < nt; ++j) dr[j] += (*R)[j] * F[j];          // update_dE!
       }
-      for (int j = 0; j < nt; ++j) dr[j] = cd(0, 1) * h->qz[j] * dr[j];  // QPARAXIAL
+      if (h->cfg.qparaxial)
+        for (int j = 0; j < nt; ++j) dr[j] = cd(0, 1) * h->qz[j] * dr[j];  // QPARAXIAL
     }
   }
+  if (!h->cfg.qparaxial) nl_transverse(h, dE);
 }
 
 void nl_step(fil_handle* h, std::vector<cd>& u, double dz) {
@@ -580,7 +634,6 @@ int filo_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if ((h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_XYT) && (!is_pow2(h->n1) || !is_pow2(h->n2))) {
     delete h; return fail(nullptr, FIL_ERR_UNSUPPORTED, "nx, ny must be powers of two");
   }
-  if (cfg->nonlinearity && !cfg->qparaxial) { delete h; return fail(nullptr, FIL_ERR_UNSUPPORTED, "QPARAXIAL=false"); }
   int n1 = h->n1, n2 = h->n2, nt = h->nt;
   h->kt1 = copyv(t->kt1, n1, 0.0);
   h->kt2 = copyv(t->kt2, n2, 0.0);

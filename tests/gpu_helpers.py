@@ -61,18 +61,23 @@ def saturating_rate(n=14):
     return I, W
 
 
-def pair(inp, precision="mixed", store_plasma=False, project=True):
-    """(CUDA simulation, oracle simulation) on the same input.  With
-    project=True the oracle drops negative frequencies after each t->w
-    transform, as the library's half-spectrum state does, so that the two
-    differ by arithmetic only."""
+def pair(inp, precision="mixed", store_plasma=False, project=None):
+    """(CUDA simulation, oracle simulation) on the same input, both with the
+    same treatment of the upper half of the spectrum: kept as the reference
+    keeps it (project=False, the RT default) or dropped after each t->w
+    transform (project=True; XYT always projects), so that the two differ
+    by arithmetic only."""
     import filament_gb as fg
     import oracle
     from filament_gb import _abi
+    if project is None:
+        project = inp["geometry"] == "XYT"
     g = fg.Simulation(inp, precision=precision)
     r = fg.Simulation(inp, binding=oracle.binding())
     if project:
         r.handle.set_option(_abi.OPT_ANALYTIC_PROJECTION, 1)
+        g.handle.set_option(_abi.OPT_ANALYTIC_PROJECTION, 1)
+        g.handle.set_field(g.field.E0, analytic=False)
     if store_plasma:
         from filament_gb import _abi
         g.handle.set_option(_abi.OPT_STORE_PLASMA, 1)

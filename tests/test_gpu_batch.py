@@ -100,7 +100,6 @@ def test_batch_member_matches_oracle_loop(gpu_lib):
     finally:
         sw.close()
     r = fg.Simulation(sweep.member_input(p, **SMALL), binding=oracle.binding())
-    r.handle.set_option(_abi.OPT_ANALYTIC_PROJECTION, 1)
     code_r, st_r = r.handle.run(0.0, 0.03, 10 ** 6)
     assert code == 0 and code_r == 1 == stats[1]["status"]
     assert stats[1]["steps"] == st_r["steps"]

@@ -105,15 +105,22 @@ def test_run_nmax(gpu_lib):
     assert code == 3 and st["steps"] == 5
 
 
-def test_half_spectrum_projection_effect_is_small(gpu_lib):
-    """The library keeps only the analytic half spectrum; the reference keeps
-    the negative-frequency content that the time guard creates.  Against the
-    literal oracle (no projection) the difference stays far below the FP32
-    error budget."""
-    inp = rt_input(PPcr=150.0, ALG="RK4")
-    g, r = pair(inp, "fp64", project=False)
-    step_both(g, r, 3, 1e-3)
-    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < 1e-6
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_upper_half_spectrum_as_the_reference(gpu_lib, precision):
+    """The negative frequencies the time guard creates: kept and propagated
+    as the reference does (the default, against the literal oracle), or
+    dropped on both sides (FIL_OPT_ANALYTIC_PROJECTION).  A narrow time
+    guard makes the upper half large enough that dropping it shows."""
+    inp = rt_input(PPcr=150.0, ALG="RK4", tguard=60.0)
+    out = {}
+    for project in (False, True):
+        g, r = pair(inp, precision, project=project)
+        step_both(g, r, 4, 1e-3)
+        Eg, Er = g.handle.get_field(), r.handle.get_field()
+        assert rel_l2(Eg, Er) < TOL[precision]
+        out[project] = Er
+    # the projection is a visible change of the method on this input
+    assert rel_l2(out[True], out[False]) > 10 * TOL["mixed"]
 
 
 @pytest.mark.parametrize("dht", ["tensor", "simt"])
@@ -265,3 +272,43 @@ def test_ereal_losses_and_plasma(gpu_lib, precision):
     assert rel_l2(g.handle.get_plasma(1), r.handle.get_plasma(1)) < tol
     step_both(g, r, 3, 1e-3)
     assert rel_l2(g.handle.get_field(), r.handle.get_field()) < tol
+
+
+@pytest.mark.parametrize("form", ["mixed", "mixed_simt", "fp64"])
+def test_nonparaxial_prefactor(gpu_lib, form):
+    """QPARAXIAL = false (nonlinear_propagators.jl:56-63, 232-241): every RK
+    stage's right-hand side goes through the Hankel pair with
+    QZ(kt, w) = QZ(w) beta / sqrt(beta^2 - kt^2) and the spectral guard in
+    between.  Narrow beam (more transverse spectrum) with plasma, RK4."""
+    from filament_gb import _abi
+    import filament_gb as fg
+    import oracle
+    precision = "fp64" if form == "fp64" else "mixed"
+    inp = rt_input(PPcr=150.0, ALG="RK4", QPARAXIAL=False, beam_a0=0.5e-3)
+    g, r = pair(inp, precision)
+    assert g.problem.config.qparaxial == 0
+    if form == "mixed_simt":
+        g.handle.set_option(_abi.OPT_DHT_SIMT, 1)
+    step_both(g, r, 3, 1e-3)
+    Eg, Er = g.handle.get_field(), r.handle.get_field()
+    assert rel_l2(Eg, Er) < TOL[precision]
+    if precision == "fp64":
+        # the paraxial prefactor gives a measurably different field
+        inp_p = rt_input(PPcr=150.0, ALG="RK4", QPARAXIAL=True, beam_a0=0.5e-3)
+        rp = fg.Simulation(inp_p, binding=oracle.binding())
+        z = 0.0
+        for _ in range(3):
+            z += 1e-3
+            rp.handle.step(z, 1e-3)
+        assert rel_l2(Eg, rp.handle.get_field()) > 100 * TOL["fp64"]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_nonparaxial_device_loop(gpu_lib, precision):
+    """The non-paraxial step inside fil_run's captured graphs, adaptive dz."""
+    inp = rt_input(PPcr=60.0, ALG="RK3", QPARAXIAL=False, dzphimax=0.1, dz_initial=1e-2, zmax=0.02)
+    g, r = pair(inp, precision)
+    code_g, st_g = g.handle.run(0.0, inp["zmax"], 10 ** 6)
+    code_r, st_r = r.handle.run(0.0, inp["zmax"], 10 ** 6)
+    assert code_g == code_r == 1 and st_g["steps"] == st_r["steps"]
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < 10 * TOL[precision]
