@@ -58,6 +58,7 @@ struct fil_handle {
   double* u_kzr = nullptr;
   void* u_kg = nullptr;
   bool full_spec = false;   // SU carried (FIL_OPT_ANALYTIC_PROJECTION off)
+  void* park = nullptr;     // [nrows][nh] complex: a step's guarded spectrum across its plasma solve
   // non-paraxial prefactor (QPARAXIAL = false, RT): per-stage buffers
   // [mpad][nh] complex (S0, k1, k of the last stage, running sum) and the
   // tensor-core path's factor QZ(kt, w) / QZ(w) * Kguard Wguard, [nh][mpad]
@@ -630,6 +631,7 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
     P.u_kzr = h->u_kzr;
     P.u_kg = (const C*)h->u_kg;
   }
+  P.s0_park = (C*)h->park;
   P.np_S0 = (C*)h->np_S0;
   P.np_K1 = (const C*)h->np_K1;
   P.np_KS = (const C*)h->np_KS;
@@ -962,7 +964,7 @@ static void free_all(fil_handle* h) {
                   h->kx2, h->ky2, h->sg1, h->sg2, h->twx, h->twy,
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
                   h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err,
-                  h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt};
+                  h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt, h->park};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -1149,6 +1151,10 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   CKC(cudaMemset(h->W1, 0, sz));
   CKC(cudaMemset(h->W2, 0, sz));
   CKC(cudaMalloc(&h->stage, (size_t)h->nrows * h->nt * es));
+  if (h->geom != FIL_GEOM_XY) {
+    CKC(cudaMalloc(&h->park, (size_t)h->nrows * h->nh * es));
+    CKC(cudaMemset(h->park, 0, (size_t)h->nrows * h->nh * es));
+  }
   CKC(cudaMalloc(&h->fluence, h->nrows * sizeof(double)));
   CKC(cudaMalloc(&h->power, h->nt * sizeof(double)));
   CKC(cudaMalloc(&h->rho_end, h->nrows * sizeof(double)));
@@ -1680,19 +1686,28 @@ static int batch_check_members(fil_batch* b) {
 // saved field state and controller of every member (tuner trials)
 struct BatchSaved {
   std::vector<void*> S;
+  std::vector<void*> U;        // the upper half of the spectrum (RT keeps it)
   std::vector<DevCtl> ctl;
 };
+static size_t upper_bytes(const fil_handle* h) {
+  return (size_t)h->nrows * h->nh * (h->fp64 ? sizeof(double2) : sizeof(float2));
+}
 static size_t state_bytes(const fil_handle* h) {
   return (size_t)h->mpad * h->nh * (h->fp64 ? sizeof(double2) : sizeof(float2));
 }
 static int batch_save(fil_batch* b, BatchSaved& sv) {
   const size_t n = b->m.size();
   sv.S.assign(n, nullptr);
+  sv.U.assign(n, nullptr);
   sv.ctl.resize(n);
   for (size_t i = 0; i < n; ++i) {
     fil_handle* h = b->m[i];
     CKB(cudaMalloc(&sv.S[i], state_bytes(h)));
     CKB(cudaMemcpyAsync(sv.S[i], h->S, state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
+    if (h->SU) {
+      CKB(cudaMalloc(&sv.U[i], upper_bytes(h)));
+      CKB(cudaMemcpyAsync(sv.U[i], h->SU, upper_bytes(h), cudaMemcpyDeviceToDevice, h->st));
+    }
     CKB(cudaMemcpyAsync(&sv.ctl[i], h->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, h->st));
     CKB(cudaStreamSynchronize(h->st));
   }
@@ -1701,6 +1716,7 @@ static int batch_save(fil_batch* b, BatchSaved& sv) {
 static int member_restore(fil_batch* b, const BatchSaved& sv, int i) {
   fil_handle* h = b->m[i];
   CKB(cudaMemcpyAsync(h->S, sv.S[i], state_bytes(h), cudaMemcpyDeviceToDevice, h->st));
+  if (sv.U[i]) CKB(cudaMemcpyAsync(h->SU, sv.U[i], upper_bytes(h), cudaMemcpyDeviceToDevice, h->st));
   CKB(cudaMemcpyAsync(h->ctl, &sv.ctl[i], sizeof(DevCtl), cudaMemcpyHostToDevice, h->st));
   CKB(cudaStreamSynchronize(h->st));
   // a trial with the other Hankel kernel left its layout in W1, W2
@@ -1718,7 +1734,10 @@ static int batch_restore(fil_batch* b, const BatchSaved& sv) {
 static void batch_free_saved(BatchSaved& sv) {
   for (void* p : sv.S)
     if (p) cudaFree(p);
+  for (void* p : sv.U)
+    if (p) cudaFree(p);
   sv.S.clear();
+  sv.U.clear();
 }
 
 // controller armed for trial steps that never stop on z or the step count

@@ -105,6 +105,9 @@ template <typename R> struct RowParams {
   C* U_out;
   const double* u_kzr;          // [row][N/2] Re KZ (zu units) in FP64: the phase KZ dz is reduced exactly
   const C* u_kg;                // [row][N/2] (Im KZ, Kguard Wguard)
+  // [row][N/2] (row stride ld): the guarded spectrum S0 of a step parked
+  // across the plasma solve (load_time_row_split)
+  C* s0_park;
   // non-paraxial prefactor (k_rowstep modes 2, 3; k_np_combine): [row][N/2]
   // complex, row stride ld; rho_g, kdrho_g hold the step's density rows
   C* np_S0;                     // t -> w transform of the guarded field
@@ -152,6 +155,43 @@ FIL_DEV void load_time_row(const RowParams<R>& P, typename C2T<R>::type* X, int 
     }
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// The pending field guard of a step without the transform round trip.  The
+// state [S, U] is the exact spectrum of E(t) = fft(S, U); the guarded
+// spectrum is ifft(g E) = [S, U] - ifft((1 - g) E), so only the guard's
+// correction (1 - g) E, small wherever the guard is 1, goes through the
+// transforms and their rounding.  Afterwards X holds g E(t) (for the
+// plasma solve); the guarded lower half is in s0_park, the upper half (when
+// kept) in U_out.  Y is scratch and free again on return.
+template <typename R, int N>
+FIL_DEV void load_time_row_split(const RowParams<R>& P, typename C2T<R>::type* X, typename C2T<R>::type* Y,
+                                 int row) {
+  typedef typename C2T<R>::type C;
+  constexpr int T = N / 16, NH = N / 2, EW = NH / T;
+  const int tid = threadIdx.x;
+  load_time_row<R, N>(P, X, row, false);
+  int iy;
+  const R gs = row_guard(P, row, &iy);
+#pragma unroll
+  for (int m = 0; m < 16; ++m) {
+    const int j = tid + m * T;
+    const R g = gs * P.gt[P.gt_bug ? iy : j];
+    const C e = X[pad16(j)];
+    Y[pad16(j)] = ((R)1 - g) * e;
+    X[pad16(j)] = g * e;
+  }
+  filfft::block_fft<C, N, +1>(Y, P.tw);
+  const R invN = (R)1 / (R)N;
+  const size_t rb = (size_t)row * P.ld;
+#pragma unroll
+  for (int m = 0; m < EW; ++m) {
+    const int k = tid + m * T;
+    P.s0_park[rb + k] = P.S_in[rb + k] - invN * Y[pad16(k)];
+    if (P.U_out) P.U_out[rb + k] = P.U_in[rb + k] - invN * Y[pad16(k + NH)];
+  }
+  __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
@@ -742,7 +782,12 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
       }
     }
   }
-  load_time_row<R, N>(P, X, row, guard);
+  // a step's pending guard without the transform round trip (the guarded
+  // spectrum to s0_park and U_out); the initial solve and the plasma-only
+  // launch of a non-paraxial step only need g E(t)
+  const bool split = mode == 0 && guard;
+  if (split) load_time_row_split<R, N>(P, X, Y, row);
+  else load_time_row<R, N>(P, X, row, guard);
   // largest |E|^2 of the row (the linear-only test below)
   R e2row = 0;
   if (!RAM && mode == 0 && P.nonlin && P.cc_max >= (R)0) {
@@ -794,17 +839,19 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   }
   if (mode == 1 || mode == 4) return;
 
-  // ---- t -> w: the analytic half in registers, the upper half (when kept)
-  // to the row's slice of U_out, where the stages read it back
-  filfft::block_fft<C, N, +1>(X, P.tw);
-  const R invN = (R)1 / (R)N;
+  // ---- the guarded spectrum: the analytic half in registers (from the
+  // parked values, or the state itself when no guard is pending); the upper
+  // half (when kept) is in U_out, where the stages read it
   C S0[EW], k1[EW], kp[EW], acc[EW];
+  {
+    const C* s0 = (split ? P.s0_park : P.S_in) + (size_t)row * P.ld;
 #pragma unroll
-  for (int m = 0; m < EW; ++m) {
-    int k = tid + m * T;
-    S0[m] = invN * X[pad16(k)];
-    if (uo) uo[k] = invN * X[pad16(k + NH)];
-    acc[m] = mk<R>(0, 0);
+    for (int m = 0; m < EW; ++m) {
+      int k = tid + m * T;
+      S0[m] = s0[k];
+      if (!split && uo && uo != P.U_in + (size_t)row * P.ld) uo[k] = P.U_in[(size_t)row * P.ld + k];
+      acc[m] = mk<R>(0, 0);
+    }
   }
   // Linear-only row: with the plasma channels off for this row (no plasma,
   // or a row left at rho0 = 0 whose losses response is below 2^-30 of its
@@ -896,16 +943,25 @@ __global__ void __launch_bounds__(N / 16) k_rowstage(RowParams<R> P) {
   const R gs = row_guard(P, row, &iy);
   auto d = [&](int m, C v) { write_out<R>(P, row, tid + m * T, v); };
   if (s == 0) {
-    load_time_row<R, N>(P, X, row, ctl->guard_pending != 0);
-    filfft::block_fft<C, N, +1>(X, P.tw);
-    const R invN = (R)1 / (R)N;
+    // the guarded spectrum without the transform round trip
+    // (load_time_row_split parks it in s0_park), kept in np_S0
     C S0[EW];
+    if (ctl->guard_pending) {
+      load_time_row_split<R, N>(P, X, Y, row);
 #pragma unroll
-    for (int m = 0; m < EW; ++m) {
-      const int k = tid + m * T;
-      S0[m] = invN * X[pad16(k)];
-      P.np_S0[rb + k] = S0[m];
-      if (uo) uo[k] = invN * X[pad16(k + NH)];
+      for (int m = 0; m < EW; ++m) {
+        const int k = tid + m * T;
+        S0[m] = P.s0_park[rb + k];
+        P.np_S0[rb + k] = S0[m];
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < EW; ++m) {
+        const int k = tid + m * T;
+        S0[m] = P.S_in[rb + k];
+        P.np_S0[rb + k] = S0[m];
+        if (uo && uo != P.U_in + rb) uo[k] = P.U_in[rb + k];
+      }
     }
     auto u = [&](int m) -> C { return S0[m]; };
     stage_rhs<R, N, NC, RAM>(P, X, Y, rho, kdrho, gs, iy, true, uo, u, d);

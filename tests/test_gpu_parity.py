@@ -119,8 +119,9 @@ def test_upper_half_spectrum_as_the_reference(gpu_lib, precision):
         Eg, Er = g.handle.get_field(), r.handle.get_field()
         assert rel_l2(Eg, Er) < TOL[precision]
         out[project] = Er
-    # the projection is a visible change of the method on this input
-    assert rel_l2(out[True], out[False]) > 10 * TOL["mixed"]
+    # the projection is a change of the method far above the FP64 form's
+    # agreement with the oracle
+    assert rel_l2(out[True], out[False]) > 100 * TOL["fp64"]
 
 
 @pytest.mark.parametrize("dht", ["tensor", "simt"])
@@ -279,12 +280,13 @@ def test_nonparaxial_prefactor(gpu_lib, form):
     """QPARAXIAL = false (nonlinear_propagators.jl:56-63, 232-241): every RK
     stage's right-hand side goes through the Hankel pair with
     QZ(kt, w) = QZ(w) beta / sqrt(beta^2 - kt^2) and the spectral guard in
-    between.  Narrow beam (more transverse spectrum) with plasma, RK4."""
+    between.  Narrow beam (more transverse spectrum) at 60 Pcr with plasma,
+    RK4."""
     from filament_gb import _abi
     import filament_gb as fg
     import oracle
     precision = "fp64" if form == "fp64" else "mixed"
-    inp = rt_input(PPcr=150.0, ALG="RK4", QPARAXIAL=False, beam_a0=0.5e-3)
+    inp = rt_input(PPcr=60.0, ALG="RK4", QPARAXIAL=False, beam_a0=0.5e-3)
     g, r = pair(inp, precision)
     assert g.problem.config.qparaxial == 0
     if form == "mixed_simt":
@@ -294,7 +296,7 @@ def test_nonparaxial_prefactor(gpu_lib, form):
     assert rel_l2(Eg, Er) < TOL[precision]
     if precision == "fp64":
         # the paraxial prefactor gives a measurably different field
-        inp_p = rt_input(PPcr=150.0, ALG="RK4", QPARAXIAL=True, beam_a0=0.5e-3)
+        inp_p = rt_input(PPcr=60.0, ALG="RK4", QPARAXIAL=True, beam_a0=0.5e-3)
         rp = fg.Simulation(inp_p, binding=oracle.binding())
         z = 0.0
         for _ in range(3):
