@@ -33,12 +33,16 @@ DECK = os.path.join(PKG, "decks", "filament_RT", "input.py")
 WORKLOAD = dict(Nr=1000, Nt=4096, rmax=5.0, tmin=-200.0, tmax=200.0, PPcr=5.0, ALG="RK4",
                 dzphimax=0.1, dz_initial=1e-2, zmax=3.0)
 # The explicit RK nonlinear step of the reference becomes unstable in this
-# workload near z = 2.29 m (the Drude free-current term grows like 1/w at the
-# lowest frequency bins and leaves the RK4 stability region once the
-# filament's plasma forms); both precision forms diverge at the same step.
-# Accuracy is compared at z = 2.25 m, after the collapse, with the intensity
-# clamped by the plasma; throughput loops stay below STABLE_Z.
-ACCURACY_ZEND = 2.25
+# workload: the FP64 oracle of the reference's method diverges at z = 2.287 m
+# (the Drude free-current term grows like 1/w at the lowest frequency bins
+# and leaves the RK4 stability region once the filament's plasma forms).  The
+# unstable mode is active well before that: a change of the FP64 field of
+# 1e-12 at z = 1.8 m grows to 3e-8 at 2.1 m and 1.6e-4 at 2.2 m.  Accuracy
+# is compared at z = 2.1 m -- the pulse has collapsed (Imax ~ 53 Iu, plasma
+# formed) and the mode is still below the FP32 resolution -- and recorded
+# along z up to 2.25 m; the timed run covers z = 0 .. 2.1 m.
+ACCURACY_ZEND = 2.1
+ACCURACY_ZS = (1.0, 1.5, 1.8, 2.0, 2.1, 2.2, 2.25)
 STABLE_Z = 2.2
 WORKLOAD_NAME = "RT filamentation Nr=1000 x Nt=4096, RK4, 5 Pcr, adaptive dz (phimax 0.1 rad)"
 
@@ -404,22 +408,28 @@ def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1,
     return out
 
 
-def accuracy_run(zend, nmax, net=None, oracle_check=True):
+def accuracy_run(zend, nmax, net=None, oracle_check=True, zs=ACCURACY_ZS):
     """The GPU forms (mixed with tensor-core and with CUDA-core Hankel
     transforms, mixed + surrogate, plain FP64) and the FP64 CPU oracle of
-    the reference's method (full spectrum kept, OpenMP on all host cores),
-    each from the same field to the same z (dz clamped on the last step);
-    relative L2 of the field and of the fluence against the oracle, and
-    against the GPU's own FP64 form."""
+    the reference's method (OpenMP on all host cores), each from the same
+    field through the same stops zs (dz clamped on the last step before
+    each); relative L2 of the field and of the fluence at every stop against
+    the oracle and against the GPU's own FP64 form.  The summary of each
+    form is the stop z = zend."""
     import numpy as np
     import filament_gb as fg
     from filament_gb import _abi
-    inp = _prepare(zmax=zend)
-    out = {"z_end": zend}
-    fields = {}
-    forms = ("mixed", "mixed_simt", "fp64") + (("mixed_surrogate",) if net is not None else ())
-    if oracle_check:
-        forms = forms + ("oracle",)
+    zs = sorted(set(list(zs) + [zend]))
+    inp = _prepare(zmax=max(zs))
+    out = {"z_end": zend, "stops": zs}
+    ref = {}
+    forms = (("oracle",) if oracle_check else ()) + ("fp64", "mixed", "mixed_simt") + \
+        (("mixed_surrogate",) if net is not None else ())
+
+    def err(a, b):
+        (Ea, Fa), (Eb, Fb) = a, b
+        return {"field_rel_l2": float(np.linalg.norm(Ea - Eb) / np.linalg.norm(Eb)),
+                "fluence_rel_l2": float(np.linalg.norm(Fa - Fb) / np.linalg.norm(Fb))}
     for prec in forms:
         if prec == "oracle":
             sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -432,29 +442,31 @@ def accuracy_run(zend, nmax, net=None, oracle_check=True):
         if prec == "mixed_surrogate":
             net.arm(sim.handle, every=SURR_EVERY, tol=SURR_TOL)
         sim.handle.set_option(_abi.OPT_CLAMP_LAST_DZ, 1)
+        series = []
+        z = 0.0
         t0 = time.perf_counter()
-        code, st = sim.handle.run(0.0, zend, nmax)
+        for zstop in zs:
+            code, st = sim.handle.run(z, zstop, nmax)
+            z = st["z"]
+            a = sim.handle.analyze()
+            f = (sim.handle.get_field(), a["fluence"])
+            row = {"z": z, "steps": int(st["steps"]), "imax": a["imax"]}
+            if prec in ("oracle", "fp64"):
+                ref[(prec, zstop)] = f
+            if prec != "oracle" and ("oracle", zstop) in ref:
+                row["vs_oracle"] = err(f, ref[("oracle", zstop)])
+            if prec not in ("oracle", "fp64"):
+                row["vs_fp64_gpu"] = err(f, ref[("fp64", zstop)])
+            series.append(row)
         wall = time.perf_counter() - t0
-        a = sim.handle.analyze()
-        fields[prec] = (sim.handle.get_field(), a["fluence"])
-        out[prec] = {"steps": int(st["steps"]), "z": st["z"], "wall_s": wall, "imax_end": a["imax"]}
+        summary = dict(next(r for r in series if abs(r["z"] - zend) < 1e-9))
+        summary.update({"wall_s": wall, "series": series})
+        out[prec] = summary
         if prec == "mixed_surrogate":
             from filament_gb import surrogate as S
             out["surrogate_stats"] = S.stats(sim.handle)
         sim.close()
-
-    def err(a, b):
-        (Ea, Fa), (Eb, Fb) = fields[a], fields[b]
-        return {"field_rel_l2": float(np.linalg.norm(Ea - Eb) / np.linalg.norm(Eb)),
-                "fluence_rel_l2": float(np.linalg.norm(Fa - Fb) / np.linalg.norm(Fb))}
-    for prec in forms:
-        if prec in ("fp64", "oracle"):
-            continue
-        out[prec]["vs_fp64_gpu"] = err(prec, "fp64")
-        if oracle_check:
-            out[prec]["vs_oracle"] = err(prec, "oracle")
     if oracle_check:
-        out["fp64"]["vs_oracle"] = err("fp64", "oracle")
         out["oracle"]["cores"] = os.cpu_count()
     return out
 
@@ -696,6 +708,10 @@ def main():
                                             and a["fluence_rel_l2"] <= 1e-3)})
         if "oracle" in acc:
             headline["fp64_gpu_vs_oracle_field_rel_l2"] = acc["fp64"]["vs_oracle"]["field_rel_l2"]
+        # the error along z: its growth past z_end is the unstable mode of
+        # the method's RK step (the oracle diverges at z = 2.287 m)
+        headline["field_rel_l2_along_z"] = {"%.2f" % r["z"]: r[key]["field_rel_l2"]
+                                            for r in acc["mixed_surrogate"]["series"]}
     line = {
         "metric": "RT z-steps/s", "value": value, "unit": "z-steps/s", "n_gpus": args.gpus,
         "steps": surr["timed_steps"], "warmup": args.warmup, "ms_per_step": t_local,

@@ -38,6 +38,7 @@ struct fil_handle {
   fil_config cfg;
   std::string err;
   int geom, n1, n2, nt, nh, nrows, mpad, nc;
+  int ld;                   // row stride of S, W1, W2 (complex): nh, or nt for XYT (both halves of the spectrum)
   bool fp64;
   cudaStream_t st = nullptr;
   // device buffers (void* to serve both precisions)
@@ -276,17 +277,19 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
   }
   // propagator tables
   {
-    std::vector<double> kt2(mp, 0.0), be(2 * nh), df(2 * nh);
+    // full-length frequency tables (the XYT transverse passes also
+    // propagate the upper half of the spectrum)
+    std::vector<double> kt2(mp, 0.0), be(2 * nt), df(2 * nt);
     for (int i = 0; i < n1; ++i) kt2[i] = t->kt1[i] * t->kt1[i];
-    for (int k = 0; k < 2 * nh; ++k) { be[k] = t->beta[k]; df[k] = t->dfr[k]; }
+    for (int k = 0; k < 2 * nt; ++k) { be[k] = t->beta[k]; df[k] = t->dfr[k]; }
     if (upload<R>(h, &h->kt2, kt2) || upload<R>(h, &h->beta, be) || upload<R>(h, &h->dfr, df)) return FIL_ERR_CUDA;
     if (t->kmax) {
-      std::vector<double> km(nh);
-      for (int k = 0; k < nh; ++k) km[k] = t->kmax[k] * t->kmax[k];
+      std::vector<double> km(nt);
+      for (int k = 0; k < nt; ++k) km[k] = t->kmax[k] * t->kmax[k];
       if (upload<R>(h, &h->kmax2, km)) return FIL_ERR_CUDA;
     }
     if (t->wguard) {
-      std::vector<double> w(t->wguard, t->wguard + nh);
+      std::vector<double> w(t->wguard, t->wguard + nt);
       if (upload<R>(h, &h->wg, w)) return FIL_ERR_CUDA;
     }
   }
@@ -585,7 +588,7 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
   P.nrows = h->nrows;
   P.n2 = h->n2;
   P.geom = h->geom;
-  P.ld = h->nh;
+  P.ld = h->ld;
   P.tw = (const C*)h->tw;
   P.g1 = (const R*)h->g1;
   P.g2 = (const R*)h->g2;
@@ -625,7 +628,12 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
   P.ctl = h->ctl;
   P.out_T = 0;
   P.ldT = h->mpad;
-  if (h->full_spec) {
+  if (h->full_spec && h->geom == FIL_GEOM_XYT) {
+    // both halves in one row of S (input) and of W1 (output); the upper
+    // half's linear step is the transverse passes' (xyfft.cu)
+    P.U_in = (const C*)h->S + h->nh;
+    P.U_out = (C*)h->W1 + h->nh;
+  } else if (h->full_spec) {
     P.U_in = (const C*)h->SU;
     P.U_out = (C*)h->SU;
     P.u_kzr = h->u_kzr;
@@ -681,22 +689,23 @@ template <typename R> static int enqueue_zstep_xyt(fil_handle* h, bool timed) {
   if (timed) CK(cudaEventRecord(h->ev[5], h->st));
   CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
   if (timed) CK(cudaEventRecord(h->ev[2], h->st));
-  const int nx = h->n1, ny = h->n2, nh = h->nh;
+  const int nx = h->n1, ny = h->n2, ld = h->ld;
+  const int ncols = h->full_spec ? h->nt : h->nh;   // frequency columns transformed
   XyParams<R> q;
   std::memset(&q, 0, sizeof q);
   q.in = (const C*)h->W1;
   q.out = (C*)h->W1;
   q.ctl = h->ctl;
   // along y: lines p = ix*ny + iy
-  q.line_stride = nh;
-  q.outer_stride = (size_t)ny * nh;
+  q.line_stride = ld;
+  q.outer_stride = (size_t)ny * ld;
   q.tw = (const C*)h->twy;
   q.scale = (R)1;
-  CK(launch_xylines<R>(q, ny, 0, nh, nx, h->st));
+  CK(launch_xylines<R>(q, ny, 0, ncols, nx, h->st));
   // along x, propagator, back along x
   XyParams<R> qx = q;
-  qx.line_stride = (size_t)ny * nh;
-  qx.outer_stride = nh;
+  qx.line_stride = (size_t)ny * ld;
+  qx.outer_stride = ld;
   qx.tw = (const C*)h->twx;
   qx.scale = (R)1 / (R)nx;
   qx.pp = prop_params<R>(h);
@@ -707,12 +716,12 @@ template <typename R> static int enqueue_zstep_xyt(fil_handle* h, bool timed) {
   qx.kt2_outer = (const R*)h->ky2;
   qx.sg_line = (const R*)h->sg1;
   qx.sg_outer = (const R*)h->sg2;
-  CK(launch_xylines<R>(qx, nx, 1, nh, ny, h->st));
+  CK(launch_xylines<R>(qx, nx, 1, ncols, ny, h->st));
   if (timed) CK(cudaEventRecord(h->ev[3], h->st));
   XyParams<R> qi = q;
   qi.out = (C*)h->S;
   qi.scale = (R)1 / (R)ny;
-  CK(launch_xylines<R>(qi, ny, 2, nh, nx, h->st));
+  CK(launch_xylines<R>(qi, ny, 2, ncols, nx, h->st));
   if (timed) CK(cudaEventRecord(h->ev[4], h->st));
   return 0;
 }
@@ -943,7 +952,7 @@ static int check_tc(fil_handle* h) {
 // zeroes the Hankel-step work buffers W1, W2 (their padding rows and
 // columns are read by the next step but written by neither path)
 static int clear_work(fil_handle* h) {
-  const size_t sz = (size_t)h->mpad * h->nh * (h->fp64 ? sizeof(double2) : sizeof(float2));
+  const size_t sz = (size_t)h->mpad * h->ld * (h->fp64 ? sizeof(double2) : sizeof(float2));
   CK(cudaMemsetAsync(h->W1, 0, sz, h->st));
   CK(cudaMemsetAsync(h->W2, 0, sz, h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -1024,8 +1033,10 @@ template <typename R> static int set_field_t(fil_handle* h, const void* E, int d
     return 0;
   }
   CK(cudaMemcpyAsync(h->stage, rows.data(), rows.size() * sizeof(R), cudaMemcpyHostToDevice, h->st));
-  CK(launch_field_in<R>((const C*)h->stage, (C*)h->S, h->full_spec ? (C*)h->SU : nullptr, h->nh, (const C*)h->tw,
-                        analytic, h->nrows, h->nt, h->st));
+  C* up = nullptr;
+  if (h->full_spec) up = (h->geom == FIL_GEOM_XYT) ? (C*)h->S + h->nh : (C*)h->SU;
+  CK(launch_field_in<R>((const C*)h->stage, (C*)h->S, up, h->ld, (const C*)h->tw, analytic, h->nrows, h->nt,
+                        h->st));
   // control block: fresh simulation, no pending guard; an armed surrogate
   // stays armed with fresh counters
   DevCtl c;
@@ -1117,6 +1128,7 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   h->n2 = cfg->n2;
   h->nt = cfg->nt;
   h->nh = cfg->geometry == FIL_GEOM_XY ? 1 : cfg->nt / 2;   // XY: the field itself, one column
+  h->ld = cfg->geometry == FIL_GEOM_XYT ? cfg->nt : h->nh;
   h->nrows = cfg->n1 * cfg->n2;
   h->mpad = (h->nrows + 127) / 128 * 128;
   h->nc = cfg->plasma ? cfg->plasma_ncomp : 0;
@@ -1132,7 +1144,7 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   }
   int rc = 0;
   const size_t es = h->fp64 ? sizeof(double2) : sizeof(float2);
-  const size_t sz = (size_t)h->mpad * h->nh * es;
+  const size_t sz = (size_t)h->mpad * h->ld * es;
 #define CKC(call)                                                                    \
   do {                                                                               \
     cudaError_t e_ = (call);                                                         \
@@ -1152,8 +1164,11 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   CKC(cudaMemset(h->W2, 0, sz));
   CKC(cudaMalloc(&h->stage, (size_t)h->nrows * h->nt * es));
   if (h->geom != FIL_GEOM_XY) {
-    CKC(cudaMalloc(&h->park, (size_t)h->nrows * h->nh * es));
-    CKC(cudaMemset(h->park, 0, (size_t)h->nrows * h->nh * es));
+    CKC(cudaMalloc(&h->park, (size_t)h->nrows * h->ld * es));
+    CKC(cudaMemset(h->park, 0, (size_t)h->nrows * h->ld * es));
+  }
+  if (h->geom == FIL_GEOM_XYT) {
+    h->full_spec = true;      // the upper half lives in columns nh .. nt - 1 of S
   }
   CKC(cudaMalloc(&h->fluence, h->nrows * sizeof(double)));
   CKC(cudaMalloc(&h->power, h->nt * sizeof(double)));
@@ -1213,10 +1228,14 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
     // on: the state is the analytic half spectrum (the upper half dropped
     // after every t->w transform); off (RT default): the upper half is kept
     // as the reference keeps it.  XYT always projects.
-    const bool full = (value == 0) && h->SU != nullptr;
+    const bool full = (value == 0) && (h->SU != nullptr || h->geom == FIL_GEOM_XYT);
     if (full != h->full_spec) {
       if (full) {   // the upper half restarts from zero
-        CK(cudaMemsetAsync(h->SU, 0, (size_t)h->nrows * h->nh * (h->fp64 ? sizeof(double2) : sizeof(float2)), h->st));
+        const size_t es = h->fp64 ? sizeof(double2) : sizeof(float2);
+        if (h->geom == FIL_GEOM_XYT)
+          CK(cudaMemset2DAsync((char*)h->S + h->nh * es, h->ld * es, 0, h->nh * es, h->nrows, h->st));
+        else
+          CK(cudaMemsetAsync(h->SU, 0, (size_t)h->nrows * h->nh * es, h->st));
         CK(cudaStreamSynchronize(h->st));
       }
       h->full_spec = full;

@@ -888,9 +888,9 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   }
 #pragma unroll
   for (int m = 0; m < EW; ++m) write_out<R>(P, row, tid + m * T, S0[m] + dz * acc[m]);
-  if (uo) {
-    // linear step of the upper half (the lower half's follows in the
-    // Hankel transforms)
+  if (uo && P.u_kzr) {
+    // linear step of the upper half in r-space (RT; the lower half's
+    // follows in the Hankel transforms; XYT transforms both halves)
     const double dzd = ctl->dz;
     const size_t base = (size_t)row * P.ld;
 #pragma unroll 2
@@ -1001,7 +1001,7 @@ __global__ void __launch_bounds__(256) k_np_combine(RowParams<R> P, int nh) {
     } else {
       P.S_out[rb + k] = v;
     }
-    if (P.U_out) P.U_out[rb + k] = upper_prop<R>(P, rb + k, P.U_out[rb + k], dzd);
+    if (P.U_out && P.u_kzr) P.U_out[rb + k] = upper_prop<R>(P, rb + k, P.U_out[rb + k], dzd);
   }
 }
 

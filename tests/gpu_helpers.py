@@ -64,14 +64,13 @@ def saturating_rate(n=14):
 def pair(inp, precision="mixed", store_plasma=False, project=None):
     """(CUDA simulation, oracle simulation) on the same input, both with the
     same treatment of the upper half of the spectrum: kept as the reference
-    keeps it (project=False, the RT default) or dropped after each t->w
-    transform (project=True; XYT always projects), so that the two differ
-    by arithmetic only."""
+    keeps it (project=False, the default) or dropped after each t->w
+    transform (project=True), so that the two differ by arithmetic only."""
     import filament_gb as fg
     import oracle
     from filament_gb import _abi
     if project is None:
-        project = inp["geometry"] == "XYT"
+        project = False
     g = fg.Simulation(inp, precision=precision)
     r = fg.Simulation(inp, binding=oracle.binding())
     if project:

@@ -98,10 +98,11 @@ def test_accuracy_leg_with_the_oracle_standing_in(monkeypatch, oracle_binding):
     monkeypatch.setattr(fg, "Simulation",
                         lambda inp, binding=None, precision="mixed": Simulation(inp, binding=oracle_binding,
                                                                                precision=precision))
-    r = bench.accuracy_run(0.02, 1000)
-    assert r["z_end"] == 0.02
+    r = bench.accuracy_run(0.02, 1000, zs=(0.01, 0.02))
+    assert r["z_end"] == 0.02 and r["stops"] == [0.01, 0.02]
     for form in ("mixed", "mixed_simt", "fp64", "oracle"):
         assert abs(r[form]["z"] - 0.02) < 1e-12 and r[form]["steps"] >= 2
+        assert [round(x["z"], 12) for x in r[form]["series"]] == [0.01, 0.02]
     for form in ("mixed", "mixed_simt"):
         assert r[form]["vs_oracle"]["field_rel_l2"] < 1e-12      # all FP64 here
         assert r[form]["vs_fp64_gpu"]["fluence_rel_l2"] < 1e-12

@@ -6,10 +6,9 @@ sizes the measurements are quoted on).
   RT 1000 x 4096, 5 Pcr, RK4, adaptive dz: the first 40 steps
   XYT 128 x 128 x 512 multifilamentation deck: three steps
 
-For RT the library keeps the upper half of the spectrum as the reference
-does and the oracle is the reference's method; for XYT both drop it after
-each t->w transform.  The FP64 form differs from the oracle by rounding
-only.  Tolerances: FP64 form 1e-10 relative L2 of the field over
+The library keeps the upper half of the spectrum as the reference does and
+the oracle is the reference's method.  The FP64 form differs from the
+oracle by rounding only.  Tolerances: FP64 form 1e-10 relative L2 of the field over
 a few steps (the accumulated rounding of two FP64 programs with different
 summation orders; 1e-9 over the 1000-step run, whose filament amplifies
 rounding differences); mixed form 1e-4 field and 1e-3 fluence (the
@@ -39,16 +38,10 @@ def _log(name, **vals):
 
 
 def _oracle_sim(inp):
-    """The oracle of the reference's method; for XYT, whose library state is
-    the analytic half spectrum, with the negative frequencies dropped after
-    each t->w transform as well."""
+    """The oracle of the reference's method."""
     import filament_gb as fg
     import oracle
-    from filament_gb import _abi
-    r = fg.Simulation(inp, binding=oracle.binding())
-    if inp["geometry"] == "XYT":
-        r.handle.set_option(_abi.OPT_ANALYTIC_PROJECTION, 1)
-    return r
+    return fg.Simulation(inp, binding=oracle.binding())
 
 
 def _final(sim):

@@ -69,3 +69,20 @@ def test_xyt_device_loop(gpu_lib):
     assert (cg, sg["steps"]) == (cr, sr["steps"])
     assert sg["z"] == pytest.approx(sr["z"], rel=1e-5)
     assert rel_l2(g.handle.get_field(), r.handle.get_field()) < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_xyt_upper_half_spectrum(gpu_lib, precision):
+    """The upper half of the spectrum (negative frequencies from the time
+    guard) goes through the transverse transform and KZ(kx, ky, w) with the
+    rest, as in the reference's full-array plan (Fields.jl:150-160,
+    spectral.jl:16-26): kept by default, dropped on both sides with
+    FIL_OPT_ANALYTIC_PROJECTION.  A narrow time guard makes it visible."""
+    inp = xyt_input(PLASMA=False, tguard=60.0, tmin=-100.0, tmax=100.0)
+    out = {}
+    for project in (False, True):
+        g, r = pair(inp, precision, project=project)
+        step_both(g, r, 4, 2e-3)
+        assert rel_l2(g.handle.get_field(), r.handle.get_field()) < TOL[precision]
+        out[project] = r.handle.get_field()
+    assert rel_l2(out[True], out[False]) > 100 * TOL["fp64"]
