@@ -93,6 +93,7 @@ struct fil_handle {
   // XYT transverse transform (xyfft.cu)
   void* kx2 = nullptr; void* ky2 = nullptr; void* sg1 = nullptr; void* sg2 = nullptr;
   void* twx = nullptr; void* twy = nullptr;
+  double* kcol = nullptr;   // XY/XYT: [nt] Re C(w) of KZ = C(w) + D(kt, w), FP64 (propagator_cd)
   // tensor-core Hankel path (mixed form)
   bool use_tc = false;
   void* MA1[3] = {nullptr, nullptr, nullptr};  // M1 = T diag(s): FP16 slices a0, a1, a2
@@ -335,6 +336,14 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     for (int i = 0; i < ny; ++i) ky2[i] = t->kt2[i] * t->kt2[i];
     if (t->sguard1) s1.assign(t->sguard1, t->sguard1 + nx);
     if (t->sguard2) s2.assign(t->sguard2, t->sguard2 + ny);
+    // the column term of KZ in FP64 (its phase is reduced in FP64)
+    std::vector<double> kc(nt);
+    for (int j = 0; j < nt; ++j) {
+      const cd b(t->beta[2 * j], t->beta[2 * j + 1]), d(t->dfr[2 * j], t->dfr[2 * j + 1]);
+      kc[j] = (c.kparaxial || b.real() >= 0.0) ? d.real() : (d - 2.0 * b).real();
+    }
+    CK(cudaMalloc((void**)&h->kcol, nt * sizeof(double)));
+    CK(cudaMemcpy(h->kcol, kc.data(), nt * sizeof(double), cudaMemcpyHostToDevice));
     if (upload<R>(h, &h->kx2, kx2) || upload<R>(h, &h->ky2, ky2) || upload<R>(h, &h->sg1, s1) ||
         upload<R>(h, &h->sg2, s2) || upload<R>(h, &h->twx, fft_twiddles(nx, sizeof(R) == 4)) ||
         upload<R>(h, &h->twy, fft_twiddles(ny, sizeof(R) == 4)))
@@ -713,6 +722,7 @@ template <typename R> static int enqueue_zstep_xyt(fil_handle* h, bool timed) {
   qx.wg = (const R*)h->wg;
   qx.wg_bug = h->bugcompat;
   qx.kt2_line = (const R*)h->kx2;
+  qx.kcol = h->kcol;
   qx.kt2_outer = (const R*)h->ky2;
   qx.sg_line = (const R*)h->sg1;
   qx.sg_outer = (const R*)h->sg2;
@@ -773,6 +783,7 @@ template <typename R> static int enqueue_zstep_xy(fil_handle* h, bool timed) {
   qx.pp.kmax2 = nullptr;
   qx.wg = (const R*)h->wg;
   qx.kt2_line = (const R*)h->kx2;
+  qx.kcol = h->kcol;
   qx.kt2_outer = (const R*)h->ky2;
   qx.sg_line = (const R*)h->sg1;
   qx.sg_outer = (const R*)h->sg2;
@@ -973,7 +984,8 @@ static void free_all(fil_handle* h) {
                   h->kx2, h->ky2, h->sg1, h->sg2, h->twx, h->twy,
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
                   h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err,
-                  h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt, h->park};
+                  h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt, h->park,
+                  h->kcol};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);

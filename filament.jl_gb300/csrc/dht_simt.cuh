@@ -97,6 +97,62 @@ FIL_DEV typename C2T<R>::type qz_ratio(const PropParams<R>& P, R kt2, int j) {
   return mk<R>(g * q.x, g * q.y);
 }
 
+// exp(i KZ dz) * guard on both sides of w = 0 (the XY/XYT transverse
+// passes, which also propagate the negative frequencies), with
+//   KZ = C(w) + D(kt, w),
+//   paraxial:      C = dfr,                D = -kt^2 / (2 beta)
+//   non-paraxial:  C = dfr + (c - beta),   D = -kt^2 / (sqrt(beta^2 - kt^2) + c),
+// c = beta where Re beta >= 0 and -beta otherwise: the same
+// sqrt(beta^2 - kt^2) - w/vf as the reference's Kfunc (spectral.jl:160-184),
+// but without the cancellation in sqrt + beta that the rationalised form
+// meets for beta < 0.  Re C dz (up to ~1e4 rad for w < 0, moving frame) is
+// reduced by the caller in FP64 and passed as cph = exp(i Re C dz).
+template <typename R>
+FIL_DEV typename C2T<R>::type propagator_cd(const PropParams<R>& P, R kt2, int j, R dz, typename C2T<R>::type cph) {
+  typedef typename C2T<R>::type C;
+  const C b = P.beta[j];
+  const C df = P.dfr[j];
+  C d = mk<R>(0, 0);
+  R cim = df.y;
+  if (P.kparaxial) {
+    if (b.x != (R)0 || b.y != (R)0) d = cdiv<R>(mk<R>(-kt2, 0), (R)2 * b);
+  } else {
+    const bool neg = b.x < (R)0;
+    const C c = neg ? mk<R>(-b.x, -b.y) : b;
+    const C b2 = cmul(b, b);
+    const C sq = csqrt_p<R>(mk<R>(b2.x - kt2, b2.y));
+    const C den = sq + c;
+    if (den.x != (R)0 || den.y != (R)0) d = cdiv<R>(mk<R>(-kt2, 0), den);
+    if (neg) cim -= (R)2 * b.y;
+  }
+  R g = (R)1;
+  if (P.kmax2) {
+    R km2 = P.kmax2[j];
+    if (km2 == (R)0) {
+      g = 0;
+    } else {
+      R q = kt2 / km2, q2 = q * q, q4 = q2 * q2, q5 = q4 * q, q10 = q5 * q5;
+      g = exp(-(q10 * q10));
+    }
+  }
+  if (P.wg) g *= P.wg[j];
+  const R amp = g * exp(-(cim + d.y) * dz);
+  R sn, cs;
+  sincos(d.x * dz, &sn, &cs);
+  const C r = cmul(cph, mk<R>(cs, sn));
+  return mk<R>(amp * r.x, amp * r.y);
+}
+
+// exp(i kc dz) for a column term kc given in FP64: the phase reduced to
+// [-pi, pi] in FP64 (in units of pi, exact), then sin/cos of pi x
+template <typename R> FIL_DEV typename C2T<R>::type colphase(double kc, double dz) {
+  const double t = kc * dz * 0.3183098861837907;
+  const R x = (R)(t - 2.0 * rint(0.5 * t));
+  R sn, cs;
+  sincospi(x, &sn, &cs);
+  return mk<R>(cs, sn);
+}
+
 template <typename R> struct GemmVec;
 template <> struct GemmVec<float> {
   static FIL_DEV void ld4(const float* p, float (&v)[4]) {

@@ -1,13 +1,14 @@
 // xyfft.cu -- the transverse 2-D transform of the XYT linear step:
 // E <- ifft2(exp(i KZ(kx, ky, w) dz) * guards * fft2(E)) on every frequency
-// column of the half spectrum.
+// column (both halves of the spectrum, as the reference's plan over the
+// full array; only the analytic half with the projection option).
 //
 // Reference: src/modules/linear_propagators/spectral.jl:104-156 (XY/XYT
 // propagator: PS = plan_fft over dims (1, 2), KZ from
 // sqrt(beta^2 - kx^2 - ky^2) in the moving frame) with the spectral guards of
 // Guards.jl:162-193, 218-262.
 //
-// The field is S[p][k], p = ix * Ny + iy, k < Nt/2 contiguous.  A transform
+// The field is S[p][k], p = ix * Ny + iy, k < Nt contiguous.  A transform
 // along one transverse axis is a batch of 1-D FFTs along a strided line; a
 // block takes KT consecutive frequency columns of one line group, so that
 // every row of the tile it loads is KT contiguous complex values.  Three
@@ -64,8 +65,9 @@ __global__ void __launch_bounds__(KT * (NL / 16)) k_xylines(XyParams<R> p) {
     R wgk = (R)1;
     if (p.wg) wgk = p.wg[p.wg_bug ? o : k];
     pp.wg = nullptr;
+    const C cph = colphase<R>(p.kcol[k], p.ctl ? p.ctl->dz : (double)p.dz_fixed);
     for (int l = gt; l < NL; l += T) {
-      C f = propagator<R>(pp, p.kt2_line[l] + ky2, k, dz);
+      C f = propagator_cd<R>(pp, p.kt2_line[l] + ky2, k, dz, cph);
       const R gg = p.sg_line[l] * sgo * wgk;
       s[pad16(l)] = cmul(s[pad16(l)], mk<R>(gg * f.x, gg * f.y));
     }

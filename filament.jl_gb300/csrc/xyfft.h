@@ -12,6 +12,7 @@ template <typename R> struct XyParams {
   R scale;                // applied on store
   // propagator (x pass)
   PropParams<R> pp;       // beta, dfr, kparaxial (kmax2, wg unused here)
+  const double* kcol;     // [columns] Re C(w) of KZ = C(w) + D(kt, w) in FP64 (propagator_cd)
   const R* wg;            // frequency guard [nh] or NULL
   int wg_bug;             // XYT: frequency guard indexed by iy (Guards.jl:314)
   const R* kt2_line;      // kx^2 along the line
