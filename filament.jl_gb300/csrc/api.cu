@@ -52,6 +52,7 @@ struct fil_handle {
   void* Cc = nullptr; void* Cf = nullptr; void* Cl = nullptr; void* Cr = nullptr; void* ramh = nullptr;
   void* kt2 = nullptr; void* beta = nullptr; void* dfr = nullptr; void* kmax2 = nullptr; void* wg = nullptr;
   void* rho_g = nullptr; void* kdrho_g = nullptr;
+  double* l_kzr = nullptr; void* l_kg = nullptr;   // T: the lower half's linear step (as u_kzr, u_kg)
   void* stage = nullptr;  // field staging [nrows][nt] complex
   // upper half of the spectrum (RT; the reference keeps it, rowkernels.cuh):
   // state [nrows][nh] complex, Re KZ [nrows][nh] FP64, (Im KZ, guard) [nrows][nh]
@@ -219,7 +220,7 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     if (t->guard1) g.assign(t->guard1, t->guard1 + n1);
     if (t->guardt) gtt.assign(t->guardt, t->guardt + nt);
     if (upload<R>(h, &h->g1, g) || upload<R>(h, &h->gt, gtt)) return FIL_ERR_CUDA;
-    if (h->geom == FIL_GEOM_XYT || h->geom == FIL_GEOM_XY) {
+    if (h->geom == FIL_GEOM_XYT || h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_R) {
       std::vector<double> g2(h->n2, 1.0);
       if (t->guard2) g2.assign(t->guard2, t->guard2 + h->n2);
       if (upload<R>(h, &h->g2, g2)) return FIL_ERR_CUDA;
@@ -257,7 +258,8 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     h->sf = scale(t->rnl_free);
     h->sl = scale(t->rnl_losses);
     h->sr = scale(t->rnl_raman);
-    if (h->geom == FIL_GEOM_XY && t->qz && t->rnl_cubic && (c.resp_mask & FIL_RESP_CUBIC)) h->c0 = coef(t->rnl_cubic, 0);
+    if ((h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_R) && t->qz && t->rnl_cubic && (c.resp_mask & FIL_RESP_CUBIC))
+      h->c0 = coef(t->rnl_cubic, 0);
     auto comb = [&](const double* rnl, double sch, void** dst) -> int {
       std::vector<double> v(2 * nh, 0.0);
       if (rnl && t->qz)
@@ -294,17 +296,17 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
       if (upload<R>(h, &h->wg, w)) return FIL_ERR_CUDA;
     }
   }
-  if (h->geom == FIL_GEOM_RT) {
-    // upper half of the spectrum, columns j = nh + k (FFTW order, w < 0 and
-    // the Nyquist bin): KZ(k_i, w_j) + frame (spectral.jl:78-101,160-184)
-    // and Kguard(k_i, w_j) Wguard(w_j) (Guards.jl:95-126), applied in
-    // r-space as the reference's broadcast does
+  // KZ(k_i, w_j) + frame (spectral.jl:78-101,160-184) and the spectral
+  // guard Kguard(k_i, w_j) Wguard(w_j) (Guards.jl:72-126) of columns
+  // j0 .. j0 + nh - 1 for every row, as the pointwise tables of table_prop:
+  // Re KZ in FP64, (Im KZ, guard) in the working precision
+  auto kz_tables = [&](int j0, double** kzr, void** kgp) -> int {
     std::vector<double> kr((size_t)nr * nh);
     std::vector<double> kg((size_t)nr * nh * 2);
     for (int i = 0; i < nr; ++i) {
       const double kt2 = t->kt1[i] * t->kt1[i];
       for (int k = 0; k < nh; ++k) {
-        const int j = nh + k;
+        const int j = j0 + k;
         const cd b(t->beta[2 * j], t->beta[2 * j + 1]), d(t->dfr[2 * j], t->dfr[2 * j + 1]);
         cd K;
         if (c.kparaxial) K = (b != cd(0, 0)) ? b - kt2 / (2.0 * b) : cd(0, 0);
@@ -321,9 +323,20 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
         kg[2 * ((size_t)i * nh + k) + 1] = g;
       }
     }
-    CK(cudaMalloc((void**)&h->u_kzr, kr.size() * sizeof(double)));
-    CK(cudaMemcpy(h->u_kzr, kr.data(), kr.size() * sizeof(double), cudaMemcpyHostToDevice));
-    if (upload<R>(h, &h->u_kg, kg)) return FIL_ERR_CUDA;
+    CK(cudaMalloc((void**)kzr, kr.size() * sizeof(double)));
+    CK(cudaMemcpy(*kzr, kr.data(), kr.size() * sizeof(double), cudaMemcpyHostToDevice));
+    return upload<R>(h, kgp, kg);
+  };
+  if (h->geom == FIL_GEOM_T) {
+    // no transverse transform: the whole linear step is pointwise in w
+    // (spectral.jl:54-75), the lower half's done by the row kernel
+    if (kz_tables(0, &h->l_kzr, &h->l_kg)) return FIL_ERR_CUDA;
+  }
+  if (h->geom == FIL_GEOM_RT || h->geom == FIL_GEOM_T) {
+    // upper half of the spectrum, columns j = nh + k (FFTW order, w < 0 and
+    // the Nyquist bin), propagated in r-space as the reference's broadcast
+    // does (its Hankel transform covers the first nh columns)
+    if (kz_tables(nh, &h->u_kzr, &h->u_kg)) return FIL_ERR_CUDA;
     CK(cudaMalloc(&h->SU, (size_t)nr * nh * 2 * sizeof(R)));
     CK(cudaMemset(h->SU, 0, (size_t)nr * nh * 2 * sizeof(R)));
     h->full_spec = true;
@@ -350,7 +363,7 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
       return FIL_ERR_CUDA;
   }
   // Hankel matrices M1 = T diag(s), M2 = diag(1/s) T, zero padded
-  if (h->geom == FIL_GEOM_RT) {
+  if (h->geom == FIL_GEOM_RT || h->geom == FIL_GEOM_R) {
     std::vector<double> m1((size_t)mp * mp, 0.0), m2((size_t)mp * mp, 0.0);
     for (int i = 0; i < n1; ++i)
       for (int k = 0; k < n1; ++k) {
@@ -364,7 +377,8 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
   {
     std::vector<double> w(nr);
     for (int i = 0; i < nr; ++i)
-      w[i] = (h->geom == FIL_GEOM_XYT || h->geom == FIL_GEOM_XY) ? c.dxdy : 2.0 * M_PI * (t->rdr ? t->rdr[i] : 0.0);
+      w[i] = (h->geom == FIL_GEOM_XYT || h->geom == FIL_GEOM_XY) ? c.dxdy
+             : (h->geom == FIL_GEOM_T) ? 1.0 : 2.0 * M_PI * (t->rdr ? t->rdr[i] : 0.0);
     CK(cudaMalloc(&h->pw, nr * sizeof(double)));
     CK(cudaMemcpy(h->pw, w.data(), nr * sizeof(double), cudaMemcpyHostToDevice));
   }
@@ -649,6 +663,8 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
     P.u_kg = (const C*)h->u_kg;
   }
   P.s0_park = (C*)h->park;
+  P.l_kzr = h->l_kzr;
+  P.l_kg = (const C*)h->l_kg;
   P.np_S0 = (C*)h->np_S0;
   P.np_K1 = (const C*)h->np_K1;
   P.np_KS = (const C*)h->np_KS;
@@ -853,9 +869,67 @@ template <typename R> static int enqueue_nonlinear_np(fil_handle* h, RowParams<R
   return 0;
 }
 
+// R (no time axis): pointwise nonlinear RK step (W1 <- S, the spatial
+// cubic response, cubic.jl:49-54), then the Hankel pair as matrix-vector
+// products with the propagator and, on the inverse's store, the field guard
+// (S <- W2 <- W1).
+template <typename R> static int enqueue_zstep_r(fil_handle* h, bool timed) {
+  typedef typename C2T<R>::type C;
+  const C* src = (const C*)h->S;
+  if (timed) CK(cudaEventRecord(h->ev[1], h->st));
+  if (h->cfg.nonlinearity) {
+    XyNlParams<R> q;
+    std::memset(&q, 0, sizeof q);
+    q.n = h->nrows;
+    q.ny = 1;
+    double a[4][4], b[4], cc[4];
+    rk_tableau(h->cfg.alg, &q.ns, a, b, cc);
+    for (int i = 0; i < 4; ++i) {
+      q.b[i] = (R)b[i];
+      for (int j = 0; j < 4; ++j) q.a[i][j] = (R)a[i][j];
+    }
+    q.c0 = mk<R>((R)h->c0.real(), (R)h->c0.imag());
+    q.g1 = (const R*)h->g1;
+    q.g2 = (const R*)h->g2;
+    q.ctl = h->ctl;
+    CK(launch_xy_nonlinear<R>(src, (C*)h->W1, q, h->st));
+    src = (const C*)h->W1;
+  }
+  if (timed) CK(cudaEventRecord(h->ev[5], h->st));
+  if (timed) CK(cudaEventRecord(h->ev[2], h->st));
+  PropParams<R> pp = prop_params<R>(h);
+  CK(launch_dht_vec<R>((const R*)h->M1, src, (C*)h->W2, h->nrows, h->mpad, pp, nullptr, h->ctl, 1, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[3], h->st));
+  CK(launch_dht_vec<R>((const R*)h->M2, (const C*)h->W2, (C*)h->S, h->nrows, h->mpad, pp, (const R*)h->g1, h->ctl,
+                       2, h->st));
+  if (timed) CK(cudaEventRecord(h->ev[4], h->st));
+  return 0;
+}
+
+// T: the row kernel does the whole step in place, its linear part pointwise
+// in w on both halves of the spectrum (l_kzr, u_kzr).
+template <typename R> static int enqueue_zstep_t(fil_handle* h, bool timed) {
+  typedef typename C2T<R>::type C;
+  RowParams<R> P = row_params<R>(h);
+  P.S_in = (const C*)h->S;
+  P.S_out = (C*)h->S;
+  if (timed) CK(cudaEventRecord(h->ev[1], h->st));
+  CK(enqueue_surrogate<R>(h, P));
+  if (timed) CK(cudaEventRecord(h->ev[5], h->st));
+  CK(launch_rowstep<R>(P, h->nt, h->cfg.plasma ? h->nc : 0, 0, h->st));
+  if (timed) {
+    CK(cudaEventRecord(h->ev[2], h->st));
+    CK(cudaEventRecord(h->ev[3], h->st));
+    CK(cudaEventRecord(h->ev[4], h->st));
+  }
+  return 0;
+}
+
 template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
   if (h->geom == FIL_GEOM_XYT) return enqueue_zstep_xyt<R>(h, timed);
   if (h->geom == FIL_GEOM_XY) return enqueue_zstep_xy<R>(h, timed);
+  if (h->geom == FIL_GEOM_R) return enqueue_zstep_r<R>(h, timed);
+  if (h->geom == FIL_GEOM_T) return enqueue_zstep_t<R>(h, timed);
   RowParams<R> P = row_params<R>(h);
   P.S_in = (const typename C2T<R>::type*)h->S;
   P.S_out = (typename C2T<R>::type*)h->W1;
@@ -912,7 +986,7 @@ template <typename R> static int enqueue_zstep(fil_handle* h, bool timed) {
 // power[t] = sum_row w_row |E|^2 (the intensities pass through the staging
 // buffer)
 template <typename R> static int enqueue_reduce(fil_handle* h, double* power, int check_done) {
-  if (h->geom == FIL_GEOM_XY) {   // power = sum F dxdy, formed on the host (fil_analyze)
+  if (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_R) {   // power = sum F w, formed on the host (fil_analyze)
     CK(launch_xy_reduce<R>((const typename C2T<R>::type*)h->S, h->fluence, h->ctl, h->nrows, check_done, h->st));
     return 0;
   }
@@ -985,7 +1059,7 @@ static void free_all(fil_handle* h) {
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
                   h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err,
                   h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt, h->park,
-                  h->kcol};
+                  h->kcol, h->l_kzr, h->l_kg};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -1035,7 +1109,7 @@ template <typename R> static int set_field_t(fil_handle* h, const void* E, int d
   typedef typename C2T<R>::type C;
   std::vector<R> rows;
   to_rows<R>(h, E, dtype, layout, rows);
-  if (h->geom == FIL_GEOM_XY) {   // no time axis: the state is the field
+  if (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_R) {   // no time axis: the state is the field
     CK(cudaMemcpyAsync(h->S, rows.data(), rows.size() * sizeof(R), cudaMemcpyHostToDevice, h->st));
     DevCtl c;
     std::memset(&c, 0, sizeof c);
@@ -1068,7 +1142,7 @@ template <typename R> static int set_field_t(fil_handle* h, const void* E, int d
 
 template <typename R> static int get_field_t(fil_handle* h, void* E, int dtype, int layout) {
   typedef typename C2T<R>::type C;
-  if (h->geom == FIL_GEOM_XY) {
+  if (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_R) {
     std::vector<R> rows((size_t)h->nrows * 2);
     CK(cudaMemcpyAsync(rows.data(), h->S, rows.size() * sizeof(R), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -1102,8 +1176,11 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (!cfg || !t || !out) return fail(h, FIL_ERR_ARG, "null argument");
   *out = nullptr;
   if (cfg->abi_version != FIL_ABI_VERSION) return fail(h, FIL_ERR_ARG, "ABI version mismatch");
-  if (cfg->geometry != FIL_GEOM_RT && cfg->geometry != FIL_GEOM_XYT && cfg->geometry != FIL_GEOM_XY)
-    return fail(h, FIL_ERR_UNSUPPORTED, "this build runs the RT, XY and XYT geometries on the GPU");
+  if (cfg->geometry < FIL_GEOM_R || cfg->geometry > FIL_GEOM_XYT) return fail(h, FIL_ERR_ARG, "unknown geometry");
+  if (cfg->geometry == FIL_GEOM_R && (cfg->nt != 1 || cfg->n2 != 1 || cfg->plasma))
+    return fail(h, FIL_ERR_ARG, "R: nt and n2 must be 1 and the plasma off");
+  if (cfg->geometry == FIL_GEOM_T && (cfg->n1 != 1 || cfg->n2 != 1))
+    return fail(h, FIL_ERR_ARG, "T: n1 and n2 must be 1");
   if (cfg->geometry == FIL_GEOM_XY &&
       (!is_pow2(cfg->n1) || !is_pow2(cfg->n2) || cfg->n1 < 64 || cfg->n1 > 4096 || cfg->n2 < 64 || cfg->n2 > 4096))
     return fail(h, FIL_ERR_UNSUPPORTED, "XY: nx and ny must be powers of two in [64, 4096]");
@@ -1112,7 +1189,8 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (cfg->geometry == FIL_GEOM_XYT &&
       (!is_pow2(cfg->n1) || !is_pow2(cfg->n2) || cfg->n1 < 64 || cfg->n1 > 1024 || cfg->n2 < 64 || cfg->n2 > 1024))
     return fail(h, FIL_ERR_UNSUPPORTED, "XYT: nx and ny must be powers of two in [64, 1024]");
-  if (cfg->geometry != FIL_GEOM_XY && (!is_pow2(cfg->nt) || cfg->nt < 512 || cfg->nt > 4096))
+  if (cfg->geometry != FIL_GEOM_XY && cfg->geometry != FIL_GEOM_R &&
+      (!is_pow2(cfg->nt) || cfg->nt < 512 || cfg->nt > 4096))
     return fail(h, FIL_ERR_UNSUPPORTED, "nt must be a power of two in [512, 4096]");
   if (cfg->n1 < 1 || cfg->n1 > 65536) return fail(h, FIL_ERR_ARG, "bad n1");
   if (cfg->nonlinearity && !cfg->qparaxial && cfg->geometry != FIL_GEOM_RT)
@@ -1124,7 +1202,8 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (cfg->plasma && (cfg->rate_n < 2 || cfg->rate_n > FIL_MAXRATE))
     return fail(h, FIL_ERR_ARG, "rate_n must be in [2, 32]");
   if (!t->kt1 || !t->beta || !t->dfr) return fail(h, FIL_ERR_ARG, "missing propagator tables");
-  if (cfg->geometry == FIL_GEOM_RT && (!t->dht || !t->dht_s)) return fail(h, FIL_ERR_ARG, "missing DHT tables");
+  if ((cfg->geometry == FIL_GEOM_RT || cfg->geometry == FIL_GEOM_R) && (!t->dht || !t->dht_s))
+    return fail(h, FIL_ERR_ARG, "missing DHT tables");
   if ((cfg->geometry == FIL_GEOM_XYT || cfg->geometry == FIL_GEOM_XY) && !t->kt2)
     return fail(h, FIL_ERR_ARG, "missing ky table");
   if (cfg->nonlinearity && !t->qz) return fail(h, FIL_ERR_ARG, "missing QZ table");
@@ -1139,7 +1218,8 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   h->n1 = cfg->n1;
   h->n2 = cfg->n2;
   h->nt = cfg->nt;
-  h->nh = cfg->geometry == FIL_GEOM_XY ? 1 : cfg->nt / 2;   // XY: the field itself, one column
+  // XY, R: the field itself, one column
+  h->nh = (cfg->geometry == FIL_GEOM_XY || cfg->geometry == FIL_GEOM_R) ? 1 : cfg->nt / 2;
   h->ld = cfg->geometry == FIL_GEOM_XYT ? cfg->nt : h->nh;
   h->nrows = cfg->n1 * cfg->n2;
   h->mpad = (h->nrows + 127) / 128 * 128;
@@ -1175,7 +1255,7 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   CKC(cudaMemset(h->W1, 0, sz));
   CKC(cudaMemset(h->W2, 0, sz));
   CKC(cudaMalloc(&h->stage, (size_t)h->nrows * h->nt * es));
-  if (h->geom != FIL_GEOM_XY) {
+  if (h->geom != FIL_GEOM_XY && h->geom != FIL_GEOM_R) {
     CKC(cudaMalloc(&h->park, (size_t)h->nrows * h->ld * es));
     CKC(cudaMemset(h->park, 0, (size_t)h->nrows * h->ld * es));
   }
@@ -1457,7 +1537,7 @@ int fil_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power, do
   rc = check_tc(h);
   if (rc) return rc;
   const DevCtl& c = *h->ctl_host;
-  if (h->geom == FIL_GEOM_XY) {   // FieldAnalyzers.jl:240-255: P = sum |E|^2 dx dy
+  if (h->geom == FIL_GEOM_XY || h->geom == FIL_GEOM_R) {   // FieldAnalyzers.jl:240-255: P = sum |E|^2 dA
     double sp = 0;
     for (int i = 0; i < nr; ++i) sp += F[i] * w[i];
     P[0] = sp;

@@ -46,6 +46,11 @@ cudaError_t launch_slice_prop(const float* W, const float2* kz, const float* gd,
 cudaError_t launch_slice_mul(const float* W, const float2* f, void* const (&s)[3], float* qb, int nh, int K,
                              const DevCtl* ctl, cudaStream_t st);
 cudaError_t launch_control(DevCtl* c, const double* fluence, const double* w, int nrows, cudaStream_t st);
+// R geometry: one Hankel matrix-vector product (dht_vec.cu); mode 1 times
+// the propagator, mode 2 times the field guard g_row
+template <typename R>
+cudaError_t launch_dht_vec(const R* M, const typename C2T<R>::type* in, typename C2T<R>::type* out, int n, int ldm,
+                           const PropParams<R>& pp, const R* g_row, DevCtl* ctl, int mode, cudaStream_t st);
 cudaError_t launch_flush(void* buf, size_t bytes, cudaStream_t st);
 cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st);
 cudaError_t launch_batch_live(DevCtl* const* c, int n, int* live, cudaStream_t st);

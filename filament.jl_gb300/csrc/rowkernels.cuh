@@ -108,6 +108,11 @@ template <typename R> struct RowParams {
   // [row][N/2] (row stride ld): the guarded spectrum S0 of a step parked
   // across the plasma solve (load_time_row_split)
   C* s0_park;
+  // T geometry (no transverse transform): the lower half's linear step
+  // exp(i KZ dz) Wguard applied by the row kernel on its output, tables as
+  // u_kzr, u_kg; the kernel then marks the field guard pending
+  const double* l_kzr;
+  const C* l_kg;
   // non-paraxial prefactor (k_rowstep modes 2, 3; k_np_combine): [row][N/2]
   // complex, row stride ld; rho_g, kdrho_g hold the step's density rows
   C* np_S0;                     // t -> w transform of the guarded field
@@ -725,14 +730,19 @@ FIL_DEV void write_out(const RowParams<R>& P, int row, int k, typename C2T<R>::t
 // and reduced there to [-1, 1] (exact: 2 rint(t/2) is representable), and
 // sin/cos of pi x need no further argument reduction.
 template <typename R>
-FIL_DEV typename C2T<R>::type upper_prop(const RowParams<R>& P, size_t idx, typename C2T<R>::type u, double dzd) {
-  const double t = __ldg(&P.u_kzr[idx]) * dzd * 0.3183098861837907;   // phase / pi
+FIL_DEV typename C2T<R>::type table_prop(const double* kzr, const typename C2T<R>::type* kgt, size_t idx,
+                                         typename C2T<R>::type u, double dzd) {
+  const double t = __ldg(&kzr[idx]) * dzd * 0.3183098861837907;   // phase / pi
   const R x = (R)(t - 2.0 * rint(0.5 * t));
-  const typename C2T<R>::type kg = P.u_kg[idx];
+  const typename C2T<R>::type kg = kgt[idx];
   const R amp = kg.y * exp(-kg.x * (R)dzd);
   R sn, cs;
   sincospi(x, &sn, &cs);
   return cmul(u, mk<R>(amp * cs, amp * sn));
+}
+template <typename R>
+FIL_DEV typename C2T<R>::type upper_prop(const RowParams<R>& P, size_t idx, typename C2T<R>::type u, double dzd) {
+  return table_prop<R>(P.u_kzr, P.u_kg, idx, u, dzd);
 }
 
 // ---------------------------------------------------------------------------
@@ -887,7 +897,12 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
     }
   }
 #pragma unroll
-  for (int m = 0; m < EW; ++m) write_out<R>(P, row, tid + m * T, S0[m] + dz * acc[m]);
+  for (int m = 0; m < EW; ++m) {
+    const int k = tid + m * T;
+    C v = S0[m] + dz * acc[m];
+    if (P.l_kzr) v = table_prop<R>(P.l_kzr, P.l_kg, (size_t)row * P.ld + k, v, (double)ctl->dz);   // T geometry
+    write_out<R>(P, row, k, v);
+  }
   if (uo && P.u_kzr) {
     // linear step of the upper half in r-space (RT; the lower half's
     // follows in the Hankel transforms; XYT transforms both halves)
@@ -899,6 +914,9 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
       uo[k] = upper_prop<R>(P, base + k, uo[k], dzd);
     }
   }
+  // T geometry: the step's linear part is done; the field guard follows at
+  // the next load (one block)
+  if (P.l_kzr && tid == 0) ctl->guard_pending = 1;
 }
 
 // One RK stage of a non-paraxial step (QPARAXIAL = false).  func! then

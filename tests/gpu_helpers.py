@@ -17,6 +17,25 @@ def rt_input(**kw):
     return fg.prepare(FIL_DECK, **base)
 
 
+def t_input(**kw):
+    """A T-geometry deck: the RT filament deck's pulse and air on one time
+    row (the beam factor taken at r = 0)."""
+    import filament_gb as fg
+    from conftest import DECKS
+    base = dict(Nt=1024, tmin=-100.0, tmax=100.0, zmax=0.02)
+    base.update(kw)
+    return fg.prepare(os.path.join(DECKS, "nonlinear_T", "input.py"), **base)
+
+
+def r_input(**kw):
+    """An R-geometry deck: a Gaussian beam with Kerr self-focusing."""
+    import filament_gb as fg
+    from conftest import DECKS
+    base = dict(Nr=256, rmax=4.0, zmax=0.02)
+    base.update(kw)
+    return fg.prepare(os.path.join(DECKS, "nonlinear_R", "input.py"), **base)
+
+
 def xyt_input(**kw):
     """The XYT multifilamentation deck on a small grid (64 x 64 x 512)."""
     import filament_gb as fg
