@@ -258,6 +258,32 @@ def surrogate_train(seed=1, iters=3000):
     return net, info
 
 
+def profile_from(form, z0, steps, train_iters):
+    """`steps` steps of the workload in the given form from z0 (reached in
+    graph mode first, not profiled), one at a time between cuProfilerStart
+    and cuProfilerStop: ncu --profile-from-start off sees those launches only."""
+    import filament_gb as fg
+    from filament_gb import _abi
+    net = surrogate_train(iters=train_iters)[0] if form == "mixed_surrogate" else None
+    inp = _prepare()
+    sim = fg.Simulation(inp, precision="fp64" if form == "fp64" else "mixed")
+    h = sim.handle
+    if net is not None:
+        net.arm(h, every=SURR_EVERY, tol=SURR_TOL)
+    z = 0.0
+    if z0 > 0:
+        code, st = h.run(0.0, z0, 10 ** 9)
+        z = st["z"]
+    h.set_option(_abi.OPT_TIMING, 1)
+    _profiler(True)
+    code, st = h.run(z, STABLE_Z, steps)
+    _profiler(False)
+    kt = h.kernel_times(7)
+    sim.close()
+    return {"profile": form, "z_start": z, "timed_steps": int(kt[5]), "ms_per_step": kt[4], "row_ms": kt[0],
+            "dht_fwd_ms": kt[1], "dht_inv_ms": kt[2]}
+
+
 def e2e_device_loop(net, zend):
     """The same metric end to end through the public API with the
     surrogate armed, over the whole run: upload of the host field, the
@@ -580,6 +606,11 @@ def main():
     ap.add_argument("--sweep-only", action="store_true", help="only the batched sweep (one JSON line)")
     ap.add_argument("--profile", action="store_true",
                     help="only the headline form's timed steps, between cuProfilerStart/Stop (for ncu)")
+    ap.add_argument("--profile-form", default="mixed_surrogate", choices=["mixed_surrogate", "mixed", "fp64"],
+                    help="--profile: the form to profile")
+    ap.add_argument("--profile-z", type=float, default=0.0,
+                    help="--profile: advance (graph mode, not profiled) to this z, then profile --steps "
+                         "steps one at a time")
     args = ap.parse_args()
     rank, local_rank, world = _env_rank()
     if world > 1:
@@ -615,6 +646,9 @@ def main():
         r = time_sweep(steps=args.sweep_steps, rank=rank, world=world, dist=dist)
         if rank == 0:
             print(json.dumps({"sweep": r}))
+        return
+    if args.profile and (args.profile_form != "mixed_surrogate" or args.profile_z > 0):
+        print(json.dumps(profile_from(args.profile_form, args.profile_z, args.steps, args.train_iters)))
         return
     # the surrogate is trained before any timed region
     net, train_info = surrogate_train(iters=args.train_iters)

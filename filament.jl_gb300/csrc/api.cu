@@ -53,6 +53,7 @@ struct fil_handle {
   void* kt2 = nullptr; void* beta = nullptr; void* dfr = nullptr; void* kmax2 = nullptr; void* wg = nullptr;
   void* rho_g = nullptr; void* kdrho_g = nullptr;
   double* l_kzr = nullptr; void* l_kg = nullptr;   // T: the lower half's linear step (as u_kzr, u_kg)
+  void* spec_g = nullptr;   // plasma scan iterates of species 2, 3 (more than two species)
   void* stage = nullptr;  // field staging [nrows][nt] complex
   // upper half of the spectrum (RT; the reference keeps it, rowkernels.cuh):
   // state [nrows][nh] complex, Re KZ [nrows][nh] FP64, (Im KZ, guard) [nrows][nh]
@@ -383,6 +384,11 @@ static int create_tables(fil_handle* h, const fil_tables* t) {
     CK(cudaMemcpy(h->pw, w.data(), nr * sizeof(double), cudaMemcpyHostToDevice));
   }
   // plasma
+  if (c.plasma && c.plasma_ncomp > 2) {
+    const size_t bytes = (size_t)nr * (c.plasma_ncomp - 2) * nt * sizeof(R);
+    CK(cudaMalloc(&h->spec_g, bytes));
+    CK(cudaMemset(h->spec_g, 0, bytes));
+  }
   if (c.plasma) {
     PlasmaParams<double>& P = h->pp;
     std::memset(&P, 0, sizeof P);
@@ -664,6 +670,7 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
   }
   P.s0_park = (C*)h->park;
   P.l_kzr = h->l_kzr;
+  P.spec_g = (R*)h->spec_g;
   P.l_kg = (const C*)h->l_kg;
   P.np_S0 = (C*)h->np_S0;
   P.np_K1 = (const C*)h->np_K1;
@@ -1059,7 +1066,7 @@ static void free_all(fil_handle* h) {
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
                   h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err,
                   h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt, h->park,
-                  h->kcol, h->l_kzr, h->l_kg};
+                  h->kcol, h->l_kzr, h->l_kg, h->spec_g};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -1198,7 +1205,10 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (cfg->nonlinearity && (cfg->resp_mask & FIL_RESP_RAMAN) && !t->raman_h)
     return fail(h, FIL_ERR_ARG, "missing Raman response table");
   if (cfg->plasma && (cfg->plasma_ncomp < 1 || cfg->plasma_ncomp > FIL_MAXCOMP))
-    return fail(h, FIL_ERR_UNSUPPORTED, "plasma_ncomp must be 1 or 2");
+    return fail(h, FIL_ERR_ARG, "plasma_ncomp must be 1 .. 4");
+  if (cfg->plasma && cfg->plasma_ncomp > 2 && cfg->nonlinearity &&
+      ((cfg->resp_mask & FIL_RESP_RAMAN) || !cfg->qparaxial))
+    return fail(h, FIL_ERR_UNSUPPORTED, "more than two species with the Raman channel or QPARAXIAL=false");
   if (cfg->plasma && (cfg->rate_n < 2 || cfg->rate_n > FIL_MAXRATE))
     return fail(h, FIL_ERR_ARG, "rate_n must be in [2, 32]");
   if (!t->kt1 || !t->beta || !t->dfr) return fail(h, FIL_ERR_ARG, "missing propagator tables");

@@ -26,7 +26,7 @@
 #pragma once
 #include "common.cuh"
 
-#define FIL_MAXCOMP 2
+#define FIL_MAXCOMP 4
 #define FIL_MAXRATE 32
 
 // Scalars in the working precision R: the FP32 kernels then issue no FP64

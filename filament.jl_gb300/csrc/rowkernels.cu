@@ -91,7 +91,9 @@ static cudaError_t launch_rowstep_n(const RowParams<R>& P, int nc, int mode, cud
   const bool ram = P.has_raman != 0;
   if (nc == 0) return ram ? launch_rowstep_t<R, N, 0, true>(P, mode, st) : launch_rowstep_t<R, N, 0, false>(P, mode, st);
   if (nc == 1) return ram ? launch_rowstep_t<R, N, 1, true>(P, mode, st) : launch_rowstep_t<R, N, 1, false>(P, mode, st);
-  return ram ? launch_rowstep_t<R, N, 2, true>(P, mode, st) : launch_rowstep_t<R, N, 2, false>(P, mode, st);
+  if (nc == 2) return ram ? launch_rowstep_t<R, N, 2, true>(P, mode, st) : launch_rowstep_t<R, N, 2, false>(P, mode, st);
+  if (ram) return cudaErrorInvalidValue;   // refused at fil_create
+  return nc == 3 ? launch_rowstep_t<R, N, 3, false>(P, mode, st) : launch_rowstep_t<R, N, 4, false>(P, mode, st);
 }
 
 template <typename R>
@@ -110,7 +112,8 @@ static cudaError_t launch_rowstage_n(const RowParams<R>& P, int nc, cudaStream_t
   const bool ram = P.has_raman != 0;
   if (nc == 0) return ram ? launch_rowstage_t<R, N, 0, true>(P, st) : launch_rowstage_t<R, N, 0, false>(P, st);
   if (nc == 1) return ram ? launch_rowstage_t<R, N, 1, true>(P, st) : launch_rowstage_t<R, N, 1, false>(P, st);
-  return ram ? launch_rowstage_t<R, N, 2, true>(P, st) : launch_rowstage_t<R, N, 2, false>(P, st);
+  if (nc == 2) return ram ? launch_rowstage_t<R, N, 2, true>(P, st) : launch_rowstage_t<R, N, 2, false>(P, st);
+  return cudaErrorInvalidValue;   // refused at fil_create
 }
 
 template <typename R>

@@ -113,6 +113,8 @@ template <typename R> struct RowParams {
   // u_kzr, u_kg; the kernel then marks the field guard pending
   const double* l_kzr;
   const C* l_kg;
+  // [row][NC - 2][N]: the iterates of species 2, 3 in the plasma scan (NC > 2)
+  R* spec_g;
   // non-paraxial prefactor (k_rowstep modes 2, 3; k_np_combine): [row][N/2]
   // complex, row stride ld; rho_g, kdrho_g hold the step's density rows
   C* np_S0;                     // t -> w transform of the guarded field
@@ -220,8 +222,16 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
   const int j0 = tid * 16;
   const bool ereal = pp.ereal;
   const bool cached = (NC == 1) && pp.powerlaw;
-  // iterate storage: species c at ub[c*NP + pad16(j)]; rho itself for NC = 1
+  // iterate storage: species c at ub[c*NP + pad16(j)] (Y holds two rows of
+  // reals); rho itself for NC = 1; species 2 and 3 of NC > 2 in the row's
+  // slice of spec_g (only the thread that owns j reads and writes it)
   R* ub = (NC == 1) ? rho : Y;
+  auto UB = [&](int c, int j) -> R& {
+    if constexpr (NC > 2) {
+      if (c >= 2) return P.spec_g[((size_t)blockIdx.x * (NC - 2) + (c - 2)) * N + j];
+    }
+    return ub[c * NP + pad16(j)];
+  };
   R* Wp = Y;          // cached W(I_j)      (NC = 1, power law)
   R* Wm = Y + NP;     // cached W(I_{j+1/2})
   R u0[NC];
@@ -382,7 +392,7 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
     for (int q = 0; q < 16; ++q) {
       int j = j0 + q;
 #pragma unroll
-      for (int c = 0; c < NC; ++c) ub[c * NP + pad16(j)] = u[c];
+      for (int c = 0; c < NC; ++c) UB(c, j) = u[c];
       if (j < N - 1) {
         point_data(j, W, ava, S0);
         Aff<R, NC> M = step_map<R, NC>(pp, uz, W, ava, false);
@@ -453,7 +463,7 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
           if (j >= N - 1) break;
           R ul[NC];
 #pragma unroll
-          for (int c = 0; c < NC; ++c) ul[c] = ub[c * NP + pad16(j)];
+          for (int c = 0; c < NC; ++c) ul[c] = UB(c, j);
           point_data(j, W, ava, S0);
           Aff<R, NC> M = step_map<R, NC>(pp, ul, W, ava, true);
           G = aff_compose<R, NC>(M, G);
@@ -466,10 +476,10 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
           R ul[NC];
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
-            ul[c] = ub[c * NP + pad16(j)];
+            ul[c] = UB(c, j);
             dmax = max(dmax, fabs(u[c] - ul[c]));
             umax = max(umax, fabs(u[c]));
-            ub[c * NP + pad16(j)] = u[c];
+            UB(c, j) = u[c];
           }
           if (j < N - 1) {
             point_data(j, W, ava, S0);
@@ -494,7 +504,7 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
     int j = j0 + q;
     R sm = 0;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) sm += ub[c * NP + pad16(j)];
+    for (int c = 0; c < NC; ++c) sm += UB(c, j);
     if (NC > 1) rho[pad16(j)] = sm;
     rmax = max(rmax, sm);
   }

@@ -21,6 +21,17 @@ cudaError_t launch_rowstep_t(const RowParams<R>& P, int mode, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// three and four ionising species (paraxial prefactor, no Raman channel)
+#define FIL_ROWSTEP_INST_NC34(R)                                                                    \
+  template cudaError_t launch_rowstep_t<R, 512, 3, false>(const RowParams<R>&, int, cudaStream_t);  \
+  template cudaError_t launch_rowstep_t<R, 512, 4, false>(const RowParams<R>&, int, cudaStream_t);  \
+  template cudaError_t launch_rowstep_t<R, 1024, 3, false>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 1024, 4, false>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 2048, 3, false>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 2048, 4, false>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 4096, 3, false>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 4096, 4, false>(const RowParams<R>&, int, cudaStream_t);
+
 #define FIL_ROWSTEP_INST(R, RAM)                                                                   \
   template cudaError_t launch_rowstep_t<R, 512, 0, RAM>(const RowParams<R>&, int, cudaStream_t);  \
   template cudaError_t launch_rowstep_t<R, 512, 1, RAM>(const RowParams<R>&, int, cudaStream_t);  \

@@ -55,6 +55,20 @@ def two_species_rates():
     return [n2, o2]
 
 
+def many_species_rates(n):
+    """n ionising species (3 or 4): N2 and O2 as two_species_rates, then an
+    argon-like (K = 10.5) and a water-like (K = 7) trace species, power laws
+    of the form of the reference's .tf tables."""
+    from filament_gb.plasma import power_law_rate
+    comps = two_species_rates()
+    comps[0]["fraction"] = 0.78
+    comps.append({"fraction": 0.01, "ionization_energy": 15.76,
+                  "ionization_rate": power_law_rate(10.5, 1e18, 2.0e10)})
+    comps.append({"fraction": 0.01, "ionization_energy": 12.62,
+                  "ionization_rate": power_law_rate(7.0, 1e18, 3.0e12)})
+    return comps[:n]
+
+
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 

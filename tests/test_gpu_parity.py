@@ -8,8 +8,8 @@ bound for whole runs is 1e-4 relative L2 field error and 1e-3 fluence error.
 import numpy as np
 import pytest
 
-from gpu_helpers import (pair, reference_air_components, rel_l2, rt_input, saturating_rate, step_both,
-                         two_species_rates)
+from gpu_helpers import (many_species_rates, pair, reference_air_components, rel_l2, rt_input, saturating_rate,
+                         step_both, two_species_rates)
 
 pytestmark = pytest.mark.gpu
 
@@ -314,3 +314,22 @@ def test_nonparaxial_device_loop(gpu_lib, precision):
     code_r, st_r = r.handle.run(0.0, inp["zmax"], 10 ** 6)
     assert code_g == code_r == 1 and st_g["steps"] == st_r["steps"]
     assert rel_l2(g.handle.get_field(), r.handle.get_field()) < 10 * TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("species", [3, 4])
+def test_more_species(gpu_lib, precision, species):
+    """Three and four ionising species (photoionization_avalanche.jl:23-27
+    loops over any number): density, loss term and full RK4 steps against
+    the oracle."""
+    inp = rt_input(PPcr=150.0, ALG="RK4")
+    inp["p_model"][1]["components"] = many_species_rates(species)
+    g, r = pair(inp, precision, store_plasma=True)
+    assert g.problem.config.plasma_ncomp == species
+    rho_g, rho_r = g.handle.get_plasma(0), r.handle.get_plasma(0)
+    assert np.max(rho_r) > 1e-6
+    tol = TOL[precision]
+    assert rel_l2(rho_g, rho_r) < tol
+    assert rel_l2(g.handle.get_plasma(1), r.handle.get_plasma(1)) < tol
+    step_both(g, r, 3, 1e-3)
+    assert rel_l2(g.handle.get_field(), r.handle.get_field()) < tol
