@@ -1,8 +1,8 @@
 // nn_tc.cu -- inference kernels of the learned plasma surrogate
 // (surrogate.cuh) with channel-last activations [row][t][64]:
 //
-//   layer 0 (3 -> 64)   k_nn_l0_cl   CUDA cores, 1728 MAC per point
-//   layer 1 (64 -> 64)  k_nn_conv_tc tcgen05, 36864 MAC per point
+//   layer 0 (3 -> 64)   CUDA cores, 1728 MAC per point, inside layer 1's kernel
+//   layer 1 (64 -> 64)  k_nn_conv_tc<false, true> tcgen05, 36864 MAC per point
 //   layer 2 (64 -> 64)  k_nn_conv_tc
 //   layer 3 (64 -> 1)   k_nn_l3_cl   CUDA cores, 576 MAC per point
 //
@@ -25,6 +25,16 @@
 // 32w .. 32w+31), warp 4 TMA producer, warp 5 MMA issuer.  Every mbarrier
 // wait is bounded and gives up once another role failed; a failure sets
 // *err and the block releases its tensor memory after its MMAs completed.
+//
+// Layer 1 with layer 0 fused (L0): its input tile is not loaded but computed.
+// Eight more warps (6-13) form the 136-row halo tile of layer-0 activations
+// of each tile from the three input channels, tanh(b0 + sum_ci sum_k
+// w0[ci][k][co] x[ci][t + k - 4]) rounded to BF16 (zero for rows outside
+// [0, T), the "same" padding of layer 1), and write it into the stage in
+// the layout the 128-byte swizzle gives a TMA copy (16-byte chunk c of row r
+// at chunk c ^ (r mod 8) of the 1024-byte aligned stage); each of them fences
+// its writes for the tensor core's proxy and arrives on the stage's full
+// barrier (count 256).  Layer 0's activations never reach HBM.
 #include <algorithm>
 #include <cstdint>
 
@@ -57,6 +67,8 @@
 static_assert(NT_SLOT + 4 <= NT_BAR_BYTES, "barrier block overflows its reserved bytes");
 static_assert(NT_A_STRIDE % 1024 == 0 && NT_A_STRIDE >= NT_A_BYTES, "stage pitch");
 #define NT_THREADS 192
+#define NT_L0_WARPS 8                  // layer-0 warps of the fused kernel
+#define NT_THREADS_L0 (NT_THREADS + 32 * NT_L0_WARPS)
 #define NT_WAIT_LIMIT (1u << 26)
 
 static __device__ __forceinline__ bool nt_wait(uint32_t bar, uint32_t parity, volatile int* fail) {
@@ -91,6 +103,9 @@ static __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
 
 struct NtParams {
   const float* bias;       // [64]
+  const __nv_bfloat16* x0; // L0: network inputs [rows][3][T]
+  const __nv_bfloat16* w0; // L0: layer-0 weights [ci][k][co]
+  const float* b0;         // L0: layer-0 bias [64]
   __nv_bfloat16* out;      // [rows][T][64] (layer 1)
   const __nv_bfloat16* w3; // layer 3 weights [ci][k] (FINAL)
   float* part;             // [rows][9][T] layer-3 partial sums (FINAL)
@@ -104,12 +119,16 @@ struct NtParams {
 // storing the activations: P_k[t] = sum_ci w3[ci][k] y[t][ci] for the nine
 // taps k (the BF16-rounded activations, as stored between layers), so that
 // out[t] = b3 + sum_k P_k[t + k - 4] (nn_out_at).
-template <bool FINAL>
-__global__ void __launch_bounds__(NT_THREADS, 1)
+template <bool FINAL, bool L0>
+__global__ void __launch_bounds__(L0 ? NT_THREADS_L0 : NT_THREADS, 1)
     k_nn_conv_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap tw, NtParams p) {
+  static_assert(!(FINAL && L0), "layer 0 is fused into layer 1 only");
   extern __shared__ __align__(1024) uint8_t nt_smem[];
   __shared__ volatile int s_fail;
   __shared__ __align__(16) float s_bias[64];
+  // L0: layer-0 weights [ci * 9 + k][co] and bias
+  __shared__ __align__(16) float s_w0[L0 ? NN_IN * NN_K * 64 : 4];
+  __shared__ __align__(16) float s_b0[L0 ? 64 : 4];
   // layer-3 weights as tap pairs: s_w3[(kp * 64 + ci) * 2 + u] = w3[ci][2 kp + u]
   // (kp < 5; the tenth tap is zero)
   __shared__ __align__(16) float s_w3[FINAL ? 5 * 64 * 2 : 4];
@@ -131,6 +150,10 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
 
   if (tid == 0) s_fail = 0;
   if (tid < 64) s_bias[tid] = p.bias[tid];
+  if (L0) {
+    for (int i = tid; i < NN_IN * NN_K * 64; i += NT_THREADS_L0) s_w0[i] = __bfloat162float(p.w0[i]);
+    if (tid < 64) s_b0[tid] = p.b0[tid];
+  }
   if (FINAL)
     for (int i = tid; i < 5 * 64 * 2; i += NT_THREADS) {
       const int u = i & 1, ci = (i >> 1) & 63, k = 2 * (i >> 7) + u;
@@ -139,7 +162,7 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
   if (warp == 0) tc::tmem_alloc(tmem_slot, 128);
   if (tid == 0) {
     for (int s = 0; s < NT_STAGES; ++s) {
-      tc::mbar_init(full_bar(s), 1);
+      tc::mbar_init(full_bar(s), L0 ? 32 * NT_L0_WARPS : 1);
       tc::mbar_init(empty_bar(s), 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -162,7 +185,7 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
       tc::mbar_expect_tx(wbar, NN_K * NT_W_BYTES);
       for (int k = 0; k < NN_K; ++k) tc::tma_load_2d(sbase + NT_W_OFF + k * NT_W_BYTES, &tw, 0, 64 * k, wbar);
       int it = 0;
-      for (int tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x, ++it) {
+      for (int tile = blockIdx.x; tile < ntiles && !s_fail && !L0; tile += gridDim.x, ++it) {
         const int b = tile / tpr, t0 = (tile - b * tpr) * NT_BM;
         const int s = it % NT_STAGES, use = it / NT_STAGES;
         if (use > 0 && !nt_wait(empty_bar(s), (use - 1) & 1, &s_fail)) break;
@@ -205,7 +228,55 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
       tc::mma_commit(done_bar);
       tc::mbar_wait(done_bar, 0, NT_WAIT_LIMIT);
     }
-  } else {
+  } else if (L0 && warp >= 6) {
+    // ---------------- layer 0 into the stages (see the header).  No
+    // barrier among these warps: each thread reads its own inputs (L1), so
+    // a thread that stops after a failed wait holds no other thread up.
+    const int lt0 = tid - NT_THREADS;                 // 0 .. 255
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x, ++it) {
+      const int b = tile / tpr, t0 = (tile - b * tpr) * NT_BM;
+      const int s = it % NT_STAGES, use = it / NT_STAGES;
+      if (use > 0 && !nt_wait(empty_bar(s), (use - 1) & 1, &s_fail)) break;
+      uint8_t* st = gbase + NT_A_OFF + s * NT_A_STRIDE;
+      const __nv_bfloat16* xb = p.x0 + (size_t)b * NN_IN * p.T;
+      // task = (halo row r, group g of 8 channels)
+      for (int task = lt0; task < NT_HALO * 8; task += 32 * NT_L0_WARPS) {
+        const int r = task >> 3, g = task & 7;
+        const int tau = t0 - NN_HALF + r;
+        uint32_t pk[4] = {0u, 0u, 0u, 0u};
+        if (tau >= 0 && tau < p.T) {
+          const float4 c0 = reinterpret_cast<const float4*>(s_b0)[2 * g];
+          const float4 c1 = reinterpret_cast<const float4*>(s_b0)[2 * g + 1];
+          float2 a[4] = {make_float2(c0.x, c0.y), make_float2(c0.z, c0.w), make_float2(c1.x, c1.y),
+                         make_float2(c1.z, c1.w)};
+#pragma unroll
+          for (int ci = 0; ci < NN_IN; ++ci) {
+#pragma unroll
+            for (int k = 0; k < NN_K; ++k) {
+              const int tt = tau + k - NN_HALF;            // zero outside [0, T)
+              const float xv = (tt >= 0 && tt < p.T) ? __bfloat162float(xb[(size_t)ci * p.T + tt]) : 0.f;
+              const float4* wq = reinterpret_cast<const float4*>(s_w0 + (ci * NN_K + k) * 64 + 8 * g);
+              const float4 w0 = wq[0], w1 = wq[1];
+              const float2 x2 = make_float2(xv, xv);
+              a[0] = fma2(make_float2(w0.x, w0.y), x2, a[0]);
+              a[1] = fma2(make_float2(w0.z, w0.w), x2, a[1]);
+              a[2] = fma2(make_float2(w1.x, w1.y), x2, a[2]);
+              a[3] = fma2(make_float2(w1.z, w1.w), x2, a[3]);
+            }
+          }
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(a[e].x), nt_tanh(a[e].y));
+            pk[e] = *reinterpret_cast<const uint32_t*>(&h);
+          }
+        }
+        *reinterpret_cast<uint4*>(st + r * 128 + ((g ^ (r & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+      tc::fence_proxy_async_smem();   // the generic-proxy writes, for the MMAs
+      nt_arrive(full_bar(s));
+    }
+  } else if (warp < 4) {
     // ---------------- epilogue: warp w owns time points 32w .. 32w+31 of the tile
     int lt = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++lt) {
@@ -425,17 +496,25 @@ cudaError_t nn_launch_out(const float* part, const float* b3, float* out, int T,
 }
 
 cudaError_t nn_launch_conv_tc(const CUtensorMap& tx, const CUtensorMap& tw, const float* bias, __nv_bfloat16* out,
-                              const __nv_bfloat16* w3, float* part, const NnRowsPlan& p, cudaStream_t st) {
+                              const __nv_bfloat16* w3, float* part, const NnRowsPlan& p, cudaStream_t st,
+                              const __nv_bfloat16* x0, const __nv_bfloat16* w0, const float* b0) {
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_nn_conv_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_nn_conv_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_nn_conv_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
+      e = cudaFuncSetAttribute(k_nn_conv_tc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_nn_conv_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
     if (e != cudaSuccess) return e;
     attr = true;
   }
+  if (x0 && part) return cudaErrorInvalidValue;   // layer 0 is fused into layer 1 only
   NtParams q;
   q.bias = bias;
+  q.x0 = x0;
+  q.w0 = w0;
+  q.b0 = b0;
   q.out = out;
   q.w3 = w3;
   q.part = part;
@@ -448,8 +527,10 @@ cudaError_t nn_launch_conv_tc(const CUtensorMap& tx, const CUtensorMap& tw, cons
   const int tiles = p.maxrows * q.tiles_per_row;
   const int grid = std::max(1, std::min(p.sms, tiles));
   if (part)
-    k_nn_conv_tc<true><<<grid, NT_THREADS, NT_SMEM, st>>>(tx, tw, q);
+    k_nn_conv_tc<true, false><<<grid, NT_THREADS, NT_SMEM, st>>>(tx, tw, q);
+  else if (x0)
+    k_nn_conv_tc<false, true><<<grid, NT_THREADS_L0, NT_SMEM, st>>>(tx, tw, q);
   else
-    k_nn_conv_tc<false><<<grid, NT_THREADS, NT_SMEM, st>>>(tx, tw, q);
+    k_nn_conv_tc<false, false><<<grid, NT_THREADS, NT_SMEM, st>>>(tx, tw, q);
   return cudaGetLastError();
 }

@@ -29,10 +29,13 @@ int nn_weight_map(CUtensorMap* m, const __nv_bfloat16* wt);
 
 cudaError_t nn_launch_l0_cl(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* y,
                             int T, int maxrows, const int* count, const int* stop, cudaStream_t st);
-// layer 1 (part == NULL: activations into out) or layer 2 with layer 3
-// applied in the epilogue (partial sums into part)
+// layer 1 (part == NULL: activations into out; with x0, w0, b0 layer 0 is
+// computed inside the kernel from the inputs x0 and tx is unused) or layer 2
+// with layer 3 applied in the epilogue (partial sums into part)
 cudaError_t nn_launch_conv_tc(const CUtensorMap& tx, const CUtensorMap& tw, const float* bias, __nv_bfloat16* out,
-                              const __nv_bfloat16* w3, float* part, const NnRowsPlan& p, cudaStream_t st);
+                              const __nv_bfloat16* w3, float* part, const NnRowsPlan& p, cudaStream_t st,
+                              const __nv_bfloat16* x0 = nullptr, const __nv_bfloat16* w0 = nullptr,
+                              const float* b0 = nullptr);
 // out [rows][T] from the partial sums [rows][9][T]
 cudaError_t nn_launch_out(const float* part, const float* b3, float* out, int T, int rows, cudaStream_t st);
 
@@ -49,9 +52,10 @@ __device__ __forceinline__ float nn_out_at(const float* __restrict__ P, float b3
 }
 
 struct fil_nn;
-// the network over the rows of the plan: layer 0 on CUDA cores, layers 1
-// and 2 on the tensor cores with layer 3 in layer 2's epilogue, leaving the
-// partial sums in p.part; surrogate.cu
+// the network over the rows of the plan: layers 0 and 1 in one kernel
+// (layer 0 on CUDA cores into layer 1's tensor-core operand), layer 2 on the
+// tensor cores with layer 3 in its epilogue, leaving the partial sums in
+// p.part; surrogate.cu
 cudaError_t nn_infer(const fil_nn* n, const NnRowsPlan& p, cudaStream_t st);
 // device pointer to the output layer's bias (the b3 of nn_out_at)
 const float* nn_out_bias(const fil_nn* n);

@@ -111,10 +111,8 @@ int nn_forward_dev(const fil_nn* n, const __nv_bfloat16* x0, __nv_bfloat16* a1, 
 int nn_time_points(const fil_nn* n) { return n->T; }
 
 cudaError_t nn_infer(const fil_nn* n, const NnRowsPlan& p, cudaStream_t st) {
-  cudaError_t e = nn_launch_l0_cl(p.x0, n->wf[0], n->p + nn_poff(0) + nn_wsize(0), p.a1, p.T, p.maxrows, p.count,
-                                  p.stop, st);
-  if (e == cudaSuccess)
-    e = nn_launch_conv_tc(p.map_a1, n->wmap[1], n->p + nn_poff(1) + nn_wsize(1), p.a2, nullptr, nullptr, p, st);
+  cudaError_t e = nn_launch_conv_tc(p.map_a1, n->wmap[1], n->p + nn_poff(1) + nn_wsize(1), p.a2, nullptr, nullptr, p,
+                                    st, p.x0, n->wf[0], n->p + nn_poff(0) + nn_wsize(0));
   if (e == cudaSuccess)
     e = nn_launch_conv_tc(p.map_a2, n->wmap[2], n->p + nn_poff(2) + nn_wsize(2), nullptr, n->wf[3], p.part, p, st);
   return e;
