@@ -32,9 +32,13 @@
 // w0[ci][k][co] x[ci][t + k - 4]) rounded to BF16 (zero for rows outside
 // [0, T), the "same" padding of layer 1), and write it into the stage in
 // the layout the 128-byte swizzle gives a TMA copy (16-byte chunk c of row r
-// at chunk c ^ (r mod 8) of the 1024-byte aligned stage); each of them fences
-// its writes for the tensor core's proxy and arrives on the stage's full
-// barrier (count 256).  Layer 0's activations never reach HBM.
+// at chunk c ^ (r mod 8) of the 1024-byte aligned stage).  Warp q owns halo
+// rows 17q .. 17q + 16, lane l the channel pair (2l, 2l + 1) with its 54
+// weights in registers; the warp stages its 25-point input window per
+// channel in its own shared buffer and walks the rows with a rolling 9-tap
+// window; a row is one 128-byte store by the warp.  Every lane fences its
+// writes for the tensor core's proxy and arrives on the stage's full barrier
+// (count 256).  Layer 0's activations never reach HBM.
 #include <algorithm>
 #include <cstdint>
 
@@ -69,6 +73,8 @@ static_assert(NT_A_STRIDE % 1024 == 0 && NT_A_STRIDE >= NT_A_BYTES, "stage pitch
 #define NT_THREADS 192
 #define NT_L0_WARPS 8                  // layer-0 warps of the fused kernel
 #define NT_THREADS_L0 (NT_THREADS + 32 * NT_L0_WARPS)
+#define NT_L0_ROWS (NT_HALO / NT_L0_WARPS)   // halo rows per layer-0 warp
+static_assert(NT_L0_ROWS * NT_L0_WARPS == NT_HALO, "the halo rows split evenly over the layer-0 warps");
 #define NT_WAIT_LIMIT (1u << 26)
 
 static __device__ __forceinline__ bool nt_wait(uint32_t bar, uint32_t parity, volatile int* fail) {
@@ -126,9 +132,8 @@ __global__ void __launch_bounds__(L0 ? NT_THREADS_L0 : NT_THREADS, 1)
   extern __shared__ __align__(1024) uint8_t nt_smem[];
   __shared__ volatile int s_fail;
   __shared__ __align__(16) float s_bias[64];
-  // L0: layer-0 weights [ci * 9 + k][co] and bias
-  __shared__ __align__(16) float s_w0[L0 ? NN_IN * NN_K * 64 : 4];
-  __shared__ __align__(16) float s_b0[L0 ? 64 : 4];
+  // L0: each layer-0 warp's input window (three channels x 25 points)
+  __shared__ float s_xw[L0 ? NT_L0_WARPS : 1][NN_IN][L0 ? NT_L0_ROWS + NN_K - 1 : 1];
   // layer-3 weights as tap pairs: s_w3[(kp * 64 + ci) * 2 + u] = w3[ci][2 kp + u]
   // (kp < 5; the tenth tap is zero)
   __shared__ __align__(16) float s_w3[FINAL ? 5 * 64 * 2 : 4];
@@ -150,10 +155,6 @@ __global__ void __launch_bounds__(L0 ? NT_THREADS_L0 : NT_THREADS, 1)
 
   if (tid == 0) s_fail = 0;
   if (tid < 64) s_bias[tid] = p.bias[tid];
-  if (L0) {
-    for (int i = tid; i < NN_IN * NN_K * 64; i += NT_THREADS_L0) s_w0[i] = __bfloat162float(p.w0[i]);
-    if (tid < 64) s_b0[tid] = p.b0[tid];
-  }
   if (FINAL)
     for (int i = tid; i < 5 * 64 * 2; i += NT_THREADS) {
       const int u = i & 1, ci = (i >> 1) & 63, k = 2 * (i >> 7) + u;
@@ -229,51 +230,66 @@ __global__ void __launch_bounds__(L0 ? NT_THREADS_L0 : NT_THREADS, 1)
       tc::mbar_wait(done_bar, 0, NT_WAIT_LIMIT);
     }
   } else if (L0 && warp >= 6) {
-    // ---------------- layer 0 into the stages (see the header).  No
-    // barrier among these warps: each thread reads its own inputs (L1), so
-    // a thread that stops after a failed wait holds no other thread up.
-    const int lt0 = tid - NT_THREADS;                 // 0 .. 255
+    // ---------------- layer 0 into the stages (see the header).  Lane 0
+    // decides each stage wait and the warp follows it (no divergence); no
+    // barrier across warps, so a warp that stops holds no other up.
+    const int q = warp - 6, c2 = 2 * lane, r0 = NT_L0_ROWS * q;
+    float2 wv[NN_IN][NN_K];
+#pragma unroll
+    for (int ci = 0; ci < NN_IN; ++ci)
+#pragma unroll
+      for (int k = 0; k < NN_K; ++k) {
+        const __nv_bfloat162 w = *reinterpret_cast<const __nv_bfloat162*>(p.w0 + (ci * NN_K + k) * 64 + c2);
+        wv[ci][k] = __bfloat1622float2(w);
+      }
+    const float2 bias0 = make_float2(p.b0[c2], p.b0[c2 + 1]);
+    float* xw = &s_xw[q][0][0];
+    constexpr int XW = NT_L0_ROWS + NN_K - 1;
     int it = 0;
-    for (int tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x, ++it) {
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
       const int b = tile / tpr, t0 = (tile - b * tpr) * NT_BM;
       const int s = it % NT_STAGES, use = it / NT_STAGES;
-      if (use > 0 && !nt_wait(empty_bar(s), (use - 1) & 1, &s_fail)) break;
-      uint8_t* st = gbase + NT_A_OFF + s * NT_A_STRIDE;
+      int ok = 1;
+      if (lane == 0) ok = !s_fail && (use == 0 || nt_wait(empty_bar(s), (use - 1) & 1, &s_fail));
+      if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+      // inputs x[ci][t0 - 8 + r0 .. t0 - 8 + r0 + 24] (zero outside [0, T))
       const __nv_bfloat16* xb = p.x0 + (size_t)b * NN_IN * p.T;
-      // task = (halo row r, group g of 8 channels)
-      for (int task = lt0; task < NT_HALO * 8; task += 32 * NT_L0_WARPS) {
-        const int r = task >> 3, g = task & 7;
-        const int tau = t0 - NN_HALF + r;
-        uint32_t pk[4] = {0u, 0u, 0u, 0u};
-        if (tau >= 0 && tau < p.T) {
-          const float4 c0 = reinterpret_cast<const float4*>(s_b0)[2 * g];
-          const float4 c1 = reinterpret_cast<const float4*>(s_b0)[2 * g + 1];
-          float2 a[4] = {make_float2(c0.x, c0.y), make_float2(c0.z, c0.w), make_float2(c1.x, c1.y),
-                         make_float2(c1.z, c1.w)};
-#pragma unroll
-          for (int ci = 0; ci < NN_IN; ++ci) {
-#pragma unroll
-            for (int k = 0; k < NN_K; ++k) {
-              const int tt = tau + k - NN_HALF;            // zero outside [0, T)
-              const float xv = (tt >= 0 && tt < p.T) ? __bfloat162float(xb[(size_t)ci * p.T + tt]) : 0.f;
-              const float4* wq = reinterpret_cast<const float4*>(s_w0 + (ci * NN_K + k) * 64 + 8 * g);
-              const float4 w0 = wq[0], w1 = wq[1];
-              const float2 x2 = make_float2(xv, xv);
-              a[0] = fma2(make_float2(w0.x, w0.y), x2, a[0]);
-              a[1] = fma2(make_float2(w0.z, w0.w), x2, a[1]);
-              a[2] = fma2(make_float2(w1.x, w1.y), x2, a[2]);
-              a[3] = fma2(make_float2(w1.z, w1.w), x2, a[3]);
-            }
-          }
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(a[e].x), nt_tanh(a[e].y));
-            pk[e] = *reinterpret_cast<const uint32_t*>(&h);
-          }
-        }
-        *reinterpret_cast<uint4*>(st + r * 128 + ((g ^ (r & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      for (int i = lane; i < NN_IN * XW; i += 32) {
+        const int ci = i / XW, j = i - ci * XW, tt = t0 - 2 * NN_HALF + r0 + j;
+        xw[i] = (tt >= 0 && tt < p.T) ? __bfloat162float(xb[(size_t)ci * p.T + tt]) : 0.f;
       }
-      tc::fence_proxy_async_smem();   // the generic-proxy writes, for the MMAs
+      __syncwarp();
+      uint8_t* st = gbase + NT_A_OFF + s * NT_A_STRIDE;
+      float win[NN_IN][NN_K];
+#pragma unroll
+      for (int ci = 0; ci < NN_IN; ++ci)
+#pragma unroll
+        for (int k = 0; k < NN_K - 1; ++k) win[ci][k + 1] = xw[ci * XW + k];
+#pragma unroll
+      for (int j = 0; j < NT_L0_ROWS; ++j) {
+        // window of row r0 + j: x at tau - 4 .. tau + 4, tau = t0 - 4 + r0 + j
+#pragma unroll
+        for (int ci = 0; ci < NN_IN; ++ci) {
+#pragma unroll
+          for (int k = 0; k < NN_K - 1; ++k) win[ci][k] = win[ci][k + 1];
+          win[ci][NN_K - 1] = xw[ci * XW + j + NN_K - 1];
+        }
+        const int r = r0 + j, tau = t0 - NN_HALF + r;
+        float2 a = bias0;
+#pragma unroll
+        for (int ci = 0; ci < NN_IN; ++ci)
+#pragma unroll
+          for (int k = 0; k < NN_K; ++k) a = fma2(wv[ci][k], make_float2(win[ci][k], win[ci][k]), a);
+        uint32_t pk = 0u;
+        if (tau >= 0 && tau < p.T) {
+          const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(a.x), nt_tanh(a.y));
+          pk = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        // channels c2, c2 + 1: byte 4 lane of the row, 16-byte chunk lane / 4
+        *reinterpret_cast<uint32_t*>(st + r * 128 + (((lane >> 2) ^ (r & 7)) << 4) + ((lane & 3) << 2)) = pk;
+      }
+      __syncwarp();                   // xw free for the next tile
+      tc::fence_proxy_async_smem();   // this lane's writes, for the MMAs
       nt_arrive(full_bar(s));
     }
   } else if (warp < 4) {
