@@ -245,6 +245,24 @@ __global__ void __launch_bounds__(L0 ? NT_THREADS_L0 : NT_THREADS, 1)
     const float2 bias0 = make_float2(p.b0[c2], p.b0[c2 + 1]);
     float* xw = &s_xw[q][0][0];
     constexpr int XW = NT_L0_ROWS + NN_K - 1;
+    constexpr int XL = (NN_IN * XW + 31) / 32;        // window values per lane
+    // this lane's window values x[ci][t0 - 8 + r0 + j] of a tile (zero
+    // outside [0, T)), loaded one tile ahead of their use
+    auto load_window = [&](int tile, float (&v)[XL]) {
+      const int b = tile / tpr, t0 = (tile - b * tpr) * NT_BM;
+      const __nv_bfloat16* xb = p.x0 + (size_t)b * NN_IN * p.T;
+#pragma unroll
+      for (int u = 0; u < XL; ++u) {
+        const int i = lane + 32 * u;
+        v[u] = 0.f;
+        if (i < NN_IN * XW) {
+          const int ci = i / XW, j = i - ci * XW, tt = t0 - 2 * NN_HALF + r0 + j;
+          if (tt >= 0 && tt < p.T) v[u] = __bfloat162float(xb[(size_t)ci * p.T + tt]);
+        }
+      }
+    };
+    float nxt[XL];
+    if ((int)blockIdx.x < ntiles) load_window(blockIdx.x, nxt);
     int it = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
       const int b = tile / tpr, t0 = (tile - b * tpr) * NT_BM;
@@ -252,13 +270,12 @@ __global__ void __launch_bounds__(L0 ? NT_THREADS_L0 : NT_THREADS, 1)
       int ok = 1;
       if (lane == 0) ok = !s_fail && (use == 0 || nt_wait(empty_bar(s), (use - 1) & 1, &s_fail));
       if (!__shfl_sync(0xffffffffu, ok, 0)) break;
-      // inputs x[ci][t0 - 8 + r0 .. t0 - 8 + r0 + 24] (zero outside [0, T))
-      const __nv_bfloat16* xb = p.x0 + (size_t)b * NN_IN * p.T;
-      for (int i = lane; i < NN_IN * XW; i += 32) {
-        const int ci = i / XW, j = i - ci * XW, tt = t0 - 2 * NN_HALF + r0 + j;
-        xw[i] = (tt >= 0 && tt < p.T) ? __bfloat162float(xb[(size_t)ci * p.T + tt]) : 0.f;
-      }
+      (void)b;
+#pragma unroll
+      for (int u = 0; u < XL; ++u)
+        if (lane + 32 * u < NN_IN * XW) xw[lane + 32 * u] = nxt[u];
       __syncwarp();
+      if (tile + (int)gridDim.x < ntiles) load_window(tile + gridDim.x, nxt);   // in flight during the rows
       uint8_t* st = gbase + NT_A_OFF + s * NT_A_STRIDE;
       float win[NN_IN][NN_K];
 #pragma unroll
@@ -275,14 +292,18 @@ __global__ void __launch_bounds__(L0 ? NT_THREADS_L0 : NT_THREADS, 1)
           win[ci][NN_K - 1] = xw[ci * XW + j + NN_K - 1];
         }
         const int r = r0 + j, tau = t0 - NN_HALF + r;
-        float2 a = bias0;
+        // one independent chain per input channel, joined at the end
+        float2 a[NN_IN];
 #pragma unroll
-        for (int ci = 0; ci < NN_IN; ++ci)
+        for (int ci = 0; ci < NN_IN; ++ci) {
+          a[ci] = ci == 0 ? bias0 : make_float2(0.f, 0.f);
 #pragma unroll
-          for (int k = 0; k < NN_K; ++k) a = fma2(wv[ci][k], make_float2(win[ci][k], win[ci][k]), a);
+          for (int k = 0; k < NN_K; ++k) a[ci] = fma2(wv[ci][k], make_float2(win[ci][k], win[ci][k]), a[ci]);
+        }
+        const float vx = (a[0].x + a[1].x) + a[2].x, vy = (a[0].y + a[1].y) + a[2].y;
         uint32_t pk = 0u;
         if (tau >= 0 && tau < p.T) {
-          const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(a.x), nt_tanh(a.y));
+          const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(vx), nt_tanh(vy));
           pk = *reinterpret_cast<const uint32_t*>(&h);
         }
         // channels c2, c2 + 1: byte 4 lane of the row, 16-byte chunk lane / 4
