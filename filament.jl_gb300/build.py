@@ -14,7 +14,8 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxe
 
 
 def sources():
-    return sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    # the row-kernel units take longest: they go to the pool first
+    return sorted((f for f in os.listdir(CSRC) if f.endswith(".cu")), key=lambda f: (not f.startswith("row"), f))
 
 
 def _newest_input():

@@ -79,6 +79,10 @@ struct fil_handle {
   int ns;
   double A0[4], A1[4], B[4];
   double sc = 1, sf = 1, sl = 1, sr = 1;   // response channel pre-scales
+  // Tsitouras 5(4) (tsit5.h): stage derivatives [nrows][7][nh] of the row
+  // kernel (T, RT, XYT); tolerances of the adaptive form
+  void* tk = nullptr;
+  double ode_atol = 1e-6, ode_rtol = 1e-3;
   double cc_max = -1;                      // linear-only row test (FP32 form), < 0: off
   std::complex<double> c0 = 0.0;           // XY: i QZ(w0) Rnl_cubic(w0)
   bool field_set = false, store_plasma = false;
@@ -648,6 +652,20 @@ template <typename R> static RowParams<R> row_params(fil_handle* h) {
     P.A1[s] = (R)h->A1[s];
     P.B[s] = (R)h->B[s];
   }
+  P.tsit = c.alg == FIL_ALG_TSIT5 ? 1 : (c.alg == FIL_ALG_ATSIT5 ? 2 : 0);
+  P.babs = (R)1;
+  if (P.tsit) {
+    double babs = 0;
+    for (int i = 0; i < TSIT_STAGES; ++i) {
+      for (int j = 0; j < TSIT_STAGES - 1; ++j) P.ta[i][j] = (R)kTsitA[i][j];
+      P.tbt[i] = (R)kTsitBt[i];
+    }
+    for (int j = 0; j < TSIT_STAGES - 1; ++j) babs += std::fabs(kTsitA[TSIT_STAGES - 1][j]);
+    P.babs = (R)babs;
+  }
+  P.tk = (C*)h->tk;
+  P.atol = h->ode_atol;
+  P.rtol = h->ode_rtol;
   P.plasma = c.plasma;
   P.pp = plasma_params_as<R>(h->pp);
   P.rho_g = (R*)h->rho_g;
@@ -759,6 +777,30 @@ template <typename R> static int enqueue_zstep_xyt(fil_handle* h, bool timed) {
   return 0;
 }
 
+// Tableau of the pointwise nonlinear step (XY, R): RK2/3/4 or Tsitouras.
+template <typename R> static void xy_tableau(const fil_handle* h, XyNlParams<R>& q) {
+  const int alg = h->cfg.alg;
+  if (alg == FIL_ALG_TSIT5 || alg == FIL_ALG_ATSIT5) {
+    q.ns = TSIT_STAGES - 1;
+    q.tsit = alg == FIL_ALG_TSIT5 ? 1 : 2;
+    for (int i = 0; i < TSIT_STAGES; ++i) {
+      for (int j = 0; j < TSIT_STAGES - 1; ++j) q.a[i][j] = (R)kTsitA[i][j];
+      q.bt[i] = (R)kTsitBt[i];
+    }
+    for (int j = 0; j < TSIT_STAGES - 1; ++j) q.b[j] = (R)kTsitA[TSIT_STAGES - 1][j];
+    q.b[TSIT_STAGES - 1] = (R)0;
+  } else {
+    double a[4][4], b[4], cc[4];
+    rk_tableau(alg, &q.ns, a, b, cc);
+    for (int i = 0; i < 4; ++i) {
+      q.b[i] = (R)b[i];
+      for (int j = 0; j < 4; ++j) q.a[i][j] = (R)a[i][j];
+    }
+  }
+  q.atol = h->ode_atol;
+  q.rtol = h->ode_rtol;
+}
+
 // XY (no time axis): pointwise nonlinear RK step (W1 <- S), fft along y,
 // fft along x with the propagator and the inverse along x, inverse along y
 // times the field guard (S <- W1)
@@ -772,12 +814,7 @@ template <typename R> static int enqueue_zstep_xy(fil_handle* h, bool timed) {
     std::memset(&q, 0, sizeof q);
     q.n = (long)nx * ny;
     q.ny = ny;
-    double a[4][4], b[4], cc[4];
-    rk_tableau(h->cfg.alg, &q.ns, a, b, cc);
-    for (int i = 0; i < 4; ++i) {
-      q.b[i] = (R)b[i];
-      for (int j = 0; j < 4; ++j) q.a[i][j] = (R)a[i][j];
-    }
+    xy_tableau<R>(h, q);
     q.c0 = mk<R>((R)h->c0.real(), (R)h->c0.imag());
     q.g1 = (const R*)h->g1;
     q.g2 = (const R*)h->g2;
@@ -889,12 +926,7 @@ template <typename R> static int enqueue_zstep_r(fil_handle* h, bool timed) {
     std::memset(&q, 0, sizeof q);
     q.n = h->nrows;
     q.ny = 1;
-    double a[4][4], b[4], cc[4];
-    rk_tableau(h->cfg.alg, &q.ns, a, b, cc);
-    for (int i = 0; i < 4; ++i) {
-      q.b[i] = (R)b[i];
-      for (int j = 0; j < 4; ++j) q.a[i][j] = (R)a[i][j];
-    }
+    xy_tableau<R>(h, q);
     q.c0 = mk<R>((R)h->c0.real(), (R)h->c0.imag());
     q.g1 = (const R*)h->g1;
     q.g2 = (const R*)h->g2;
@@ -1066,7 +1098,7 @@ static void free_all(fil_handle* h) {
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
                   h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err,
                   h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt, h->park,
-                  h->kcol, h->l_kzr, h->l_kg, h->spec_g};
+                  h->kcol, h->l_kzr, h->l_kg, h->spec_g, h->tk};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -1202,6 +1234,12 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (cfg->n1 < 1 || cfg->n1 > 65536) return fail(h, FIL_ERR_ARG, "bad n1");
   if (cfg->nonlinearity && !cfg->qparaxial && cfg->geometry != FIL_GEOM_RT)
     return fail(h, FIL_ERR_UNSUPPORTED, "QPARAXIAL=false is built for the RT geometry");
+  if (cfg->alg < FIL_ALG_RK2 || cfg->alg > FIL_ALG_ATSIT5) return fail(h, FIL_ERR_ARG, "unknown ALG");
+  if (cfg->nonlinearity && cfg->alg > FIL_ALG_RK4 && (!cfg->qparaxial || (cfg->plasma && cfg->plasma_ncomp > 2)))
+    return fail(h, FIL_ERR_UNSUPPORTED, "Tsit5/ATsit5 with QPARAXIAL=false or more than two species");
+  if (cfg->plasma && (cfg->plasma_alg < FIL_ALG_RK2 || cfg->plasma_alg > FIL_ALG_RK4))
+    return fail(h, cfg->plasma_alg > FIL_ALG_RK4 && cfg->plasma_alg <= FIL_ALG_ATSIT5 ? FIL_ERR_UNSUPPORTED : FIL_ERR_ARG,
+                "plasma ALG must be RK2, RK3 or RK4");
   if (cfg->nonlinearity && (cfg->resp_mask & FIL_RESP_RAMAN) && !t->raman_h)
     return fail(h, FIL_ERR_ARG, "missing Raman response table");
   if (cfg->plasma && (cfg->plasma_ncomp < 1 || cfg->plasma_ncomp > FIL_MAXCOMP))
@@ -1268,6 +1306,10 @@ int fil_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (h->geom != FIL_GEOM_XY && h->geom != FIL_GEOM_R) {
     CKC(cudaMalloc(&h->park, (size_t)h->nrows * h->ld * es));
     CKC(cudaMemset(h->park, 0, (size_t)h->nrows * h->ld * es));
+    if (cfg->nonlinearity && cfg->alg > FIL_ALG_RK4) {
+      CKC(cudaMalloc(&h->tk, (size_t)h->nrows * TSIT_STAGES * h->nh * es));
+      CKC(cudaMemset(h->tk, 0, (size_t)h->nrows * TSIT_STAGES * h->nh * es));
+    }
   }
   if (h->geom == FIL_GEOM_XYT) {
     h->full_spec = true;      // the upper half lives in columns nh .. nt - 1 of S
@@ -1342,6 +1384,10 @@ int fil_set_option(fil_handle* h, int option, int64_t value) {
       }
       h->full_spec = full;
     }
+  }
+  else if (option == FIL_OPT_ODE_RTOL || option == FIL_OPT_ODE_ATOL) {
+    if (value <= 0) return fail(h, FIL_ERR_ARG, "tolerance must be positive");
+    (option == FIL_OPT_ODE_RTOL ? h->ode_rtol : h->ode_atol) = (double)value * 1e-12;
   }
   else {
     return fail(h, FIL_ERR_ARG, "unknown option");
@@ -1587,6 +1633,15 @@ int fil_get_stats(fil_handle* h, fil_stats* st) {
   st->steps = c.steps;
   st->status = c.status;
   st->flags = c.flags | (std::min(c.newton_max, 255) << 8);
+  return FIL_OK;
+}
+
+int fil_get_ode_stats(fil_handle* h, int64_t out[2]) {
+  if (!h || !out) return fail(h, FIL_ERR_ARG, "null argument");
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  out[0] = (int64_t)h->ctl_host->ode_attempts;
+  out[1] = (int64_t)h->ctl_host->ode_rejects;
   return FIL_OK;
 }
 

@@ -89,6 +89,15 @@ template <typename R, int N> static size_t x_smem() {
 template <typename R, int N>
 static cudaError_t launch_rowstep_n(const RowParams<R>& P, int nc, int mode, cudaStream_t st) {
   const bool ram = P.has_raman != 0;
+  if (P.tsit && mode == 0) {   // Tsitouras step kernels (nc <= 2, checked at fil_create)
+    if (nc == 0)
+      return ram ? launch_rowstep_t<R, N, 0, true, true>(P, mode, st) : launch_rowstep_t<R, N, 0, false, true>(P, mode, st);
+    if (nc == 1)
+      return ram ? launch_rowstep_t<R, N, 1, true, true>(P, mode, st) : launch_rowstep_t<R, N, 1, false, true>(P, mode, st);
+    if (nc == 2)
+      return ram ? launch_rowstep_t<R, N, 2, true, true>(P, mode, st) : launch_rowstep_t<R, N, 2, false, true>(P, mode, st);
+    return cudaErrorInvalidValue;
+  }
   if (nc == 0) return ram ? launch_rowstep_t<R, N, 0, true>(P, mode, st) : launch_rowstep_t<R, N, 0, false>(P, mode, st);
   if (nc == 1) return ram ? launch_rowstep_t<R, N, 1, true>(P, mode, st) : launch_rowstep_t<R, N, 1, false>(P, mode, st);
   if (nc == 2) return ram ? launch_rowstep_t<R, N, 2, true>(P, mode, st) : launch_rowstep_t<R, N, 2, false>(P, mode, st);

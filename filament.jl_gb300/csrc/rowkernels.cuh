@@ -14,6 +14,7 @@
 #include "plasma.cuh"
 #include "surrogate_consts.h"
 #include "nn_tc.h"
+#include "tsit5.h"
 
 // Device control block: written by the controller kernel, read by the step
 // kernels (fil_run) or set by the host (fil_step).
@@ -36,11 +37,15 @@ struct DevCtl {
   unsigned long long nn_diff_acc;   // judge step: max |rho_net - rho_ode| (bits)
   double nn_tol, nn_err, nn_err_max;
   double nn_rows_sum;         // sum of nn_rows over the steps that used the network
+  // adaptive nonlinear step (FIL_ALG_ATSIT5): substep attempts and
+  // rejections, summed over the transverse points and steps
+  unsigned long long ode_attempts, ode_rejects;
 };
 
 #define FIL_FLAG_NAN 1
 #define FIL_FLAG_ISTOP 2
 #define FIL_FLAG_NEWTON 4
+#define FIL_FLAG_ODE 8
 
 template <typename R> struct RowParams {
   typedef typename C2T<R>::type C;
@@ -62,6 +67,14 @@ template <typename R> struct RowParams {
   const C* ramh;                // Raman response H(w) [N] (raman.jl:21-31)
   int ns;                       // RK stages
   R A0[4], A1[4], B[4];         // stage input U_s = S0 + dz (A0 k1 + A1 kprev)
+  // Tsitouras 5(4) (tsit5.h): 1 one step of dz, 2 adaptive substeps.  The
+  // stage derivatives live in tk [row][7][N/2]; ta[s][j], tb = ta[6],
+  // tbt = b - bhat; babs = sum |b_s| (1 for RK2/3/4)
+  int tsit;
+  R ta[7][6], tbt[7];
+  R babs;
+  C* tk;
+  double atol, rtol;
   // plasma
   int plasma;
   PlasmaParams<R> pp;
@@ -766,9 +779,11 @@ FIL_DEV typename C2T<R>::type upper_prop(const RowParams<R>& P, size_t idx, type
 // of a step only (with the surrogate when armed), rho and Kdrho rows to
 // rho_g, kdrho_g: the first launch of a non-paraxial step (k_rowstage).
 // RAM: the Raman channel (compiled only where used, it costs registers).
+// TS: the Tsitouras methods (FIL_ALG_TSIT5/ATSIT5, P.tsit), in kernels of
+// their own so that the RK2/3/4 kernels keep their registers.
 // Blocks are held to 128 registers so that two (4096-point rows) to sixteen
 // (512-point rows, the XYT geometry) share an SM.
-template <typename R, int N, int NC, bool RAM>
+template <typename R, int N, int NC, bool RAM, bool TS>
 __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(RowParams<R> P, int mode) {
   typedef typename C2T<R>::type C;
   constexpr int T = N / 16, NH = N / 2, EW = NH / T, NP = N + N / 16;
@@ -781,6 +796,11 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   Aff<R, (NC > 0 ? NC : 1)>* ascratch = reinterpret_cast<Aff<R, (NC > 0 ? NC : 1)>*>(rscratch + 32);
   PlasmaSmem<R>* tabs = reinterpret_cast<PlasmaSmem<R>*>(ascratch + 32);
   __shared__ int s_flag;
+  __shared__ double s_dred[32];
+  __shared__ struct {
+    OdeStep o;
+    int k1s, rej, ok, fin;
+  } s_ode;   // FIL_ALG_ATSIT5 controller of the row
   bool ych = true;   // the plasma channels (Y) carry a response for this row
 
   DevCtl* ctl = P.ctl;
@@ -890,20 +910,99 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
     for (int m = 0; m < EW; ++m) s2 = max(s2, S0[m].x * S0[m].x + S0[m].y * S0[m].y);
     s2 = block_max<R>(s2, rscratch);
     const R emax = sqrt(e2row);
-    lin_only = !plas_row && dz * (P.has_cubic ? P.cc_max : (R)0) * emax * e2row <= (R)4.656612873077393e-10 * sqrt(s2);
+    lin_only = !plas_row &&
+               dz * P.babs * (P.has_cubic ? P.cc_max : (R)0) * emax * e2row <= (R)4.656612873077393e-10 * sqrt(s2);
   }
   if (P.nonlin && !lin_only) {
     int iy;
     const R gs = row_guard(P, row, &iy);
-    for (int s = 0; s < P.ns; ++s) {
-      const R a0 = (R)P.A0[s], a1 = (R)P.A1[s], bs = (R)P.B[s];
-      auto u = [&](int m) -> C { return s > 0 ? S0[m] + (dz * a0) * k1[m] + (dz * a1) * kp[m] : S0[m]; };
+    // One call site of stage_rhs for every method (it inlines the row's
+    // transforms).  RK2/3/4: U_s = S0 + dz (A0 k1 + A1 k_prev), k1 and
+    // k_prev in registers.  Tsitouras: U_s = S0 + h sum_j a_sj k_j with the
+    // k_j in this row's slots of tk (each thread reads back only the points
+    // it wrote); the first and the seventh stage swap slots on acceptance
+    // (first same as last).
+    const int tsit = TS ? P.tsit : 0;   // compiled out of the RK2/3/4 kernels
+    const int ns = tsit ? (tsit == 2 ? 7 : 6) : P.ns;
+    C* tk = tsit ? P.tk + (size_t)row * 7 * NH : nullptr;
+    // the adaptive controller lives in shared memory (thread 0 updates it
+    // between two barriers): no FP64 state is held in registers across the
+    // stages
+    if (tsit == 2) {
+      if (tid == 0) {
+        ode_begin(s_ode.o, ctl->dz);
+        s_ode.k1s = 0;
+        s_ode.rej = 0;
+      }
+      __syncthreads();
+    }
+    int s = 0;
+    for (;;) {
+      const R h = tsit == 2 ? (R)s_ode.o.h : dz;
+      const int k1s = tsit == 2 ? s_ode.k1s : 0;   // slot of k_1 (0 or 6)
+      auto slot = [&](int j) -> C* { return tk + (size_t)(j == 0 ? k1s : (j == 6 ? 6 - k1s : j)) * NH; };
+      auto u = [&](int m) -> C {
+        if (!tsit) return s > 0 ? S0[m] + (dz * (R)P.A0[s]) * k1[m] + (dz * (R)P.A1[s]) * kp[m] : S0[m];
+        const int k = tid + m * T;
+        C v = S0[m];
+        if (s == 6) return v + h * acc[m];
+        for (int j = 0; j < s; ++j) v = v + (h * P.ta[s][j]) * slot(j)[k];
+        return v;
+      };
       auto d = [&](int m, C v) {
-        if (s == 0) k1[m] = v;
-        kp[m] = v;
-        acc[m] = acc[m] + bs * v;
+        if (!tsit) {
+          if (s == 0) k1[m] = v;
+          kp[m] = v;
+          acc[m] = acc[m] + (R)P.B[s] * v;
+          return;
+        }
+        slot(s)[tid + m * T] = v;
+        if (s < 6) acc[m] = acc[m] + P.ta[6][s] * v;
       };
       stage_rhs<R, N, NC, RAM>(P, X, Y, rho, kdrho, gs, iy, ych, uo, u, d);
+      if (++s < ns) continue;
+      if (tsit != 2) break;
+      // the attempt's error norm over the row (FP64 sum in a fixed order)
+      double q = 0;
+#pragma unroll
+      for (int m = 0; m < EW; ++m) {
+        const int k = tid + m * T;
+        C e = mk<R>(0, 0);
+#pragma unroll
+        for (int j = 0; j < 7; ++j) e = e + P.tbt[j] * slot(j)[k];
+        e = h * e;
+        const C y1 = S0[m] + h * acc[m];
+        const double sc = P.atol + P.rtol * fmax(sqrt((double)cabs2(S0[m])), sqrt((double)cabs2(y1)));
+        const double r = sqrt((double)cabs2(e)) / sc;
+        q += r * r;
+      }
+      q = block_sum<double>(q, s_dred);   // ends with a barrier
+      if (tid == 0) {
+        int fin;
+        const int ok = ode_after(s_ode.o, sqrt(q / (double)NH), ctl->dz, &fin);
+        if (ok) s_ode.k1s = 6 - s_ode.k1s;
+        else s_ode.rej += 1;
+        s_ode.ok = ok;
+        s_ode.fin = fin;
+        if (fin) {
+          atomicAdd(&ctl->ode_attempts, (unsigned long long)s_ode.o.attempts);
+          atomicAdd(&ctl->ode_rejects, (unsigned long long)s_ode.rej);
+          if (fin == 2) atomicOr(&ctl->flags, FIL_FLAG_ODE);
+        }
+      }
+      __syncthreads();
+      const int ok = s_ode.ok, fin = s_ode.fin, k1n = s_ode.k1s;
+      // the next attempt starts at stage 2: its sum of b_s k_s holds k_1
+      // (after the last one S0 is the result: the sum is cleared).  Thread 0
+      // writes s_ode again only after the next attempt's block_sum barrier.
+#pragma unroll
+      for (int m = 0; m < EW; ++m) {
+        const int k = tid + m * T;
+        if (ok) S0[m] = S0[m] + h * acc[m];
+        acc[m] = fin ? mk<R>(0, 0) : P.ta[6][0] * tk[(size_t)k1n * NH + k];
+      }
+      if (fin) break;
+      s = 1;
     }
   }
 #pragma unroll

@@ -11,15 +11,30 @@ static size_t rowstep_smem() {
          sizeof(PlasmaSmem<R>);
 }
 
-template <typename R, int N, int NC, bool RAM>
+template <typename R, int N, int NC, bool RAM, bool TS>
 cudaError_t launch_rowstep_t(const RowParams<R>& P, int mode, cudaStream_t st) {
   size_t sm = rowstep_smem<R, N, NC>();
   cudaError_t e =
-      cudaFuncSetAttribute(k_rowstep<R, N, NC, RAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      cudaFuncSetAttribute(k_rowstep<R, N, NC, RAM, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k_rowstep<R, N, NC, RAM><<<P.nrows, N / 16, sm, st>>>(P, mode);
+  k_rowstep<R, N, NC, RAM, TS><<<P.nrows, N / 16, sm, st>>>(P, mode);
   return cudaGetLastError();
 }
+
+// the Tsitouras methods (up to two species)
+#define FIL_ROWSTEP_INST_TS(R, RAM)                                                                      \
+  template cudaError_t launch_rowstep_t<R, 512, 0, RAM, true>(const RowParams<R>&, int, cudaStream_t);  \
+  template cudaError_t launch_rowstep_t<R, 512, 1, RAM, true>(const RowParams<R>&, int, cudaStream_t);  \
+  template cudaError_t launch_rowstep_t<R, 512, 2, RAM, true>(const RowParams<R>&, int, cudaStream_t);  \
+  template cudaError_t launch_rowstep_t<R, 1024, 0, RAM, true>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 1024, 1, RAM, true>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 1024, 2, RAM, true>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 2048, 0, RAM, true>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 2048, 1, RAM, true>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 2048, 2, RAM, true>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 4096, 0, RAM, true>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 4096, 1, RAM, true>(const RowParams<R>&, int, cudaStream_t); \
+  template cudaError_t launch_rowstep_t<R, 4096, 2, RAM, true>(const RowParams<R>&, int, cudaStream_t);
 
 // three and four ionising species (paraxial prefactor, no Raman channel)
 #define FIL_ROWSTEP_INST_NC34(R)                                                                    \

@@ -133,27 +133,92 @@ cudaError_t launch_xylines(const XyParams<R>& p, int nl, int mode, int nh, int n
 // XY geometry (no time axis): the state is E(x, y) itself.
 // Nonlinear step (nonlinear_propagators.jl:38-74 with cubic.jl:49-54,
 // F = 3/4 |E|^2 E): dE/dz = C0 * g(x, y) * F(E), C0 = i QZ(w0) Rnl(w0), an
-// explicit RK step per point; writes the result into `out`.
+// explicit RK step per point; writes the result into `out`.  With the
+// adaptive Tsitouras pair each point chooses its own substeps (its error
+// norm is |e| / (atol + rtol max(|y0|, |y1|))).  Also the R geometry (one
+// column, ny = 1).
 template <typename R>
 __global__ void __launch_bounds__(256) k_xy_nonlinear(const typename C2T<R>::type* in, typename C2T<R>::type* out,
                                                       XyNlParams<R> p) {
   typedef typename C2T<R>::type C;
   const long i = blockIdx.x * 256L + threadIdx.x;
   if (p.ctl && p.ctl->done) return;
-  if (i >= p.n) return;
+  const bool live = i < p.n;
   const R dz = p.ctl ? (R)p.ctl->dz : p.dz_fixed;
-  const int ix = (int)(i / p.ny), iy = (int)(i - (long)ix * p.ny);
+  const long ii = live ? i : 0;
+  const int ix = (int)(ii / p.ny), iy = (int)(ii - (long)ix * p.ny);
   const R g = p.g1[ix] * p.g2[iy];
-  const C e0 = in[i];
-  C k[4], acc = mk<R>(0, 0);
-  for (int s = 0; s < p.ns; ++s) {
-    C u = e0;
-    for (int l = 0; l < s; ++l) u = u + (dz * p.a[s][l]) * k[l];
+  auto rhs = [&](C u) -> C {
     const R f = g * (R)0.75 * (u.x * u.x + u.y * u.y);
-    k[s] = cmul(p.c0, mk<R>(f * u.x, f * u.y));
-    acc = acc + p.b[s] * k[s];
+    return cmul(p.c0, mk<R>(f * u.x, f * u.y));
+  };
+  C y = in[ii];
+  C k[7];
+  if (p.tsit != 2) {
+    C acc = mk<R>(0, 0);
+#pragma unroll
+    for (int s = 0; s < 7; ++s) {
+      if (s < p.ns) {
+        C u = y;
+#pragma unroll
+        for (int l = 0; l < s; ++l) u = u + (dz * p.a[s][l]) * k[l];
+        k[s] = rhs(u);
+        acc = acc + p.b[s] * k[s];
+      }
+    }
+    if (live) out[i] = y + dz * acc;
+    return;
   }
-  out[i] = e0 + dz * acc;
+  OdeStep o;
+  ode_begin(o, p.ctl ? p.ctl->dz : (double)p.dz_fixed);
+  const double dzd = o.h;
+  unsigned rejects = 0;
+  int fin = 0;
+  k[0] = rhs(y);
+  while (live) {
+    const R h = (R)o.h;
+    C acc = mk<R>(0, 0);
+#pragma unroll
+    for (int s = 1; s < 7; ++s) {
+      acc = acc + p.b[s - 1] * k[s - 1];
+      C u = y;
+      if (s < 6) {
+#pragma unroll
+        for (int l = 0; l < s; ++l) u = u + (h * p.a[s][l]) * k[l];
+      } else {
+        u = u + h * acc;
+      }
+      k[s] = rhs(u);
+    }
+    C e = mk<R>(0, 0);
+#pragma unroll
+    for (int j = 0; j < 7; ++j) e = e + p.bt[j] * k[j];
+    e = h * e;
+    const C y1 = y + h * acc;
+    const double sc = p.atol + p.rtol * fmax(sqrt((double)cabs2(y)), sqrt((double)cabs2(y1)));
+    const int ok = ode_after(o, sqrt((double)cabs2(e)) / sc, dzd, &fin);
+    if (ok) {
+      y = y1;
+      k[0] = k[6];
+    } else {
+      ++rejects;
+    }
+    if (fin) break;
+  }
+  if (live) out[i] = y;
+  // counts: one atomic per warp
+  unsigned long long na = live ? (unsigned long long)o.attempts : 0ull, nr = rejects;
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    na += __shfl_xor_sync(0xffffffffu, na, d);
+    nr += __shfl_xor_sync(0xffffffffu, nr, d);
+  }
+  const unsigned gave_up = __ballot_sync(0xffffffffu, fin == 2);
+  if ((threadIdx.x & 31) == 0 && p.ctl) {
+    atomicAdd(&p.ctl->ode_attempts, na);
+    atomicAdd(&p.ctl->ode_rejects, nr);
+    if (gave_up) atomicOr(&p.ctl->flags, FIL_FLAG_ODE);
+  }
 }
 
 // Reductions of the XY field (FieldAnalyzers.jl:240-255): F = |E|^2 per

@@ -30,7 +30,12 @@ template <typename R> struct XyNlParams {
   typedef typename C2T<R>::type C;
   long n;                 // nx * ny
   int ny, ns;
-  R a[4][4], b[4];        // RK tableau
+  R a[7][6], b[7];        // explicit RK tableau (ns stages)
+  // Tsitouras 5(4) (tsit5.h): 1 one step of dz (ns = 6), 2 adaptive
+  // substeps per point (first same as last, bt = b - bhat)
+  int tsit;
+  R bt[7];
+  double atol, rtol;
   C c0;                   // i QZ(w0) Rnl_cubic(w0)
   const R* g1;            // field guard along x, y
   const R* g2;

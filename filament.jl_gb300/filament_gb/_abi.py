@@ -20,7 +20,7 @@ FIL_ERR_NOMEM = -7
 
 GEOM = {"R": 0, "T": 1, "RT": 2, "XY": 3, "XYT": 4}
 PREC = {"mixed": 0, "fp64": 1}
-ALG = {"RK2": 2, "RK3": 3, "RK4": 4}
+ALG = {"RK2": 2, "RK3": 3, "RK4": 4, "Tsit5": 5, "ATsit5": 6}
 
 RESP_CUBIC = 1
 RESP_FREE = 2
@@ -40,6 +40,8 @@ OPT_CLAMP_LAST_DZ = 3
 OPT_TIMING = 4
 OPT_ANALYTIC_PROJECTION = 5
 OPT_DHT_SIMT = 6
+OPT_ODE_RTOL = 7     # value = rtol x 1e12
+OPT_ODE_ATOL = 8     # value = atol x 1e12
 
 _dp = C.POINTER(C.c_double)
 
@@ -125,6 +127,7 @@ class Binding:
         self.analyze = fn("analyze", C.c_int, [vp, C.POINTER(fil_stats), _dp, _dp, _dp])
         self.get_stats = fn("get_stats", C.c_int, [vp, C.POINTER(fil_stats)])
         self.kernel_times = fn("kernel_times", C.c_int, [vp, _dp, C.c_int])
+        self.get_ode_stats = fn("get_ode_stats", C.c_int, [vp, C.POINTER(C.c_int64)])
 
     def check(self, h, code, what):
         if code < 0:

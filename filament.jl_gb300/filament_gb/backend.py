@@ -126,6 +126,13 @@ class Handle:
                   "kernel_times")
         return out
 
+    def ode_stats(self):
+        """ATsit5: (substep attempts, rejected attempts), summed over the
+        transverse points and steps."""
+        out = np.zeros(2, np.int64)
+        self._chk(self.b.get_ode_stats(self.h, out.ctypes.data_as(C.POINTER(C.c_int64))), "get_ode_stats")
+        return int(out[0]), int(out[1])
+
 
 def _batch_fns(lib):
     vp = C.c_void_p

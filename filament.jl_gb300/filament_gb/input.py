@@ -24,7 +24,7 @@ def _namespace(deck_dir):
         "math": math, "np": np, "pi": math.pi,
         "C0": constants.C0, "EPS0": constants.EPS0, "MU0": constants.MU0,
         "QE": constants.QE, "ME": constants.ME, "HBAR": constants.HBAR,
-        "RK2": "RK2", "RK3": "RK3", "RK4": "RK4",
+        "RK2": "RK2", "RK3": "RK3", "RK4": "RK4", "Tsit5": "Tsit5", "ATsit5": "ATsit5",
         "init_cubic": _responses.init_cubic,
         "init_current_free": _responses.init_current_free,
         "init_current_losses": _responses.init_current_losses,

@@ -70,6 +70,17 @@ extern "C" {
 #define FIL_ALG_RK2 2     /* midpoint                                       */
 #define FIL_ALG_RK3 3     /* Kutta third order                              */
 #define FIL_ALG_RK4 4     /* classic fourth order                           */
+/* Tsitouras 5(4) pair (Ch. Tsitouras, Comput. Math. Appl. 62 (2011) 770-775),
+ * nonlinear step only (input ALG), paraxial prefactor (QPARAXIAL = true):   */
+#define FIL_ALG_TSIT5 5   /* fifth order, one step of dz: six evaluations   */
+#define FIL_ALG_ATSIT5 6  /* the same pair with the embedded error estimate:
+                             substeps of [z, z + dz] chosen per transverse
+                             point (rows are independent ODE systems in the
+                             paraxial step), err = RMS over the point's
+                             spectrum of |e| / (atol + rtol max(|y0|, |y1|)),
+                             accept err <= 1, h <- h min(fmax, max(0.2,
+                             0.9 err^-1/5)), fmax 10 (1 after a rejection),
+                             first-same-as-last; see FIL_OPT_ODE_RTOL/ATOL */
 
 /* ---- nonlinear response channels (src/modules/medium_responses) --------- */
 #define FIL_RESP_CUBIC 1u   /* cubic.jl: F = Re(E)^3 or 3/4|E|^2 Re(E)       */
@@ -113,6 +124,12 @@ extern "C" {
                                   (spectral.jl:16-26; its Hankel transform
                                   covers the first Nt/2 columns).  RT only;
                                   XYT always projects.                     */
+#define FIL_OPT_ODE_RTOL 7     /* FIL_ALG_ATSIT5 relative tolerance, value =
+                                  rtol x 1e12 (default 1e9: rtol = 1e-3)   */
+#define FIL_OPT_ODE_ATOL 8     /* FIL_ALG_ATSIT5 absolute tolerance in the
+                                  units of the state (spectral amplitude in
+                                  T, RT, XYT; field in R, XY), value = atol x
+                                  1e12 (default 1e6: atol = 1e-6)          */
 
 typedef struct fil_config {
   int32_t abi_version;   /* FIL_ABI_VERSION                                  */
@@ -193,7 +210,9 @@ typedef struct fil_stats {
   int32_t status;   /* last stop reason / error code                         */
   int32_t flags;    /* device status bits: 1 NaN seen, 2 Istop, 4 Newton
                        iteration cap hit in the plasma scan; bits 8-15: the
-                       largest Newton iteration count of any plasma solve  */
+                       largest Newton iteration count of any plasma solve;
+                       8 an adaptive nonlinear step (FIL_ALG_ATSIT5) gave up
+                       after 256 attempts at one point                     */
 } fil_stats;
 
 typedef struct fil_handle fil_handle;
@@ -262,6 +281,11 @@ int fil_get_stats(fil_handle* h, fil_stats* st);
  * 4 whole step; ms[5] = number of timed steps; ms[6] = the surrogate
  * network's part of ms[0].                                                  */
 int fil_kernel_times(fil_handle* h, double* ms, int n);
+
+/* Adaptive nonlinear step (FIL_ALG_ATSIT5): counts since fil_create, summed
+ * over the transverse points and steps: out[0] substep attempts, out[1]
+ * rejected attempts.  Zero for the fixed-step methods.                     */
+int fil_get_ode_stats(fil_handle* h, int64_t out[2]);
 
 /* ---- linear propagator without device allocation ----------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

@@ -39,7 +39,14 @@
 //     exactly as the reference's full-array broadcast (spectral.jl:22).
 //   * Analytic spectrum (AnalyticSignals.rsig2aspec!): ifft, bin 0 kept,
 //     bins 1..Nt/2-1 doubled, bins Nt/2..Nt-1 zeroed.
-//   * RK tableaux (ODEIntegrators): RK2 midpoint, RK3 Kutta, RK4 classic.
+//   * RK tableaux (ODEIntegrators): RK2 midpoint, RK3 Kutta, RK4 classic;
+//     Tsit5 / ATsit5 as the published Tsitouras 5(4) pair (Comput. Math.
+//     Appl. 62 (2011) 770-775) with, for ATsit5, the textbook controller
+//     (Hairer-Norsett-Wanner I, II.4) per transverse point: RMS error norm
+//     over the point's analytic spectrum with atol + rtol max(|y0|, |y1|),
+//     factor 0.9 err^-1/5 clamped to [0.2, 10] (1 after a rejection),
+//     first same as last.  ODEIntegrators' own controller is not vendored:
+//     the adaptive form's step choices are parity-unpinned.
 //   * Rates (TabulatedFunctions): log-log linear interpolation, tfpower =
 //     segment slope; linterp = linear interpolation between time samples.
 //   * FFT sizes: powers of two.
@@ -107,9 +114,10 @@ static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 // ----------------------------------------------------------- RK tableaux --
 struct Tableau {
   int s;
-  double a[4][4];
-  double b[4];
-  double c[4];
+  double a[7][7];
+  double b[7];
+  double c[7];
+  double bt[7];   // b - bhat of an embedded pair (Tsitouras)
 };
 static Tableau tableau(int alg) {
   Tableau t;
@@ -125,6 +133,25 @@ static Tableau tableau(int alg) {
     t.a[2][0] = -1.0; t.a[2][1] = 2.0;
     t.b[0] = 1.0 / 6.0; t.b[1] = 4.0 / 6.0; t.b[2] = 1.0 / 6.0;
     t.c[1] = 0.5; t.c[2] = 1.0;
+  } else if (alg == FIL_ALG_TSIT5 || alg == FIL_ALG_ATSIT5) {   // Tsitouras 5(4)
+    static const double A[7][6] = {
+        {0, 0, 0, 0, 0, 0},
+        {0.161, 0, 0, 0, 0, 0},
+        {-0.008480655492356989, 0.335480655492357, 0, 0, 0, 0},
+        {2.897153057105493, -6.359448489975075, 4.3622954328695815, 0, 0, 0},
+        {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525, 0, 0},
+        {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383, 0},
+        {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}};
+    static const double BT[7] = {-0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
+                                 -0.1447110071732629, 0.5823571654525552, -0.45808210592918697, 1.0 / 66.0};
+    static const double C[7] = {0, 0.161, 0.327, 0.9, 0.9800255409045097, 1, 1};
+    t.s = 6;
+    for (int i = 0; i < 7; ++i) {
+      for (int j = 0; j < 6; ++j) t.a[i][j] = A[i][j];
+      t.c[i] = C[i];
+      t.bt[i] = BT[i];
+    }
+    for (int j = 0; j < 6; ++j) t.b[j] = A[6][j];
   } else {                           // classic RK4
     t.s = 4;
     t.a[1][0] = 0.5; t.a[2][1] = 0.5; t.a[3][2] = 1.0;
@@ -169,6 +196,8 @@ struct fil_handle {
   long steps = 0;
   double imax = 0, rhomax = 0;
   int status = 0;
+  double ode_atol = 1e-6, ode_rtol = 1e-3;   // ATsit5
+  long long ode_attempts = 0, ode_rejects = 0;
 };
 
 namespace {
@@ -569,7 +598,13 @@ void nl_rhs(fil_handle* h, const std::vector<cd>& U, std::vector<cd>& dE) {
   if (!h->cfg.qparaxial) nl_transverse(h, dE);
 }
 
+void nl_step_adaptive(fil_handle* h, std::vector<cd>& u, double dz);
+
 void nl_step(fil_handle* h, std::vector<cd>& u, double dz) {
+  if (h->cfg.alg == FIL_ALG_ATSIT5) {
+    nl_step_adaptive(h, u, dz);
+    return;
+  }
   const Tableau& T = h->tab_nl;
   size_t n = u.size();
   std::vector<std::vector<cd>> k(T.s, std::vector<cd>(n));
@@ -588,6 +623,105 @@ void nl_step(fil_handle* h, std::vector<cd>& u, double dz) {
     for (int s = 0; s < T.s; ++s)
       if (T.b[s] != 0.0) v += T.b[s] * k[s][i];
     u[i] += dz * v;
+  }
+}
+
+// ATsit5: every transverse point p (its nt values u[p nt ..]) integrates
+// [z, z + dz] in substeps of its own; all points advance attempt by attempt
+// together (the right-hand side is evaluated on the whole field, each point
+// with its own substep; points already done are carried along unchanged).
+// The error norm of a point runs over its first nh values (the analytic
+// half: the right-hand side is zero above).
+void nl_step_adaptive(fil_handle* h, std::vector<cd>& u, double dz) {
+  const Tableau& T = h->tab_nl;
+  const size_t n = u.size();
+  const long np = h->ntr;
+  const size_t row = n / (size_t)np;
+  const int nh = h->nh;
+  struct Pt { double hs, zdone; bool last, rejected, done; int attempts, rej; };
+  std::vector<Pt> pt(np, Pt{dz, 0.0, true, false, false, 0, 0});
+  std::vector<std::vector<cd>> k(7, std::vector<cd>(n));
+  std::vector<cd> U(n), acc(n);
+  nl_rhs(h, u, k[0]);
+  for (;;) {
+    bool any = false;
+    for (long p = 0; p < np; ++p) any = any || !pt[p].done;
+    if (!any) break;
+    for (size_t i = 0; i < n; ++i) acc[i] = T.b[0] * k[0][i];
+    for (int s = 1; s < 7; ++s) {
+      for (long p = 0; p < np; ++p) {
+        const double hp = pt[p].hs;
+        for (size_t i = (size_t)p * row; i < (size_t)(p + 1) * row; ++i) {
+          cd v = u[i];
+          if (s < 6)
+            for (int l = 0; l < s; ++l) v += (hp * T.a[s][l]) * k[l][i];
+          else
+            v += hp * acc[i];
+          U[i] = v;
+        }
+      }
+      nl_rhs(h, U, k[s]);
+      if (s < 6)
+        for (size_t i = 0; i < n; ++i) acc[i] += T.b[s] * k[s][i];
+    }
+    for (long p = 0; p < np; ++p) {
+      Pt& q = pt[p];
+      if (q.done) continue;
+      const double hp = q.hs;
+      double sum = 0;
+      for (int j = 0; j < nh; ++j) {
+        const size_t i = (size_t)p * row + j;
+        cd e = 0;
+        for (int l = 0; l < 7; ++l) e += T.bt[l] * k[l][i];
+        e = hp * e;
+        const cd y1 = u[i] + hp * acc[i];
+        const double a0 = std::sqrt(u[i].real() * u[i].real() + u[i].imag() * u[i].imag());
+        const double a1 = std::sqrt(y1.real() * y1.real() + y1.imag() * y1.imag());
+        const double r = std::sqrt(e.real() * e.real() + e.imag() * e.imag()) / (h->ode_atol + h->ode_rtol * std::max(a0, a1));
+        sum += r * r;
+      }
+      const double err = std::sqrt(sum / nh);
+      q.attempts += 1;
+      bool accept;
+      double fac = 1.0;
+      bool fin = false;
+      if (std::isnan(err)) {
+        accept = true;
+        fin = true;
+      } else if (err <= 1.0) {
+        accept = true;
+        q.zdone += hp;
+        if (q.last) {
+          fin = true;
+        } else {
+          fac = err > 0.0 ? 0.9 * std::pow(err, -0.2) : 10.0;
+          fac = std::max(std::min(fac, q.rejected ? 1.0 : 10.0), 0.2);
+          q.rejected = false;
+        }
+      } else {
+        accept = false;
+        fac = std::max(0.9 * std::pow(err, -0.2), 0.2);
+        q.rejected = true;
+        q.rej += 1;
+      }
+      if (accept)
+        for (size_t i = (size_t)p * row; i < (size_t)(p + 1) * row; ++i) {
+          u[i] = u[i] + hp * acc[i];
+          k[0][i] = k[6][i];
+        }
+      if (!fin) {
+        q.hs = hp * fac;
+        const double rem = dz - q.zdone;
+        q.last = q.hs >= rem;
+        if (q.last) q.hs = rem;
+        if (q.attempts >= 256) fin = true;
+      }
+      if (fin) {
+        q.done = true;
+        h->ode_attempts += q.attempts;
+        h->ode_rejects += q.rej;
+      }
+    }
   }
 }
 
@@ -666,7 +800,16 @@ int filo_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
     h->kfix = copyv(t->kfix, nc, 0.0);
     h->rlx = copyv(t->rate_lx, (size_t)nc * cfg->rate_n, 0.0);
     h->rly = copyv(t->rate_ly, (size_t)nc * cfg->rate_n, 0.0);
+    if (cfg->plasma_alg < FIL_ALG_RK2 || cfg->plasma_alg > FIL_ALG_RK4) {
+      delete h;
+      return fail(nullptr, FIL_ERR_UNSUPPORTED, "plasma ALG must be RK2, RK3 or RK4");
+    }
     h->tab_pl = tableau(cfg->plasma_alg);
+  }
+  if (cfg->alg < FIL_ALG_RK2 || cfg->alg > FIL_ALG_ATSIT5) { delete h; return fail(nullptr, FIL_ERR_ARG, "unknown ALG"); }
+  if (cfg->alg == FIL_ALG_ATSIT5 && cfg->nonlinearity && !cfg->qparaxial) {
+    delete h;   // the non-paraxial right-hand side couples the transverse points
+    return fail(nullptr, FIL_ERR_UNSUPPORTED, "ATsit5 with QPARAXIAL=false");
   }
   h->tab_nl = tableau(cfg->alg);
   if (h->has_t) h->pt.init(nt);
@@ -680,11 +823,20 @@ int filo_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
 
 int filo_destroy(fil_handle* h) { delete h; return FIL_OK; }
 
+int filo_get_ode_stats(fil_handle* h, int64_t out[2]) {
+  if (!h || !out) return fail(h, FIL_ERR_ARG, "null argument");
+  out[0] = h->ode_attempts;
+  out[1] = h->ode_rejects;
+  return FIL_OK;
+}
+
 int filo_set_option(fil_handle* h, int opt, int64_t v) {
   if (!h) return fail(nullptr, FIL_ERR_ARG, "null handle");
   if (opt == FIL_OPT_XYT_GUARD_BUGCOMPAT) h->bugcompat = v != 0;
   else if (opt == FIL_OPT_CLAMP_LAST_DZ) h->clamp_last = v != 0;
   else if (opt == FIL_OPT_ANALYTIC_PROJECTION) h->project = v != 0;
+  else if (opt == FIL_OPT_ODE_RTOL) h->ode_rtol = (double)v * 1e-12;
+  else if (opt == FIL_OPT_ODE_ATOL) h->ode_atol = (double)v * 1e-12;
   return FIL_OK;
 }
 
