@@ -338,7 +338,7 @@ def time_xyt(steps, warmup=3):
     return out
 
 
-def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1, dist=None):
+def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1, dist=None, oracle_members=8):
     """The 64-pulse parameter sweep: members drawn from `seed` (Nr from
     {256, 512, 1000}, Nt from {1024, 2048, 4096}, 2-10 Pcr, +-500 fs^2 chirp,
     w0 0.5-2 mm; RK4, adaptive dz, the workload's air model) in one batch,
@@ -346,7 +346,9 @@ def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1,
     batch steps, then `steps` batch steps timed on the host clock around
     fil_batch_run (the batch's ~3 GB state is far larger than L2).
     Accuracy: every member's field and fluence against the plain FP64 form
-    run alone from the same initial field to the same z (last dz clamped).
+    run alone from the same initial field to the same z (last dz clamped),
+    and the `oracle_members` cheapest members' fields against the FP64 CPU
+    oracle run to the same z.
     With world > 1 each rank runs its shard of the members on its own GPU
     (no exchange); the wall time and the error maxima are reduced by MAX
     over the ranks, the z-steps by SUM (strong scaling: the member set is
@@ -365,7 +367,7 @@ def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1,
            "l2": "batch state ~3 GB, larger than L2"}
     err = None
     sw = None
-    wall, taken, errs, ferrs, zs = 0.0, [], [], [], []
+    wall, taken, errs, ferrs, zs, oerrs = 0.0, [], [], [], [], []
     try:
         if params:
             t0 = time.perf_counter()
@@ -405,6 +407,21 @@ def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1,
                     ref.close()
                     errs.append(float(np.linalg.norm(E[i] - Ed) / np.linalg.norm(Ed)))
                     ferrs.append(float(np.linalg.norm(F[i] - Fd) / np.linalg.norm(Fd)))
+                # the FP64 CPU oracle (checker) on the cheapest members, at
+                # each member's own z_end
+                if oracle_members > 0:
+                    import oracle
+                    order = sorted(range(len(params)), key=lambda i: (sweep.step_cost(params[i]), i))
+                    t0 = time.perf_counter()
+                    for i in order[:oracle_members]:
+                        r = fg.Simulation(sweep.member_input(params[i]), binding=oracle.binding())
+                        r.handle.set_option(_abi.OPT_CLAMP_LAST_DZ, 1)
+                        r.handle.run(0.0, zs[i], 10 ** 6)
+                        Eo = r.handle.get_field()
+                        r.close()
+                        oerrs.append((mine[i], params[i]["Nr"], params[i]["Nt"],
+                                      float(np.linalg.norm(E[i] - Eo) / np.linalg.norm(Eo))))
+                    out["oracle_s"] = time.perf_counter() - t0
     except Exception as e:
         err = str(e)
     if sw is not None:
@@ -431,6 +448,10 @@ def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1,
         if world == 1:
             out["accuracy_vs_fp64"].update({"field_rel_l2_median": float(np.median(errs)),
                                             "z_end_min": min(zs), "z_end_max": max(zs)})
+        if oerrs:
+            out["accuracy_vs_oracle"] = {
+                "members": [{"member": m, "Nr": a, "Nt": b, "field_rel_l2": e} for m, a, b, e in oerrs],
+                "field_rel_l2_max": max(e for *_, e in oerrs)}
     return out
 
 
@@ -783,8 +804,9 @@ def main():
                      "dht_tensor": {"kernel": "k_dht_tc (tcgen05 kind::f16, 6 slice products), inverse transform",
                                     "achieved_tflops_f16": dht_tf,
                                     "ms_per_launch": surr["dht_inv_ms"]},
-                     "surrogate_tensor": {"kernels": "k_nn_l0_cl, 2 x k_nn_conv_tc (tcgen05 kind::f16 BF16), "
-                                                     "k_nn_l3_cl",
+                     "surrogate_tensor": {"kernels": "k_nn_conv_tc<0, 1> (layer 0 on CUDA cores + layer 1 on "
+                                                     "tcgen05 kind::f16 BF16), k_nn_conv_tc<1, 0> (layer 2 "
+                                                     "+ layer 3's per-tap partial sums)",
                                           "achieved_tflops_bf16": nn_tf, "peak_tflops_bf16": bf16,
                                           "frac": (nn_tf / bf16) if (nn_tf and bf16) else None}},
         "cpu_baseline": {"value": sps_cpu, "unit": "z-steps/s", "cores": os.cpu_count(), "kind": "port",

@@ -1041,6 +1041,18 @@ template <typename R> static int enqueue_reduce(fil_handle* h, double* power, in
   return 0;
 }
 
+// integral power spectrum (fil_analyze_spectrum): per-row |2 Sr N dt|^2,
+// then the weighted column sum
+template <typename R> static int enqueue_spectrum(fil_handle* h, double* S) {
+  RowParams<R> P = row_params<R>(h);
+  P.S_in = (const typename C2T<R>::type*)h->S;
+  const int nw = h->nt / 2 + 1;
+  R* tmp = (R*)h->stage;   // [nrows][nw] of the [nrows][nt] staging buffer
+  CK(launch_rowspec<R>(P, h->nt, tmp, h->st));
+  CK(launch_colsum<R>(tmp, h->pw, S, h->nrows, nw, h->st));
+  return 0;
+}
+
 static int zstep(fil_handle* h, bool timed) {
   return h->fp64 ? enqueue_zstep<double>(h, timed) : enqueue_zstep<float>(h, timed);
 }
@@ -1617,6 +1629,22 @@ int fil_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power, do
     st->flags = c.flags;
   }
   if (c.flags & FIL_FLAG_NAN) return fail(h, FIL_ERR_NAN, "non-finite field");
+  return FIL_OK;
+}
+
+int fil_analyze_spectrum(fil_handle* h, double* S, int nw) {
+  if (!h || !S) return fail(h, FIL_ERR_ARG, "null argument");
+  if (!h->field_set) return fail(h, FIL_ERR_STATE, "field not set");
+  if (h->geom != FIL_GEOM_RT && h->geom != FIL_GEOM_XYT && h->geom != FIL_GEOM_T)
+    return fail(h, FIL_ERR_UNSUPPORTED, "the integral spectrum needs a time axis");
+  if (nw != h->nt / 2 + 1) return fail(h, FIL_ERR_ARG, "nw must be nt/2 + 1");
+  double* d = h->power;   // [nt] >= nw doubles, recomputed by the next fil_analyze
+  CK(cudaMemsetAsync(d, 0, nw * sizeof(double), h->st));
+  int rc = h->fp64 ? enqueue_spectrum<double>(h, d) : enqueue_spectrum<float>(h, d);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(h->an_host, d, nw * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  std::memcpy(S, h->an_host, nw * sizeof(double));
   return FIL_OK;
 }
 

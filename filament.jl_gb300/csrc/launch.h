@@ -26,6 +26,8 @@ cudaError_t launch_rowreduce(const RowParams<R>& P, int n, double* fluence, R* I
 template <typename R>
 cudaError_t launch_colsum(const R* I, const double* w, double* power, int nrows, int nt, cudaStream_t st);
 template <typename R>
+cudaError_t launch_rowspec(const RowParams<R>& P, int n, R* out, cudaStream_t st);
+template <typename R>
 cudaError_t launch_field_in(const typename C2T<R>::type* E, typename C2T<R>::type* S, typename C2T<R>::type* U,
                             int ld, const typename C2T<R>::type* tw, int analytic, int nrows, int n,
                             cudaStream_t st);

@@ -3,8 +3,9 @@
 //
 //   layer 0 (3 -> 64)   CUDA cores, 1728 MAC per point, inside layer 1's kernel
 //   layer 1 (64 -> 64)  k_nn_conv_tc<false, true> tcgen05, 36864 MAC per point
-//   layer 2 (64 -> 64)  k_nn_conv_tc
-//   layer 3 (64 -> 1)   k_nn_l3_cl   CUDA cores, 576 MAC per point
+//   layer 2 (64 -> 64)  k_nn_conv_tc<true, false> tcgen05, 36864 MAC per point
+//   layer 3 (64 -> 1)   layer 2's epilogue (nine per-tap partial sums, 576
+//                       MAC per point), summed where the density is formed
 //
 // The 64 -> 64 convolution is an implicit GEMM per tile of 128 time points:
 //   Y[t][co] = sum_k sum_ci X[t + k - 4][ci] W_k[co][ci],
@@ -390,91 +391,6 @@ __global__ void __launch_bounds__(L0 ? NT_THREADS_L0 : NT_THREADS, 1)
   if (s_fail && tid == 0) atomicExch(p.err, 1);
 }
 
-// ---------------------------------------------------------------------------
-// Layer 0 (3 -> 64, tanh): x [rows][3][T] -> y [rows][T][64].  A block of
-// 128 threads takes one (row, 256-point tile) work item at a time (flat
-// index over rows x tiles, stride gridDim.x); each thread computes all 64
-// channels of two time points (tile + tid, tile + tid + 128): their 2 x 27
-// inputs in registers, the weights broadcast from shared memory as float4
-// (eight FMA per shared load).
-__global__ void __launch_bounds__(128) k_nn_l0_cl(const __nv_bfloat16* __restrict__ x,
-                                                  const __nv_bfloat16* __restrict__ w,   // [ci][k][co]
-                                                  const float* __restrict__ bias, __nv_bfloat16* y, int T,
-                                                  int maxrows, const int* count, const int* stop) {
-  constexpr int NTH = 128, TT = 2 * NTH, W2 = TT + NN_K - 1, NI = NN_IN * NN_K;
-  __shared__ float xs[NN_IN][W2];
-  __shared__ __align__(16) float ws[NI][64];
-  __shared__ __align__(16) float bs[64];
-  if (stop && *stop) return;
-  const int nb = count ? min(*count, maxrows) : maxrows;
-  const int tid = threadIdx.x;
-  for (int i = tid; i < NI * 64; i += NTH) ws[i / 64][i % 64] = __bfloat162float(w[i]);
-  if (tid < 64) bs[tid] = bias[tid];
-  const int tiles = (T + TT - 1) / TT;
-  for (int item = blockIdx.x; item < nb * tiles; item += gridDim.x) {
-    const int b = item / tiles, t0 = (item - b * tiles) * TT;
-    __syncthreads();
-    for (int i = tid; i < NN_IN * W2; i += NTH) {
-      const int ci = i / W2, j = i - ci * W2, tt = t0 + j - NN_HALF;
-      xs[ci][j] = (tt >= 0 && tt < T) ? __bfloat162float(x[((size_t)b * NN_IN + ci) * T + tt]) : 0.f;
-    }
-    __syncthreads();
-    float xa[NI], xb[NI];
-#pragma unroll
-    for (int ci = 0; ci < NN_IN; ++ci)
-#pragma unroll
-      for (int k = 0; k < NN_K; ++k) {
-        xa[ci * NN_K + k] = xs[ci][tid + k];
-        xb[ci * NN_K + k] = xs[ci][tid + NTH + k];
-      }
-    const int ta = t0 + tid, tb = ta + NTH;
-    uint4* da = reinterpret_cast<uint4*>(y + ((size_t)b * T + ta) * 64);
-    uint4* db = reinterpret_cast<uint4*>(y + ((size_t)b * T + tb) * 64);
-#pragma unroll 1
-    for (int g = 0; g < 8; ++g) {
-      const float4 c0 = reinterpret_cast<const float4*>(bs)[2 * g], c1 = reinterpret_cast<const float4*>(bs)[2 * g + 1];
-      float aa[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-      float ab[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-      // channel pairs in fma.rn.f32x2 (the same per-lane FMA sequence)
-      float2 a2[4], b2[4];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        a2[e] = make_float2(aa[2 * e], aa[2 * e + 1]);
-        b2[e] = make_float2(ab[2 * e], ab[2 * e + 1]);
-      }
-#pragma unroll
-      for (int i = 0; i < NI; ++i) {
-        const float4 w0 = reinterpret_cast<const float4*>(ws[i])[2 * g];
-        const float4 w1 = reinterpret_cast<const float4*>(ws[i])[2 * g + 1];
-        const float2 wv[4] = {make_float2(w0.x, w0.y), make_float2(w0.z, w0.w), make_float2(w1.x, w1.y),
-                              make_float2(w1.z, w1.w)};
-        const float2 xa2 = make_float2(xa[i], xa[i]), xb2 = make_float2(xb[i], xb[i]);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          a2[e] = fma2(wv[e], xa2, a2[e]);
-          b2[e] = fma2(wv[e], xb2, b2[e]);
-        }
-      }
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        aa[2 * e] = a2[e].x;
-        aa[2 * e + 1] = a2[e].y;
-        ab[2 * e] = b2[e].x;
-        ab[2 * e + 1] = b2[e].y;
-      }
-      uint32_t pa[4], pb[4];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const __nv_bfloat162 ha = __floats2bfloat162_rn(nt_tanh(aa[2 * e]), nt_tanh(aa[2 * e + 1]));
-        const __nv_bfloat162 hb = __floats2bfloat162_rn(nt_tanh(ab[2 * e]), nt_tanh(ab[2 * e + 1]));
-        pa[e] = *reinterpret_cast<const uint32_t*>(&ha);
-        pb[e] = *reinterpret_cast<const uint32_t*>(&hb);
-      }
-      if (ta < T) da[g] = make_uint4(pa[0], pa[1], pa[2], pa[3]);
-      if (tb < T) db[g] = make_uint4(pb[0], pb[1], pb[2], pb[3]);
-    }
-  }
-}
 
 // Network output from the layer-3 partial sums (the inference path outside
 // the row kernel): out[b][t] = b3 + sum_k P_k[t + k - 4].
@@ -506,24 +422,6 @@ int nn_weight_map(CUtensorMap* m, const __nv_bfloat16* wt) {
   const unsigned long long d[2] = {64ull, (unsigned long long)NN_K * 64ull};
   const unsigned box[2] = {64u, 64u};
   return tc_make_map_bf16(m, wt, 2, d, box);
-}
-
-cudaError_t nn_launch_l0_cl(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* y,
-                            int T, int maxrows, const int* count, const int* stop, cudaStream_t st) {
-  static int resident = 0;   // blocks per SM at this kernel's register and shared-memory use
-  if (!resident) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_nn_l0_cl, 128, 0);
-    if (e != cudaSuccess) return e;
-    resident = std::max(1, resident);
-  }
-  int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
-                                                cudaSuccess || sms < 1)
-    sms = 152;
-  const int tiles = (T + 255) / 256;
-  const int grid = std::max(1, std::min(maxrows * tiles, sms * resident));
-  k_nn_l0_cl<<<grid, 128, 0, st>>>(x, w, bias, y, T, maxrows, count, stop);
-  return cudaGetLastError();
 }
 
 cudaError_t nn_launch_out(const float* part, const float* b3, float* out, int T, int rows, cudaStream_t st) {

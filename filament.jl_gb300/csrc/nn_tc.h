@@ -26,9 +26,6 @@ int nn_plan_init(NnRowsPlan* p);
 // weights of one 64 -> 64 layer: W[k][co][ci] BF16 and its TMA map
 // {64, 9 * 64}, box {64, 64}
 int nn_weight_map(CUtensorMap* m, const __nv_bfloat16* wt);
-
-cudaError_t nn_launch_l0_cl(const __nv_bfloat16* x, const __nv_bfloat16* w, const float* bias, __nv_bfloat16* y,
-                            int T, int maxrows, const int* count, const int* stop, cudaStream_t st);
 // layer 1 (part == NULL: activations into out; with x0, w0, b0 layer 0 is
 // computed inside the kernel from the inputs x0 and tx is unused) or layer 2
 // with layer 3 applied in the epilogue (partial sums into part)

@@ -161,6 +161,26 @@ cudaError_t launch_rowreduce(const RowParams<R>& P, int n, double* fl, R* Iout, 
   return cudaErrorInvalidValue;
 }
 template <typename R>
+cudaError_t launch_rowspec(const RowParams<R>& P, int n, R* out, cudaStream_t st) {
+  size_t sm = 0;
+  switch (n) {
+#define FIL_ROWSPEC_CASE(NN)                                                                              \
+  case NN: {                                                                                              \
+    sm = x_smem<R, NN>();                                                                                 \
+    cudaError_t e = cudaFuncSetAttribute(k_rowspec<R, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
+    if (e != cudaSuccess) return e;                                                                       \
+    k_rowspec<R, NN><<<P.nrows, NN / 16, sm, st>>>(P, out);                                               \
+    return cudaGetLastError();                                                                            \
+  }
+    FIL_ROWSPEC_CASE(512)
+    FIL_ROWSPEC_CASE(1024)
+    FIL_ROWSPEC_CASE(2048)
+    FIL_ROWSPEC_CASE(4096)
+#undef FIL_ROWSPEC_CASE
+  }
+  return cudaErrorInvalidValue;
+}
+template <typename R>
 cudaError_t launch_colsum(const R* I, const double* w, double* power, int nrows, int nt, cudaStream_t st) {
   dim3 grid((nt + 255) / 256, (nrows + 63) / 64);
   k_colsum<R><<<grid, 256, 0, st>>>(I, w, power, nrows, nt);
@@ -263,6 +283,7 @@ cudaError_t launch_setdz(DevCtl* c, double z, double dz, cudaStream_t st) {
   template cudaError_t launch_np_combine<R>(const RowParams<R>&, int, cudaStream_t);                   \
   template cudaError_t launch_rowreduce<R>(const RowParams<R>&, int, double*, R*, int, cudaStream_t);   \
   template cudaError_t launch_colsum<R>(const R*, const double*, double*, int, int, cudaStream_t);       \
+  template cudaError_t launch_rowspec<R>(const RowParams<R>&, int, R*, cudaStream_t);                    \
   template cudaError_t launch_field_in<R>(const C2T<R>::type*, C2T<R>::type*, C2T<R>::type*, int,         \
                                           const C2T<R>::type*, int, int, int, cudaStream_t);             \
   template cudaError_t launch_field_out<R>(const RowParams<R>&, int, C2T<R>::type*, cudaStream_t);      \

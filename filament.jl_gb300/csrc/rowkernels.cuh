@@ -186,12 +186,21 @@ FIL_DEV void load_time_row(const RowParams<R>& P, typename C2T<R>::type* X, int 
 // plasma solve); the guarded lower half is in s0_park, the upper half (when
 // kept) in U_out.  Y is scratch and free again on return.
 template <typename R, int N>
+FIL_DEV void split_guard_row(const RowParams<R>& P, typename C2T<R>::type* X, typename C2T<R>::type* Y, int row);
+template <typename R, int N>
 FIL_DEV void load_time_row_split(const RowParams<R>& P, typename C2T<R>::type* X, typename C2T<R>::type* Y,
                                  int row) {
+  load_time_row<R, N>(P, X, row, false);
+  split_guard_row<R, N>(P, X, Y, row);
+}
+// The second half of load_time_row_split, on X = E(t) loaded without the
+// guard (k_rowstep calls the two halves itself so that its row load, and
+// the transform in it, is inlined once).
+template <typename R, int N>
+FIL_DEV void split_guard_row(const RowParams<R>& P, typename C2T<R>::type* X, typename C2T<R>::type* Y, int row) {
   typedef typename C2T<R>::type C;
   constexpr int T = N / 16, NH = N / 2, EW = NH / T;
   const int tid = threadIdx.x;
-  load_time_row<R, N>(P, X, row, false);
   int iy;
   const R gs = row_guard(P, row, &iy);
 #pragma unroll
@@ -704,8 +713,13 @@ FIL_DEV void stage_rhs(const RowParams<R>& P, typename C2T<R>::type* X, typename
     Y[pad16(j)] = mk<R>(g * (R)P.sf * ff, g * (R)P.sl * fl);
   }
   const bool plas = NC > 0 && (P.has_free || P.has_losses) && ych;
-  if (P.has_cubic || RAM) filfft::block_fft<C, N, +1>(X, P.tw);   // rsig2aspec!
-  if (plas) filfft::block_fft<C, N, +1>(Y, P.tw);
+  // rsig2aspec! of both buffers through one inlined transform (a second
+  // copy of its code would only compete for the instruction cache)
+#pragma unroll 1
+  for (int f = 0; f < 2; ++f) {
+    const bool on = f ? plas : (P.has_cubic || RAM);   // block-uniform
+    if (on) filfft::block_fft<C, N, +1>(f ? Y : X, P.tw);
+  }
   __syncthreads();
 #pragma unroll
   for (int m = 0; m < EW; ++m) {
@@ -826,8 +840,8 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   // spectrum to s0_park and U_out); the initial solve and the plasma-only
   // launch of a non-paraxial step only need g E(t)
   const bool split = mode == 0 && guard;
-  if (split) load_time_row_split<R, N>(P, X, Y, row);
-  else load_time_row<R, N>(P, X, row, guard);
+  load_time_row<R, N>(P, X, row, guard && !split);
+  if (split) split_guard_row<R, N>(P, X, Y, row);
   // largest |E|^2 of the row (the linear-only test below)
   R e2row = 0;
   if (!RAM && mode == 0 && P.nonlin && P.cc_max >= (R)0) {
@@ -1284,6 +1298,32 @@ __global__ void __launch_bounds__(N / 16) k_rowreduce(RowParams<R> P, double* fl
     __syncthreads();
     const int slot = s_slot;
     if (slot >= 0) nn_features<R, N>(P, X, P.nn_feat + (size_t)slot * 3 * N);
+  }
+}
+
+// Integral power spectrum (FieldAnalyzers.jl:180-197, 320-336), per row:
+// the field as the analyzer sees it (E(t), the pending field guard applied,
+// as k_rowreduce), its spectrum Sa = ifft(E) (FFTW's ifft, 1/N), the real
+// spectrum Sr = aspec2rspec(Sa) on the nw = N/2 + 1 bins of rfftfreq, and
+// out[row][k] = |2 Sr_k N dt|^2: with Sr_0 = Sa_0, Sr_k = Sa_k / 2 (0 < k <
+// N/2) and the Nyquist bin Sr_{N/2} = Sa_{N/2} as the state holds it,
+// 2 Sr_k N = c_k X_k, X = the unscaled +1 transform, c = 2, 1, ..., 1, 2.
+// k_colsum then forms S[k] = sum_row w_row out[row][k].
+template <typename R, int N>
+__global__ void __launch_bounds__(N / 16) k_rowspec(RowParams<R> P, R* out) {
+  typedef typename C2T<R>::type C;
+  constexpr int T = N / 16, NH = N / 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* X = reinterpret_cast<C*>(smem_raw);
+  const int row = blockIdx.x, tid = threadIdx.x;
+  load_time_row<R, N>(P, X, row, P.ctl->guard_pending != 0);
+  filfft::block_fft<C, N, +1>(X, P.tw);
+  const R dt = P.dt;
+  for (int k = tid; k <= NH; k += T) {
+    const C x = X[pad16(k)];
+    const R c = (k == 0 || k == NH) ? (R)2 : (R)1;
+    const R a = c * dt;
+    out[(size_t)row * (NH + 1) + k] = a * a * (x.x * x.x + x.y * x.y);
   }
 }
 

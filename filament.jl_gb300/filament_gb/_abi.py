@@ -128,6 +128,7 @@ class Binding:
         self.get_stats = fn("get_stats", C.c_int, [vp, C.POINTER(fil_stats)])
         self.kernel_times = fn("kernel_times", C.c_int, [vp, _dp, C.c_int])
         self.get_ode_stats = fn("get_ode_stats", C.c_int, [vp, C.POINTER(C.c_int64)])
+        self.analyze_spectrum = fn("analyze_spectrum", C.c_int, [vp, _dp, C.c_int])
 
     def check(self, h, code, what):
         if code < 0:

@@ -52,8 +52,10 @@ class FieldAnalyzer:
             self.rpl = 2 * radius(grid.r, rho_end)
             self.tau = radius(grid.t, P)
             self.W = d["energy"]
+            self.S = self.handle.spectrum()           # FieldAnalyzers.jl:180-197
         elif g == "XY":                                # FieldAnalyzers.jl:240-255
             I = F.reshape(grid.Nx, grid.Ny)
+            self.I = I
             ix, iy = np.unravel_index(np.argmax(I), I.shape)
             self.ax = radius(grid.x, I[:, iy])
             self.ay = radius(grid.y, I[ix, :])
@@ -67,4 +69,6 @@ class FieldAnalyzer:
             self.ax = radius(grid.x, Fxy[:, iy])
             self.ay = radius(grid.y, Fxy[ix, :])
             self.W = d["energy"]
+            self.rho = rho_end.reshape(grid.Nx, grid.Ny)
+            self.S = self.handle.spectrum()           # FieldAnalyzers.jl:320-336
         return self

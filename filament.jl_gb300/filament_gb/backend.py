@@ -126,6 +126,14 @@ class Handle:
                   "kernel_times")
         return out
 
+    def spectrum(self):
+        """Integral power spectrum S over the nt/2 + 1 bins of rfftfreq
+        (FieldAnalyzers.jl:180-197, 320-336)."""
+        nw = self.problem.config.nt // 2 + 1
+        out = np.zeros(nw)
+        self._chk(self.b.analyze_spectrum(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), nw), "analyze_spectrum")
+        return out
+
     def ode_stats(self):
         """ATsit5: (substep attempts, rejected attempts), summed over the
         transverse points and steps."""

@@ -19,7 +19,7 @@ from .constants import C0
 from .grids import Grid
 from .guards import Guard_build
 from .problem import Problem
-from .writeplots import PlotDAT
+from .writeplots import PlotDAT, PlotNPZ
 
 
 class Field:
@@ -107,7 +107,7 @@ def run(input, binding=None, precision="mixed", device_loop=False, write_files=T
         outdir=None):
     """Filament.run (Filament.jl:51-108).  Returns the Simulation."""
     sim = Simulation(input, binding, precision)
-    plotdat = None
+    plotdat = plotnpz = None
     if write_files:
         prefix = input["prefix"]
         base = outdir if outdir is not None else input.get("deck_dir", ".")
@@ -115,11 +115,19 @@ def run(input, binding=None, precision="mixed", device_loop=False, write_files=T
         os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
         plotdat = PlotDAT(path + "plot.dat", sim.geometry, sim.unit)
         plotdat.write(sim.analyzer)
-    main_loop(sim, plotdat, device_loop)
+        # plot.h5's content (Filament.jl:95-99): z-data every lam0/2, fields every dz_plothdf
+        plotnpz = PlotNPZ(path, sim.geometry, sim.unit, sim.z, input["dz_plothdf"],
+                          input["lam0"] / 2 / sim.unit.z)
+        plotnpz.write(sim.handle, sim.analyzer, sim.z)
+    try:
+        main_loop(sim, plotdat, device_loop, plotnpz)
+    finally:
+        if plotnpz is not None:
+            plotnpz.close()
     return sim
 
 
-def main_loop(sim, plotdat, device_loop=False):
+def main_loop(sim, plotdat, device_loop=False, plotnpz=None):
     """Filament.jl:111-184."""
     z = sim.z
     if device_loop:
@@ -128,6 +136,8 @@ def main_loop(sim, plotdat, device_loop=False):
         sim.analyzer.analyze(sim.z)
         if plotdat is not None:
             plotdat.write(sim.analyzer)
+        if plotnpz is not None:
+            plotnpz.write(sim.handle, sim.analyzer, sim.z)
         return code
     while z < sim.zmax:
         dz = sim.dzadaptive(sim.analyzer)
@@ -136,6 +146,8 @@ def main_loop(sim, plotdat, device_loop=False):
         sim.analyzer.analyze(z)
         if plotdat is not None:
             plotdat.write(sim.analyzer)
+        if plotnpz is not None:
+            plotnpz.write(sim.handle, sim.analyzer, z)
         if sim.analyzer.Imax > sim.Istop:
             break
     sim.z = z

@@ -1,6 +1,9 @@
 """plot.dat writer (src/modules/WritePlots.jl:18-216): three header lines
 (names, SI units, dimensionless unit values) and one row per analyzer call,
-every value as %18.12e."""
+every value as %18.12e.  PlotNPZ: the content of the reference's plot.h5
+(WritePlots.jl:218-507) in NumPy containers, there being no HDF5 library
+here: the z-data group as plot_zdata.npz and the field snapshots as
+plot_field_NNN.npy."""
 
 
 def fmt(x):
@@ -51,3 +54,71 @@ def read_dat(fname):
     """readdlm(fname, comments=true) equivalent: the numeric rows."""
     import numpy as np
     return np.loadtxt(fname, comments="#", ndmin=2)
+
+
+class PlotNPZ:
+    """WritePlots.PlotHDF (WritePlots.jl:218-368) without HDF5.  zdata
+    (every call with z >= znext_zdata, step dz_zdata = lam0/2/zu): z and,
+    RT: Fzr, rhozr, Fzt, iSzf; XYT: Fzxy, rhozxy, iSzf; XY: Izx, Izy (the
+    intensity through the grid centre), written to <prefix>plot_zdata.npz by
+    flush()/close().  Fields (z >= znext_field, step dz_plothdf, and not at
+    the previous z-data point): <prefix>plot_field_NNN.npy, Re(E) for RT and
+    XYT, E otherwise, with the z values in <prefix>plot_fields_z.npy."""
+
+    def __init__(self, prefix, geometry, unit, z, dz_field, dz_zdata):
+        import numpy as np
+        self.np = np
+        self.prefix = prefix
+        self.geometry = geometry
+        self.unit = unit
+        self.dz_field = dz_field
+        self.znext_field = z
+        self.zprev_field = None
+        self.ifield = 1
+        self.field_z = []
+        self.dz_zdata = dz_zdata
+        self.znext_zdata = z
+        self.zdata = {}
+
+    def write(self, handle, analyzer, z):
+        """WritePlots.writeHDF (WritePlots.jl:286-307)."""
+        if z != self.zprev_field and z >= self.znext_field:
+            E = handle.get_field()
+            if self.geometry in ("RT", "XYT"):
+                E = E.real
+            self.np.save("%splot_field_%03d.npy" % (self.prefix, self.ifield), E)
+            self.field_z.append(z)
+            self.np.save("%splot_fields_z.npy" % self.prefix, self.np.asarray(self.field_z))
+            self.ifield += 1
+            self.znext_field += self.dz_field
+        if z >= self.znext_zdata:
+            self._zdata(analyzer)
+            self.zprev_field = z
+            self.znext_zdata = z + self.dz_zdata
+
+    def _add(self, name, v):
+        self.zdata.setdefault(name, []).append(self.np.array(v, copy=True))
+
+    def _zdata(self, a):
+        g = self.geometry
+        self._add("z", a.z)
+        if g == "RT":
+            self._add("Fzr", a.Fr)
+            self._add("rhozr", a.rho)
+            self._add("Fzt", a.Ft)
+            self._add("iSzf", a.S)
+        elif g == "XYT":
+            self._add("Fzxy", a.Fxy)
+            self._add("rhozxy", a.rho)
+            self._add("iSzf", a.S)
+        elif g == "XY":
+            I = a.I
+            self._add("Izx", I[:, I.shape[1] // 2])
+            self._add("Izy", I[I.shape[0] // 2, :])
+
+    def flush(self):
+        if self.zdata:
+            self.np.savez("%splot_zdata.npz" % self.prefix,
+                          **{k: self.np.stack(v) for k, v in self.zdata.items()})
+
+    close = flush

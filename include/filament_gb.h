@@ -271,6 +271,14 @@ int fil_run(fil_handle* h, double z0, double zmax, int64_t nmax,
 int fil_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power,
                 double* rho_end);
 
+/* Integral power spectrum of the current field (FieldAnalyzers.jl:180-197
+ * RT, :320-336 XYT): S[k] = sum over the transverse points of
+ * w |2 Sr_k Nt dt|^2, Sr = aspec2rspec(ifft(E)) on the nw = Nt/2 + 1 bins of
+ * rfftfreq(Nt), w = 2 pi r dr (RT), dx dy (XYT), 1 (T).  Bin 0 and the
+ * Nyquist bin count twice (Sr_0 = Sa_0; the Nyquist bin as the state holds
+ * it), the others once (Sr_k = Sa_k / 2).  T, RT, XYT; nw = Nt/2 + 1. */
+int fil_analyze_spectrum(fil_handle* h, double* S, int nw);
+
 /* Current controller state without launching work beyond a copy. */
 int fil_get_stats(fil_handle* h, fil_stats* st);
 

@@ -1003,6 +1003,33 @@ int filo_analyze(fil_handle* h, fil_stats* st, double* fluence, double* power, d
   return FIL_OK;
 }
 
+// FieldAnalyzers.jl:180-197 (RT), :320-336 (XYT): S = sum_p w_p |2 Sr N dt|^2
+// over the rfftfreq bins, Sa = ifft(E_p), Sr = aspec2rspec(Sa): bin 0 and the
+// Nyquist bin as Sa holds them, the interior bins halved (AnalyticSignals is
+// not vendored: the Nyquist bin's treatment is unpinned).
+int filo_analyze_spectrum(fil_handle* h, double* S, int nw) {
+  if (!h || !S) return fail(h, FIL_ERR_ARG, "null argument");
+  if (!h->has_t) return fail(h, FIL_ERR_UNSUPPORTED, "the integral spectrum needs a time axis");
+  const int nt = h->nt, nh = nt / 2;
+  if (nw != nh + 1) return fail(h, FIL_ERR_ARG, "nw must be nt/2 + 1");
+  const double dt = h->cfg.dt;
+  std::vector<cd> x(nt), work(nt);
+  for (int k = 0; k < nw; ++k) S[k] = 0.0;
+  for (long p = 0; p < h->ntr; ++p) {
+    for (int j = 0; j < nt; ++j) x[j] = h->E[(size_t)p * nt + j];
+    h->pt.run(x.data(), 1, +1, work.data());   // ifft
+    double w = 1.0;
+    if (h->geom == FIL_GEOM_RT) w = 2.0 * M_PI * h->rdr[p];
+    else if (h->geom == FIL_GEOM_XYT) w = h->cfg.dxdy;
+    for (int k = 0; k < nw; ++k) {
+      const double half = (k == 0 || k == nh) ? 1.0 : 0.5;
+      const cd v = 2.0 * half * x[k] * (double)nt * dt;
+      S[k] += w * std::norm(v);
+    }
+  }
+  return FIL_OK;
+}
+
 int filo_kernel_times(fil_handle* h, double* ms, int n) {
   (void)h;
   for (int i = 0; i < n; ++i) ms[i] = 0;

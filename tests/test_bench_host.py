@@ -44,7 +44,7 @@ class _Sweep:
 
 
 class _Ref:
-    def __init__(self, inp, precision=None):
+    def __init__(self, inp, precision=None, binding=None):
         h = _Member()
         h.set_option = lambda *a: None
         h.run = lambda z0, zmax, nmax: (1, {})
@@ -62,13 +62,18 @@ def test_sweep_leg_reports_every_member(monkeypatch):
     from filament_gb import sweep
     monkeypatch.setattr(sweep, "Sweep", _Sweep)
     monkeypatch.setattr(fg, "Simulation", _Ref)
-    r = bench.time_sweep(n=6, steps=4, warmup=1)
-    assert "error" not in r
+    r = bench.time_sweep(n=6, steps=4, warmup=1, oracle_members=3)
+    assert "error" not in r, r.get("error")
     assert r["members"] == 6 and r["ranks"] == 1
     assert r["z_steps_total"] == 24 and r["status"] == [3] * 6
     assert r["tuner"]["branches"] == 2
     acc = r["accuracy_vs_fp64"]
     assert abs(acc["field_rel_l2_max"] - 1e-5) < 1e-9 and abs(acc["field_rel_l2_median"] - 1e-5) < 1e-9
+    # the three cheapest members against the (stand-in) oracle
+    oc = r["accuracy_vs_oracle"]
+    assert len(oc["members"]) == 3 and abs(oc["field_rel_l2_max"] - 1e-5) < 1e-9
+    costs = sorted(sweep.step_cost(p) for p in sweep.draw(6, 0))
+    assert sorted(sweep.step_cost(dict(Nr=m["Nr"], Nt=m["Nt"])) for m in oc["members"]) == costs[:3]
 
 
 def test_c1_leg_with_the_oracle_standing_in(monkeypatch, oracle_binding):

@@ -105,3 +105,28 @@ def test_batch_member_matches_oracle_loop(gpu_lib):
     assert stats[1]["steps"] == st_r["steps"]
     assert stats[1]["z"] == pytest.approx(st_r["z"], rel=1e-5)
     assert rel_l2(E, r.handle.get_field()) < 1e-4
+
+
+def test_every_member_matches_the_oracle_at_z_end(gpu_lib):
+    """The sweep's per-member accuracy against the FP64 oracle of the
+    reference's method (its loop: adaptive dz, plasma, RK4) at each
+    member's own end of a 0.1 m run on the device controller, past the
+    first adaptive-step reductions of the 25-60 Pcr members."""
+    import filament_gb as fg
+    import oracle
+    from filament_gb import sweep
+    sw = sweep.Sweep(MEMBERS, **SMALL)
+    try:
+        code, stats = sw.run(zmax=0.1, nmax=10 ** 6, z0=0.0)
+        E = sw.fields()
+    finally:
+        sw.close()
+    errs = []
+    for i, p in enumerate(MEMBERS):
+        r = fg.Simulation(sweep.member_input(p, **SMALL), binding=oracle.binding())
+        code_r, st_r = r.handle.run(0.0, 0.1, 10 ** 6)
+        assert code_r == 1 == stats[i]["status"] and stats[i]["steps"] == st_r["steps"]
+        errs.append(rel_l2(E[i], r.handle.get_field()))
+        r.close()
+    print("per-member field error against the oracle at z = 0.1 m:", ["%.2e" % e for e in errs])
+    assert max(errs) < 1e-4

@@ -51,12 +51,23 @@ def test_tsit5_steps(gpu_lib, geom, precision):
     g, r = pair(INPUTS[geom](ALG="Tsit5"), precision)
     step_both(g, r, 3, DZ[geom])
     Eg, Er = g.handle.get_field(), r.handle.get_field()
-    assert rel_l2(Eg, Er) < TOL[precision]
+    e = rel_l2(Eg, Er)
+    assert e < TOL[precision]
     assert g.handle.ode_stats() == (0, 0)
-    # the step differs from RK4's (the method is not silently RK4)
-    g4, r4 = pair(INPUTS[geom](ALG="RK4"), "fp64")
-    step_both(g4, r4, 3, DZ[geom])
-    assert rel_l2(r4.handle.get_field(), Er) > 1e3 * TOL["fp64"] or geom == "XYT"
+    if precision == "fp64" and geom != "XYT":
+        # the method is Tsitouras, not RK4: the FP64 field is far closer to
+        # the oracle's Tsit5 step than to its RK4 step (the two methods
+        # differ by ~1e-10 here, the forms by ~1e-13)
+        import filament_gb as fg
+        import oracle
+        r4 = fg.Simulation(INPUTS[geom](ALG="RK4"), binding=oracle.binding())
+        z = 0.0
+        for _ in range(3):
+            z += DZ[geom]
+            r4.handle.step(z, DZ[geom])
+        d4 = rel_l2(Eg, r4.handle.get_field())
+        print("%s: Tsit5 GPU vs oracle Tsit5 %.2e, vs oracle RK4 %.2e" % (geom, e, d4))
+        assert d4 > 10 * e
 
 
 # (geometry, dz, steps, field scale, rtol = atol) per precision; the FP64
