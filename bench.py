@@ -338,6 +338,20 @@ def time_xyt(steps, warmup=3):
     return out
 
 
+def _oracle_module():
+    """oracle/oracle.py (the FP64 CPU checker), imported by file: the repo
+    root's oracle/ directory would otherwise shadow it as a namespace
+    package."""
+    d = os.path.join(ROOT, "oracle")
+    if d not in sys.path:
+        sys.path.insert(0, d)
+    mod = sys.modules.get("oracle")
+    if mod is not None and not hasattr(mod, "binding"):
+        del sys.modules["oracle"]
+    import oracle
+    return oracle
+
+
 def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1, dist=None, oracle_members=8):
     """The 64-pulse parameter sweep: members drawn from `seed` (Nr from
     {256, 512, 1000}, Nt from {1024, 2048, 4096}, 2-10 Pcr, +-500 fs^2 chirp,
@@ -410,7 +424,7 @@ def time_sweep(n=64, seed=0, steps=40, warmup=3, accuracy=True, rank=0, world=1,
                 # the FP64 CPU oracle (checker) on the cheapest members, at
                 # each member's own z_end
                 if oracle_members > 0:
-                    import oracle
+                    oracle = _oracle_module()
                     order = sorted(range(len(params)), key=lambda i: (sweep.step_cost(params[i]), i))
                     t0 = time.perf_counter()
                     for i in order[:oracle_members]:
@@ -479,8 +493,7 @@ def accuracy_run(zend, nmax, net=None, oracle_check=True, zs=ACCURACY_ZS):
                 "fluence_rel_l2": float(np.linalg.norm(Fa - Fb) / np.linalg.norm(Fb))}
     for prec in forms:
         if prec == "oracle":
-            sys.path.insert(0, os.path.join(ROOT, "oracle"))
-            import oracle
+            oracle = _oracle_module()
             sim = fg.Simulation(inp, binding=oracle.binding())
         else:
             sim = fg.Simulation(inp, precision="fp64" if prec == "fp64" else "mixed")
@@ -562,8 +575,7 @@ def time_c1(cpu_steps=300):
     all host cores, `cpu_steps` steps from z = 0 (a bounded sample)."""
     import numpy as np
     import filament_gb as fg
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
+    oracle = _oracle_module()
     inp = fg.prepare(DECK)
     out = {"workload": "RT 256x1024, 3 Pcr, RK2, dz = 1 mm fixed, z = 0..1 m"}
     fields = {}
@@ -595,8 +607,7 @@ def time_c1(cpu_steps=300):
 
 def cpu_oracle(steps):
     import filament_gb as fg
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
+    oracle = _oracle_module()
     inp = _prepare()
     sim = fg.Simulation(inp, binding=oracle.binding())
     t0 = time.perf_counter()

@@ -43,6 +43,20 @@ analyze(h, F, P, rho_end) = ccall((:fil_analyze, LIB), Cint,
     (Ptr{Cvoid}, Ptr{FilStats}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), h, C_NULL, F, P, rho_end)
 get_field!(h, E::Array{ComplexF64}) =
     ccall((:fil_get_field, LIB), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}, Cint, Cint), h, E, 1, 0)
+# FieldAnalyzers.jl:180-197 / 320-336: the integral power spectrum S (Nt/2 + 1 bins)
+function spectrum(h, nt)
+    S = zeros(nt ÷ 2 + 1)
+    ccall((:fil_analyze_spectrum, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}, Cint), h, S, length(S))
+    return S
+end
+# ALG = Tsit5() / ATsit5(): FIL_ALG_TSIT5 = 5, FIL_ALG_ATSIT5 = 6 in FilConfig.alg;
+# ATsit5 tolerances (option 7 rtol, 8 atol, value = tol * 1e12) and substep counts
+set_option(h, opt, value) = ccall((:fil_set_option, LIB), Cint, (Ptr{Cvoid}, Cint, Int64), h, opt, value)
+function ode_stats(h)
+    out = zeros(Int64, 2)
+    ccall((:fil_get_ode_stats, LIB), Cint, (Ptr{Cvoid}, Ptr{Int64}), h, out)
+    return out[1], out[2]
+end
 
 # batched sweep: members on uneven grids, one CUDA graph per z-step
 function create_batch(cfgs::Vector{FilConfig}, tabs::Vector{FilTables})

@@ -54,10 +54,12 @@ def test_tsit5_steps(gpu_lib, geom, precision):
     e = rel_l2(Eg, Er)
     assert e < TOL[precision]
     assert g.handle.ode_stats() == (0, 0)
-    if precision == "fp64" and geom != "XYT":
+    if precision == "fp64" and geom in ("T", "R"):
         # the method is Tsitouras, not RK4: the FP64 field is far closer to
-        # the oracle's Tsit5 step than to its RK4 step (the two methods
-        # differ by ~1e-10 here, the forms by ~1e-13)
+        # the oracle's Tsit5 step than to its RK4 step (T: the row kernel's
+        # variant, the methods differ by 8e-6; R: the pointwise kernel,
+        # 2e-10; in RT, XY and XYT the steps are too small to tell them apart
+        # at FP64 resolution)
         import filament_gb as fg
         import oracle
         r4 = fg.Simulation(INPUTS[geom](ALG="RK4"), binding=oracle.binding())
