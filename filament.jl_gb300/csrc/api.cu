@@ -1713,6 +1713,7 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
   arm_surrogate(h, c);
   CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
   CK(cudaStreamSynchronize(h->st));
+  h->gen += 1;   // a batch holding this handle rebuilds its graph
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -1882,7 +1883,6 @@ static int batch_check_members(fil_batch* b) {
   for (size_t i = 0; i < b->m.size(); ++i) {
     fil_handle* h = b->m[i];
     if (!h->field_set) return bfail(b, FIL_ERR_STATE, "member " + std::to_string(i) + ": field not set");
-    if (h->nn) return bfail(b, FIL_ERR_UNSUPPORTED, "member " + std::to_string(i) + ": surrogate armed (not batched)");
   }
   return 0;
 }

@@ -130,3 +130,35 @@ def test_every_member_matches_the_oracle_at_z_end(gpu_lib):
         r.close()
     print("per-member field error against the oracle at z = 0.1 m:", ["%.2e" % e for e in errs])
     assert max(errs) < 1e-4
+
+
+def test_member_with_the_surrogate_matches_its_single_run(gpu_lib):
+    """A member may arm the learned surrogate (its network kernels run on
+    the member's own buffers inside the batch graph): its batch run equals
+    the same problem armed and run alone, and the unarmed member equals its
+    plain single run."""
+    import filament_gb as fg
+    from filament_gb import surrogate as S
+    from filament_gb import sweep
+    p0, p1 = MEMBERS[0], MEMBERS[1]
+    net = S.Surrogate(p1["Nt"], seed=2)   # untrained: the g = 0 closed form
+    zmax, nmax = 0.05, 30
+    single = fg.Simulation(sweep.member_input(p1, **SMALL))
+    net.arm(single.handle, every=5, tol=1.0)
+    code_s, st_s = single.handle.run(0.0, zmax, nmax)
+    E1 = single.handle.get_field()
+    used_single = S.stats(single.handle)["steps_used"]
+    single.close()
+    _, _, E0 = _single(p0, False, zmax, nmax)
+    sw = sweep.Sweep([p0, p1], **SMALL)
+    try:
+        net.arm(sw.batch.members[1], every=5, tol=1.0)
+        code, stats = sw.run(zmax=zmax, nmax=nmax, z0=0.0)
+        E = sw.fields()
+        used = S.stats(sw.batch.members[1])["steps_used"]
+    finally:
+        sw.close()
+    net.close()
+    assert used == used_single > 0
+    assert stats[1]["steps"] == st_s["steps"]
+    assert rel_l2(E[1], E1) < 1e-12 and rel_l2(E[0], E0) < 1e-12
