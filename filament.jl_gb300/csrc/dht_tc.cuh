@@ -19,15 +19,15 @@
 // two from the row maximum of A, qb_cj one from the maximum of column j over
 // the 64-wide K chunk c.  All slices are exact FP16 values.  Over one chunk
 // the head sum sum_k a0 b0 is an integer below 2^23, which the tensor core
-// computes exactly.  The four correction products
-// a0 b1 + a1 b0 + a1 b1 + a0 b2 (together below 2^-8 of the head) go to a
-// second accumulator, whose round-toward-zero error is ~2^-28 of the
-// result.  Dropped: a2 b0, below 2^-22 of the head term (|a2| <= 2^-12
-// against |a0| <= 1024; a rounding residual of either sign, so no bias, at
-// the level of the FP32 accumulation itself), and a1 b2, a2 b1, a2 b2, below
-// 2^-29.  The a2 slice is therefore never loaded.  The consumer warps add
-// each chunk's two accumulators times qb_cj into FP32 registers (round to
-// nearest) and apply qa_i in the epilogue.
+// computes exactly.  The five correction products
+// a0 b1 + a1 b0 + a1 b1 + a0 b2 + a2 b0 (together below 2^-8 of the head) go
+// to a second accumulator, whose round-toward-zero error is ~2^-28 of the
+// result; the dropped products a1 b2, a2 b1, a2 b2 are below 2^-29.  (Also
+// dropping a2 b0, below 2^-22 of the head, made the transforms 3-6% faster
+// but raised the 1000 x 4096 workload's field error against the FP64 oracle
+// at z = 2.1 m from 3.1e-5 to 4.0e-5: the filament amplifies it.)  The
+// consumer warps add each chunk's two accumulators times qb_cj into FP32
+// registers (round to nearest) and apply qa_i in the epilogue.
 //
 // k_slice cuts the FP32 operand B (written by the row kernel) into its
 // slices and chunk scales once, so the GEMM streams FP16 tiles with TMA
@@ -36,7 +36,7 @@
 //
 // GEMM roles (320 threads): warps 0-7 drain the accumulators and run the
 // epilogue; warp 8 issues the TMA loads; warp 9 issues the MMAs.  Tile
-// 128 x 128, K stage 32 (five stages of five 8 KB slice tiles, 64-byte
+// 128 x 128, K stage 32 (four stages of six 8 KB slice tiles, 64-byte
 // swizzle), accumulation chunk 64, two accumulator pairs in 512
 // tensor-memory columns (ping-pong between chunks).  Every mbarrier wait is
 // bounded and also gives up once another role has failed; a failure sets
@@ -51,11 +51,11 @@
 #define TC_BN 128
 #define TC_BK 32                               // K per shared-memory stage
 #define TC_CHUNK 64                            // K per exact chunk (scale block of B)
-#define TC_STAGES 5
+#define TC_STAGES 4
 #define TC_CONSUMERS 256
 #define TC_THREADS (TC_CONSUMERS + 64)
 #define TC_SLICE_BYTES (TC_BM * TC_BK * 2)     // one FP16 slice tile, 64-byte swizzle
-#define TC_STAGE_BYTES (5 * TC_SLICE_BYTES)   // a0, a1, b0, b1, b2
+#define TC_STAGE_BYTES (6 * TC_SLICE_BYTES)   // a0, a1, a2, b0, b1, b2
 #define TC_SMEM_BYTES (TC_STAGES * TC_STAGE_BYTES + 1024 + 256)
 #define TC_WAIT_LIMIT (1u << 26)
 #define TC_OFF_A(s) ((s) * TC_SLICE_BYTES)
@@ -70,7 +70,7 @@
 #define TC_BAR_SLOT (8u * (2 * TC_STAGES + 5))
 static_assert(TC_BAR_SLOT + 4 <= 256, "k_dht_tc barrier block overflows its 256 bytes");
 static_assert(TC_STAGE_BYTES % 1024 == 0, "stage pitch keeps the 1024-byte alignment of the slices");
-#define TC_OFF_B(s) ((2 + (s)) * TC_SLICE_BYTES)
+#define TC_OFF_B(s) ((3 + (s)) * TC_SLICE_BYTES)
 
 // bounded wait that also stops when *fail is set by another role
 __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile int* fail) {
@@ -280,6 +280,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc::mbar_expect_tx(full_bar(s), TC_STAGE_BYTES);
         tc::tma_load_2d(st + TC_OFF_A(0), &tA0, kb * TC_BK, bm, full_bar(s));
         tc::tma_load_2d(st + TC_OFF_A(1), &tA1, kb * TC_BK, bm, full_bar(s));
+        tc::tma_load_2d(st + TC_OFF_A(2), &tA2, kb * TC_BK, bm, full_bar(s));
         tc::tma_load_2d(st + TC_OFF_B(0), &tB0, kb * TC_BK, bn, full_bar(s));
         tc::tma_load_2d(st + TC_OFF_B(1), &tB1, kb * TC_BK, bn, full_bar(s));
         tc::tma_load_2d(st + TC_OFF_B(2), &tB2, kb * TC_BK, bn, full_bar(s));
@@ -304,7 +305,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
         for (int kk = 0; kk < TC_BK / 16; ++kk) {
           const uint32_t ko = (uint32_t)(kk * 32);   // 16 FP16 = 32 bytes
-          const uint64_t a0 = tc::desc_k64(st + TC_OFF_A(0) + ko), a1 = tc::desc_k64(st + TC_OFF_A(1) + ko);
+          const uint64_t a0 = tc::desc_k64(st + TC_OFF_A(0) + ko), a1 = tc::desc_k64(st + TC_OFF_A(1) + ko),
+                         a2 = tc::desc_k64(st + TC_OFF_A(2) + ko);
           const uint64_t b0 = tc::desc_k64(st + TC_OFF_B(0) + ko), b1 = tc::desc_k64(st + TC_OFF_B(1) + ko),
                          b2 = tc::desc_k64(st + TC_OFF_B(2) + ko);
           const uint32_t accum = (first && kk == 0) ? 0u : 1u;
@@ -313,6 +315,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           tc::mma_f16(small, a1, b0, idesc, 1);
           tc::mma_f16(small, a1, b1, idesc, 1);
           tc::mma_f16(small, a0, b2, idesc, 1);
+          tc::mma_f16(small, a2, b0, idesc, 1);
         }
         tc::mma_commit(empty_bar(s));
         if (!first) tc::mma_commit(accf_bar(b));
