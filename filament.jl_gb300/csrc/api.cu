@@ -1879,6 +1879,10 @@ static int batch_build_graph(fil_batch* b) {
   return 0;
 }
 
+// Members may arm the learned surrogate: its tensor-core network kernels and
+// k_dht_tc both allocate tensor memory and the branches run concurrently,
+// but a CTA of either kernel takes more than half of an SM's shared memory,
+// so no two of them are resident on one SM together.
 static int batch_check_members(fil_batch* b) {
   for (size_t i = 0; i < b->m.size(); ++i) {
     fil_handle* h = b->m[i];
