@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
 // ---------------------------------------------------------------------------
 // Layers 0 and 1, both on the tensor cores (the network's first launch).
 // Per tile of 128 time points t0 .. t0 + 127 of a row:
-//   im2col (warps 10-13): A0[r][kk] = x[ci][t0 - 8 + r + k] for kk = 9 ci + k
+//   im2col (warps 14-17): A0[r][kk] = x[ci][t0 - 8 + r + k] for kk = 9 ci + k
 //     < 27 (zero for kk = 27 .. 31 and for times outside [0, T), layer 0's
 //     "same" padding), r = 0 .. 135 the 136 halo rows of layer 1; BF16 rows of
 //     128 B in the 128-byte swizzle (only the first 64 bytes are read), two
@@ -306,16 +306,17 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
 //     layer-0 products of tile i + 1 are issued before layer 1's of tile i.
 //     Layer 1 as in k_nn_conv_tc: nine taps, each a 128-byte row shift into
 //     the halo tile.
-//   layer-0 epilogue (warps 6-9, one per tensor-memory lane quadrant): bias,
-//     tanh, BF16 of row r = lane + 32 q (the quadrant-3 warp also rows 128 ..
-//     135 from the second product's lanes 120 .. 127), zero where t0 - 4 + r
-//     is outside [0, T) (layer 1's padding), written into the layer-1 stage
-//     in the 128-byte swizzle; proxy fence; arrive on the stage's barrier.
+//   layer-0 epilogue (warps 6-13, two per tensor-memory lane quadrant q, one
+//     per half of the channels): bias, tanh, BF16 of row r = lane + 32 q (the
+//     quadrant-3 warps also rows 128 .. 135 from the second product's lanes
+//     120 .. 127), zero where t0 - 4 + r is outside [0, T) (layer 1's
+//     padding), written into the layer-1 stage in the 128-byte swizzle; proxy
+//     fence; arrive on the stage's barrier.
 //   layer-1 epilogue (warps 0-3) and the layer-1 weights (warp 4): as in
 //   k_nn_conv_tc.
 // Every wait is bounded and gives up once another role failed.
 #define L1_STAGES 5
-#define L01_WARPS 14
+#define L01_WARPS 18
 #define L01_THREADS (32 * L01_WARPS)
 #define L01_A0_BYTES (NT_HALO * 128)                         // 17408, a multiple of 1024
 #define L01_A_OFF (NN_K * NT_W_BYTES)                         // layer-1 stages
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
   if (warp == 0) tc::tmem_alloc(tmem_slot, 512);
   if (tid == 0) {
     for (int s = 0; s < L1_STAGES; ++s) {
-      tc::mbar_init(full_bar(s), 128);
+      tc::mbar_init(full_bar(s), 256);
       tc::mbar_init(empty_bar(s), 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -396,7 +397,7 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
       tc::mbar_init(acce_bar(b), 4);
       tc::mbar_init(a0f_bar(b), 128);
       tc::mbar_init(c0f_bar(b), 1);
-      tc::mbar_init(c0e_bar(b), 4);
+      tc::mbar_init(c0e_bar(b), 8);
     }
     tc::mbar_init(wbar, 1);
     tc::mbar_init(done_bar, 1);
@@ -467,12 +468,12 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
       tc::mma_commit(done_bar);
       tc::mbar_wait(done_bar, 0, NT_WAIT_LIMIT);
     }
-  } else if (warp >= 10) {
+  } else if (warp >= 14) {
     // ---------------- im2col of layer 0's input.  Lane l writes the BF16
     // pair kk = 2 (l mod 16), + 1 (fixed channel and tap offsets) of the rows
     // 34 w + (l / 16) + 2 m of its warp's 34; the next tile's window is
     // loaded into registers while this tile's rows are written.
-    const int w = warp - 10;
+    const int w = warp - 14;
     uint16_t* xw = reinterpret_cast<uint16_t*>(gbase + L01_XW_OFF) + w * NN_IN * L01_XW;
     const uint16_t* x0 = reinterpret_cast<const uint16_t*>(p.x0);
     const int pr = lane & 15, r1 = lane >> 4;
@@ -519,15 +520,17 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
       nt_arrive(a0f_bar(b));
     }
   } else if (warp >= 6) {
-    // ---------------- layer-0 epilogue into the layer-1 stages
-    const int q = warp & 3;
-    // one row of 64 layer-0 outputs (accumulator columns c0 .. c0 + 63 of
-    // this lane) -> row r of stage st, 16-byte chunk j at j ^ (r & 7)
-    auto put_row = [&](uint8_t* st, int r, int tau, const uint32_t (&v0)[32], const uint32_t (&v1)[32]) {
+    // ---------------- layer-0 epilogue into the layer-1 stages: warps
+    // 6-13, two per tensor-memory lane quadrant q, warp half h taking the
+    // channels 32 h .. 32 h + 31 (16-byte chunks 4 h .. 4 h + 3 of a row)
+    const int q = warp & 3, h = (warp - 6) >> 2;
+    // 32 layer-0 outputs of one row (accumulator columns of this warp's
+    // half) -> row r of stage st, 16-byte chunk j at j ^ (r & 7)
+    auto put_row = [&](uint8_t* st, int r, int tau, const uint32_t (&v)[32]) {
       const bool in = tau >= 0 && tau < p.T;
-      const float4* bv = reinterpret_cast<const float4*>(s_b0);
+      const float4* bv = reinterpret_cast<const float4*>(s_b0 + 32 * h);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
+      for (int j = 0; j < 4; ++j) {
         uint32_t pk[4] = {0u, 0u, 0u, 0u};
         if (in) {
           const float4 b0 = bv[2 * j], b1 = bv[2 * j + 1];
@@ -535,13 +538,12 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             const int c = 8 * j + 2 * e;
-            const float x0v = __uint_as_float(c < 32 ? v0[c] : v1[c - 32]) + bb[2 * e];
-            const float x1v = __uint_as_float(c + 1 < 32 ? v0[c + 1] : v1[c + 1 - 32]) + bb[2 * e + 1];
-            const __nv_bfloat162 h = __floats2bfloat162_rn(nt_tanh(x0v), nt_tanh(x1v));
-            pk[e] = *reinterpret_cast<const uint32_t*>(&h);
+            const __nv_bfloat162 hv = __floats2bfloat162_rn(nt_tanh(__uint_as_float(v[c]) + bb[2 * e]),
+                                                            nt_tanh(__uint_as_float(v[c + 1]) + bb[2 * e + 1]));
+            pk[e] = *reinterpret_cast<const uint32_t*>(&hv);
           }
         }
-        *reinterpret_cast<uint4*>(st + r * 128 + ((j ^ (r & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        *reinterpret_cast<uint4*>(st + r * 128 + (((4 * h + j) ^ (r & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     };
     for (int i = 0; i < ntl; ++i) {
@@ -551,24 +553,20 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
       int row, t0;
       tile_of(i, &row, &t0);
       (void)row;
-      const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + 128u + 128u * b;
-      uint32_t r0[32], r1[32];
-      tc::tmem_ld32_async(taddr, r0);
-      tc::tmem_ld32_async(taddr + 32u, r1);
-      tc::tmem_wait_ld(r0);
-      tc::tmem_wait_ld(r1);
+      const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + 128u + 128u * b + 32u * h;
+      uint32_t v[32];
+      tc::tmem_ld32_async(taddr, v);
+      tc::tmem_wait_ld(v);
       const int s = i % L1_STAGES, use = i / L1_STAGES;
       if (use > 0 && !nt_wait(empty_bar(s), (use - 1) & 1, &s_fail)) break;
       uint8_t* st = gbase + L01_A_OFF + s * NT_A_STRIDE;
       const int r = 32 * q + lane;
-      put_row(st, r, t0 - NN_HALF + r, r0, r1);
+      put_row(st, r, t0 - NN_HALF + r, v);
       if (q == 3) {
         // rows 128 .. 135: the second product's rows 8 + l, lanes l = 120 .. 127
-        tc::tmem_ld32_async(taddr + 64u, r0);
-        tc::tmem_ld32_async(taddr + 96u, r1);
-        tc::tmem_wait_ld(r0);
-        tc::tmem_wait_ld(r1);
-        if (lane >= 24) put_row(st, 104 + lane, t0 - NN_HALF + 104 + lane, r0, r1);
+        tc::tmem_ld32_async(taddr + 64u, v);
+        tc::tmem_wait_ld(v);
+        if (lane >= 24) put_row(st, 104 + lane, t0 - NN_HALF + 104 + lane, v);
       }
       tc::tc_fence_before();
       __syncwarp();
