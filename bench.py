@@ -815,9 +815,9 @@ def main():
                      "dht_tensor": {"kernel": "k_dht_tc (tcgen05 kind::f16, 6 slice products), inverse transform",
                                     "achieved_tflops_f16": dht_tf,
                                     "ms_per_launch": surr["dht_inv_ms"]},
-                     "surrogate_tensor": {"kernels": "k_nn_conv_tc<0, 1> (layer 0 on CUDA cores + layer 1 on "
-                                                     "tcgen05 kind::f16 BF16), k_nn_conv_tc<1, 0> (layer 2 "
-                                                     "+ layer 3's per-tap partial sums)",
+                     "surrogate_tensor": {"kernels": "k_nn_l01_tc (layers 0 and 1 on tcgen05 kind::f16 BF16), "
+                                                     "k_nn_conv_tc<1> (layer 2 + layer 3's per-tap partial "
+                                                     "sums)",
                                           "achieved_tflops_bf16": nn_tf, "peak_tflops_bf16": bf16,
                                           "frac": (nn_tf / bf16) if (nn_tf and bf16) else None}},
         "cpu_baseline": {"value": sps_cpu, "unit": "z-steps/s", "cores": os.cpu_count(), "kind": "port",
