@@ -300,15 +300,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const bool first = (kb & 1) == 0;
         if (first && (c >> 1) > 0 && !tc_wait(acce_bar(b), ((c >> 1) - 1) & 1, &s_fail)) break;
         tc::tc_fence_after();
-        const uint32_t st = sbase + s * TC_STAGE_BYTES;
+        const uint64_t ds = tc::desc_k64(sbase + s * TC_STAGE_BYTES);
         const uint32_t big = tmem + (uint32_t)(b * 256), small = big + 128u;
 #pragma unroll
         for (int kk = 0; kk < TC_BK / 16; ++kk) {
           const uint32_t ko = (uint32_t)(kk * 32);   // 16 FP16 = 32 bytes
-          const uint64_t a0 = tc::desc_k64(st + TC_OFF_A(0) + ko), a1 = tc::desc_k64(st + TC_OFF_A(1) + ko),
-                         a2 = tc::desc_k64(st + TC_OFF_A(2) + ko);
-          const uint64_t b0 = tc::desc_k64(st + TC_OFF_B(0) + ko), b1 = tc::desc_k64(st + TC_OFF_B(1) + ko),
-                         b2 = tc::desc_k64(st + TC_OFF_B(2) + ko);
+          const uint64_t a0 = tc::desc_add(ds, TC_OFF_A(0) + ko), a1 = tc::desc_add(ds, TC_OFF_A(1) + ko),
+                         a2 = tc::desc_add(ds, TC_OFF_A(2) + ko);
+          const uint64_t b0 = tc::desc_add(ds, TC_OFF_B(0) + ko), b1 = tc::desc_add(ds, TC_OFF_B(1) + ko),
+                         b2 = tc::desc_add(ds, TC_OFF_B(2) + ko);
           const uint32_t accum = (first && kk == 0) ? 0u : 1u;
           tc::mma_f16(big, a0, b0, idesc, accum);
           tc::mma_f16(small, a0, b1, idesc, accum);

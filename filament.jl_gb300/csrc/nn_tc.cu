@@ -195,16 +195,14 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
           if (!nt_wait(full_bar(s), (lt / NT_STAGES) & 1, &s_fail)) break;
           tc::tc_fence_after();
           const uint32_t acc = tmem + (uint32_t)(buf * 64);
-          const uint32_t a = sbase + NT_A_OFF + s * NT_A_STRIDE;
-#pragma unroll 1
-          for (int k = 0; k < NN_K; ++k) {
-            const uint32_t ak = a + 128u * k, w = sbase + NT_W_OFF + k * NT_W_BYTES;
+          // tap k: A k rows into the halo tile, W_k; 16 channels = 32 bytes per MMA
+          const uint64_t da = tc::desc_k128(sbase + NT_A_OFF + s * NT_A_STRIDE), dw = tc::desc_k128(sbase + NT_W_OFF);
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {   // 16 channels = 32 bytes per MMA
-              tc::mma_f16(acc, tc::desc_k128(ak + 32u * kk), tc::desc_k128(w + 32u * kk), idesc,
-                          (k | kk) ? 1u : 0u);
-            }
-          }
+          for (int k = 0; k < NN_K; ++k)
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+              tc::mma_f16(acc, tc::desc_add(da, 128u * k + 32u * kk), tc::desc_add(dw, k * NT_W_BYTES + 32u * kk),
+                          idesc, (k | kk) ? 1u : 0u);
           tc::mma_commit(empty_bar(s));
           tc::mma_commit(accf_bar(buf));
         }
@@ -432,14 +430,14 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
         if (!nt_wait(a0f_bar(b), u & 1, &s_fail)) return false;            // im2col of tile i
         if (u > 0 && !nt_wait(c0e_bar(b), (u - 1) & 1, &s_fail)) return false;   // acc0[b] drained
         tc::tc_fence_after();
-        const uint32_t a = sbase + L01_A0_OFF + b * L01_A0_BYTES, w0 = sbase + L01_W0_OFF;
+        const uint64_t da = tc::desc_k128(sbase + L01_A0_OFF + b * L01_A0_BYTES), dw = tc::desc_k128(sbase + L01_W0_OFF);
         const uint32_t acc = tmem + 128u + 128u * b;
 #pragma unroll
         for (int h = 0; h < 2; ++h)          // rows 0 .. 127, rows 8 .. 135
 #pragma unroll
           for (int kk = 0; kk < 2; ++kk)     // K = 32 in two steps of 16
-            tc::mma_f16(acc + 64u * h, tc::desc_k128(a + 1024u * h + 32u * kk), tc::desc_k128(w0 + 32u * kk),
-                        idesc, kk ? 1u : 0u);
+            tc::mma_f16(acc + 64u * h, tc::desc_add(da, 1024u * h + 32u * kk), tc::desc_add(dw, 32u * kk), idesc,
+                        kk ? 1u : 0u);
         tc::mma_commit(c0f_bar(b));
         return true;
       };
@@ -452,14 +450,13 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
           if (!nt_wait(full_bar(s), (i / L1_STAGES) & 1, &s_fail)) break;
           tc::tc_fence_after();
           const uint32_t acc = tmem + (uint32_t)(buf * 64);
-          const uint32_t a = sbase + L01_A_OFF + s * NT_A_STRIDE;
-#pragma unroll 1
-          for (int k = 0; k < NN_K; ++k) {
-            const uint32_t ak = a + 128u * k, w = sbase + k * NT_W_BYTES;
+          const uint64_t da = tc::desc_k128(sbase + L01_A_OFF + s * NT_A_STRIDE), dw = tc::desc_k128(sbase);
+#pragma unroll
+          for (int k = 0; k < NN_K; ++k)
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk)
-              tc::mma_f16(acc, tc::desc_k128(ak + 32u * kk), tc::desc_k128(w + 32u * kk), idesc, (k | kk) ? 1u : 0u);
-          }
+              tc::mma_f16(acc, tc::desc_add(da, 128u * k + 32u * kk), tc::desc_add(dw, k * NT_W_BYTES + 32u * kk),
+                          idesc, (k | kk) ? 1u : 0u);
           tc::mma_commit(empty_bar(s));
           tc::mma_commit(accf_bar(buf));
         }

@@ -187,6 +187,11 @@ __device__ __forceinline__ uint64_t desc_k64(uint32_t saddr) {
   d |= (uint64_t)4 << 61;                              // 64-byte swizzle
   return d;
 }
+// A descriptor of the matrix starting `bytes` (a multiple of 16) further on:
+// the start address is the low 14-bit field in 16-byte units and every
+// shared-memory address is below 2^18, so the sum never carries out of it.
+// Lets an MMA loop form its descriptors with one add of an immediate.
+__device__ __forceinline__ uint64_t desc_add(uint64_t d, uint32_t bytes) { return d + (uint64_t)(bytes >> 4); }
 // Instruction descriptor, kind::f16: D f32, A/B f16, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
   return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
