@@ -160,3 +160,34 @@ def test_c3_xyt_128_matches_oracle(gpu_lib, oracle_binding, precision):
         assert ef < 1e-10 and ff < 1e-10
     else:
         assert ef < 1e-5 and ff < 1e-5
+
+
+@pytest.mark.parametrize("alg", ["Tsit5", "ATsit5"])
+def test_c2_tsitouras_steps_match_oracle(gpu_lib, oracle_binding, alg):
+    """The 1000 x 4096 workload with the Tsitouras step (ALG = Tsit5, and
+    ATsit5 at its default tolerances): eight device-loop steps of the FP64
+    and the mixed form against the oracle, the adaptive form's substep
+    counts included."""
+    import filament_gb as fg
+    kw = dict(C2)
+    kw["ALG"] = alg
+    inp = fg.prepare(FIL_DECK, **kw)
+    r = _oracle_sim(inp)
+    code_r, st_r = r.handle.run(0.0, inp["zmax"], 8)
+    Er, Fr, _ = _final(r)
+    ode_r = r.handle.ode_stats()
+    r.close()
+    for precision in ("fp64", "mixed"):
+        g = fg.Simulation(inp, precision=precision)
+        code_g, st_g = g.handle.run(0.0, inp["zmax"], 8)
+        Eg, Fg, _ = _final(g)
+        ode_g = g.handle.ode_stats()
+        g.close()
+        assert st_g["steps"] == st_r["steps"] == 8
+        ef, ff = rel_l2(Eg, Er), rel_l2(Fg, Fr)
+        _log("c2_%s_%s" % (alg, precision), field=ef, fluence=ff, ode=list(ode_g), ode_oracle=list(ode_r))
+        if precision == "fp64":
+            assert ef < 1e-10 and ff < 1e-10
+            assert ode_g == ode_r
+        else:
+            assert ef < 1e-5 and ff < 1e-5
