@@ -119,6 +119,7 @@ struct fil_handle {
   float* nn_out = nullptr;     // [nrows][nt] network output, or [nrows][9][nt] layer-3 partial sums
   int* nn_slot = nullptr;      // [nrows]
   int* nn_err = nullptr;       // tensor-core inference: a wait timed out
+  uint8_t* nn_tflag = nullptr; // [nrows][nt/128] tile flags of the surrogate rows (nn_features)
   NnRowsPlan nn_plan;          // tensor-core inference over the buffers above
   bool nn_tc = false;          // nt is a multiple of 128: tensor-core path
   int nn_every = 1;
@@ -716,6 +717,7 @@ template <typename R> static cudaError_t enqueue_surrogate(fil_handle* h, RowPar
   if (!h->nn) return cudaSuccess;
   P.nn_slot = h->nn_slot;
   P.nn_out = h->nn_out;
+  P.nn_tflag = h->nn_tflag;
   if (h->nn_tc) {
     P.nn_part = 1;
     P.nn_b3 = nn_out_bias(h->nn);
@@ -1031,9 +1033,10 @@ template <typename R> static int enqueue_reduce(fil_handle* h, double* power, in
   }
   RowParams<R> P = row_params<R>(h);
   P.S_in = (const typename C2T<R>::type*)h->S;
-  if (h->nn && check_done) {   // the stepping loop: flag the rows for the surrogate
+  if (h->nn && check_done) {   // the stepping loop: flag the rows (and their tiles) for the surrogate
     P.nn_feat = (__nv_bfloat16*)h->nn_feat;
     P.nn_slot = h->nn_slot;
+    P.nn_tflag = h->nn_tflag;
   }
   R* I = power ? (R*)h->stage : nullptr;
   CK(launch_rowreduce<R>(P, h->nt, h->fluence, I, check_done, h->st));
@@ -1108,7 +1111,7 @@ static void free_all(fil_handle* h) {
                   h->qa1, h->qa2, h->BS[0], h->BS[1], h->BS[2], h->qb, h->kzt, h->gdt, h->tc_err,
                   h->kx2, h->ky2, h->sg1, h->sg2, h->twx, h->twy,
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
-                  h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err,
+                  h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err, h->nn_tflag,
                   h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt, h->park,
                   h->kcol, h->l_kzr, h->l_kg, h->spec_g, h->tk};
   for (void* p : bufs)
@@ -1690,6 +1693,8 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
       CK(cudaMemset(h->nn_slot, 0xff, (size_t)h->nrows * sizeof(int)));
       CK(cudaMalloc((void**)&h->nn_err, sizeof(int)));
       CK(cudaMemset(h->nn_err, 0, sizeof(int)));
+      CK(cudaMalloc((void**)&h->nn_tflag, (size_t)h->nrows * (h->nt / 128)));
+      CK(cudaMemset(h->nn_tflag, 3, (size_t)h->nrows * (h->nt / 128)));
       NnRowsPlan& pl = h->nn_plan;
       std::memset(&pl, 0, sizeof pl);
       pl.x0 = (const __nv_bfloat16*)h->nn_feat;
@@ -1701,6 +1706,7 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
       pl.count = &h->ctl->nn_rows;
       pl.stop = &h->ctl->done;
       pl.err = h->nn_err;
+      pl.tflag = h->nn_tflag;
       h->nn_tc = nn_plan_init(&pl) == 0;
     }
   }

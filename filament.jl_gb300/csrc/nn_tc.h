@@ -16,6 +16,7 @@ struct NnRowsPlan {
   const int* count;          // device row count (NULL: maxrows)
   const int* stop;           // device flag: non-zero skips the launches (or NULL)
   int* err;                  // set to 1 when a bounded wait gave up
+  const uint8_t* tflag;      // [rows][T/128] tile flags, bit 1: run the tile (NULL: every tile)
   CUtensorMap map_a1, map_a2;   // 3-D maps {64, T, rows}, box {64, 136, 1} (a tile with its halo)
   int sms;                   // persistent grid size of the tensor-core layers
 };
@@ -49,9 +50,9 @@ __device__ __forceinline__ float nn_out_at(const float* __restrict__ P, float b3
 }
 
 struct fil_nn;
-// the network over the rows of the plan: layers 0 and 1 in one kernel
-// (layer 0 on CUDA cores into layer 1's tensor-core operand), layer 2 on the
-// tensor cores with layer 3 in its epilogue, leaving the partial sums in
+// the network over the rows of the plan: layers 0 and 1 in one tensor-core
+// kernel (layer 0 through an im2col tile into layer 1's operand), layer 2 on
+// the tensor cores with layer 3 in its epilogue, leaving the partial sums in
 // p.part; surrogate.cu
 cudaError_t nn_infer(const fil_nn* n, const NnRowsPlan& p, cudaStream_t st);
 // device pointer to the output layer's bias (the b3 of nn_out_at)

@@ -99,6 +99,10 @@ template <typename R> struct RowParams {
   const float* nn_out;
   int nn_part;
   const float* nn_b3;
+  // [slot][N/128] tile flags of the surrogate's rows (nn_features): bit 0 the
+  // network's g enters the density in the tile, bit 1 the network runs on
+  // it (bit 0 of the tile or of a neighbour); NULL: every tile both
+  uint8_t* nn_tflag;
   // linear-only rows (FP32 form): max_k |i QZ Rnl_cubic (k ? 2 : 1)| (the
   // Kerr coefficient before the channel pre-scale); < 0 disables the test
   R cc_max;
@@ -555,7 +559,8 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 // rho[], kdrho[] and returns max rho.
 template <typename R, int N, int NC>
 FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typename C2T<R>::type* X,
-                     const float* __restrict__ g, R* rho, R* kdrho, Aff<R, 1>* ascratch, R* rscratch, bool judge) {
+                     const float* __restrict__ g, R* rho, R* kdrho, Aff<R, 1>* ascratch, R* rscratch, bool judge,
+                     int slot) {
   typedef typename C2T<R>::type C;
   const PlasmaParams<R>& pp = P.pp;
   const int j0 = threadIdx.x * 16;
@@ -564,6 +569,9 @@ FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 #pragma unroll
   for (int c = 0; c < NC; ++c) kappa += pp.rava_nt[c] * pp.rho_nt[c];
   const float b3 = P.nn_part ? __ldg(P.nn_b3) : 0.f;
+  // the thread's 16 points lie in one 128-point tile: g there, or g = 0 where
+  // the tile flag says it cannot matter (nn_features)
+  const bool use_g = !P.nn_tflag || (P.nn_tflag[(size_t)slot * (N / 128) + j0 / 128] & 1);
   // quadrature weights of the stage points t_j, t_j + dt/2, t_{j+1}
   R qw[3] = {0, 0, 0};
   for (int st = 0; st < pp.ns; ++st) qw[pp.pidx[st]] += pp.b[st];
@@ -603,8 +611,11 @@ FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
       const C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
       const C em = (R)0.5 * (e0 + e1);
       const R A = qw[0] * e0.x * e0.x + qw[1] * em.x * em.x + qw[2] * e1.x * e1.x;
-      const float gr = P.nn_part ? nn_out_at(g, b3, j, N) : __ldg(&g[j]);
-      const float gj = fminf(fmaxf(gr, NN_G_LO), NN_G_HI);
+      float gj = 0.f;
+      if (use_g) {
+        const float gr = P.nn_part ? nn_out_at(g, b3, j, N) : __ldg(&g[j]);
+        gj = fminf(fmaxf(gr, NN_G_LO), NN_G_HI);
+      }
       w += kappa * A * dt * -expm1(-S) * exp((R)gj);
     }
     S += wb;
@@ -866,13 +877,13 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
       R rmax;
       const float* gslot = P.nn_out + (size_t)slot * N * (P.nn_part ? NN_K : 1);
       if (nn_row && !judge) {
-        rmax = nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, false);
+        rmax = nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, false, slot);
       } else {
         rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag,
                                     stepping ? (R)ctl->rhomax : (R)0, dz, &ych);
         if (judge) {
           // rows not flagged carry rho0 in the surrogate form
-          const R diff = nn_row ? nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, true)
+          const R diff = nn_row ? nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, true, slot)
                                 : max(rmax - (R)NC * P.pp.rho0, (R)0);
           if (tid == 0) atomic_max_nonneg(&ctl->nn_diff_acc, (double)diff);
         }
@@ -1154,7 +1165,7 @@ __global__ void __launch_bounds__(256) k_np_combine(RowParams<R> P, int nh) {
 // over t_i, the midpoint of the interpolated field and t_{i+1}, as in
 // nn_density).  Thread t owns j = 16t .. 16t+15; f is [3][N] (BF16).
 template <typename R, int N>
-FIL_DEV void nn_features(const RowParams<R>& P, const typename C2T<R>::type* X, __nv_bfloat16* f) {
+FIL_DEV void nn_features(const RowParams<R>& P, const typename C2T<R>::type* X, __nv_bfloat16* f, int slot) {
   typedef typename C2T<R>::type C;
   __shared__ PlasmaSmem<R> tabs;
   __shared__ Aff<R, 1> sc[32];
@@ -1199,6 +1210,47 @@ FIL_DEV void nn_features(const RowParams<R>& P, const typename C2T<R>::type* X, 
   G.L[0][0] = 0;
   G.B[0] = tsum;
   R S = aff_block_exclusive_scan<R, 1>(G, sc).B[0];
+  if (P.nn_tflag) {
+    // Tile flags.  g enters the density only through the avalanche term
+    // kappa A_j dt (1 - e^{-S_j}) e^{g_j} (nn_density), at most e^{NN_G_HI}
+    // times its g = 0 value.  A 128-point tile whose sum of that bound is at
+    // most 2^-30 of the row's base exponent S_total changes the density by
+    // less than 2^-30 of its scale with any g: there the density uses g = 0
+    // (bit 0 clear).  The network runs on the tiles with bit 0 and on their
+    // neighbours (bit 1), so that the receptive field (+-16 points over the
+    // four layers) of every tile that uses g is computed.
+    __shared__ R s_tot;
+    __shared__ uint8_t s_act[N / 128];
+    R kappa = 0;
+    for (int c = 0; c < pp.nc; ++c) kappa += pp.rava_nt[c] * pp.rho_nt[c];
+    R av = 0, Sj = S;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int j = j0 + q;
+      if (j < N - 1) {
+        const C e0 = X[pad16(j)], e1 = X[pad16(j + 1)];
+        const C em = (R)0.5 * (e0 + e1);
+        const R A = qw[0] * e0.x * e0.x + qw[1] * em.x * em.x + qw[2] * e1.x * e1.x;
+        av += kappa * A * pp.dt * -expm1(-Sj);
+      }
+      Sj += wl[q];
+    }
+    // the tile's 8 threads (16 points each) are consecutive lanes
+    av += __shfl_xor_sync(0xffffffffu, av, 1);
+    av += __shfl_xor_sync(0xffffffffu, av, 2);
+    av += __shfl_xor_sync(0xffffffffu, av, 4);
+    if (threadIdx.x == blockDim.x - 1) s_tot = S + tsum;
+    __syncthreads();
+    const int tile = j0 / 128;
+    if ((threadIdx.x & 7) == 0) s_act[tile] = av * exp((R)NN_G_HI) > ldexp(s_tot, -30) ? 1 : 0;
+    __syncthreads();
+    if ((threadIdx.x & 7) == 0) {
+      constexpr int NT = N / 128;
+      const uint8_t a = s_act[tile];
+      const uint8_t d = a | (tile > 0 ? s_act[tile - 1] : 0) | (tile + 1 < NT ? s_act[tile + 1] : 0);
+      P.nn_tflag[(size_t)slot * NT + tile] = (uint8_t)(a | (d << 1));
+    }
+  }
   // the thread's 16 consecutive points of each channel, packed and written
   // as two 16-byte stores per channel (one channel at a time, the scanned
   // channel first so that its per-step rates are released early)
@@ -1297,7 +1349,7 @@ __global__ void __launch_bounds__(N / 16) k_rowreduce(RowParams<R> P, double* fl
   if (P.nn_feat) {
     __syncthreads();
     const int slot = s_slot;
-    if (slot >= 0) nn_features<R, N>(P, X, P.nn_feat + (size_t)slot * 3 * N);
+    if (slot >= 0) nn_features<R, N>(P, X, P.nn_feat + (size_t)slot * 3 * N, slot);
   }
 }
 
