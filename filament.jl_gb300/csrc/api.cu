@@ -1071,10 +1071,10 @@ static void arm_surrogate(const fil_handle* h, DevCtl& c) {
   c.nn_judge = 0;
   c.nn_every = h->nn ? h->nn_every : 1;
   c.nn_tol = h->nn ? h->nn_tol : 0;
-  c.nn_count = c.nn_rows = 0;
+  c.nn_count = c.nn_rows = c.nn_tiles = 0;
   c.nn_steps = c.nn_used = c.nn_judged = c.nn_rejected = 0;
   c.nn_diff_acc = 0;
-  c.nn_err = c.nn_err_max = c.nn_rows_sum = 0;
+  c.nn_err = c.nn_err_max = c.nn_rows_sum = c.nn_tiles_sum = 0;
 }
 
 static int check_tc(fil_handle* h) {
@@ -1505,6 +1505,7 @@ static int arm_run(fil_handle* h, double z0, double zmax, int64_t nmax) {
   c.clamp_last = h->clamp_last;
   c.imax_acc = 0;
   c.nn_count = 0;
+  c.nn_tiles = 0;
   CK(cudaMemcpyAsync(h->ctl, &c, sizeof c, cudaMemcpyHostToDevice, h->st));
   CK(cudaStreamSynchronize(h->st));
   return 0;
@@ -1732,10 +1733,11 @@ int fil_get_surrogate_stats(fil_handle* h, double* out, int n) {
   int rc = read_ctl(h);
   if (rc) return rc;
   const DevCtl& c = *h->ctl_host;
-  const double v[9] = {(double)c.nn_on, (double)c.nn_use, (double)c.nn_steps, (double)c.nn_used,
-                       (double)c.nn_judged, (double)c.nn_rejected, c.nn_err, c.nn_err_max,
-                       c.nn_used ? c.nn_rows_sum / (double)c.nn_used : 0.0};
-  for (int i = 0; i < n; ++i) out[i] = i < 9 ? v[i] : 0.0;
+  const double v[10] = {(double)c.nn_on, (double)c.nn_use, (double)c.nn_steps, (double)c.nn_used,
+                        (double)c.nn_judged, (double)c.nn_rejected, c.nn_err, c.nn_err_max,
+                        c.nn_used ? c.nn_rows_sum / (double)c.nn_used : 0.0,
+                        c.nn_used ? c.nn_tiles_sum / (double)c.nn_used : 0.0};
+  for (int i = 0; i < n; ++i) out[i] = i < 10 ? v[i] : 0.0;
   return FIL_OK;
 }
 

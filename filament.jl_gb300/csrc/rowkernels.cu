@@ -51,6 +51,7 @@ __global__ void k_control(DevCtl* c, const double* __restrict__ fluence, const d
     if (c->nn_use && !c->nn_judge) {
       c->nn_used += 1;
       c->nn_rows_sum += c->nn_rows;
+      c->nn_tiles_sum += c->nn_tiles;
     }
     c->nn_steps += 1;
   } else {
@@ -58,6 +59,7 @@ __global__ void k_control(DevCtl* c, const double* __restrict__ fluence, const d
     c->nn_rows = 0;
   }
   c->nn_count = 0;
+  c->nn_tiles = 0;
   c->z += dz;
   c->dz = dz;
   c->steps += 1;
@@ -72,6 +74,7 @@ __global__ void k_setdz(DevCtl* c, double z, double dz) {
   c->nn_judge = 0;   // single steps solve the plasma equation
   c->nn_rows = 0;
   c->nn_count = 0;
+  c->nn_tiles = 0;
   c->rhomax = __longlong_as_double((long long)c->rhomax_acc);
   c->rhomax_acc = 0;
   c->z = z;

@@ -37,6 +37,8 @@ struct DevCtl {
   unsigned long long nn_diff_acc;   // judge step: max |rho_net - rho_ode| (bits)
   double nn_tol, nn_err, nn_err_max;
   double nn_rows_sum;         // sum of nn_rows over the steps that used the network
+  int nn_tiles;               // 128-point tiles the network runs on, of the flagged rows (atomic)
+  double nn_tiles_sum;        // sum of nn_tiles over the steps that used the network
   // adaptive nonlinear step (FIL_ALG_ATSIT5): substep attempts and
   // rejections, summed over the transverse points and steps
   unsigned long long ode_attempts, ode_rejects;
@@ -1249,6 +1251,14 @@ FIL_DEV void nn_features(const RowParams<R>& P, const typename C2T<R>::type* X, 
       const uint8_t a = s_act[tile];
       const uint8_t d = a | (tile > 0 ? s_act[tile - 1] : 0) | (tile + 1 < NT ? s_act[tile + 1] : 0);
       P.nn_tflag[(size_t)slot * NT + tile] = (uint8_t)(a | (d << 1));
+    }
+    if (threadIdx.x == 0) {
+      // tiles of this row that the network runs on (the executed work)
+      constexpr int NT = N / 128;
+      int run = 0;
+      for (int t = 0; t < NT; ++t)
+        run += s_act[t] | (t > 0 ? s_act[t - 1] : 0) | (t + 1 < NT ? s_act[t + 1] : 0);
+      atomicAdd(&P.ctl->nn_tiles, run);
     }
   }
   // the thread's 16 consecutive points of each channel, packed and written

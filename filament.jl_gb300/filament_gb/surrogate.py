@@ -322,7 +322,7 @@ def disarm(handle):
 
 
 STAT_KEYS = ("armed", "in_use", "steps", "steps_used", "checks", "checks_failed", "err_last", "err_max",
-             "rows_mean")
+             "rows_mean", "tiles_mean")
 
 
 def stats(handle):

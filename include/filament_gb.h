@@ -366,7 +366,8 @@ int fil_nn_train(fil_nn* n, const float* feat, const float* target, const float*
 int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol);
 /* out[0..n): armed, in use, steps since armed, steps that used the network,
  * checks, failed checks, last error, largest error, mean rows per step
- * that used the network                                                    */
+ * that used the network, mean 128-point tiles per such step that the
+ * network ran on (tiles whose output cannot reach the density are skipped) */
 int fil_get_surrogate_stats(fil_handle* h, double* out, int n);
 
 /* ---- batched parameter sweep ------------------------------------------------

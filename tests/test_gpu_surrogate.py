@@ -213,6 +213,8 @@ def test_trained_network_in_the_loop(trained):
     assert s["checks"] == 2
     if s["checks_failed"] == 0:
         assert s["steps_used"] == 38 and s["err_max"] <= 1e-3 and s["rows_mean"] > 0
+        # the network runs on at most every tile of the rows it takes
+        assert 0 < s["tiles_mean"] <= s["rows_mean"] * (512 / 128) + 1e-9   # Nt = 512
     else:
         assert s["err_max"] > 1e-3
     assert rel_l2(E1, E0) < 1e-3
