@@ -120,6 +120,7 @@ struct fil_handle {
   int* nn_slot = nullptr;      // [nrows]
   int* nn_err = nullptr;       // tensor-core inference: a wait timed out
   uint8_t* nn_tflag = nullptr; // [nrows][nt/128] tile flags of the surrogate rows (nn_features)
+  int* nn_tlist = nullptr;     // [nrows * nt/128] list of the tiles the network runs (nn_features)
   NnRowsPlan nn_plan;          // tensor-core inference over the buffers above
   bool nn_tc = false;          // nt is a multiple of 128: tensor-core path
   int nn_every = 1;
@@ -1037,6 +1038,7 @@ template <typename R> static int enqueue_reduce(fil_handle* h, double* power, in
     P.nn_feat = (__nv_bfloat16*)h->nn_feat;
     P.nn_slot = h->nn_slot;
     P.nn_tflag = h->nn_tflag;
+    P.nn_tlist = h->nn_tc ? h->nn_tlist : nullptr;
   }
   R* I = power ? (R*)h->stage : nullptr;
   CK(launch_rowreduce<R>(P, h->nt, h->fluence, I, check_done, h->st));
@@ -1071,7 +1073,7 @@ static void arm_surrogate(const fil_handle* h, DevCtl& c) {
   c.nn_judge = 0;
   c.nn_every = h->nn ? h->nn_every : 1;
   c.nn_tol = h->nn ? h->nn_tol : 0;
-  c.nn_count = c.nn_rows = c.nn_tiles = 0;
+  c.nn_count = c.nn_rows = c.nn_tiles = c.nn_tiles_run = 0;
   c.nn_steps = c.nn_used = c.nn_judged = c.nn_rejected = 0;
   c.nn_diff_acc = 0;
   c.nn_err = c.nn_err_max = c.nn_rows_sum = c.nn_tiles_sum = 0;
@@ -1111,7 +1113,7 @@ static void free_all(fil_handle* h) {
                   h->qa1, h->qa2, h->BS[0], h->BS[1], h->BS[2], h->qb, h->kzt, h->gdt, h->tc_err,
                   h->kx2, h->ky2, h->sg1, h->sg2, h->twx, h->twy,
                   h->MA1[0], h->MA1[1], h->MA1[2], h->MA2[0], h->MA2[1], h->MA2[2],
-                  h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err, h->nn_tflag,
+                  h->nn_feat, h->nn_a1, h->nn_a2, h->nn_out, h->nn_slot, h->nn_err, h->nn_tflag, h->nn_tlist,
                   h->SU, h->u_kzr, h->u_kg, h->np_S0, h->np_K1, h->np_KS, h->np_ACC, h->qrt, h->park,
                   h->kcol, h->l_kzr, h->l_kg, h->spec_g, h->tk};
   for (void* p : bufs)
@@ -1696,6 +1698,8 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
       CK(cudaMemset(h->nn_err, 0, sizeof(int)));
       CK(cudaMalloc((void**)&h->nn_tflag, (size_t)h->nrows * (h->nt / 128)));
       CK(cudaMemset(h->nn_tflag, 3, (size_t)h->nrows * (h->nt / 128)));
+      CK(cudaMalloc((void**)&h->nn_tlist, (size_t)h->nrows * (h->nt / 128) * sizeof(int)));
+      CK(cudaMemset(h->nn_tlist, 0, (size_t)h->nrows * (h->nt / 128) * sizeof(int)));
       NnRowsPlan& pl = h->nn_plan;
       std::memset(&pl, 0, sizeof pl);
       pl.x0 = (const __nv_bfloat16*)h->nn_feat;
@@ -1707,7 +1711,8 @@ int fil_set_surrogate(fil_handle* h, const fil_nn* nn, int every, double tol) {
       pl.count = &h->ctl->nn_rows;
       pl.stop = &h->ctl->done;
       pl.err = h->nn_err;
-      pl.tflag = h->nn_tflag;
+      pl.tlist = h->nn_tlist;
+      pl.tcount = &h->ctl->nn_tiles_run;
       h->nn_tc = nn_plan_init(&pl) == 0;
     }
   }

@@ -106,7 +106,26 @@ struct NtParams {
   const int* count;
   const int* stop;
   int* err;
-  const uint8_t* tflag;    // [rows][tiles_per_row], bit 1: the tile is run (NULL: every tile)
+  const int* tlist;        // the tiles to run: the first *tcount entries (NULL: every tile)
+  const int* tcount;
+};
+
+// The tiles a block runs: entries blockIdx.x + i gridDim.x of the tile list
+// (or of all tiles without one), i < ntl.  Every role of the block walks the
+// same sequence.  Entries are clamped to the tiles of the counted rows.
+struct NtTiles {
+  const int* list;
+  int total, ntl, last;
+  __device__ NtTiles(const NtParams& p, int ntiles) {
+    list = p.tlist;
+    total = p.tlist ? min(*p.tcount, ntiles) : ntiles;
+    ntl = (int)blockIdx.x < total ? (total - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    last = ntiles - 1;
+  }
+  __device__ int at(int i) const {
+    const int k = (int)blockIdx.x + i * (int)gridDim.x;
+    return list ? max(0, min(__ldg(&list[k]), last)) : k;
+  }
 };
 
 // FINAL (layer 2): the epilogue applies layer 3 to its own point instead of
@@ -124,8 +143,9 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
   __shared__ __align__(16) float s_w3[FINAL ? 5 * 64 * 2 : 4];
   if (p.stop && *p.stop) return;
   const int nrows = p.count ? min(*p.count, p.maxrows) : p.maxrows;
-  const int ntiles = nrows * p.tiles_per_row;
-  if ((int)blockIdx.x >= ntiles) return;   // block-uniform, before any barrier
+  const NtTiles tiles(p, nrows * p.tiles_per_row);
+  const int ntl = tiles.ntl;
+  if (ntl == 0) return;   // block-uniform, before any barrier
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t raw = tc::smem_u32(nt_smem);
   const uint32_t sbase = (raw + 1023u) & ~1023u;
@@ -164,7 +184,6 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot_g;
   const int tpr = p.tiles_per_row;
-  auto run_tile = [&](int tile) { return !p.tflag || (p.tflag[tile] & 2); };
 
   if (warp == 4) {
     // ---------------- producer: weights once, then one activation tile per tap
@@ -172,14 +191,13 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
       tc::mbar_expect_tx(wbar, NN_K * NT_W_BYTES);
       for (int k = 0; k < NN_K; ++k) tc::tma_load_2d(sbase + NT_W_OFF + k * NT_W_BYTES, &tw, 0, 64 * k, wbar);
       int it = 0;
-      for (int tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x) {
-        if (!run_tile(tile)) continue;
+      for (; it < ntl && !s_fail; ++it) {
+        const int tile = tiles.at(it);
         const int b = tile / tpr, t0 = (tile - b * tpr) * NT_BM;
         const int s = it % NT_STAGES, use = it / NT_STAGES;
         if (use > 0 && !nt_wait(empty_bar(s), (use - 1) & 1, &s_fail)) break;
         tc::mbar_expect_tx(full_bar(s), NT_A_BYTES);
         tc::tma_load_3d(sbase + NT_A_OFF + s * NT_A_STRIDE, &tx, 0, t0 - NN_HALF, b, full_bar(s));
-        ++it;
       }
       // wait for the last loads so that no copy lands after the block exits
       nt_wait(wbar, 0, &s_fail);
@@ -191,9 +209,7 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
     if (lane == 0) {
       const uint32_t idesc = tc::idesc_bf16(NT_BM, 64);
       if (nt_wait(wbar, 0, &s_fail)) {
-        int lt = 0;
-        for (int tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x) {
-          if (!run_tile(tile)) continue;
+        for (int lt = 0; lt < ntl && !s_fail; ++lt) {
           const int buf = lt & 1, ub = lt >> 1;
           if (ub > 0 && !nt_wait(acce_bar(buf), (ub - 1) & 1, &s_fail)) break;
           const int s = lt % NT_STAGES;
@@ -210,7 +226,6 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
                           idesc, (k | kk) ? 1u : 0u);
           tc::mma_commit(empty_bar(s));
           tc::mma_commit(accf_bar(buf));
-          ++lt;
         }
       }
       // no MMA may still write tensor memory when it is released
@@ -219,12 +234,10 @@ __global__ void __launch_bounds__(NT_THREADS, 1)
     }
   } else if (warp < 4) {
     // ---------------- epilogue: warp w owns time points 32w .. 32w+31 of the tile
-    int lt = 0;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-      if (!run_tile(tile)) continue;
+    for (int lt = 0; lt < ntl; ++lt) {
+      const int tile = tiles.at(lt);
       const int buf = lt & 1;
-      ++lt;
-      if (!nt_wait(accf_bar(buf), ((lt - 1) >> 1) & 1, &s_fail)) break;
+      if (!nt_wait(accf_bar(buf), (lt >> 1) & 1, &s_fail)) break;
       tc::tc_fence_after();
       const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(buf * 64);
       uint32_t r0[32], r1[32];
@@ -357,8 +370,9 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
   __shared__ __align__(16) float s_b0[64];      // layer 0
   if (p.stop && *p.stop) return;
   const int nrows = p.count ? min(*p.count, p.maxrows) : p.maxrows;
-  const int ntiles = nrows * p.tiles_per_row;
-  if ((int)blockIdx.x >= ntiles) return;   // block-uniform, before any barrier
+  const NtTiles tiles(p, nrows * p.tiles_per_row);
+  const int ntl = tiles.ntl;
+  if (ntl == 0) return;   // block-uniform, before any barrier
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t raw = tc::smem_u32(nt_smem);
   const uint32_t sbase = (raw + 1023u) & ~1023u;
@@ -374,19 +388,7 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
   const uint32_t wbar = bars + L01_WBAR, done_bar = bars + L01_DONE, tmem_slot = bars + L01_SLOT;
   volatile uint32_t* tmem_slot_g = reinterpret_cast<volatile uint32_t*>(gbase + L01_BAR_OFF + L01_SLOT);
 
-  __shared__ int s_ntl;
-  // this block's tiles: blockIdx.x + i gridDim.x, those the flags say to run
-  auto run_tile = [&](int tile) { return !p.tflag || (p.tflag[tile] & 2); };
-  auto next_run = [&](int tile) {   // the first tile to run at or after `tile` in this block's sequence
-    while (tile < ntiles && !run_tile(tile)) tile += (int)gridDim.x;
-    return tile;
-  };
-  if (tid == 0) {
-    s_fail = 0;
-    int n = 0;
-    for (int tile = next_run((int)blockIdx.x); tile < ntiles; tile = next_run(tile + (int)gridDim.x)) ++n;
-    s_ntl = n;
-  }
+  if (tid == 0) s_fail = 0;
   if (tid < 64) {
     s_bias[tid] = p.bias[tid];
     s_b0[tid] = p.b0[tid];
@@ -426,7 +428,6 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot_g;
   const int tpr = p.tiles_per_row;
-  const int ntl = s_ntl;   // tiles this block runs; the roles walk them with next_run
   auto tile_of = [&](int tile, int* b, int* t0) {
     *b = tile / tpr;
     *t0 = (tile - *b * tpr) * NT_BM;
@@ -510,11 +511,9 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
           nx[ci][m] = (j < L01_XW && t >= 0 && t < p.T) ? xr[(size_t)ci * p.T + t] : (uint16_t)0;
         }
     };
-    int cur = next_run((int)blockIdx.x);
-    if (ntl > 0) load_window(cur);
+    load_window(tiles.at(0));
     for (int i = 0; i < ntl; ++i) {
       const int b = i & 1, u = i >> 1;
-      const int nxt = next_run(cur + (int)gridDim.x);
       int ok = 1;
       if (lane == 0) ok = !s_fail && (u == 0 || nt_wait(c0f_bar(b), (u - 1) & 1, &s_fail));   // A0[b] free
       if (!__shfl_sync(0xffffffffu, ok, 0)) break;
@@ -524,7 +523,7 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
         for (int m = 0; m < XM; ++m)
           if (lane + 32 * m < L01_XW) xw[ci * L01_XW + lane + 32 * m] = nx[ci][m];
       __syncwarp();
-      if (i + 1 < ntl) load_window(nxt);   // in flight while the rows are written
+      if (i + 1 < ntl) load_window(tiles.at(i + 1));   // in flight while the rows are written
       uint8_t* a0 = gbase + L01_A0_OFF + b * L01_A0_BYTES;
 #pragma unroll
       for (int m = 0; m < 17; ++m) {
@@ -535,7 +534,6 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
       __syncwarp();                   // xw free for the next tile
       tc::fence_proxy_async_smem();
       nt_arrive(a0f_bar(b));
-      cur = nxt;
     }
   } else if (warp >= 6) {
     // ---------------- layer-0 epilogue into the layer-1 stages: warps
@@ -564,10 +562,9 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
         *reinterpret_cast<uint4*>(st + r * 128 + (((4 * h + j) ^ (r & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     };
-    int cur = (int)blockIdx.x;
     for (int i = 0; i < ntl; ++i) {
       const int b = i & 1, u = i >> 1;
-      cur = next_run(i == 0 ? cur : cur + (int)gridDim.x);
+      const int cur = tiles.at(i);
       if (!nt_wait(c0f_bar(b), u & 1, &s_fail)) break;
       tc::tc_fence_after();
       int row, t0;
@@ -596,10 +593,9 @@ __global__ void __launch_bounds__(L01_THREADS, 1)
     }
   } else {
     // ---------------- layer-1 epilogue: warp w owns time points 32w .. 32w+31 of the tile
-    int cur = (int)blockIdx.x;
     for (int i = 0; i < ntl; ++i) {
       const int buf = i & 1;
-      cur = next_run(i == 0 ? cur : cur + (int)gridDim.x);
+      const int cur = tiles.at(i);
       if (!nt_wait(accf_bar(buf), (i >> 1) & 1, &s_fail)) break;
       tc::tc_fence_after();
       const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(buf * 64);
@@ -715,7 +711,8 @@ cudaError_t nn_launch_conv_tc(const CUtensorMap& tx, const CUtensorMap& tw, cons
   q.count = p.count;
   q.stop = p.stop;
   q.err = p.err;
-  q.tflag = p.tflag;
+  q.tlist = p.tlist;
+  q.tcount = p.tcount;
   const int tiles = p.maxrows * q.tiles_per_row;
   const int grid = std::max(1, std::min(p.sms, tiles));
   if (part)

@@ -16,7 +16,10 @@ struct NnRowsPlan {
   const int* count;          // device row count (NULL: maxrows)
   const int* stop;           // device flag: non-zero skips the launches (or NULL)
   int* err;                  // set to 1 when a bounded wait gave up
-  const uint8_t* tflag;      // [rows][T/128] tile flags, bit 1: run the tile (NULL: every tile)
+  // the tiles to run: the first *tcount entries of tlist (row * T/128 +
+  // tile), in any order; NULL: every tile of the rows
+  const int* tlist;
+  const int* tcount;
   CUtensorMap map_a1, map_a2;   // 3-D maps {64, T, rows}, box {64, 136, 1} (a tile with its halo)
   int sms;                   // persistent grid size of the tensor-core layers
 };

@@ -48,6 +48,7 @@ __global__ void k_control(DevCtl* c, const double* __restrict__ fluence, const d
     }
     c->nn_judge = (c->nn_steps % c->nn_every) == 0;
     c->nn_rows = (c->nn_use || c->nn_judge) ? c->nn_count : 0;
+    c->nn_tiles_run = (c->nn_use || c->nn_judge) ? c->nn_tiles : 0;
     if (c->nn_use && !c->nn_judge) {
       c->nn_used += 1;
       c->nn_rows_sum += c->nn_rows;
@@ -57,6 +58,7 @@ __global__ void k_control(DevCtl* c, const double* __restrict__ fluence, const d
   } else {
     c->nn_judge = 0;
     c->nn_rows = 0;
+    c->nn_tiles_run = 0;
   }
   c->nn_count = 0;
   c->nn_tiles = 0;
@@ -74,7 +76,7 @@ __global__ void k_setdz(DevCtl* c, double z, double dz) {
   c->nn_judge = 0;   // single steps solve the plasma equation
   c->nn_rows = 0;
   c->nn_count = 0;
-  c->nn_tiles = 0;
+  c->nn_tiles = c->nn_tiles_run = 0;
   c->rhomax = __longlong_as_double((long long)c->rhomax_acc);
   c->rhomax_acc = 0;
   c->z = z;

@@ -38,6 +38,7 @@ struct DevCtl {
   double nn_tol, nn_err, nn_err_max;
   double nn_rows_sum;         // sum of nn_rows over the steps that used the network
   int nn_tiles;               // 128-point tiles the network runs on, of the flagged rows (atomic)
+  int nn_tiles_run;           // entries of the tile list the network runs in this step
   double nn_tiles_sum;        // sum of nn_tiles over the steps that used the network
   // adaptive nonlinear step (FIL_ALG_ATSIT5): substep attempts and
   // rejections, summed over the transverse points and steps
@@ -105,6 +106,9 @@ template <typename R> struct RowParams {
   // network's g enters the density in the tile, bit 1 the network runs on
   // it (bit 0 of the tile or of a neighbour); NULL: every tile both
   uint8_t* nn_tflag;
+  // [slots x N/128] list of the tiles with bit 1 (slot * N/128 + tile), each
+  // row's tiles at a range reserved with the nn_tiles count (or NULL)
+  int* nn_tlist;
   // linear-only rows (FP32 form): max_k |i QZ Rnl_cubic (k ? 2 : 1)| (the
   // Kerr coefficient before the channel pre-scale); < 0 disables the test
   R cc_max;
@@ -1253,12 +1257,17 @@ FIL_DEV void nn_features(const RowParams<R>& P, const typename C2T<R>::type* X, 
       P.nn_tflag[(size_t)slot * NT + tile] = (uint8_t)(a | (d << 1));
     }
     if (threadIdx.x == 0) {
-      // tiles of this row that the network runs on (the executed work)
+      // the row's tiles that the network runs on, appended to the tile list
+      // at a range reserved by the count (the list's order does not matter:
+      // every tile is computed on its own)
       constexpr int NT = N / 128;
+      auto runs = [&](int t) { return s_act[t] | (t > 0 ? s_act[t - 1] : 0) | (t + 1 < NT ? s_act[t + 1] : 0); };
       int run = 0;
-      for (int t = 0; t < NT; ++t)
-        run += s_act[t] | (t > 0 ? s_act[t - 1] : 0) | (t + 1 < NT ? s_act[t + 1] : 0);
-      atomicAdd(&P.ctl->nn_tiles, run);
+      for (int t = 0; t < NT; ++t) run += runs(t);
+      int at = atomicAdd(&P.ctl->nn_tiles, run);
+      if (P.nn_tlist)
+        for (int t = 0; t < NT; ++t)
+          if (runs(t)) P.nn_tlist[at++] = slot * NT + t;
     }
   }
   // the thread's 16 consecutive points of each channel, packed and written
