@@ -832,9 +832,10 @@ def main():
         "e2e": e2e,
         "e2e_host_loop_plain": e2e_plain,
         "clocks": clocks,
-        # per timed step: row reduction, controller, 4 network layers, row
-        # kernel, 2 x (slice + tensor-core transform)
-        "gpu_launches": 11 * surr["timed_steps"],
+        # per timed step: row reduction, controller, 2 network launches
+        # (layers 0-1, layers 2-3), row kernel, slice, forward transform,
+        # propagator + slice, inverse transform
+        "gpu_launches": 9 * surr["timed_steps"],
         "headline": headline,
     }
     print(json.dumps(line))
