@@ -144,6 +144,31 @@ def closed_form_density(E, g, pe, dt):
     return ra + (rnt - ra) * -np.expm1(-St)
 
 
+def tile_flags(E, pe, dt, tile=128):
+    """Tile flags of the rows E [rows][nt] (the rule nn_features in
+    csrc/rowkernels.cuh applies in the row reduction, here in FP64).
+
+    g enters the density only through the avalanche term
+    kappa A_j dt (1 - e^{-S_j}) e^{g_j}, at most e^{G_RANGE[1]} times its
+    g = 0 value.  Bit 0: the sum of that bound over the tile exceeds 2^-30
+    of the row's base exponent S_total = dt sum_j Wb_j, so the density uses
+    g there; elsewhere it uses g = 0.  Bit 1: the network runs on the tile
+    (bit 0 of the tile or of a neighbour, which covers the four layers'
+    receptive field of +-16 points).  Returns uint8 [rows][nt / tile]."""
+    E = np.atleast_2d(np.asarray(E))
+    rows, nt = E.shape
+    wb, S = _base_exponent(pe, E, dt)
+    av = np.zeros((rows, nt))
+    av[:, :-1] = quad_ava(pe, E) * dt * -np.expm1(-S)
+    per_tile = av.reshape(rows, nt // tile, tile).sum(axis=2)
+    s_total = wb.sum(axis=1, keepdims=True)
+    a = per_tile * np.exp(G_RANGE[1]) > np.ldexp(s_total, -30)
+    d = a.copy()
+    d[:, 1:] |= a[:, :-1]
+    d[:, :-1] |= a[:, 1:]
+    return a.astype(np.uint8) | (d.astype(np.uint8) << 1)
+
+
 def training_pairs(E, rho, pe, dt, row_frac=1e-9, resolve=1e-6, floor=0.0):
     """Network inputs, targets and loss weights from time rows of the field
     E [rows][nt] (complex analytic signal) and the density rho [rows][nt]

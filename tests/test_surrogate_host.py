@@ -101,3 +101,34 @@ def test_training_rows_below_the_threshold_are_dropped():
     rho[1] = np.linspace(0, 1e-15, nt)
     f, d, m = S.training_pairs(E, rho, pe, 0.1)
     assert f.shape[0] == 1
+
+
+def test_skipped_tiles_cannot_change_the_density():
+    """The tile rule of the row reduction (surrogate.tile_flags): with g = 0
+    on the tiles without bit 0 the closed-form density stays within 2^-24
+    of its scale of the density with any g in range there, on rows where
+    most tiles are skipped (ahead of the pulse S = 0, behind it A ~ 0)."""
+    from filament_gb import surrogate as S
+    pe = _PE()
+    nt, dt = 2048, 0.05
+    t = (np.arange(nt) - nt / 4) * dt
+    E = np.array([np.sqrt(a * np.exp(-(t / 3.0) ** 2)) * np.exp(1j * 3.0 * t) for a in (0.5, 1.0, 2.0)])
+    fl = S.tile_flags(E, pe, dt)
+    assert fl.shape == (3, nt // 128)
+    use, run = (fl & 1) > 0, (fl & 2) > 0
+    assert np.all(run[use])                     # the tiles using g are run
+    assert 0 < np.mean(run) < 0.5               # and most are skipped
+    # every tile using g has both neighbours run (receptive field)
+    assert np.all(run[:, 1:][use[:, :-1]]) and np.all(run[:, :-1][use[:, 1:]])
+    rng = np.random.default_rng(5)
+    mask = np.repeat(use, 128, axis=1)
+    scale = np.max(S.closed_form_density(E, np.zeros((3, nt)), pe, dt))
+    for g in (np.full((3, nt), S.G_RANGE[1]), np.full((3, nt), S.G_RANGE[0]),
+              rng.uniform(*S.G_RANGE, size=(3, nt))):
+        full = S.closed_form_density(E, g, pe, dt)
+        masked = S.closed_form_density(E, np.where(mask, g, 0.0), pe, dt)
+        assert np.max(np.abs(full - masked)) <= 2.0 ** -24 * scale
+    # the rule is not vacuous: g on the tiles with bit 0 does change it
+    g = np.full((3, nt), S.G_RANGE[1])
+    assert np.max(np.abs(S.closed_form_density(E, g, pe, dt)
+                         - S.closed_form_density(E, np.zeros((3, nt)), pe, dt))) > 1e-3 * scale
