@@ -31,7 +31,8 @@ function create(cfg::FilConfig, tab::FilTables)
     rc < 0 && error(unsafe_string(ccall((:fil_last_error, LIB), Cstring, (Ptr{Cvoid},), C_NULL)))
     return h[]
 end
-set_field(h, E::Array{ComplexF64}) =                      # column-major E[Nr, Nt], real signal
+destroy(h) = ccall((:fil_destroy, LIB), Cint, (Ptr{Cvoid},), h)
+set_field(h, E::Array{ComplexF64}) =                     # column-major E[Nr, Nt], real signal
     ccall((:fil_set_field, LIB), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}, Cint, Cint, Cint), h, E, 1, 0, 0)
 zstep(h, z, dz) = ccall((:fil_step, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cdouble), h, z, dz)
 function run!(h, z0, zmax, nmax)
@@ -56,6 +57,16 @@ function ode_stats(h)
     out = zeros(Int64, 2)
     ccall((:fil_get_ode_stats, LIB), Cint, (Ptr{Cvoid}, Ptr{Int64}), h, out)
     return out[1], out[2]
+end
+# learned plasma surrogate counters: armed, in use, steps, steps that used the
+# network, checks, failed checks, last and largest check error, mean rows and
+# mean 128-point tiles per step that used the network
+const SURROGATE_STAT_KEYS = (:armed, :in_use, :steps, :steps_used, :checks, :checks_failed,
+                             :err_last, :err_max, :rows_mean, :tiles_mean)
+function surrogate_stats(h)
+    out = zeros(length(SURROGATE_STAT_KEYS))
+    ccall((:fil_get_surrogate_stats, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Cint), h, out, length(out))
+    return NamedTuple{SURROGATE_STAT_KEYS}(Tuple(out))
 end
 
 # batched sweep: members on uneven grids, one CUDA graph per z-step

@@ -31,6 +31,19 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, n), n
 
 
+def test_julia_binding_calls_declared_symbols():
+    """Julia is absent here, so the ccall shim (julia/FilamentGB.jl) is not
+    run; every symbol it binds must still be one the header declares, and
+    the handle's core entry points must all be bound."""
+    jl = open(os.path.join(ROOT, "filament.jl_gb300", "julia", "FilamentGB.jl")).read()
+    called = set(re.findall(r"ccall\(\(:(fil_[a-z_0-9]+)\s*,", jl))
+    names = set(declared_functions())
+    assert called and called <= names, sorted(called - names)
+    for n in ("fil_create", "fil_destroy", "fil_set_field", "fil_get_field", "fil_run", "fil_analyze",
+              "fil_analyze_spectrum", "fil_get_surrogate_stats", "fil_create_batch", "fil_batch_run"):
+        assert n in called, n
+
+
 def test_oracle_exports_same_abi(oracle_binding):
     """The oracle mirrors the problem-handle ABI; the handle-free device
     buffer entry point, the learned surrogate (whose CPU reference is
