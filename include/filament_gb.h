@@ -209,10 +209,10 @@ typedef struct fil_stats {
   int64_t steps;    /* z-steps taken on this handle                          */
   int32_t status;   /* last stop reason / error code                         */
   int32_t flags;    /* device status bits: 1 NaN seen, 2 Istop, 4 Newton
-                       iteration cap hit in the plasma scan; bits 8-15: the
-                       largest Newton iteration count of any plasma solve;
-                       8 an adaptive nonlinear step (FIL_ALG_ATSIT5) gave up
-                       after 256 attempts at one point                     */
+                       iteration cap hit in the plasma scan, 8 an adaptive
+                       nonlinear step (FIL_ALG_ATSIT5) gave up after 256
+                       attempts at one point; bits 8-15: the largest
+                       Newton iteration count of any plasma solve          */
 } fil_stats;
 
 typedef struct fil_handle fil_handle;

@@ -44,6 +44,41 @@ def test_julia_binding_calls_declared_symbols():
         assert n in called, n
 
 
+def _c_struct(name):
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), src, flags=re.S).group(1)
+    out = []
+    for ty, field, n in re.findall(r"(int32_t|uint32_t|int64_t|double)\s+(\w+)(?:\[(\d+)\])?;", body):
+        out.append((field, ty, int(n) if n else 1))
+    return out
+
+
+def _jl_struct(name):
+    jl = open(os.path.join(ROOT, "filament.jl_gb300", "julia", "FilamentGB.jl")).read()
+    body = re.search(r"struct %s\b(.*?)\nend" % name, jl, flags=re.S).group(1)
+    types = {"Int32": "int32_t", "UInt32": "uint32_t", "Int64": "int64_t", "Float64": "double"}
+    out = []
+    for field, ty in re.findall(r"(\w+)::((?:NTuple\{\d+,\w+\})|\w+)", body):
+        m = re.match(r"NTuple\{(\d+),(\w+)\}", ty)
+        out.append((field, types[m.group(2)], int(m.group(1))) if m else (field, types[ty], 1))
+    return out
+
+
+@pytest.mark.parametrize("c_name, jl_name", [("fil_config", "FilConfig"), ("fil_stats", "FilStats")])
+def test_julia_structs_mirror_the_header(c_name, jl_name):
+    """The Julia mirrors of the ABI structs list the header's fields in its
+    order with the same C types (a ccall passes them by layout)."""
+    assert _jl_struct(jl_name) == _c_struct(c_name)
+
+
+def test_julia_tables_hold_every_pointer():
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    body = re.search(r"typedef struct fil_tables \{(.*?)\} fil_tables;", src, flags=re.S).group(1)
+    n = len(re.findall(r"const double\*\s+\w+;", body))
+    jl = open(os.path.join(ROOT, "filament.jl_gb300", "julia", "FilamentGB.jl")).read()
+    assert re.search(r"p::NTuple\{(\d+),Ptr\{Float64\}\}", jl).group(1) == str(n)
+
+
 def test_oracle_exports_same_abi(oracle_binding):
     """The oracle mirrors the problem-handle ABI; the handle-free device
     buffer entry point, the learned surrogate (whose CPU reference is
