@@ -71,6 +71,30 @@ def test_julia_structs_mirror_the_header(c_name, jl_name):
     assert _jl_struct(jl_name) == _c_struct(c_name)
 
 
+@pytest.mark.parametrize("c_name", ["fil_config", "fil_stats", "fil_tables"])
+def test_python_structs_mirror_the_header(c_name):
+    """The ctypes mirrors in filament_gb/_abi.py: the header's fields in
+    its order with the same C types."""
+    import ctypes as C
+    import filament_gb._abi as abi
+    types = {C.c_int32: "int32_t", C.c_uint32: "uint32_t", C.c_int64: "int64_t", C.c_double: "double"}
+    got = []
+    for field, ty in getattr(abi, c_name)._fields_:
+        if issubclass(ty, C.Array):
+            got.append((field, types[ty._type_], ty._length_))
+        elif ty is C.POINTER(C.c_double):
+            got.append((field, "const double*", 1))
+        else:
+            got.append((field, types[ty], 1))
+    if c_name == "fil_tables":
+        src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+        body = re.search(r"typedef struct fil_tables \{(.*?)\} fil_tables;", src, flags=re.S).group(1)
+        want = [(f, "const double*", 1) for f in re.findall(r"const double\*\s+(\w+);", body)]
+    else:
+        want = _c_struct(c_name)
+    assert got == want
+
+
 def test_julia_tables_hold_every_pointer():
     src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
     body = re.search(r"typedef struct fil_tables \{(.*?)\} fil_tables;", src, flags=re.S).group(1)
