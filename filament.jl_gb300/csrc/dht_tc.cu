@@ -5,12 +5,10 @@
 
 cudaError_t launch_dht_tc(const CUtensorMap (&a)[3], const CUtensorMap (&b)[3], const TcGemmParams& p, int M,
                           int N, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_dht_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  // set on every launch (a host call, legal under stream capture): the
+  // attribute belongs to the current device's context
+  cudaError_t e = cudaFuncSetAttribute(k_dht_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
+  if (e != cudaSuccess) return e;
   if (M % TC_BM || N % TC_BN || p.K % TC_CHUNK) return cudaErrorInvalidValue;
   dim3 grid(N / TC_BN, M / TC_BM);
   k_dht_tc<<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(a[0], a[1], a[2], b[0], b[1], b[2], p);

@@ -681,22 +681,18 @@ cudaError_t nn_launch_out(const float* part, const float* b3, float* out, int T,
 cudaError_t nn_launch_conv_tc(const CUtensorMap& tx, const CUtensorMap& tw, const float* bias, __nv_bfloat16* out,
                               const __nv_bfloat16* w3, float* part, const NnRowsPlan& p, cudaStream_t st,
                               const __nv_bfloat16* x0, const __nv_bfloat16* w0, const float* b0) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_nn_conv_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_nn_conv_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
   if (x0 && part) return cudaErrorInvalidValue;   // layer 0 is fused into layer 1 only
-  static bool attr01 = false;
-  if (x0 && !attr01) {
-    cudaError_t e = cudaFuncSetAttribute(k_nn_l01_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, L01_SMEM);
-    if (e != cudaSuccess) return e;
-    attr01 = true;
-  }
+  // the launched kernel's shared-memory limit, set on every launch (a host
+  // call, legal under stream capture): the attribute belongs to the current
+  // device's context
+  cudaError_t e;
+  if (part)
+    e = cudaFuncSetAttribute(k_nn_conv_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
+  else if (x0)
+    e = cudaFuncSetAttribute(k_nn_l01_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, L01_SMEM);
+  else
+    e = cudaFuncSetAttribute(k_nn_conv_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, NT_SMEM);
+  if (e != cudaSuccess) return e;
   NtParams q;
   q.bias = bias;
   q.x0 = x0;
