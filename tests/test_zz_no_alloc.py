@@ -1,10 +1,12 @@
 """fil_hankel_propagate_noalloc: the linear propagator of an RT z-step for
 callers that cannot allocate device memory where they need it.  Its output
-is checked against the library's ordinary entry point (fil_step of a
-linear-only problem) on two calls in a row, with the same 1e-5 relative L2
-tolerance as the other mixed-precision parity tests.  The caller (this test)
-owns every input and output buffer; the entry point uses only its fixed
-device array."""
+is checked on two calls in a row against the library's ordinary entry point
+(fil_step of a linear-only problem), with the same 1e-5 relative L2
+tolerance as the other mixed-precision parity tests, and against the FP64
+oracle's steps of the same problem (within the sum of that tolerance and
+the mixed form's own 1e-5 bound against the oracle).  The caller (this
+test) owns every input and output buffer; the entry point uses only its
+fixed device array."""
 import ctypes as C
 
 import numpy as np
@@ -50,6 +52,8 @@ def test_noalloc_propagator_matches_fil_step(gpu_lib):
     from filament_gb import Simulation
     inp = rt_input(NONLINEARITY=False, PLASMA=False)
     sim = Simulation(inp, precision="mixed")
+    import oracle
+    ref = Simulation(inp, binding=oracle.binding())
     p = sim.problem
     nr, nt = p.config.n1, p.config.nt
     nh, mpad = nt // 2, ((nr + 127) // 128) * 128
@@ -86,14 +90,19 @@ def test_noalloc_propagator_matches_fil_step(gpu_lib):
     S1 = call(S)
     sim.handle.step(dz, dz)
     E1 = sim.handle.get_field()
+    ref.handle.step(dz, dz)
     assert rel_l2(_to_time(S1, nr, nt, G), E1) < TOL
+    assert rel_l2(_to_time(S1, nr, nt, G), ref.handle.get_field()) < 2 * TOL
     # call 2 reuses the fixed array: guard the previous result, then propagate
     S = _half_spectrum(_to_time(S1, nr, nt, G), nh, mpad, analytic_doubling=False)
     S2 = call(S)
     sim.handle.step(2 * dz, dz)
     E2 = sim.handle.get_field()
+    ref.handle.step(2 * dz, dz)
     assert rel_l2(_to_time(S2, nr, nt, G), E2) < TOL
+    assert rel_l2(_to_time(S2, nr, nt, G), ref.handle.get_field()) < 2 * TOL
     sim.close()
+    ref.close()
 
 
 def test_noalloc_rejects_sizes_beyond_the_fixed_array(gpu_lib):
