@@ -1070,11 +1070,11 @@ static int reduce(fil_handle* h, double* power, int check_done) {
 static void arm_surrogate(const fil_handle* h, DevCtl& c) {
   c.nn_on = h->nn ? 1 : 0;
   c.nn_use = 1;
-  c.nn_judge = 0;
+  c.nn_check = 0;
   c.nn_every = h->nn ? h->nn_every : 1;
   c.nn_tol = h->nn ? h->nn_tol : 0;
   c.nn_count = c.nn_rows = c.nn_tiles = c.nn_tiles_run = 0;
-  c.nn_steps = c.nn_used = c.nn_judged = c.nn_rejected = 0;
+  c.nn_steps = c.nn_used = c.nn_checked = c.nn_rejected = 0;
   c.nn_diff_acc = 0;
   c.nn_err = c.nn_err_max = c.nn_rows_sum = c.nn_tiles_sum = 0;
 }
@@ -1739,7 +1739,7 @@ int fil_get_surrogate_stats(fil_handle* h, double* out, int n) {
   if (rc) return rc;
   const DevCtl& c = *h->ctl_host;
   const double v[10] = {(double)c.nn_on, (double)c.nn_use, (double)c.nn_steps, (double)c.nn_used,
-                        (double)c.nn_judged, (double)c.nn_rejected, c.nn_err, c.nn_err_max,
+                        (double)c.nn_checked, (double)c.nn_rejected, c.nn_err, c.nn_err_max,
                         c.nn_used ? c.nn_rows_sum / (double)c.nn_used : 0.0,
                         c.nn_used ? c.nn_tiles_sum / (double)c.nn_used : 0.0};
   for (int i = 0; i < n; ++i) out[i] = i < 10 ? v[i] : 0.0;

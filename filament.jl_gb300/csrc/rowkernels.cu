@@ -34,29 +34,29 @@ __global__ void k_control(DevCtl* c, const double* __restrict__ fluence, const d
   }
   if (c->clamp_last && c->z + dz > c->zmax) dz = c->zmax - c->z;
   if (c->nn_on) {
-    // the step just taken was a judge step: every row ran the ODE, rhomax is
+    // the step just taken was a check step: every row ran the ODE, rhomax is
     // its maximum
-    if (c->nn_judge) {
+    if (c->nn_check) {
       const double diff = __longlong_as_double((long long)c->nn_diff_acc);
       const double err = rhomax > 0 ? diff / rhomax : (diff > 0 ? 1.0 : 0.0);
       c->nn_err = err;
       c->nn_err_max = fmax(c->nn_err_max, err);
-      c->nn_judged += 1;
+      c->nn_checked += 1;
       c->nn_use = err <= c->nn_tol;
       if (!c->nn_use) c->nn_rejected += 1;
       c->nn_diff_acc = 0;
     }
-    c->nn_judge = (c->nn_steps % c->nn_every) == 0;
-    c->nn_rows = (c->nn_use || c->nn_judge) ? c->nn_count : 0;
-    c->nn_tiles_run = (c->nn_use || c->nn_judge) ? c->nn_tiles : 0;
-    if (c->nn_use && !c->nn_judge) {
+    c->nn_check = (c->nn_steps % c->nn_every) == 0;
+    c->nn_rows = (c->nn_use || c->nn_check) ? c->nn_count : 0;
+    c->nn_tiles_run = (c->nn_use || c->nn_check) ? c->nn_tiles : 0;
+    if (c->nn_use && !c->nn_check) {
       c->nn_used += 1;
       c->nn_rows_sum += c->nn_rows;
       c->nn_tiles_sum += c->nn_tiles;
     }
     c->nn_steps += 1;
   } else {
-    c->nn_judge = 0;
+    c->nn_check = 0;
     c->nn_rows = 0;
     c->nn_tiles_run = 0;
   }
@@ -73,7 +73,7 @@ __global__ void k_control(DevCtl* c, const double* __restrict__ fluence, const d
 // fil_step: latch the plasma maximum of the previous solve, set z and dz.
 __global__ void k_setdz(DevCtl* c, double z, double dz) {
   c->done = 0;
-  c->nn_judge = 0;   // single steps solve the plasma equation
+  c->nn_check = 0;   // single steps solve the plasma equation
   c->nn_rows = 0;
   c->nn_count = 0;
   c->nn_tiles = c->nn_tiles_run = 0;

@@ -27,14 +27,14 @@ struct DevCtl {
   double dz0, phimax, phik, phip, istop;
   // learned plasma surrogate (surrogate.cuh).  Armed (nn_on) it supplies the
   // density of the rows the reduction flags; every nn_every-th step is a
-  // judge step on which the ODE solves every row and the largest
+  // check step on which the ODE solves every row and the largest
   // |rho_net - rho_ode| / max rho_ode is measured.  The network is used on
   // the following steps only while that error is at most nn_tol (nn_use).
-  int nn_on, nn_use, nn_judge, nn_every;
+  int nn_on, nn_use, nn_check, nn_every;
   int nn_count;               // rows flagged by this step's reduction (atomic)
   int nn_rows;                // rows the network runs on in this step
-  long long nn_steps, nn_used, nn_judged, nn_rejected;
-  unsigned long long nn_diff_acc;   // judge step: max |rho_net - rho_ode| (bits)
+  long long nn_steps, nn_used, nn_checked, nn_rejected;
+  unsigned long long nn_diff_acc;   // check step: max |rho_net - rho_ode| (bits)
   double nn_tol, nn_err, nn_err_max;
   double nn_rows_sum;         // sum of nn_rows over the steps that used the network
   int nn_tiles;               // 128-point tiles the network runs on, of the flagged rows (atomic)
@@ -560,12 +560,12 @@ FIL_DEV R plasma_row(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
 // loss term Kdrho_j = sum_c K_c W_c(I_j) (rho_nt,c - rho_{j+1} rho_nt,c / rho_nt),
 // 0 at the last point (the photoionisation-only density of
 // plasma_equations.jl:63-70 approximated by rho).  Thread t owns
-// j = 16t .. 16t+15 as in plasma_row.  judge: compare with the density in
+// j = 16t .. 16t+15 as in plasma_row.  check_step: compare with the density in
 // rho[] instead of writing it; returns max |difference|.  Otherwise writes
 // rho[], kdrho[] and returns max rho.
 template <typename R, int N, int NC>
 FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typename C2T<R>::type* X,
-                     const float* __restrict__ g, R* rho, R* kdrho, Aff<R, 1>* ascratch, R* rscratch, bool judge,
+                     const float* __restrict__ g, R* rho, R* kdrho, Aff<R, 1>* ascratch, R* rscratch, bool check_step,
                      int slot) {
   typedef typename C2T<R>::type C;
   const PlasmaParams<R>& pp = P.pp;
@@ -637,7 +637,7 @@ FIL_DEV R nn_density(const RowParams<R>& P, const PlasmaSmem<R>& tabs, const typ
     const int j = j0 + q;
     S += wl[q];
     const R rnext = ra + (rnt - ra) * -expm1(-S);
-    if (judge) {
+    if (check_step) {
       out = max(out, fabs(rcur - rho[pad16(j)]));
     } else {
       rho[pad16(j)] = rcur;
@@ -871,23 +871,23 @@ __global__ void __launch_bounds__(N / 16, N <= 1024 ? 8192 / N : 2) k_rowstep(Ro
   }
 
   // ---- plasma: the ODE solve, or the surrogate's density for the rows the
-  // reduction flagged.  On a judge step every row is solved and the flagged
+  // reduction flagged.  On a check step every row is solved and the flagged
   // rows also measure the surrogate against the solution.
   if constexpr (NC > 0) {
     if (P.plasma) {
       const bool stepping = mode == 0 || mode == 4;
       const int slot = (P.nn_out && stepping) ? P.nn_slot[row] : -1;
       const bool nn_row = slot >= 0 && slot < ctl->nn_rows;
-      const bool judge = P.nn_out && stepping && ctl->nn_judge;
+      const bool check_step = P.nn_out && stepping && ctl->nn_check;
       Aff<R, 1>* sc1 = reinterpret_cast<Aff<R, 1>*>(ascratch);
       R rmax;
       const float* gslot = P.nn_out + (size_t)slot * N * (P.nn_part ? NN_K : 1);
-      if (nn_row && !judge) {
+      if (nn_row && !check_step) {
         rmax = nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, false, slot);
       } else {
         rmax = plasma_row<R, N, NC>(P, *tabs, X, rho, kdrho, reinterpret_cast<R*>(Y), ascratch, rscratch, &s_flag,
                                     stepping ? (R)ctl->rhomax : (R)0, dz, &ych);
-        if (judge) {
+        if (check_step) {
           // rows not flagged carry rho0 in the surrogate form
           const R diff = nn_row ? nn_density<R, N, NC>(P, *tabs, X, gslot, rho, kdrho, sc1, rscratch, true, slot)
                                 : max(rmax - (R)NC * P.pp.rho0, (R)0);
@@ -1353,7 +1353,7 @@ __global__ void __launch_bounds__(N / 16) k_rowreduce(RowParams<R> P, double* fl
     if (!isfinite(tot)) atomicOr(&ctl->flags, FIL_FLAG_NAN);
     else atomic_max_nonneg(&ctl->imax_acc, bm);
     // learned surrogate: the coming step needs the network (it is in use,
-    // or the step is a judge step) and the plasma solve would not skip the
+    // or the step is a check step) and the plasma solve would not skip the
     // row -> take a slot for its features
     int slot = -1;
     if (P.nn_feat && ctl->nn_on && (ctl->nn_use || ctl->nn_steps % ctl->nn_every == 0) && isfinite(tot)) {

@@ -334,7 +334,7 @@ class Surrogate:
 
     def arm(self, handle, every=20, tol=1e-3):
         """Use the network for the plasma density of `handle` (a backend
-        Handle) inside its device loop, judged every `every` steps."""
+        Handle) inside its device loop, checked every `every` steps."""
         L = _bind(handle.b)
         handle.b.check(handle.h, L.fil_set_surrogate(handle.h, self.h, int(every), float(tol)), "set_surrogate")
         handle._surrogate = self
