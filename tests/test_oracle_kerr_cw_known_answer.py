@@ -1,0 +1,112 @@
+"""Known answer of the oracle's nonlinear step: the Kerr response (cubic,
+without third-harmonic generation) and the Raman response on a continuous
+wave.
+
+A field that is one frequency bin k0 of the time window, E(t) = a e(t) with
+|e(t)| = 1, has constant |E|^2 = |a|^2.  Without the time guard (tguard = 0
+makes the window 1 everywhere, Guards.jl:322-375) the sources stay on that
+bin:
+  cubic, calc_cubic_nothg (cubic.jl:41-46): F = 3/4 |E|^2 Re(E), analytic
+    spectrum 3/4 |a|^2 a;
+  Raman, calc_raman_nothg (raman.jl:57-77): the circular convolution of the
+    constant 3/4 |E|^2 with H is 3/4 |a|^2 H(w = 0), then times Re(E).
+So every RK stage of func! (nonlinear_propagators.jl:38-67) is a multiple
+of the same bin and the step is the RK step of the scalar equation
+  da/dz = i (QZ Rnl_cubic + QZ Rnl_raman H(0)) 3/4 |a|^2 a,
+followed by the linear step exp(i KZ dz) Wguard (Models.jl:75-121).  With
+QZ = mu0 w^2 / (2 beta) zu / Eu and Rnl = eps0 chi3 Eu^3, chi3 = 4/3 n0^2
+eps0 c n2 (cubic.jl:4-13), the coefficient is the textbook self-phase rate
+w n0 n2 Iu zu / (n(w) c) per unit |a|^2, and H(0), the integral of the
+response, is 1 for the air response of Mlejnek et al.  The step's phase
+(0.5 rad) puts the RK steps 3e-3 (RK4) to 5e-2 (RK2) from the exact
+solution a e^{i gamma |a|^2 dz}.
+"""
+import numpy as np
+import pytest
+import scipy.constants as sc
+
+from gpu_helpers import t_input
+
+N2 = 1e-23
+DZ = 1e-3
+AMP2 = 640.0          # |a|^2 in Iu = 1e16 W/m^2
+
+
+def _complex(v):
+    return np.ascontiguousarray(v, dtype=np.float64).view(np.complex128)
+
+
+def _rk(alg, f, y, h):
+    """Midpoint RK2, Kutta's RK3, the classical RK4 (the nonlinear step's
+    integrators)."""
+    k1 = f(y)
+    if alg == "RK2":
+        return y + h * f(y + h / 2 * k1)
+    k2 = f(y + h / 2 * k1)
+    if alg == "RK3":
+        k3 = f(y - h * k1 + 2 * h * k2)
+        return y + h / 6 * (k1 + 4 * k2 + k3)
+    k3 = f(y + h / 2 * k2)
+    k4 = f(y + h * k3)
+    return y + h / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+
+
+@pytest.mark.parametrize("raman", [False, True], ids=["kerr", "kerr+raman"])
+@pytest.mark.parametrize("alg", ["RK2", "RK3", "RK4"])
+def test_cw_step_is_the_rk_step_of_self_phase_modulation(oracle_binding, alg, raman):
+    import filament_gb as fg
+    from filament_gb.responses import init_raman, raman_response_air
+    # a window of 2 ps holds the Raman response (decay time 77 fs) to 3e-5
+    inp = t_input(Nt=4096, tmin=-1000.0, tmax=1000.0, ALG=alg, tguard=0.0)
+    responses, pe, keys = inp["p_model"]
+    cubic = [dict(r, THG=False, n2=N2 / 2 if raman else N2) for r in responses if "n2" in r]
+    assert len(cubic) == 1
+    if raman:
+        cubic.append({"init": init_raman, "THG": False, "n2": N2 / 2, "raman_response": raman_response_air})
+    inp["p_model"] = (cubic, pe, dict(keys, PLASMA=False, ALG=alg))
+    sim = fg.Simulation(inp, binding=oracle_binding)
+    prob, h = sim.problem, sim.handle
+    a = prob._arrays
+    nt, dt = prob.config.nt, prob.config.dt
+    tu, zu, Iu = 1e-15, 1.0, 1e16               # the deck's units
+    assert np.all(np.asarray(a["guardt"]) == 1.0)
+
+    w = 2 * np.pi * np.fft.fftfreq(nt, dt * tu)
+    k0 = int(round(2 * np.pi * sc.c / 800e-9 / w[1]))   # the bin of the carrier
+    S0 = np.zeros(nt, complex)
+    S0[k0] = np.sqrt(AMP2)
+    h.set_field(np.fft.fft(S0), analytic=True)
+    h.step(DZ, DZ)
+    E1 = h.get_field()
+
+    qz = _complex(a["qz"])[k0]
+    coef = qz * _complex(a["rnl_cubic"])[k0] * 0.75
+    if raman:
+        H0 = _complex(a["raman_h"])[0]
+        assert abs(H0 - 1.0) < 1e-3                # the response integrates to one
+        coef += qz * _complex(a["rnl_raman"])[k0] * 0.75 * H0
+    # the self-phase rate from the constants and the medium's beta(w) * zu
+    gamma = w[k0] ** 2 * zu * N2 * Iu / (_complex(a["beta"])[k0].real / zu * sc.c ** 2)
+    gamma *= (_complex(a["beta"])[k0].real * sc.c / w[k0])   # n0 ~ n(w_k0)
+    assert coef.imag == pytest.approx(0.0, abs=1e-12 * abs(coef))
+    assert coef.real == pytest.approx(gamma, rel=1e-3 if raman else 1e-7)
+    assert 0.4 < coef.real * AMP2 * DZ < 0.6
+
+    lin = np.asarray(a["wguard"])[k0] * np.exp(1j * _complex(a["dfr"])[k0] * DZ)
+
+    def field(y1):
+        S1 = np.zeros(nt, complex)
+        S1[k0] = lin * y1
+        return np.fft.fft(S1)
+
+    def err(E):
+        return np.linalg.norm(E - E1) / np.linalg.norm(E1)
+
+    f = lambda y: 1j * coef * abs(y) ** 2 * y
+    y0 = np.sqrt(AMP2) + 0j
+    assert err(field(_rk(alg, f, y0, DZ))) < 1e-12
+    # the answer tells the integrators apart, and from the exact solution
+    others = [_rk(o, f, y0, DZ) for o in ("RK2", "RK3", "RK4") if o != alg]
+    others.append(y0 * np.exp(1j * coef * AMP2 * DZ))
+    assert min(err(field(y)) for y in others) > 1e-3
+    sim.close()
