@@ -110,3 +110,62 @@ def test_cw_step_is_the_rk_step_of_self_phase_modulation(oracle_binding, alg, ra
     others.append(y0 * np.exp(1j * coef * AMP2 * DZ))
     assert min(err(field(y)) for y in others) > 1e-3
     sim.close()
+
+
+@pytest.mark.parametrize("alg", ["RK2", "RK3", "RK4"])
+def test_cw_step_with_multiphoton_losses(oracle_binding, alg):
+    """The losses response (current_losses.jl:4-46) on the same continuous
+    wave: the plasma solve sees the constant I = |a|^2, so Kdrho is a
+    constant kappa at every point but the last, where it is 0
+    (plasma_equations.jl:45-69).  The wave's phase is chosen so that Re(E)
+    vanishes at that last point; then F = Kdrho Re(E) / |E|^2 is
+    kappa Re(E) / |a|^2 at every point, with analytic spectrum kappa a / |a|^2
+    on the bin, and the step is the RK step of da/dz = c kappa a / |a|^2,
+    c = i QZ Rnl_losses = -hbar w0 rhou zu n0 / (4 n(w) tu Iu).  A rate
+    table that is small at this intensity keeps Kdrho constant to 2e-12
+    over the window; a neutral density scaled up by 1e12 makes the losses
+    change the field by 1e-3 in the step."""
+    import filament_gb as fg
+    from filament_gb.plasma import power_law_rate
+    inp = t_input(Nt=4096, tmin=-1000.0, tmax=1000.0, ALG=alg, tguard=0.0)
+    responses, pe, keys = inp["p_model"]
+    losses = [dict(r, EREAL=False) for r in responses if "EREAL" in r]
+    assert len(losses) == 1
+    tu, zu, Iu, rhou = 1e-15, 1.0, 1e16, 2.5e25      # the deck's units
+    pe = dict(pe, nuc=0.0, rho_nt=5.4e24 * 1e12, KDEP=True,
+              components=[{"fraction": 1.0, "ionization_energy": 12.06,
+                           "ionization_rate": power_law_rate(8.0, AMP2 * Iu, 2.5)}])
+    inp["p_model"] = (losses, pe, dict(keys, PLASMA=True, ALG=alg))
+    sim = fg.Simulation(inp, binding=oracle_binding)
+    prob, h = sim.problem, sim.handle
+    a = prob._arrays
+    nt, dt = prob.config.nt, prob.config.dt
+    w = 2 * np.pi * np.fft.fftfreq(nt, dt * tu)
+    k0 = int(round(2 * np.pi * sc.c / 800e-9 / w[1]))
+    a0 = np.sqrt(AMP2) * 1j * np.exp(2j * np.pi * k0 * (nt - 1) / nt)   # Re(E) = 0 at the last point
+    S0 = np.zeros(nt, complex)
+    S0[k0] = a0
+    h.set_field(np.fft.fft(S0), analytic=True)
+    h.step(DZ, DZ)
+    E1 = h.get_field()
+    kd = h.get_plasma(1)
+    kappa = kd[0]
+    assert kd[-1] == 0.0 and np.max(np.abs(kd[:-1] - kappa)) <= 1e-11 * kappa
+
+    c = 1j * _complex(a["qz"])[k0] * _complex(a["rnl_losses"])[k0]
+    w0 = 2 * np.pi * sc.c / 800e-9
+    assert c.imag == pytest.approx(0.0, abs=1e-12 * abs(c))
+    assert c.real == pytest.approx(-sc.hbar * w0 * rhou * zu / (4 * tu * Iu), rel=1e-6)
+
+    lin = np.asarray(a["wguard"])[k0] * np.exp(1j * _complex(a["dfr"])[k0] * DZ)
+
+    def err(y1):
+        S1 = np.zeros(nt, complex)
+        S1[k0] = lin * y1
+        return np.linalg.norm(np.fft.fft(S1) - E1) / np.linalg.norm(E1)
+
+    f = lambda y: c * kappa * y / abs(y) ** 2
+    assert 5e-4 < abs(c * kappa * DZ) / AMP2 < 5e-3
+    assert err(_rk(alg, f, a0, DZ)) < 1e-13
+    assert err(a0) > 1e-4                       # the losses act
+    sim.close()
