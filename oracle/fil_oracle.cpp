@@ -27,10 +27,17 @@
 // (test/test_diffraction_r.jl, test_diffraction_rt.jl, test_diffraction_xy.jl,
 // test_dispersion_t.jl, test_dispersion_rt.jl), run against this oracle in
 // tests/test_oracle_known_answers.py with the reference's tolerances.  The
-// nonlinear responses, the plasma equation, the RK tableaux and the adaptive
-// step have no reference test and no runnable reference here (Julia is
-// absent): for those parts parity is unpinned; they follow the cited source
-// lines.
+// nonlinear half has no reference test with numbers and no runnable
+// reference here (Julia is absent); it is pinned by closed forms instead:
+// the plasma solve with the reference's rate tables, with and without the
+// avalanche term (tests/test_oracle_plasma_known_answers.py); the steps of
+// the free-current, Kerr (no third harmonic), Raman and losses responses
+// under each RK tableau, where the step reduces to a known recursion
+// (tests/test_oracle_free_current_known_answer.py,
+// tests/test_oracle_kerr_cw_known_answer.py); the adaptive step
+// (tests/test_oracle_adaptive_step.py).  The third-harmonic forms, the EREAL
+// variants and the Tsitouras controller remain parity-unpinned; they follow
+// the cited source lines.
 //
 // Choices where the reference relies on un-vendored dependencies:
 //   * QDHT (HankelTransforms): E <- diag(1/s) T D T diag(s) E on the first
