@@ -35,9 +35,9 @@
 // under each RK tableau, where the step reduces to a known recursion
 // (tests/test_oracle_free_current_known_answer.py,
 // tests/test_oracle_kerr_cw_known_answer.py); the adaptive step
-// (tests/test_oracle_adaptive_step.py).  The third-harmonic forms, the EREAL
-// variants and the Tsitouras controller remain parity-unpinned; they follow
-// the cited source lines.
+// (tests/test_oracle_adaptive_step.py).  The third-harmonic forms, the
+// losses' EREAL variant and the Tsitouras controller remain parity-unpinned;
+// they follow the cited source lines.
 //
 // Choices where the reference relies on un-vendored dependencies:
 //   * QDHT (HankelTransforms): E <- diag(1/s) T D T diag(s) E on the first

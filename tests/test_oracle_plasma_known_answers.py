@@ -41,14 +41,22 @@ def test_reference_rate_tables_are_read_as_tabulated():
         assert tf.power(xm) == pytest.approx(order, rel=1e-9)
 
 
+PHASE = 0.6   # rad: Re(E)^2 = cos^2(0.6) |E|^2 for the EREAL cases
+
+
+@pytest.mark.parametrize("ereal", [False, True], ids=["I=|E|^2", "EREAL: I=Re(E)^2"])
 @pytest.mark.parametrize("i_iu", [3.0, 20.0, 60.0])
-def test_oracle_plasma_matches_closed_form_with_reference_tables(oracle_binding, i_iu):
+def test_oracle_plasma_matches_closed_form_with_reference_tables(oracle_binding, i_iu, ereal):
+    """The field is constant in t with phase 0.6 rad, so the rate's argument
+    (photoionization_avalanche.jl:1-17: |E|^2, or Re(E)^2 with EREAL) is the
+    constant I = A^2 or A^2 cos^2(0.6)."""
     import filament_gb as fg
     from filament_gb import _abi
     inp = rt_input(Nr=4, Nt=512, PPcr=1.0)
     pe = inp["p_model"][1]
     pe["components"] = reference_air_components()
     pe["KDEP"] = True
+    pe["EREAL"] = ereal
     pe["rho_nt"] = 2.5e25
     pe["nuc"] = 0.0                      # no avalanche: Rava = 0
     pe["ALG"] = "RK3"
@@ -57,7 +65,7 @@ def test_oracle_plasma_matches_closed_form_with_reference_tables(oracle_binding,
     assert np.all(prob.pe.rava == 0.0)
     h = fg.Handle(prob, oracle_binding)
     nr, nt = prob.config.n1, prob.config.nt
-    amp = np.sqrt(i_iu * np.array([1.0, 0.5, 0.25, 0.0]))
+    amp = np.sqrt(i_iu * np.array([1.0, 0.5, 0.25, 0.0])) * np.exp(1j * PHASE)
     E = np.repeat(amp[:, None], nt, axis=1).astype(np.complex128)   # |E|^2 constant in t
     h.set_field(E, analytic=True)
     rho = h.get_plasma(0)
@@ -65,7 +73,7 @@ def test_oracle_plasma_matches_closed_form_with_reference_tables(oracle_binding,
     dt = prob.config.dt
     j = np.arange(nt)
     for r in range(nr):
-        I = abs(amp[r]) ** 2
+        I = amp[r].real ** 2 if ereal else abs(amp[r]) ** 2
         rho_ref = np.zeros(nt)
         kd_ref = np.zeros(nt)
         for c, tf in enumerate(prob.pe.tfs):
