@@ -31,13 +31,13 @@
 // reference here (Julia is absent); it is pinned by closed forms instead:
 // the plasma solve with the reference's rate tables, with and without the
 // avalanche term (tests/test_oracle_plasma_known_answers.py); the steps of
-// the free-current, Kerr (no third harmonic), Raman and losses responses
-// under each RK tableau, where the step reduces to a known recursion
-// (tests/test_oracle_free_current_known_answer.py,
+// the free-current, Kerr, Raman (with and without the third harmonic) and
+// losses responses under the RK tableaux, where the step reduces to a known
+// recursion (tests/test_oracle_free_current_known_answer.py,
 // tests/test_oracle_kerr_cw_known_answer.py); the adaptive step
-// (tests/test_oracle_adaptive_step.py).  The third-harmonic forms, the
-// losses' EREAL variant and the Tsitouras controller remain parity-unpinned;
-// they follow the cited source lines.
+// (tests/test_oracle_adaptive_step.py).  The losses' EREAL variant and the
+// Tsitouras controller remain parity-unpinned; they follow the cited source
+// lines.
 //
 // Choices where the reference relies on un-vendored dependencies:
 //   * QDHT (HankelTransforms): E <- diag(1/s) T D T diag(s) E on the first

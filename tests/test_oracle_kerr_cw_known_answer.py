@@ -1,6 +1,6 @@
-"""Known answer of the oracle's nonlinear step: the Kerr response (cubic,
-without third-harmonic generation) and the Raman response on a continuous
-wave.
+"""Known answers of the oracle's nonlinear step on continuous waves: the
+Kerr (cubic) and Raman responses, without and with third-harmonic
+generation, and the multiphoton losses.
 
 A field that is one frequency bin k0 of the time window, E(t) = a e(t) with
 |e(t)| = 1, has constant |E|^2 = |a|^2.  Without the time guard (tguard = 0
@@ -168,4 +168,93 @@ def test_cw_step_with_multiphoton_losses(oracle_binding, alg):
     assert 5e-4 < abs(c * kappa * DZ) / AMP2 < 5e-3
     assert err(_rk(alg, f, a0, DZ)) < 1e-13
     assert err(a0) > 1e-4                       # the losses act
+    sim.close()
+
+
+def _re(A):
+    """Real part of the analytic field sum_m A_m e^{-i m th} as the
+    coefficients R_f of e^{-i f th}, f of either sign."""
+    R = {}
+    for m, c in A.items():
+        R[m] = R.get(m, 0) + c / 2
+        R[-m] = R.get(-m, 0) + np.conj(c) / 2
+    return R
+
+
+def _mul(P, Q):
+    out = {}
+    for f, p in P.items():
+        for g, q in Q.items():
+            out[f + g] = out.get(f + g, 0) + p * q
+    return out
+
+
+def _axpy(A, h, B):
+    out = dict(A)
+    for m, c in B.items():
+        out[m] = out.get(m, 0) + h * c
+    return out
+
+
+@pytest.mark.parametrize("raman", [False, True], ids=["kerr-thg", "kerr-thg+raman-thg"])
+def test_third_harmonic_forms_by_harmonic_algebra(oracle_binding, raman):
+    """The third-harmonic forms, calc_cubic (F = Re(E)^3, cubic.jl:33-38) and
+    calc_raman (F = (H * Re(E)^2) Re(E), raman.jl:46-55), on a wave at a low
+    bin k0 = 3: a field that is a sum of odd harmonics m k0 stays one, its
+    sources are finite trigonometric polynomials, and the RK4 step of
+    func! follows exactly in the harmonic coefficients (no harmonic of the
+    four stages, up to 81 k0, reaches Nyquist, so the grid's transforms
+    are exact).  The analytic spectrum doubles the positive harmonics and
+    drops the negative ones; the Raman convolution multiplies harmonic f of
+    Re(E)^2 by H at bin f k0 (mod Nt)."""
+    import filament_gb as fg
+    from filament_gb.responses import init_raman, raman_response_air
+    k0, nt, amp2 = 3, 1024, 1.6e3       # self-phase 0.05 rad at k0
+    inp = t_input(Nt=nt, ALG="RK4", tguard=0.0)
+    responses, pe, keys = inp["p_model"]
+    cubic = [dict(r, THG=True, n2=N2 / 2 if raman else N2) for r in responses if "n2" in r]
+    if raman:
+        cubic.append({"init": init_raman, "THG": True, "n2": N2 / 2, "raman_response": raman_response_air})
+    inp["p_model"] = (cubic, pe, dict(keys, PLASMA=False, ALG="RK4"))
+    sim = fg.Simulation(inp, binding=oracle_binding)
+    prob, h = sim.problem, sim.handle
+    a = prob._arrays
+    assert np.all(np.asarray(a["guardt"]) == 1.0)
+    S0 = np.zeros(nt, complex)
+    S0[k0] = np.sqrt(amp2)
+    h.set_field(np.fft.fft(S0), analytic=True)
+    h.step(DZ, DZ)
+    S1 = np.fft.ifft(h.get_field())
+
+    qz = _complex(a["qz"])
+    rc = _complex(a["rnl_cubic"])
+    rr = _complex(a["rnl_raman"]) if raman else None
+    H = _complex(a["raman_h"]) if raman else None
+    assert 81 * k0 < nt // 2
+
+    def rhs(A):
+        Re = _re(A)
+        R2 = _mul(Re, Re)
+        F = {f: rc[(f * k0) % nt] * c for f, c in _mul(R2, Re).items()}
+        if raman:
+            R2h = {f: c * H[(f * k0) % nt] for f, c in R2.items()}
+            for f, c in _mul(R2h, Re).items():
+                F[f] = F.get(f, 0) + rr[(f * k0) % nt] * c
+        # analytic spectrum (positive harmonics doubled), then i QZ
+        return {f: 1j * qz[f * k0] * 2 * c for f, c in F.items() if f > 0}
+
+    A0 = {1: np.sqrt(amp2) + 0j}
+    k1 = rhs(A0)
+    k2 = rhs(_axpy(A0, DZ / 2, k1))
+    k3 = rhs(_axpy(A0, DZ / 2, k2))
+    k4 = rhs(_axpy(A0, DZ, k3))
+    A1 = A0
+    for kk, wgt in ((k1, 1), (k2, 2), (k3, 2), (k4, 1)):
+        A1 = _axpy(A1, DZ * wgt / 6, kk)
+    want = np.zeros(nt, complex)
+    lin = np.asarray(a["wguard"]) * np.exp(1j * _complex(a["dfr"]) * DZ)
+    for m, c in A1.items():
+        want[m * k0] = lin[m * k0] * c
+    assert abs(A1[3]) > 1e-3 * abs(A1[1])        # the third harmonic is generated
+    assert np.linalg.norm(S1 - want) <= 1e-12 * np.linalg.norm(want)
     sim.close()
