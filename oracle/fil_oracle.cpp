@@ -34,7 +34,8 @@
 // the free-current, Kerr, Raman (with and without the third harmonic) and
 // losses responses under the RK tableaux, where the step reduces to a known
 // recursion (tests/test_oracle_free_current_known_answer.py,
-// tests/test_oracle_kerr_cw_known_answer.py); the adaptive step
+// tests/test_oracle_kerr_cw_known_answer.py,
+// tests/test_oracle_spatial_kerr_known_answer.py); the adaptive step
 // (tests/test_oracle_adaptive_step.py).  The losses' EREAL variant and the
 // Tsitouras controller remain parity-unpinned; they follow the cited source
 // lines.
