@@ -23,7 +23,7 @@ import numpy as np
 import pytest
 import scipy.constants as sc
 
-from gpu_helpers import t_input
+from gpu_helpers import rt_input, t_input
 
 RHO0 = 2.5e24      # m^-3
 NUC = 5e12         # collision frequency of the free-current response (1/s)
@@ -89,3 +89,77 @@ def test_free_current_step_is_the_rk_polynomial_of_the_plasma_dispersion(oracle_
     others = [P[o] for o in P if o != alg] + [np.exp]
     assert min(err(one_step(lam_tab, f)) for f in others) > 1e-4
     sim.close()
+
+
+@pytest.mark.parametrize("qparaxial", [True, False], ids=["RT paraxial", "RT non-paraxial"])
+def test_rt_free_current_step_and_the_nonparaxial_prefactor(oracle_binding, qparaxial):
+    """The same plasma in RT, on a 50 um beam whose transverse spectrum
+    reaches kt ~ 0.3% of beta.  In the Hankel domain (E^ = T diag(s) E,
+    E = diag(1/s) T E^, Fields.jl:105-111) the step is diagonal:
+      E^1 = D(kt, w) P(lambda(kt, w) dz) E^0,
+      D = exp(i KZ dz) Kguard Wguard, KZ = sqrt(beta^2 - kt^2) - w / vf
+      (KPARAXIAL = false, spectral.jl:16-26, 160-184; Guards.jl:95-126),
+    with lambda = i QZ Rnl rho0 for the paraxial prefactor, and
+    lambda = i QZ beta / sqrt(beta^2 - kt^2) Rnl rho0 Kguard Wguard for
+    the non-paraxial one (func!'s transform, prefactor and spectral guard,
+    nonlinear_propagators.jl:56-63, 232-242).  The tolerance covers the
+    Hankel matrix's departure from an involution (T T = I to 2.4e-10); the
+    two prefactors differ by 3e-6 on this beam."""
+    import filament_gb as fg
+    from filament_gb.plasma import power_law_rate
+    inp = rt_input(Nr=128, rmax=0.5, rguard=0.1, beam_a0=50e-6, Nt=2048, tmin=-250.0, tmax=250.0,
+                   ALG="RK4", QPARAXIAL=qparaxial)
+    responses, pe, keys = inp["p_model"]
+    free = [dict(r, nuc=NUC) for r in responses if "nuc" in r and "mr" in r]
+    pe = dict(pe, nuc=0.0, rho0=RHO0,
+              components=[{"fraction": 1.0, "ionization_energy": 12.06,
+                           "ionization_rate": power_law_rate(8.0, 1e18, 1e-200)}])
+    inp["p_model"] = (free, pe, dict(keys, ALG="RK4", QPARAXIAL=qparaxial))
+    sim = fg.Simulation(inp, binding=oracle_binding)
+    prob, h = sim.problem, sim.handle
+    a = prob._arrays
+    nr, nt = prob.config.n1, prob.config.nt
+    rhou = inp["p_unit"][-1]
+    E0 = h.get_field()
+    h.step(DZ, DZ)
+    E1 = h.get_field()
+
+    beta, dfr = _complex(a["beta"]), _complex(a["dfr"])
+    qz, rnl = _complex(a["qz"]), _complex(a["rnl_free"])
+    kt, kmax, wg = np.asarray(a["kt1"]), np.asarray(a["kmax"]), np.asarray(a["wguard"])
+    T, s = np.asarray(a["dht"]), np.asarray(a["dht_s"])
+    G = np.asarray(a["guard1"])[:, None] * np.asarray(a["guardt"])[None, :]
+    j = np.arange(1, nt // 2)
+    Kg = np.zeros((nr, nt))
+    Kg[:, j] = np.exp(-((kt[:, None] ** 2 / kmax[None, j] ** 2)) ** 20)
+    kz = np.sqrt(beta[None, :] ** 2 - kt[:, None] ** 2 + 0j)
+    D = np.exp(1j * (kz - (beta - dfr)[None, :]) * DZ) * Kg * wg[None, :]
+
+    def lam(nonparaxial):
+        out = np.zeros((nr, nt), complex)
+        base = 1j * qz[None, j] * rnl[None, j] * RHO0 / rhou
+        if nonparaxial:
+            out[:, j] = base * beta[None, j] / kz[:, j] * Kg[:, j] * wg[None, j]
+        else:
+            out[:, j] = np.broadcast_to(base, (nr, len(j)))
+        return out
+
+    def one_step(nonparaxial):
+        S0 = np.fft.ifft(E0, axis=1)
+        P = P_RK4(lam(nonparaxial) * DZ)
+        if nonparaxial:
+            Eh = P * (T @ (s[:, None] * S0))
+        else:
+            Eh = T @ (s[:, None] * (P * S0))
+        return G * np.fft.fft((1.0 / s)[:, None] * (T @ (D * Eh)), axis=1)
+
+    def err(E):
+        return np.linalg.norm(E - E1) / np.linalg.norm(E1)
+
+    assert err(one_step(not qparaxial)) < 1e-8
+    assert err(one_step(qparaxial)) > 1e-6        # the prefactors are told apart
+    sim.close()
+
+
+def P_RK4(x):
+    return P["RK4"](x)
