@@ -6,6 +6,7 @@ construction sequence and its loop:
 With device_loop=True the whole loop (controller included) runs on the
 device through fil_run and plot.dat receives the final state only.
 """
+import datetime
 import math
 import os
 
@@ -20,6 +21,7 @@ from .grids import Grid
 from .guards import Guard_build
 from .problem import Problem
 from .writeplots import PlotDAT, PlotNPZ
+from .infos import Info, PhaseTimer, clock
 
 
 class Field:
@@ -107,12 +109,15 @@ def run(input, binding=None, precision="mixed", device_loop=False, write_files=T
         outdir=None):
     """Filament.run (Filament.jl:51-108).  Returns the Simulation."""
     sim = Simulation(input, binding, precision)
-    plotdat = plotnpz = None
+    plotdat = plotnpz = info = None
     if write_files:
         prefix = input["prefix"]
         base = outdir if outdir is not None else input.get("deck_dir", ".")
         path = os.path.join(base, prefix)
         os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+        # info.txt (Filament.jl:88-89)
+        info = Info(path + "info.txt", sim.geometry, sim.unit, sim.grid, sim.field.w0, sim.medium,
+                    sim.analyzer, input["p_info"])
         plotdat = PlotDAT(path + "plot.dat", sim.geometry, sim.unit)
         plotdat.write(sim.analyzer)
         # plot.h5's content (Filament.jl:95-99): z-data every lam0/2, fields every dz_plothdf
@@ -120,35 +125,57 @@ def run(input, binding=None, precision="mixed", device_loop=False, write_files=T
                           input["lam0"] / 2 / sim.unit.z)
         plotnpz.write(sim.handle, sim.analyzer, sim.z)
     try:
-        main_loop(sim, plotdat, device_loop, plotnpz)
+        main_loop(sim, plotdat, device_loop, plotnpz, info)
     finally:
         if plotnpz is not None:
             plotnpz.close()
     return sim
 
 
-def main_loop(sim, plotdat, device_loop=False, plotnpz=None):
-    """Filament.jl:111-184."""
+def main_loop(sim, plotdat, device_loop=False, plotnpz=None, info=None):
+    """Filament.jl:111-184.  With `info`, the per-phase wall times (without
+    the first step) and the start, end and run times go to info.txt."""
     z = sim.z
+    timer = PhaseTimer()
+    start = datetime.datetime.now()
+
+    def timed(name, f, *a):
+        t0 = clock()
+        r = f(*a)
+        timer.add(name, clock() - t0)
+        return r
+
+    def write(zz):
+        if plotdat is not None:
+            timed("writeDAT", plotdat.write, sim.analyzer)
+        if plotnpz is not None:
+            timed("writeHDF", plotnpz.write, sim.handle, sim.analyzer, zz)
+
+    code = 0
     if device_loop:
-        code, st = sim.handle.run(z, sim.zmax, 2 ** 62)
+        code, st = timed("zstep", sim.handle.run, z, sim.zmax, 2 ** 62)
         sim.z = st["z"]
-        sim.analyzer.analyze(sim.z)
-        if plotdat is not None:
-            plotdat.write(sim.analyzer)
-        if plotnpz is not None:
-            plotnpz.write(sim.handle, sim.analyzer, sim.z)
-        return code
-    while z < sim.zmax:
-        dz = sim.dzadaptive(sim.analyzer)
-        z = z + dz
-        sim.handle.step(z, dz)
-        sim.analyzer.analyze(z)
-        if plotdat is not None:
-            plotdat.write(sim.analyzer)
-        if plotnpz is not None:
-            plotnpz.write(sim.handle, sim.analyzer, z)
-        if sim.analyzer.Imax > sim.Istop:
-            break
-    sim.z = z
-    return 0
+        timed("field analyzer", sim.analyzer.analyze, sim.z)
+        write(sim.z)
+    else:
+        first = True
+        while z < sim.zmax:
+            dz = sim.dzadaptive(sim.analyzer)
+            z = z + dz
+            timed("zstep", sim.handle.step, z, dz)
+            timed("field analyzer", sim.analyzer.analyze, z)
+            write(z)
+            if sim.analyzer.Imax > sim.Istop:
+                if info is not None:
+                    info.message("Stop (Imax >= Istop): z=%s[zu], z=%s[m]" % (z, z * sim.unit.z))
+                break
+            if first:          # the first step's set-up is not in the timings
+                timer.reset()
+                first = False
+        sim.z = z
+    if info is not None:
+        end = datetime.datetime.now()
+        info.message(timer.table())
+        info.message("Start time: %s\nEnd time:   %s\nRun time:   %s" % (start.isoformat(), end.isoformat(),
+                                                                           end - start))
+    return code

@@ -115,5 +115,6 @@ def prepare(fname, **overrides):
         "p_guard": p_guard,
         "p_model": (responses, plasma_equation, keys),
         "p_dzadaptive": p_dz,
-        "p_info": (file_input,),
+        "p_info": (file_input, os.path.join(deck_dir, ns["file_initial_condition"]),
+                   os.path.join(deck_dir, ns["file_medium"])),
     }

@@ -93,6 +93,29 @@ def dispersion_length(medium, w, t0):
     return math.inf if k2 == 0 else t0 ** 2 / abs(k2)
 
 
+def dispersion_length3(medium, w, t0):
+    """Media.jl:99-107 (t0^3 / |k3|)."""
+    k3 = k3_func(medium, w)
+    return math.inf if k3 == 0 else t0 ** 3 / abs(k3)
+
+
+def absorption_coefficient(medium, w):
+    """Media.jl:64-67: Im(beta), by field."""
+    return beta_func(medium, w).imag
+
+
+def absorption_length(medium, w):
+    """Media.jl:110-118, as the reference states it (ga / 2 for ga != 0)."""
+    ga = absorption_coefficient(medium, w)
+    return math.inf if ga == 0 else ga / 2
+
+
+def nonlinearity_length(medium, w, I0):
+    """Media.jl:137-145: 1 / (|n2| I0 w / c)."""
+    n2 = medium.n2
+    return math.inf if n2 == 0 else 1.0 / (abs(n2.real if isinstance(n2, complex) else n2) * I0 * w / C0)
+
+
 def chi3_func(medium, w):
     """Media.jl:121-125."""
     n = refractive_index(medium, w)
