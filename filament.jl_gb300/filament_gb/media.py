@@ -127,7 +127,8 @@ def critical_power(medium, w):
     Rcr = 3.79
     lam = 2 * math.pi * C0 / w
     n = refractive_index(medium, w)
-    return Rcr * lam ** 2 / (8.0 * math.pi * abs(n.real) * abs(medium.n2))
+    den = 8.0 * math.pi * abs(n.real) * abs(medium.n2)
+    return math.inf if den == 0 else Rcr * lam ** 2 / den      # a Kerr-free medium: infinite
 
 
 def selffocusing_length(medium, w, a0, P):
