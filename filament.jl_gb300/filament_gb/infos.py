@@ -7,6 +7,7 @@ The sections are the reference's, with its names, units and descriptions;
 the layout of each is a list of rows (name, value in SI, unit, text)."""
 import datetime
 import math
+import os
 import subprocess
 import time
 
@@ -34,7 +35,6 @@ def _banner(title):
 
 def vcs_revision():
     """Infos.jl:85-98: branch and commit of the source tree, if any."""
-    import os
     here = os.path.dirname(os.path.abspath(__file__))
     try:
         b = subprocess.run(["git", "rev-parse", "--abbrev-ref", "HEAD"], cwd=here, capture_output=True,
