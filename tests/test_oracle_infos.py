@@ -74,3 +74,24 @@ def test_info_file(oracle_binding, tmp_path, geom):
     if geom == "XY":
         assert set(grid) == {"dx", "dy", "dkx", "dky", "kxc", "kyc"}
     assert math.isinf(medium["La"][0])                      # air without absorption
+
+
+def test_stop_message_and_timings(oracle_binding, tmp_path):
+    """A run that reaches Istop says so in info.txt (Filament.jl:160-163) and
+    times its phases without the first step (Filament.jl:166-170)."""
+    import filament_gb as fg
+    deck, kw = CASES["RT"]
+    inp = fg.prepare(deck, **dict(kw, zmax=0.01, Istop=0.5))     # Imax is 0.92 at z = 0
+    run = fg.run(inp, binding=oracle_binding, write_files=True, outdir=str(tmp_path))
+    run.close()
+    text = open(os.path.join(str(tmp_path), inp["prefix"], "info.txt")).read()
+    assert "Stop (Imax >= Istop): z=" in text
+    inp = fg.prepare(deck, **dict(kw, zmax=0.005))
+    run = fg.run(inp, binding=oracle_binding, write_files=True, outdir=str(tmp_path / "b"))
+    run.close()
+    text = open(os.path.join(str(tmp_path / "b"), inp["prefix"], "info.txt")).read()
+    table = text.split("Runtime information", 1)[1]
+    rows = {l.split()[0]: l.split() for l in table.splitlines() if l and l.split()[0] in
+            ("zstep", "field", "writeDAT", "writeHDF")}
+    assert int(rows["zstep"][1]) == 4                  # 5 steps of 1 mm, the first not timed
+    assert set(rows) == {"zstep", "field", "writeDAT", "writeHDF"}
