@@ -764,6 +764,14 @@ const char* filo_last_error(const fil_handle* h) { return h ? h->err.c_str() : g
 int filo_create(const fil_config* cfg, const fil_tables* t, fil_handle** out) {
   if (!cfg || !t || !out) return fail(nullptr, FIL_ERR_ARG, "null argument");
   if (cfg->abi_version != FIL_ABI_VERSION) return fail(nullptr, FIL_ERR_ARG, "ABI version mismatch");
+  if (cfg->geometry < FIL_GEOM_R || cfg->geometry > FIL_GEOM_XYT) return fail(nullptr, FIL_ERR_ARG, "unknown geometry");
+  if (cfg->n1 < 1 || cfg->n2 < 1 || cfg->nt < 1) return fail(nullptr, FIL_ERR_ARG, "bad n1, n2 or nt");
+  if (cfg->plasma && (cfg->plasma_ncomp < 1 || cfg->plasma_ncomp > 4))
+    return fail(nullptr, FIL_ERR_ARG, "plasma_ncomp must be 1 .. 4");
+  if (cfg->plasma && cfg->rate_n < 2) return fail(nullptr, FIL_ERR_ARG, "rate_n must be at least 2");
+  if (cfg->plasma && (cfg->plasma_alg < FIL_ALG_RK2 || cfg->plasma_alg > FIL_ALG_RK4))
+    return fail(nullptr, cfg->plasma_alg > FIL_ALG_RK4 && cfg->plasma_alg <= FIL_ALG_ATSIT5 ? FIL_ERR_UNSUPPORTED : FIL_ERR_ARG,
+                "plasma ALG must be RK2, RK3 or RK4");
   fil_handle* h = new fil_handle();
   h->cfg = *cfg;
   h->geom = cfg->geometry;

@@ -1,0 +1,105 @@
+"""fil_create's argument checks (csrc/api.cu), which run before any device
+call, so they are tested here without a GPU: each invalid configuration is
+refused with the documented code and a message.  A configuration that is
+invalid in itself is refused by the CUDA library and the oracle alike; one
+beyond what the CUDA path is built for (Nt outside [512, 4096], the
+Tsitouras step with the non-paraxial prefactor or more than two species) by
+the library alone, while the oracle, like the reference, runs it.  A valid
+configuration passes the checks (the library then stops at "no CUDA
+device" on a machine without one, the oracle builds the handle)."""
+import ctypes
+
+import pytest
+
+from gpu_helpers import rt_input
+
+
+def _problem():
+    import filament_gb as fg
+    return fg.Simulation(rt_input(), make_handle=False).problem
+
+
+def _copy(cfg):
+    import filament_gb._abi as abi
+    out = abi.fil_config()
+    ctypes.memmove(ctypes.byref(out), ctypes.byref(cfg), ctypes.sizeof(cfg))
+    return out
+
+
+def _bindings(oracle_binding):
+    import build as b
+    import filament_gb._abi as abi
+    return {"library": abi.Binding(b.build(), "fil_"), "oracle": oracle_binding}
+
+
+CASES = [   # field, value, code, message, refused by the oracle too
+    ("abi_version", 999, "ARG", b"version", True),
+    ("geometry", 9, "ARG", b"geometry", True),
+    ("nt", 1000, "UNSUPPORTED", b"power of two", True),
+    ("nt", 256, "UNSUPPORTED", b"power of two", False),
+    ("nt", 8192, "UNSUPPORTED", b"power of two", False),
+    ("n1", 0, "ARG", b"n1", True),
+    ("alg", 9, "ARG", b"ALG", True),
+    ("plasma_alg", 5, "UNSUPPORTED", b"plasma ALG", True),
+    ("plasma_alg", 0, "ARG", b"plasma ALG", True),
+    ("plasma_ncomp", 5, "ARG", b"plasma_ncomp", True),
+    ("rate_n", 1, "ARG", b"rate_n", True),
+]
+
+
+@pytest.mark.parametrize("field, value, code, text, both", CASES, ids=["%s=%s" % (c[0], c[1]) for c in CASES])
+def test_invalid_configs_are_refused(oracle_binding, field, value, code, text, both):
+    import filament_gb._abi as abi
+    prob = _problem()
+    cfg = _copy(prob.config)
+    setattr(cfg, field, value)
+    for name, bd in _bindings(oracle_binding).items():
+        if name == "oracle" and not both:
+            continue
+        h = ctypes.c_void_p()
+        rc = bd.create(ctypes.byref(cfg), ctypes.byref(prob.tables), ctypes.byref(h))
+        assert rc == getattr(abi, "FIL_ERR_" + code), (name, rc)
+        assert text.lower() in bd.last_error(None).lower(), (name, bd.last_error(None))
+        assert not h.value
+
+
+def test_tsitouras_refusals(oracle_binding):
+    """The CUDA Tsitouras step is built for the paraxial prefactor and up to
+    two species; the oracle refuses only the adaptive form with the
+    non-paraxial prefactor (whose right-hand side couples the points)."""
+    import filament_gb._abi as abi
+    prob = _problem()
+    b = _bindings(oracle_binding)
+    for change, oracle_refuses in (({"alg": abi.ALG["Tsit5"], "qparaxial": 0}, False),
+                                   ({"alg": abi.ALG["ATsit5"], "qparaxial": 0}, True),
+                                   ({"alg": abi.ALG["ATsit5"], "plasma_ncomp": 3}, False)):
+        cfg = _copy(prob.config)
+        for k, v in change.items():
+            setattr(cfg, k, v)
+        h = ctypes.c_void_p()
+        rc = b["library"].create(ctypes.byref(cfg), ctypes.byref(prob.tables), ctypes.byref(h))
+        assert rc == abi.FIL_ERR_UNSUPPORTED, (change, rc)
+        if oracle_refuses:
+            rc = b["oracle"].create(ctypes.byref(cfg), ctypes.byref(prob.tables), ctypes.byref(h))
+            assert rc == abi.FIL_ERR_UNSUPPORTED, (change, rc)
+
+
+def test_valid_config_passes_the_checks(oracle_binding):
+    import filament_gb._abi as abi
+    prob = _problem()
+    b = _bindings(oracle_binding)
+    h = ctypes.c_void_p()
+    rc = b["oracle"].create(ctypes.byref(prob.config), ctypes.byref(prob.tables), ctypes.byref(h))
+    assert rc == abi.FIL_OK and h.value
+    b["oracle"].destroy(h)
+    rc = b["library"].create(ctypes.byref(prob.config), ctypes.byref(prob.tables), ctypes.byref(h))
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except ImportError:
+        has_gpu = False
+    if has_gpu:
+        assert rc == abi.FIL_OK
+        b["library"].destroy(h)
+    else:
+        assert rc == abi.FIL_ERR_CUDA and b"device" in b["library"].last_error(None)
