@@ -103,3 +103,25 @@ def test_valid_config_passes_the_checks(oracle_binding):
         b["library"].destroy(h)
     else:
         assert rc == abi.FIL_ERR_CUDA and b"device" in b["library"].last_error(None)
+
+
+@pytest.mark.parametrize("mpad, nh, text", [(4096, 1024, b"exceeds"), (128, 2 ** 30 + 64, b"exceeds"),
+                                            (100, 64, b"mpad"), (128, 0, b"2*nh"), (128, 96, b"2*nh")])
+def test_noalloc_entry_checks_its_sizes_first(mpad, nh, text):
+    """fil_hankel_propagate_noalloc (csrc/noalloc.cu) refuses sizes that are
+    malformed or beyond its fixed 16 MiB array before any device call; the
+    pointers (non-null, never dereferenced) stand for device buffers."""
+    import build as b
+    lib = ctypes.CDLL(b.build())
+    f = lib.fil_hankel_propagate_noalloc
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p] * 7 + [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
+    err = lib.fil_last_error
+    err.restype = ctypes.c_char_p
+    err.argtypes = [ctypes.c_void_p]
+    one = ctypes.c_void_p(16)
+    rc = f(one, one, one, one, one, None, None, 0, one, one, mpad, nh, 1e-3, None)
+    assert rc == -1 and text in err(None)
+    rc = f(None, one, one, one, one, None, None, 0, one, one, 128, 64, 1e-3, None)
+    assert rc == -1 and b"null" in err(None)
