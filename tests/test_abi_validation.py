@@ -125,3 +125,27 @@ def test_noalloc_entry_checks_its_sizes_first(mpad, nh, text):
     assert rc == -1 and text in err(None)
     rc = f(None, one, one, one, one, None, None, 0, one, one, 128, 64, 1e-3, None)
     assert rc == -1 and b"null" in err(None)
+
+
+def test_null_handle_is_refused_by_every_entry_point(oracle_binding):
+    """Every entry point taking a handle answers FIL_ERR_ARG to a null one
+    (before touching anything else), in the library and the oracle."""
+    import filament_gb._abi as abi
+    import build as b
+    for bd in (abi.Binding(b.build(), "fil_"), oracle_binding):
+        st = abi.fil_stats()
+        buf = (ctypes.c_double * 8)()
+        i64 = (ctypes.c_int64 * 2)()
+        calls = [lambda: bd.step(None, 0.0, 1e-3),
+                 lambda: bd.run(None, 0.0, 1.0, 1, ctypes.byref(st)),
+                 lambda: bd.analyze(None, ctypes.byref(st), buf, buf, buf),
+                 lambda: bd.get_stats(None, ctypes.byref(st)),
+                 lambda: bd.set_option(None, 0, 0),
+                 lambda: bd.set_field(None, ctypes.cast(buf, ctypes.c_void_p), abi.DTYPE_C128, 0, 0),
+                 lambda: bd.get_field(None, ctypes.cast(buf, ctypes.c_void_p), abi.DTYPE_C128, 0),
+                 lambda: bd.get_plasma(None, 0, ctypes.cast(buf, ctypes.c_void_p), 0, 0),
+                 lambda: bd.kernel_times(None, buf, 8),
+                 lambda: bd.get_ode_stats(None, i64),
+                 lambda: bd.analyze_spectrum(None, buf, 8)]
+        for k, call in enumerate(calls):
+            assert call() == abi.FIL_ERR_ARG, (bd.prefix, k)
