@@ -220,7 +220,10 @@ int fil_nn_create(int nt, uint64_t seed, fil_nn** out) {
     return 0;
   };
   const int np = nn_nparams();
-  if (cudaStreamCreateWithFlags(&n->st, cudaStreamNonBlocking) != cudaSuccess) rc = FIL_ERR_CUDA;
+  {
+    const cudaError_t e = cudaStreamCreateWithFlags(&n->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = nn_fail(n, FIL_ERR_CUDA, std::string("cudaStreamCreateWithFlags: ") + cudaGetErrorString(e));
+  }
   for (void** p : {(void**)&n->p, (void**)&n->m, (void**)&n->v, (void**)&n->g})
     if (!rc) rc = mk(p, np * sizeof(float));
   if (!rc) rc = mk((void**)&n->loss, sizeof(float));

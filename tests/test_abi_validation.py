@@ -149,3 +149,37 @@ def test_null_handle_is_refused_by_every_entry_point(oracle_binding):
                  lambda: bd.analyze_spectrum(None, buf, 8)]
         for k, call in enumerate(calls):
             assert call() == abi.FIL_ERR_ARG, (bd.prefix, k)
+
+
+def test_network_and_batch_entry_points_check_their_arguments():
+    """The learned surrogate's and the batched sweep's entry points refuse
+    null handles and bad sizes before any device work, and a failure to
+    create a network states its cause."""
+    import build as b
+    L = ctypes.CDLL(b.build())
+    vp = ctypes.c_void_p
+
+    def f(name, res, args):
+        g = getattr(L, name)
+        g.restype, g.argtypes = res, args
+        return g
+
+    assert f("fil_nn_nparams", ctypes.c_int, [])() == 76225
+    create = f("fil_nn_create", ctypes.c_int, [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(vp)])
+    last = f("fil_nn_last_error", ctypes.c_char_p, [vp])
+    assert create(512, 1, None) == -1
+    assert create(8, 1, ctypes.byref(vp())) == -1 and b"argument" in last(None)
+    for name, args, vals in [("fil_nn_get_params", [vp, vp], [None, None]),
+                             ("fil_nn_set_params", [vp, vp], [None, None]),
+                             ("fil_nn_forward", [vp, vp, ctypes.c_int, vp], [None, None, 1, None]),
+                             ("fil_nn_infer", [vp, vp, ctypes.c_int, vp], [None, None, 1, None]),
+                             ("fil_set_surrogate", [vp, vp, ctypes.c_int, ctypes.c_double], [None, None, 1, 1.0]),
+                             ("fil_get_surrogate_stats", [vp, vp, ctypes.c_int], [None, None, 0]),
+                             ("fil_batch_tune", [vp, ctypes.c_int, vp, ctypes.c_int], [None, 1, None, 0]),
+                             ("fil_batch_plan", [vp, vp, vp, vp], [None, None, None, None]),
+                             ("fil_create_batch", [ctypes.c_int, vp, vp, ctypes.POINTER(vp)],
+                              [0, None, None, ctypes.byref(vp())])]:
+        assert f(name, ctypes.c_int, args)(*vals) == -1, name
+    assert f("fil_batch_member", vp, [vp, ctypes.c_int])(None, 0) is None
+    assert f("fil_nn_destroy", ctypes.c_int, [vp])(None) == 0          # destroying nothing is fine
+    assert f("fil_batch_destroy", ctypes.c_int, [vp])(None) == 0
