@@ -183,3 +183,20 @@ def test_network_and_batch_entry_points_check_their_arguments():
     assert f("fil_batch_member", vp, [vp, ctypes.c_int])(None, 0) is None
     assert f("fil_nn_destroy", ctypes.c_int, [vp])(None) == 0          # destroying nothing is fine
     assert f("fil_batch_destroy", ctypes.c_int, [vp])(None) == 0
+
+
+@pytest.mark.parametrize("table, text", [("beta", b"propagator"), ("kt1", b"propagator"), ("dht", b"DHT"),
+                                         ("qz", b"QZ"), ("rate_lx", b"plasma tables")])
+def test_missing_tables_are_refused(table, text):
+    """fil_create refuses a problem whose required table is missing
+    (csrc/api.cu), before any device call."""
+    import filament_gb._abi as abi
+    import build as b
+    prob = _problem()
+    tab = abi.fil_tables()
+    ctypes.memmove(ctypes.byref(tab), ctypes.byref(prob.tables), ctypes.sizeof(tab))
+    setattr(tab, table, None)
+    bd = abi.Binding(b.build(), "fil_")
+    h = ctypes.c_void_p()
+    assert bd.create(ctypes.byref(prob.config), ctypes.byref(tab), ctypes.byref(h)) == abi.FIL_ERR_ARG
+    assert text in bd.last_error(None)
