@@ -24,7 +24,11 @@ def _complex(v):
 
 
 def _rk(alg, f, y, h):
-    """Midpoint RK2, Kutta's RK3, the classical RK4."""
+    """Midpoint RK2, Kutta's RK3, the classical RK4 and the Tsitouras 5(4)
+    step (its coefficients as the library states them, csrc/tsit5.h)."""
+    if alg == "Tsit5":
+        from test_oracle_kerr_cw_known_answer import _rk as rk_cw
+        return rk_cw(alg, f, y, h)
     k1 = f(y)
     if alg == "RK2":
         return y + h * f(y + h / 2 * k1)
@@ -44,7 +48,7 @@ def _xy_input(**kw):
     return fg.prepare(os.path.join(DECKS, "diffraction_XY", "input.py"), **base)
 
 
-@pytest.mark.parametrize("geom, alg", [("R", "RK2"), ("R", "RK3"), ("R", "RK4"), ("XY", "RK4")])
+@pytest.mark.parametrize("geom, alg", [("R", "RK2"), ("R", "RK3"), ("R", "RK4"), ("R", "Tsit5"), ("XY", "RK4")])
 def test_spatial_kerr_step_is_the_pointwise_rk_step(oracle_binding, geom, alg):
     import filament_gb as fg
     make = r_input if geom == "R" else _xy_input
@@ -72,7 +76,7 @@ def test_spatial_kerr_step_is_the_pointwise_rk_step(oracle_binding, geom, alg):
     lin.handle.set_field(E0, analytic=True)
     lin.handle.step(dz, dz)
     assert np.linalg.norm(lin.handle.get_field() - E1) > 1e-3 * np.linalg.norm(E1)
-    for other in ("RK2", "RK3", "RK4"):
+    for other in ("RK2", "RK3", "RK4", "Tsit5"):
         if other != alg:
             No = _rk(other, lambda y: 1j * c * G * np.abs(y) ** 2 * y, E0, dz)
             assert np.linalg.norm(No - N) > 1e-6 * np.linalg.norm(N)
