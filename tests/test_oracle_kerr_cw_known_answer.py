@@ -277,3 +277,81 @@ def test_third_harmonic_forms_by_harmonic_algebra(oracle_binding, raman):
     assert abs(A1[3]) > 1e-3 * abs(A1[1])        # the third harmonic is generated
     assert np.linalg.norm(S1 - want) <= 1e-12 * np.linalg.norm(want)
     sim.close()
+
+
+def _tsitouras_bt():
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                            "filament.jl_gb300", "csrc", "tsit5.h")).read()
+    body = src.split("kTsitBt[TSIT_STAGES] = {", 1)[1].split("};", 1)[0]
+    return [float(v) for v in re.findall(r"-?\d+\.\d+(?:e-?\d+)?", body)]
+
+
+def _atsit5(f, y, dz, rtol, atol, nh):
+    """The adaptive Tsitouras step as the library states it (csrc/tsit5.h,
+    ode_after): FSAL stages, error e = h sum btilde_j k_j, RMS norm over the
+    point's nh analytic bins (one of them non-zero here), factor
+    0.9 err^-1/5 clamped to [0.2, 10] (1 after a rejection)."""
+    a, bt = _tsitouras(), _tsitouras_bt()
+    h, zdone, last, rejected, attempts, rejects = dz, 0.0, True, False, 0, 0
+    k0 = f(y)
+    while True:
+        k = [k0]
+        for s_ in range(1, 6):
+            k.append(f(y + h * sum(a[s_][j] * k[j] for j in range(s_))))
+        y1 = y + h * sum(a[6][j] * k[j] for j in range(6))
+        k.append(f(y1))
+        e = h * sum(bt[j] * k[j] for j in range(7))
+        err = abs(e) / (atol + rtol * max(abs(y), abs(y1))) / np.sqrt(nh)
+        attempts += 1
+        if err <= 1.0:
+            zdone += h
+            y, k0 = y1, k[6]
+            if last:
+                return y, attempts, rejects
+            fac = 0.9 * err ** -0.2 if err > 0 else 10.0
+            fac = max(min(fac, 1.0 if rejected else 10.0), 0.2)
+            rejected = False
+        else:
+            fac = max(0.9 * err ** -0.2, 0.2)
+            rejected, rejects = True, rejects + 1
+        h *= fac
+        last = h >= dz - zdone
+        if last:
+            h = dz - zdone
+
+
+def test_cw_adaptive_tsitouras_step(oracle_binding):
+    """ATsit5 on the continuous wave: the substeps, their number and the
+    rejections follow the stated controller exactly."""
+    import filament_gb as fg
+    from filament_gb import _abi
+    inp = t_input(Nt=1024, ALG="ATsit5", tguard=0.0)
+    responses, pe, keys = inp["p_model"]
+    cubic = [dict(r, THG=False, n2=N2) for r in responses if "n2" in r]
+    inp["p_model"] = (cubic, pe, dict(keys, PLASMA=False, ALG="ATsit5"))
+    sim = fg.Simulation(inp, binding=oracle_binding)
+    prob, h = sim.problem, sim.handle
+    a = prob._arrays
+    rtol, atol = 1e-7, 1e-9
+    h.set_option(_abi.OPT_ODE_RTOL, int(round(rtol * 1e12)))
+    h.set_option(_abi.OPT_ODE_ATOL, int(round(atol * 1e12)))
+    nt, dt = prob.config.nt, prob.config.dt
+    w = 2 * np.pi * np.fft.fftfreq(nt, dt * 1e-15)
+    k0 = int(round(2 * np.pi * sc.c / 800e-9 / w[1]))
+    S0 = np.zeros(nt, complex)
+    S0[k0] = np.sqrt(AMP2)
+    h.set_field(np.fft.fft(S0), analytic=True)
+    h.step(DZ, DZ)
+    E1 = h.get_field()
+    attempts, rejects = h.ode_stats()
+    coef = _complex(a["qz"])[k0] * _complex(a["rnl_cubic"])[k0] * 0.75
+    y1, n_att, n_rej = _atsit5(lambda y: 1j * coef * abs(y) ** 2 * y, np.sqrt(AMP2) + 0j, DZ, rtol, atol, nt // 2)
+    assert n_att > 3                                   # the tolerance forces substeps
+    S1 = np.zeros(nt, complex)
+    S1[k0] = np.asarray(a["wguard"])[k0] * np.exp(1j * _complex(a["dfr"])[k0] * DZ) * y1
+    assert np.linalg.norm(np.fft.fft(S1) - E1) <= 1e-12 * np.linalg.norm(E1)
+    assert (attempts, rejects) == (n_att, n_rej)
+    print("ATsit5 on the wave: %d attempts, %d rejected" % (n_att, n_rej))
+    sim.close()
