@@ -112,3 +112,27 @@ def test_accuracy_leg_with_the_oracle_standing_in(monkeypatch, oracle_binding):
         assert r[form]["vs_oracle"]["field_rel_l2"] < 1e-12      # all FP64 here
         assert r[form]["vs_fp64_gpu"]["fluence_rel_l2"] < 1e-12
     assert r["fp64"]["vs_oracle"]["field_rel_l2"] < 1e-12
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` times the FP64 oracle on the host threads
+    (W untimed and K timed z-steps of the workload) and prints one JSON line
+    with the arm's metric, the reference marker, its CPU baseline and an e2e
+    block without device copies."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                          "--steps", "2", "--warmup", "3"], capture_output=True, text=True, timeout=600,
+                         cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == "RT z-steps/s" and line["unit"] == "z-steps/s"
+    assert line["steps"] == 2 and line["warmup"] == 3 and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["cpu_baseline"]["value"] == line["value"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": "z-steps/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["config"]["Nr"] == 1000 and line["config"]["Nt"] == 4096
